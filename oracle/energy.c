@@ -1,0 +1,1202 @@
+/*
+ * energy.c -- ORACLE (test infrastructure): literal restatement of VALENCE's
+ * guess-energy path.  Each routine names the reference lines it follows
+ * (src/valence.F90 unless stated otherwise).  Arrays keep the reference's
+ * 1-based, column-major conventions so the index arithmetic reads like the
+ * Fortran.  Differences from the reference that do not change arithmetic:
+ *   - the 2e task loop is spread over OpenMP threads (the reference spreads it
+ *     over MPI ranks round-robin, valence.F90:1158-1163), each with private
+ *     determinant workspaces; partial sums are added in thread order;
+ *   - contracted AO shell-quartet ERI blocks are computed once and cached,
+ *     where the reference calls simint for every shell quartet of every
+ *     int2e call (valence.F90:3316-3427).
+ */
+#include "oracle_internal.h"
+
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define A2(a, ld, i, j) (a)[((size_t)(j)-1) * (size_t)(ld) + (size_t)(i)-1]
+
+typedef struct {
+  vo_input *in;
+  int nelec, nalpha, nbeta, padded, nnd, nsp;
+  int *bra, *ket; /* 1-based, length nelec+1 */
+  double *wdet;   /* nelec x nelec */
+  double *schwarz;
+  double *abra_docc_un, *bbra_docc_un, *aket_docc_un, *bket_docc_un;
+  int ld_du; /* ndocc+nunpd (>=1) */
+  /* basis */
+  int ngsh;
+  vo_shell *gsh;
+  int *gfirst; /* first global shell of atom (1-based atom) */
+  double angn[120];
+  int max_obs;
+  /* ERI cache over canonical shell quartets */
+  double **eri_cache;
+  size_t ncanon;
+} vo_state;
+
+typedef struct {
+  vo_state *st;
+  int *bra_a, *bra_b, *ket_a, *ket_b, *bexch, *kexch;
+  double *abra_npair, *bbra_npair, *aket, *bket;
+  int dme_b[3], dme_k[3];
+  double *ci, *cj, *ck, *cl; /* coeffi..l, 1-based */
+  int *xpnew, *atom_ndf, *ndf2orb;
+  double *blk;
+  double sint, hint, gint;
+  long long ndens2;
+} vo_ctx;
+
+static int shell_size(int l) { return (l + 1) * (l + 2) / 2; }
+static int funmin(int l) { return 1 + l * (l + 1) * (l + 2) / 6; }
+
+/* ------------------------------------------------------------------ */
+/* basis preparation: norm_prim (valence.F90:2264-2305), dblfac (:2314),
+ * cartesian + setangn (:2337-2421) */
+
+static double dblfac(int n) {
+  double d = 1.0;
+  for (int i = 3; i <= n; i += 2) d *= (double)i;
+  return d;
+}
+
+static void norm_prim(int l, int n, const double *ex, double *cc, const double *uc) {
+  double pi32 = pow(acos(-1.0), 1.5);
+  double fac = pi32 * dblfac(2 * l - 1) * pow(2.0, -l);
+  double fax = -1.5 - l;
+  for (int i = 0; i < n; ++i) {
+    double sovl = fac * pow(2.0 * ex[i], fax);
+    cc[i] = uc[i] * pow(sovl, -0.5);
+  }
+  double sovl = 0.0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) sovl += fac * cc[i] * cc[j] * pow(ex[i] + ex[j], fax);
+  sovl = pow(sovl, -0.5);
+  for (int i = 0; i < n; ++i) cc[i] *= sovl;
+}
+
+static void setangn(vo_state *st, int nang) {
+  double ashl[16], ashi[16];
+  int ij = 0;
+  for (int i = 0; i <= nang; ++i) {
+    double fii = 1.0;
+    for (int j = 1; j <= 2 * i - 1; j += 2) fii *= (double)j;
+    fii = sqrt(fii);
+    ashl[i] = fii;
+    ashi[i] = 1.0 / fii;
+  }
+  /* CCA order (valence.F90:2364-2378) */
+  for (int i = 0; i <= nang; ++i)
+    for (int k = 0; k < shell_size(i); ++k) {
+      int x, y, z;
+      vo_cart_comp(i, k, &x, &y, &z);
+      ij++;
+      st->angn[ij] = ashl[i] * ashi[x] * ashi[y] * ashi[z];
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* ERI cache keyed by canonical (ab|cd) with a>=b, c>=d, ab>=cd */
+
+static size_t tri(size_t i) { return i * (i + 1) / 2; }
+
+static const double *eri_block_canon(vo_state *st, int a, int b, int c, int d) {
+  size_t ab = tri((size_t)a) + (size_t)b, cd = tri((size_t)c) + (size_t)d;
+  size_t key = tri(ab) + cd;
+  double *p = __atomic_load_n(&st->eri_cache[key], __ATOMIC_ACQUIRE);
+  if (p) return p;
+  int n = shell_size(st->gsh[a].l) * shell_size(st->gsh[b].l) * shell_size(st->gsh[c].l) *
+          shell_size(st->gsh[d].l);
+  double *blk = (double *)malloc(sizeof(double) * (size_t)n);
+  vo_shell_eri(&st->gsh[a], &st->gsh[b], &st->gsh[c], &st->gsh[d], blk);
+  double *expected = NULL;
+  if (!__atomic_compare_exchange_n(&st->eri_cache[key], &expected, blk, 0, __ATOMIC_ACQ_REL,
+                                   __ATOMIC_ACQUIRE)) {
+    free(blk);
+    return expected;
+  }
+  return blk;
+}
+
+/* ordered block (ga gb | gc gd) in a-major layout, as simint returns it */
+static void eri_block(vo_state *st, int ga, int gb, int gc, int gd, double *out) {
+  int sa = ga, sb = gb, sc = gc, sd = gd;
+  int swab = 0, swcd = 0, swpair = 0;
+  if (sa < sb) {
+    int t = sa;
+    sa = sb;
+    sb = t;
+    swab = 1;
+  }
+  if (sc < sd) {
+    int t = sc;
+    sc = sd;
+    sd = t;
+    swcd = 1;
+  }
+  size_t ab = tri((size_t)sa) + (size_t)sb, cd = tri((size_t)sc) + (size_t)sd;
+  if (ab < cd) {
+    int t;
+    t = sa;
+    sa = sc;
+    sc = t;
+    t = sb;
+    sb = sd;
+    sd = t;
+    swpair = 1;
+  }
+  const double *blk = eri_block_canon(st, sa, sb, sc, sd);
+  int n[4] = {shell_size(st->gsh[ga].l), shell_size(st->gsh[gb].l), shell_size(st->gsh[gc].l),
+              shell_size(st->gsh[gd].l)};
+  int m[4] = {shell_size(st->gsh[sa].l), shell_size(st->gsh[sb].l), shell_size(st->gsh[sc].l),
+              shell_size(st->gsh[sd].l)};
+  for (int i = 0; i < n[0]; ++i)
+    for (int j = 0; j < n[1]; ++j)
+      for (int k = 0; k < n[2]; ++k)
+        for (int l = 0; l < n[3]; ++l) {
+          int ii = i, jj = j, kk = k, ll = l, t;
+          if (swab) {
+            t = ii;
+            ii = jj;
+            jj = t;
+          }
+          if (swcd) {
+            t = kk;
+            kk = ll;
+            ll = t;
+          }
+          if (swpair) {
+            t = ii;
+            ii = kk;
+            kk = t;
+            t = jj;
+            jj = ll;
+            ll = t;
+          }
+          out[((i * n[1] + j) * n[2] + k) * n[3] + l] = blk[((ii * m[1] + jj) * m[2] + kk) * m[3] + ll];
+        }
+}
+
+/* ------------------------------------------------------------------ */
+/* ndf2obs (valence.F90:2191-2247) and the weight scatter shared by
+ * ovint / int1e / int2e (e.g. :3221-3282) */
+
+static void ndf2obs(vo_ctx *cx, int iorb, int indf) {
+  vo_input *in = cx->st->in;
+  int mx = in->mxctr;
+  int ib = 0;
+  for (int iat = 1; iat <= in->orbas_atnum[indf - 1]; ++iat) {
+    A2(cx->atom_ndf, 2, 1, iat) = ib + 1;
+    int it = in->atom_t[in->orbas_atset[(iat - 1) + mx * (indf - 1)] - 1];
+    int mnshi = in->map_atom2shell[it - 1];
+    int mxshi = mnshi + in->num_shell_atom[it - 1] - 1;
+    for (int ish = mnshi; ish <= mxshi; ++ish) ib += shell_size(in->ang_mom[ish - 1]);
+    A2(cx->atom_ndf, 2, 2, iat) = ib;
+  }
+  ib = 1;
+  for (int iat = 1; iat <= in->orbas_atnum[iorb - 1]; ++iat) {
+    for (int jat = 1; jat <= in->orbas_atnum[indf - 1]; ++jat)
+      if (in->orbas_atset[(jat - 1) + mx * (indf - 1)] == in->orbas_atset[(iat - 1) + mx * (iorb - 1)])
+        cx->ndf2orb[jat] = ib;
+    int it = in->atom_t[in->orbas_atset[(iat - 1) + mx * (iorb - 1)] - 1];
+    int mnshi = in->map_atom2shell[it - 1];
+    int mxshi = mnshi + in->num_shell_atom[it - 1] - 1;
+    for (int ish = mnshi; ish <= mxshi; ++ish) ib += shell_size(in->ang_mom[ish - 1]);
+  }
+  int i = 0, j = 0;
+  for (int b = in->map_orbs[indf - 1]; b <= in->map_orbs[indf] - 1; ++b) {
+    for (int ia = 1; ia <= in->orbas_atnum[indf - 1]; ++ia)
+      if (in->xpset[b - 1] >= A2(cx->atom_ndf, 2, 1, ia) && in->xpset[b - 1] <= A2(cx->atom_ndf, 2, 2, ia))
+        j = cx->ndf2orb[ia] - A2(cx->atom_ndf, 2, 1, ia);
+    i++;
+    cx->xpnew[i] = in->xpset[b - 1] + j;
+  }
+}
+
+static void scatter(vo_ctx *cx, int io, double *c) {
+  vo_input *in = cx->st->in;
+  for (int i = 1; i <= cx->st->max_obs; ++i) c[i] = 0.0;
+  for (int i = in->map_orbs[io - 1]; i <= in->map_orbs[io] - 1; ++i) {
+    if (in->xpset[i - 1] < 1) {
+      int indf = in->xpset[i - 1] + in->norbs;
+      ndf2obs(cx, io, indf);
+      int k = 0;
+      for (int j = in->map_orbs[indf - 1]; j <= in->map_orbs[indf] - 1; ++j) {
+        k++;
+        c[cx->xpnew[k]] += in->coeff[j - 1] * in->coeff[i - 1];
+      }
+    } else {
+      c[in->xpset[i - 1]] += in->coeff[i - 1];
+    }
+  }
+}
+
+static int gshell_of(vo_state *st, int atom, int ish_in_atom) { return st->gfirst[atom] + ish_in_atom; }
+
+/* ovint (valence.F90:2891-3012) */
+static void ovint(vo_ctx *cx, int io, int jo) {
+  vo_state *st = cx->st;
+  vo_input *in = st->in;
+  int mx = in->mxctr;
+  scatter(cx, io, cx->ci);
+  scatter(cx, jo, cx->cj);
+  double sint = 0.0;
+  double dij[128], buf[128];
+  int loxi = 0;
+  for (int ic = 1; ic <= in->orbas_atnum[io - 1]; ++ic) {
+    int ia = in->orbas_atset[(ic - 1) + mx * (io - 1)];
+    int it = in->atom_t[ia - 1];
+    int mnshi = in->map_atom2shell[it - 1], mxshi = mnshi + in->num_shell_atom[it - 1] - 1;
+    for (int ii = mnshi; ii <= mxshi; ++ii) {
+      int li = in->ang_mom[ii - 1];
+      int loxj = 0;
+      for (int jc = 1; jc <= in->orbas_atnum[jo - 1]; ++jc) {
+        int ja = in->orbas_atset[(jc - 1) + mx * (jo - 1)];
+        int jt = in->atom_t[ja - 1];
+        int mnshj = in->map_atom2shell[jt - 1], mxshj = mnshj + in->num_shell_atom[jt - 1] - 1;
+        for (int jj = mnshj; jj <= mxshj; ++jj) {
+          int lj = in->ang_mom[jj - 1];
+          int n = 0, iao = loxi;
+          for (int i = funmin(li); i < funmin(li) + shell_size(li); ++i) {
+            iao++;
+            int jao = loxj;
+            for (int j = funmin(lj); j < funmin(lj) + shell_size(lj); ++j) {
+              jao++;
+              dij[n++] = st->angn[i] * st->angn[j] * cx->ci[iao] * cx->cj[jao];
+            }
+          }
+          vo_shell_overlap_kinetic(&st->gsh[gshell_of(st, ia, ii - mnshi)], &st->gsh[gshell_of(st, ja, jj - mnshj)],
+                                   buf, NULL);
+          for (int k = 0; k < n; ++k) sint += dij[k] * buf[k];
+          loxj += shell_size(lj);
+        }
+      }
+      loxi += shell_size(li);
+    }
+  }
+  cx->sint = sint;
+}
+
+/* int1e (valence.F90:3022-3176) */
+static void int1e(vo_ctx *cx, int io, int jo) {
+  vo_state *st = cx->st;
+  vo_input *in = st->in;
+  int mx = in->mxctr;
+  scatter(cx, io, cx->ci);
+  scatter(cx, jo, cx->cj);
+  double hint = 0.0;
+  double dij[128], buf[128];
+  int loxi = 0;
+  for (int ic = 1; ic <= in->orbas_atnum[io - 1]; ++ic) {
+    int ia = in->orbas_atset[(ic - 1) + mx * (io - 1)];
+    int it = in->atom_t[ia - 1];
+    int mnshi = in->map_atom2shell[it - 1], mxshi = mnshi + in->num_shell_atom[it - 1] - 1;
+    for (int ii = mnshi; ii <= mxshi; ++ii) {
+      int li = in->ang_mom[ii - 1];
+      int loxj = 0;
+      for (int jc = 1; jc <= in->orbas_atnum[jo - 1]; ++jc) {
+        int ja = in->orbas_atset[(jc - 1) + mx * (jo - 1)];
+        int jt = in->atom_t[ja - 1];
+        int mnshj = in->map_atom2shell[jt - 1], mxshj = mnshj + in->num_shell_atom[jt - 1] - 1;
+        for (int jj = mnshj; jj <= mxshj; ++jj) {
+          int lj = in->ang_mom[jj - 1];
+          int nn = 0, iao = loxi;
+          for (int i = funmin(li); i < funmin(li) + shell_size(li); ++i) {
+            iao++;
+            int jao = loxj;
+            for (int j = funmin(lj); j < funmin(lj) + shell_size(lj); ++j) {
+              jao++;
+              dij[nn++] = st->angn[i] * st->angn[j] * cx->cj[jao] * cx->ci[iao];
+            }
+          }
+          const vo_shell *A = &st->gsh[gshell_of(st, ia, ii - mnshi)], *B = &st->gsh[gshell_of(st, ja, jj - mnshj)];
+          vo_shell_overlap_kinetic(A, B, NULL, buf);
+          for (int k = 0; k < nn; ++k) hint += dij[k] * buf[k];
+          for (int ictr = 1; ictr <= in->natom; ++ictr) {
+            double z = in->nuc_charge[in->atom_t[ictr - 1] - 1];
+            if (fabs(z) > 1e-12) {
+              vo_shell_nuclear(A, B, z, &in->coords[3 * (ictr - 1)], buf);
+              for (int k = 0; k < nn; ++k) hint += dij[k] * buf[k];
+            }
+          }
+          loxj += shell_size(lj);
+        }
+      }
+      loxi += shell_size(li);
+    }
+  }
+  cx->hint = hint;
+}
+
+/* int2e (valence.F90:3184-3438): (io jo | ko lo) with per-shell LCAO weight
+ * screens sum(coeff^2) > dtol */
+static void int2e(vo_ctx *cx, int io, int jo, int ko, int lo) {
+  vo_state *st = cx->st;
+  vo_input *in = st->in;
+  int mx = in->mxctr;
+  double dtol = in->dtol;
+  scatter(cx, io, cx->ci);
+  scatter(cx, jo, cx->cj);
+  scatter(cx, ko, cx->ck);
+  scatter(cx, lo, cx->cl);
+  double gint = 0.0;
+  double dij[128], dkl[128];
+  int ish_beg = 1;
+  for (int ia = 1; ia <= in->orbas_atnum[io - 1]; ++ia) {
+    int ic = in->orbas_atset[(ia - 1) + mx * (io - 1)];
+    int it = in->atom_t[ic - 1];
+    int mnshi = in->map_atom2shell[it - 1], mxshi = mnshi + in->num_shell_atom[it - 1] - 1;
+    for (int ii = mnshi; ii <= mxshi; ++ii) {
+      int li = in->ang_mom[ii - 1];
+      double sum = 0.0;
+      for (int i = ish_beg; i <= ish_beg + shell_size(li) - 1; ++i) sum += cx->ci[i] * cx->ci[i];
+      if (sum > dtol) {
+        int jsh_beg = 1;
+        for (int ja = 1; ja <= in->orbas_atnum[jo - 1]; ++ja) {
+          int jc = in->orbas_atset[(ja - 1) + mx * (jo - 1)];
+          int jt = in->atom_t[jc - 1];
+          int mnshj = in->map_atom2shell[jt - 1], mxshj = mnshj + in->num_shell_atom[jt - 1] - 1;
+          for (int jj = mnshj; jj <= mxshj; ++jj) {
+            int lj = in->ang_mom[jj - 1];
+            sum = 0.0;
+            for (int i = jsh_beg; i <= jsh_beg + shell_size(lj) - 1; ++i) sum += cx->cj[i] * cx->cj[i];
+            if (sum > dtol) {
+              int ksh_beg = 1;
+              for (int ka = 1; ka <= in->orbas_atnum[ko - 1]; ++ka) {
+                int kc = in->orbas_atset[(ka - 1) + mx * (ko - 1)];
+                int kt = in->atom_t[kc - 1];
+                int mnshk = in->map_atom2shell[kt - 1], mxshk = mnshk + in->num_shell_atom[kt - 1] - 1;
+                for (int kk = mnshk; kk <= mxshk; ++kk) {
+                  int lk = in->ang_mom[kk - 1];
+                  sum = 0.0;
+                  for (int i = ksh_beg; i <= ksh_beg + shell_size(lk) - 1; ++i) sum += cx->ck[i] * cx->ck[i];
+                  if (sum > dtol) {
+                    int lsh_beg = 1;
+                    for (int la = 1; la <= in->orbas_atnum[lo - 1]; ++la) {
+                      int lc = in->orbas_atset[(la - 1) + mx * (lo - 1)];
+                      int lt = in->atom_t[lc - 1];
+                      int mnshl = in->map_atom2shell[lt - 1], mxshl = mnshl + in->num_shell_atom[lt - 1] - 1;
+                      for (int ll = mnshl; ll <= mxshl; ++ll) {
+                        int lll = in->ang_mom[ll - 1];
+                        sum = 0.0;
+                        for (int i = lsh_beg; i <= lsh_beg + shell_size(lll) - 1; ++i)
+                          sum += cx->cl[i] * cx->cl[i];
+                        if (sum > dtol) {
+                          int kl = 0, kao = 0;
+                          for (int k = funmin(lk); k < funmin(lk) + shell_size(lk); ++k) {
+                            kao++;
+                            double faci = st->angn[k];
+                            int lao = 0;
+                            for (int l = funmin(lll); l < funmin(lll) + shell_size(lll); ++l) {
+                              lao++;
+                              dkl[kl++] = faci * st->angn[l] * cx->ck[ksh_beg + kao - 1] * cx->cl[lsh_beg + lao - 1];
+                            }
+                          }
+                          int ij = 0, iao = 0;
+                          for (int i = funmin(li); i < funmin(li) + shell_size(li); ++i) {
+                            iao++;
+                            double faci = st->angn[i];
+                            int jao = 0;
+                            for (int j = funmin(lj); j < funmin(lj) + shell_size(lj); ++j) {
+                              jao++;
+                              dij[ij++] = faci * st->angn[j] * cx->ci[ish_beg + iao - 1] * cx->cj[jsh_beg + jao - 1];
+                            }
+                          }
+                          eri_block(st, gshell_of(st, ic, ii - mnshi), gshell_of(st, jc, jj - mnshj),
+                                    gshell_of(st, kc, kk - mnshk), gshell_of(st, lc, ll - mnshl), cx->blk);
+                          int n = 0;
+                          for (int i = 0; i < ij; ++i)
+                            for (int k = 0; k < kl; ++k) {
+                              gint += dkl[k] * dij[i] * cx->blk[n];
+                              n++;
+                            }
+                        }
+                        lsh_beg += shell_size(lll);
+                      }
+                    }
+                  }
+                  ksh_beg += shell_size(lk);
+                }
+              }
+            }
+            jsh_beg += shell_size(lj);
+          }
+        }
+      }
+      ish_beg += shell_size(li);
+    }
+  }
+  cx->gint = gint;
+}
+
+/* ------------------------------------------------------------------ */
+/* determinants: givens_single (givens.F90:230-262) and givdr
+ * (valence.F90:2067-2144, USE_FORTRAN_VERSION path) */
+
+static void givens_single(double *a, int lda, int n, double tol) {
+  for (int j = 1; j <= n - 1; ++j)
+    for (int i = n; i >= j + 1; --i) {
+      double cx = A2(a, lda, j, i - 1);
+      double sx = A2(a, lda, j, i);
+      double r = cx * cx + sx * sx;
+      if (fabs(r) > tol) {
+        r = pow(r, -0.5);
+        cx *= r;
+        sx *= r;
+        for (int k = 1; k <= n; ++k) {
+          double t1 = A2(a, lda, k, i - 1);
+          double t2 = A2(a, lda, k, i);
+          A2(a, lda, k, i - 1) = t1 * cx + t2 * sx;
+          A2(a, lda, k, i) = -t1 * sx + t2 * cx;
+        }
+      }
+    }
+}
+
+static double givdr(int max_n, int n, double *a, double tol) {
+  givens_single(a, max_n, n, tol);
+  double d = 1.0;
+  for (int i = 1; i <= n; ++i) d *= A2(a, max_n, i, i);
+  return d;
+}
+
+/* check_spin_and_locate (valence.F90:2670-2714) */
+static void check_spin_and_locate(int sb, int sk, const int *ba, const int *bb, const int *ka, const int *kb, int nalpha,
+                                  int nbeta, int *lab, int *lak, int *lbb, int *lbk, int *both_a, int *both_b) {
+  int bra_is_a = 0, ket_is_a = 0, bra_is_b = 0, ket_is_b = 0;
+  for (int i = 1; i <= nalpha; ++i) {
+    if (sb == ba[i]) {
+      bra_is_a = 1;
+      *lab = i;
+    }
+    if (sk == ka[i]) {
+      ket_is_a = 1;
+      *lak = i;
+    }
+  }
+  for (int i = 1; i <= nbeta; ++i) {
+    if (sb == bb[i]) {
+      bra_is_b = 1;
+      *lbb = i;
+    }
+    if (sk == kb[i]) {
+      ket_is_b = 1;
+      *lbk = i;
+    }
+  }
+  *both_a = bra_is_a && ket_is_a;
+  *both_b = bra_is_b && ket_is_b;
+}
+
+/* build_abket (valence.F90:2524-2586) */
+static void build_abket(vo_ctx *cx, int dima, int dimb) {
+  vo_state *st = cx->st;
+  vo_input *in = st->in;
+  int npair = in->npair, ndocc = in->ndocc, nunpd = in->nunpd, ld = st->padded, ldu = st->ld_du;
+  if (npair > 0) {
+    for (int k = 1; k <= npair; ++k) {
+      for (int l = 1 + npair; l <= dima; ++l) A2(cx->aket, ld, l, k) = A2(st->abra_docc_un, ldu, l - npair, cx->ket_a[k]);
+      for (int l = 1 + npair; l <= dimb; ++l) A2(cx->bket, ld, l, k) = A2(st->bbra_docc_un, ldu, l - npair, cx->ket_b[k]);
+    }
+    for (int k = 1; k <= dima; ++k)
+      for (int l = 1; l <= npair; ++l) A2(cx->aket, ld, l, k) = A2(cx->abra_npair, npair, l, cx->ket_a[k]);
+    for (int k = 1; k <= dimb; ++k)
+      for (int l = 1; l <= npair; ++l) A2(cx->bket, ld, l, k) = A2(cx->bbra_npair, npair, l, cx->ket_b[k]);
+  }
+  for (int k = 1; k <= ndocc; ++k) {
+    for (int l = 1 + npair; l <= npair + ndocc; ++l) {
+      A2(cx->aket, ld, l, k + npair) = A2(st->aket_docc_un, ldu, l - npair, k);
+      A2(cx->bket, ld, l, k + npair) = A2(st->bket_docc_un, ldu, l - npair, k);
+    }
+    for (int l = 1 + npair + ndocc; l <= npair + nunpd + ndocc; ++l)
+      A2(cx->aket, ld, l, k + npair) = A2(st->aket_docc_un, ldu, l - npair, k);
+  }
+  for (int k = 1 + ndocc; k <= ndocc + nunpd; ++k)
+    for (int l = 1 + npair; l <= npair + ndocc + nunpd; ++l)
+      A2(cx->aket, ld, l, k + npair) = A2(st->aket_docc_un, ldu, l - npair, k);
+}
+
+/* det (valence.F90:1895-2056) */
+static void det(vo_ctx *cx, int dima, int dimb, int nord, double *dens, double *xdens, int calc_dens, int calc_x) {
+  vo_state *st = cx->st;
+  int nalpha = st->nalpha, nbeta = st->nbeta, ld = st->padded;
+  double dtol = st->in->dtol;
+  int erep_nz = 0, x_nz = 0;
+  double ad = 0.0, bd = 0.0;
+  int lab = 0, lak = 0, lbb = 0, lbk = 0, both_a = 0, both_b = 0;
+  if (calc_dens) {
+    for (int iord = 1; iord <= nord; ++iord) {
+      check_spin_and_locate(cx->dme_b[iord], cx->dme_k[iord], cx->bra_a, cx->bra_b, cx->ket_a, cx->ket_b, nalpha,
+                            nbeta, &lab, &lak, &lbb, &lbk, &both_a, &both_b);
+      if (both_a) {
+        for (int i = 1; i <= nalpha; ++i) {
+          A2(cx->aket, ld, lab, i) = 0.0;
+          A2(cx->aket, ld, i, lak) = 0.0;
+        }
+        A2(cx->aket, ld, lab, lak) = 1.0;
+      } else if (both_b) {
+        for (int i = 1; i <= nbeta; ++i) {
+          A2(cx->bket, ld, lbb, i) = 0.0;
+          A2(cx->bket, ld, i, lbk) = 0.0;
+        }
+        A2(cx->bket, ld, lbb, lbk) = 1.0;
+      } else {
+        break;
+      }
+    }
+    erep_nz = both_b || both_a;
+  }
+  int setup_erep = calc_dens && erep_nz;
+  if (calc_x) {
+    for (int iord = 1; iord <= nord; ++iord) {
+      check_spin_and_locate(cx->dme_b[iord], cx->dme_k[nord - iord + 1], cx->bra_a, cx->bra_b, cx->ket_a, cx->ket_b,
+                            nalpha, nbeta, &lab, &lak, &lbb, &lbk, &both_a, &both_b);
+      if (both_a) {
+        if (!setup_erep) {
+          for (int i = 1; i <= nalpha; ++i) {
+            A2(cx->aket, ld, lab, i) = 0.0;
+            A2(cx->aket, ld, i, lak) = 0.0;
+          }
+          A2(cx->aket, ld, lab, lak) = 1.0;
+        }
+      } else if (both_b) {
+        if (!setup_erep) {
+          for (int i = 1; i <= nbeta; ++i) {
+            A2(cx->bket, ld, lbb, i) = 0.0;
+            A2(cx->bket, ld, i, lbk) = 0.0;
+          }
+          A2(cx->bket, ld, lbb, lbk) = 1.0;
+        }
+      } else {
+        break;
+      }
+    }
+    x_nz = both_a || both_b;
+  }
+  int setup_x = calc_x && x_nz;
+  if (setup_erep || setup_x) {
+    if (dima == 0)
+      ad = 1.0;
+    else if (dima == 1)
+      ad = A2(cx->aket, ld, 1, 1);
+    else
+      ad = givdr(ld, nalpha, cx->aket, dtol);
+    if (dimb == 0)
+      bd = 1.0;
+    else if (dimb == 1)
+      bd = A2(cx->bket, ld, 1, 1);
+    else
+      bd = givdr(ld, nbeta, cx->bket, dtol);
+  }
+  if (setup_erep) *dens += ad * bd;
+  if (setup_x && !setup_erep) *xdens -= ad * bd;
+  if (setup_x && setup_erep) *xdens += ad * bd;
+}
+
+/* dket (valence.F90:1777-1870) */
+static void dket(vo_ctx *cx, int nord, int nexk, int dima, int dimb, double *dens, double *xdens, int jsc, int cd,
+                 int cx_) {
+  vo_input *in = cx->st->in;
+  int npair = in->npair;
+#define PSC(k, s, isc) in->pair_sc[((k)-1) + npair * ((s)-1 + 2 * ((isc)-1))]
+  for (int k = 1; k <= npair; ++k) {
+    cx->ket_a[k] = PSC(k, 1, jsc);
+    cx->ket_b[k] = PSC(k, 2, jsc);
+  }
+  build_abket(cx, dima, dimb);
+  det(cx, dima, dimb, nord, dens, xdens, cd, cx_);
+  for (int jo = 1; jo <= nexk; ++jo) {
+    for (int k = 1; k <= jo; ++k) cx->kexch[k] = k;
+    for (int k = 1; k <= npair; ++k) {
+      cx->ket_a[k] = PSC(k, 1, jsc);
+      cx->ket_b[k] = PSC(k, 2, jsc);
+    }
+    for (int k = 1; k <= jo; ++k) {
+      int t = cx->ket_a[k];
+      cx->ket_a[k] = cx->ket_b[k];
+      cx->ket_b[k] = t;
+    }
+    build_abket(cx, dima, dimb);
+    det(cx, dima, dimb, nord, dens, xdens, cd, cx_);
+    int j = jo;
+    while (cx->kexch[1] < 1 + nexk - jo) {
+      if (cx->kexch[j] < j + nexk - jo) {
+        cx->kexch[j]++;
+        for (int k = j + 1; k <= jo; ++k) cx->kexch[k] = cx->kexch[k - 1] + 1;
+        for (int k = 1; k <= npair; ++k) {
+          cx->ket_a[k] = PSC(k, 1, jsc);
+          cx->ket_b[k] = PSC(k, 2, jsc);
+        }
+        for (int k = 1; k <= jo; ++k) {
+          int l = cx->kexch[k];
+          int t = cx->ket_a[l];
+          cx->ket_a[l] = cx->ket_b[l];
+          cx->ket_b[l] = t;
+        }
+        build_abket(cx, dima, dimb);
+        det(cx, dima, dimb, nord, dens, xdens, cd, cx_);
+        j = jo;
+      } else {
+        j = j - 1;
+      }
+    }
+  }
+}
+
+static void load_bra_npair(vo_ctx *cx) {
+  vo_state *st = cx->st;
+  int npair = st->in->npair;
+  for (int l = 1; l <= st->nelec; ++l)
+    for (int k = 1; k <= npair; ++k) {
+      A2(cx->abra_npair, npair, k, l) = A2(st->wdet, st->nelec, cx->bra_a[k], l);
+      A2(cx->bbra_npair, npair, k, l) = A2(st->wdet, st->nelec, cx->bra_b[k], l);
+    }
+}
+
+/* dbra (valence.F90:1648-1761) */
+static void dbra(vo_ctx *cx, int nord, int nexb, int nexk, int dima, int dimb, double *dens, double *xdens, int isc,
+                 int jsc, int cd, int cx_) {
+  vo_input *in = cx->st->in;
+  int npair = in->npair;
+  for (int k = 1; k <= npair; ++k) {
+    cx->bra_a[k] = PSC(k, 1, isc);
+    cx->bra_b[k] = PSC(k, 2, isc);
+  }
+  load_bra_npair(cx);
+  dket(cx, nord, nexk, dima, dimb, dens, xdens, jsc, cd, cx_);
+  for (int io = 1; io <= nexb; ++io) {
+    for (int k = 1; k <= io; ++k) cx->bexch[k] = k;
+    for (int k = 1; k <= npair; ++k) {
+      cx->bra_a[k] = PSC(k, 1, isc);
+      cx->bra_b[k] = PSC(k, 2, isc);
+    }
+    for (int k = 1; k <= io; ++k) {
+      int t = cx->bra_a[k];
+      cx->bra_a[k] = cx->bra_b[k];
+      cx->bra_b[k] = t;
+    }
+    load_bra_npair(cx);
+    dket(cx, nord, nexk, dima, dimb, dens, xdens, jsc, cd, cx_);
+    int i = io;
+    while (cx->bexch[1] < 1 + nexb - io) {
+      if (cx->bexch[i] < i + nexb - io) {
+        cx->bexch[i]++;
+        for (int k = i + 1; k <= io; ++k) cx->bexch[k] = cx->bexch[k - 1] + 1;
+        for (int k = 1; k <= npair; ++k) {
+          cx->bra_a[k] = PSC(k, 1, isc);
+          cx->bra_b[k] = PSC(k, 2, isc);
+        }
+        for (int k = 1; k <= io; ++k) {
+          int l = cx->bexch[k];
+          int t = cx->bra_a[l];
+          cx->bra_a[l] = cx->bra_b[l];
+          cx->bra_b[l] = t;
+        }
+        load_bra_npair(cx);
+        dket(cx, nord, nexk, dima, dimb, dens, xdens, jsc, cd, cx_);
+        i = io;
+      } else {
+        i = i - 1;
+      }
+    }
+  }
+#undef PSC
+}
+
+/* density (valence.F90:1535-1600, spinopt = .false.) and density_sc
+ * (:1612-1633) */
+static void density(vo_ctx *cx, int nord, double *dens, double *xdens, int cd, int cx_) {
+  vo_input *in = cx->st->in;
+  int dima = in->npair + in->ndocc + in->nunpd, dimb = in->npair + in->ndocc;
+  if (in->nspinc > 0) {
+    *dens = 0.0;
+    *xdens = 0.0;
+    for (int isc = 1; isc <= in->nspinc; ++isc)
+      for (int jsc = 1; jsc <= in->nspinc; ++jsc) {
+        double d = 0.0, x = 0.0;
+        dbra(cx, nord, in->npair, in->npair, dima, dimb, &d, &x, isc, jsc, cd, cx_);
+        *dens += d * in->coeff_sc[isc - 1] * in->coeff_sc[jsc - 1];
+        *xdens += x * in->coeff_sc[isc - 1] * in->coeff_sc[jsc - 1];
+      }
+  } else {
+    *dens = 0.0;
+    *xdens = 0.0;
+    build_abket(cx, dima, dimb);
+    det(cx, dima, dimb, nord, dens, xdens, cd, cx_);
+  }
+}
+
+/* set_up_unpaired_docc (valence.F90:2444-2517): the per-context part */
+static void ctx_setup_lists(vo_ctx *cx) {
+  vo_input *in = cx->st->in;
+  int npair = in->npair, nunpd = in->nunpd, ndocc = in->ndocc;
+  int j = 2 * npair + 1;
+  for (int i = npair + 1; i <= npair + nunpd; ++i) {
+    cx->bra_a[i] = j;
+    cx->ket_a[i] = j;
+    j++;
+  }
+  j = 2 * npair + nunpd + 1;
+  for (int i = npair + nunpd + 1; i <= npair + nunpd + ndocc; ++i) {
+    cx->bra_a[i] = j;
+    cx->ket_a[i] = j;
+    j += 2;
+  }
+  j = 2 * npair + nunpd + 2;
+  for (int i = npair + 1; i <= npair + ndocc; ++i) {
+    cx->bra_b[i] = j;
+    cx->ket_b[i] = j;
+    j += 2;
+  }
+}
+
+static void state_setup_docc_un(vo_state *st, vo_ctx *cx) {
+  vo_input *in = st->in;
+  int npair = in->npair, dima = npair + in->ndocc + in->nunpd, dimb = npair + in->ndocc, ldu = st->ld_du;
+  for (int j = 1; j <= 2 * npair; ++j) {
+    for (int i = 1; i <= dima - npair; ++i)
+      A2(st->abra_docc_un, ldu, i, j) = A2(st->wdet, st->nelec, cx->bra_a[i + npair], j);
+    for (int i = 1; i <= dimb - npair; ++i)
+      A2(st->bbra_docc_un, ldu, i, j) = A2(st->wdet, st->nelec, cx->bra_b[i + npair], j);
+  }
+  for (int i = 1; i <= dima - npair; ++i)
+    for (int j = 1; j <= dima - npair; ++j)
+      A2(st->aket_docc_un, ldu, j, i) = A2(st->wdet, st->nelec, cx->bra_a[j + npair], cx->ket_a[i + npair]);
+  for (int i = 1; i <= dimb - npair; ++i)
+    for (int j = 1; j <= dimb - npair; ++j)
+      A2(st->bket_docc_un, ldu, j, i) = A2(st->wdet, st->nelec, cx->bra_b[j + npair], cx->ket_b[i + npair]);
+}
+
+static vo_ctx *ctx_new(vo_state *st) {
+  vo_ctx *cx = (vo_ctx *)calloc(1, sizeof(vo_ctx));
+  vo_input *in = st->in;
+  cx->st = st;
+  int na = st->nalpha + 2, nel = st->nelec + 2;
+  cx->bra_a = (int *)calloc(na, sizeof(int));
+  cx->bra_b = (int *)calloc(na, sizeof(int));
+  cx->ket_a = (int *)calloc(na, sizeof(int));
+  cx->ket_b = (int *)calloc(na, sizeof(int));
+  cx->bexch = (int *)calloc(in->npair + 2, sizeof(int));
+  cx->kexch = (int *)calloc(in->npair + 2, sizeof(int));
+  cx->abra_npair = (double *)calloc((size_t)(in->npair + 1) * nel, sizeof(double));
+  cx->bbra_npair = (double *)calloc((size_t)(in->npair + 1) * nel, sizeof(double));
+  cx->aket = (double *)calloc((size_t)(st->padded + 1) * na, sizeof(double));
+  cx->bket = (double *)calloc((size_t)(st->padded + 1) * na, sizeof(double));
+  cx->ci = (double *)calloc(st->max_obs + 2, sizeof(double));
+  cx->cj = (double *)calloc(st->max_obs + 2, sizeof(double));
+  cx->ck = (double *)calloc(st->max_obs + 2, sizeof(double));
+  cx->cl = (double *)calloc(st->max_obs + 2, sizeof(double));
+  cx->xpnew = (int *)calloc(in->xpmax + 2 + in->totlen, sizeof(int));
+  cx->atom_ndf = (int *)calloc(2 * (size_t)(in->mxctr + 1), sizeof(int));
+  cx->ndf2orb = (int *)calloc(in->mxctr + 2, sizeof(int));
+  cx->blk = (double *)malloc(sizeof(double) * 10000 * 2);
+  ctx_setup_lists(cx);
+  return cx;
+}
+
+static void ctx_free(vo_ctx *cx) {
+  if (!cx) return;
+  free(cx->bra_a);
+  free(cx->bra_b);
+  free(cx->ket_a);
+  free(cx->ket_b);
+  free(cx->bexch);
+  free(cx->kexch);
+  free(cx->abra_npair);
+  free(cx->bbra_npair);
+  free(cx->aket);
+  free(cx->bket);
+  free(cx->ci);
+  free(cx->cj);
+  free(cx->ck);
+  free(cx->cl);
+  free(cx->xpnew);
+  free(cx->atom_ndf);
+  free(cx->ndf2orb);
+  free(cx->blk);
+  free(cx);
+}
+
+/* ------------------------------------------------------------------ */
+
+static void xm_dtriang(long long ij, int *i, int *j) {
+  long long ii = (long long)sqrt((double)(2 * ij));
+  long long k = (ii * ii + ii) / 2;
+  while (k < ij) {
+    ii++;
+    k = (ii * ii + ii) / 2;
+  }
+  *i = (int)ii;
+  *j = (int)(ij - (ii * ii - ii) / 2);
+}
+
+static int indx(int i, int j) {
+  int ix = i > j ? i : j;
+  int mn = i < j ? i : j;
+  return (ix * ix - ix) / 2 + mn;
+}
+
+static vo_state *g_last_state = NULL; /* kept for vo_int2e/vo_ovint after an energy */
+
+static void state_free(vo_state *st) {
+  if (!st) return;
+  free(st->bra);
+  free(st->ket);
+  free(st->wdet);
+  free(st->schwarz);
+  free(st->abra_docc_un);
+  free(st->bbra_docc_un);
+  free(st->aket_docc_un);
+  free(st->bket_docc_un);
+  free(st->gsh);
+  free(st->gfirst);
+  if (st->eri_cache) {
+    for (size_t i = 0; i < st->ncanon; ++i) free(st->eri_cache[i]);
+    free(st->eri_cache);
+  }
+  free(st);
+}
+
+/* calculate_vsvb_energy set-up (valence.F90:70-182) */
+static vo_state *state_new(vo_input *in) {
+  vo_state *st = (vo_state *)calloc(1, sizeof(vo_state));
+  st->in = in;
+  for (int i = 1; i <= in->natom_t; ++i) {
+    int mnshi = in->map_atom2shell[i - 1], mxshi = mnshi + in->num_shell_atom[i - 1] - 1;
+    for (int j = mnshi; j <= mxshi; ++j) {
+      int k = in->map_shell2prim[j - 1];
+      norm_prim(in->ang_mom[j - 1], in->map_shell2prim[j] - k, &in->exponent[k - 1], &in->con_coeff[k - 1],
+                &in->uncoef[k - 1]);
+    }
+  }
+  setangn(st, in->nang > 3 ? in->nang : 3);
+  /* global shells */
+  st->gfirst = (int *)calloc(in->natom + 2, sizeof(int));
+  int ng = 0;
+  for (int a = 1; a <= in->natom; ++a) {
+    st->gfirst[a] = ng;
+    ng += in->num_shell_atom[in->atom_t[a - 1] - 1];
+  }
+  st->ngsh = ng;
+  st->gsh = (vo_shell *)calloc(ng + 1, sizeof(vo_shell));
+  for (int a = 1; a <= in->natom; ++a) {
+    int it = in->atom_t[a - 1];
+    int mnshi = in->map_atom2shell[it - 1];
+    for (int s = 0; s < in->num_shell_atom[it - 1]; ++s) {
+      int sh = mnshi + s;
+      vo_shell *g = &st->gsh[st->gfirst[a] + s];
+      g->l = in->ang_mom[sh - 1];
+      int k = in->map_shell2prim[sh - 1];
+      g->nprim = in->map_shell2prim[sh] - k;
+      g->alpha = &in->exponent[k - 1];
+      g->coef = &in->con_coeff[k - 1];
+      for (int d = 0; d < 3; ++d) g->xyz[d] = in->coords[3 * (a - 1) + d];
+    }
+  }
+  size_t np = tri((size_t)ng);
+  st->ncanon = tri(np);
+  st->eri_cache = (double **)calloc(st->ncanon + 1, sizeof(double *));
+  /* max OBS size (:118-130) */
+  st->max_obs = 0;
+  for (int i = 1; i <= in->norbs; ++i) {
+    int n = 0;
+    for (int j = 1; j <= in->orbas_atnum[i - 1]; ++j) {
+      int it = in->atom_t[in->orbas_atset[(j - 1) + in->mxctr * (i - 1)] - 1];
+      int mnshi = in->map_atom2shell[it - 1], mxshi = mnshi + in->num_shell_atom[it - 1] - 1;
+      for (int k = mnshi; k <= mxshi; ++k) n += shell_size(in->ang_mom[k - 1]);
+    }
+    if (n > st->max_obs) st->max_obs = n;
+  }
+  st->nelec = 2 * in->npair + 2 * in->ndocc + in->nunpd;
+  st->nalpha = in->npair + in->nunpd + in->ndocc;
+  st->nbeta = in->npair + in->ndocc;
+  st->padded = st->nalpha > 0 ? st->nalpha : 1;
+  st->nnd = 2 * in->npair + in->nunpd;
+  st->nsp = st->nnd + in->ndocc;
+  st->bra = (int *)calloc(st->nelec + 2, sizeof(int));
+  st->ket = (int *)calloc(st->nelec + 2, sizeof(int));
+  st->wdet = (double *)calloc((size_t)st->nelec * st->nelec + 1, sizeof(double));
+  st->ld_du = in->ndocc + in->nunpd > 0 ? in->ndocc + in->nunpd : 1;
+  st->abra_docc_un = (double *)calloc((size_t)st->ld_du * (2 * in->npair + 1), sizeof(double));
+  st->bbra_docc_un = (double *)calloc((size_t)st->ld_du * (2 * in->npair + 1), sizeof(double));
+  st->aket_docc_un = (double *)calloc((size_t)st->ld_du * st->ld_du, sizeof(double));
+  st->bket_docc_un = (double *)calloc((size_t)st->ld_du * st->ld_du, sizeof(double));
+  int norbz = st->nsp + 1;
+  st->schwarz = (double *)calloc((size_t)(norbz * norbz + norbz) / 2 + 1, sizeof(double));
+  return st;
+}
+
+int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
+  memset(res, 0, sizeof(*res));
+  if (g_last_state) {
+    state_free(g_last_state);
+    g_last_state = NULL;
+  }
+  memcpy(in->coeff, in->coeff_raw, sizeof(double) * in->totlen);
+  vo_state *st = state_new(in);
+  /* nuclear repulsion (tools_module.F90:19-40) */
+  double nre = 0.0;
+  for (int i = 2; i <= in->natom; ++i)
+    for (int j = 1; j <= i - 1; ++j) {
+      double zij = in->nuc_charge[in->atom_t[i - 1] - 1] * in->nuc_charge[in->atom_t[j - 1] - 1];
+      if (fabs(zij) > 1e-12) {
+        double rsq = 0.0;
+        for (int d = 0; d < 3; ++d) {
+          double x = in->coords[3 * (i - 1) + d] - in->coords[3 * (j - 1) + d];
+          rsq += x * x;
+        }
+        if (rsq > 1e-5) nre += zij * pow(rsq, -0.5);
+      }
+    }
+  res->enucrep = nre;
+  vo_ctx *c0 = ctx_new(st);
+  /* normal(): NDFs first, then the orbitals (valence.F90:144-145, 2157-2182) */
+  int nfirst = 2 * in->npair + in->nunpd + in->ndocc + 1;
+  for (int i = nfirst; i <= in->norbs; ++i) {
+    ovint(c0, i, i);
+    double s = pow(c0->sint, -0.5);
+    for (int j = in->map_orbs[i - 1]; j <= in->map_orbs[i] - 1; ++j) in->coeff[j - 1] *= s;
+  }
+  for (int i = 1; i <= in->norbs - in->ndf; ++i) {
+    ovint(c0, i, i);
+    double s = pow(c0->sint, -0.5);
+    for (int j = in->map_orbs[i - 1]; j <= in->map_orbs[i] - 1; ++j) in->coeff[j - 1] *= s;
+  }
+  /* guess_energy bra/ket (valence.F90:324-336) */
+  int nnd = st->nnd;
+  for (int i = 1; i <= nnd; ++i) {
+    st->bra[i] = i;
+    st->ket[i] = i;
+  }
+  {
+    int i = nnd + 1;
+    for (int idocc = nnd + 1; idocc <= nnd + in->ndocc; ++idocc) {
+      st->bra[i] = idocc;
+      st->ket[i] = idocc;
+      st->bra[i + 1] = idocc;
+      st->ket[i + 1] = idocc;
+      i += 2;
+    }
+  }
+  int nelec = st->nelec;
+  /* wfndet (valence.F90:1440-1480) */
+  for (int i = 1; i <= nelec; ++i)
+    for (int j = 1; j <= i; ++j) {
+      ovint(c0, st->bra[i], st->ket[j]);
+      A2(st->wdet, nelec, i, j) = c0->sint;
+      A2(st->wdet, nelec, j, i) = c0->sint;
+    }
+  /* schwarz_ints (valence.F90:1489-1523) */
+  int nsp = st->nsp;
+  for (int i = 1; i <= nsp; ++i)
+    for (int j = 1; j <= i; ++j) {
+      int ie = i > nnd ? 2 * i - nnd : i;
+      int je = j > nnd ? 2 * j - nnd : j;
+      int2e(c0, st->bra[ie], st->ket[je], st->bra[ie], st->ket[je]);
+      st->schwarz[indx(i, j)] = sqrt(c0->gint);
+    }
+  /* vsvb_energy (valence.F90:1010-1434), iorb=0, spinav=.false.,
+   * ijkl symmetry enabled */
+  state_setup_docc_un(st, c0);
+  double energy = 0.0, wfnorm = 0.0;
+  for (int i = 1; i <= nelec; ++i) {
+    int i_docc = i > nnd;
+    for (int j = 1; j <= nelec; ++j) {
+      int j_docc = j > nnd;
+      if (i_docc && j_docc && (i % 2) != (j % 2)) continue;
+      ovint(c0, st->bra[i], st->ket[j]);
+      int1e(c0, st->bra[i], st->ket[j]);
+      c0->dme_b[1] = i;
+      c0->dme_k[1] = j;
+      double d1 = 0.0, dummy = 0.0;
+      density(c0, 1, &d1, &dummy, 1, 0);
+      wfnorm += c0->sint * d1;
+      energy += c0->hint * d1;
+    }
+  }
+  wfnorm /= (double)nelec;
+  res->e1 = energy;
+  long long ntij = ((long long)nsp * nsp + nsp) / 2;
+  long long ntasks = (ntij * ntij + ntij) / 2;
+  res->ntasks = ntasks;
+  double itol = in->itol;
+  int nth = 1;
+#ifdef _OPENMP
+  nth = nthreads > 0 ? nthreads : omp_get_max_threads();
+#endif
+  double *part = (double *)calloc(nth, sizeof(double));
+  long long *pcount = (long long *)calloc(nth, sizeof(long long));
+#pragma omp parallel num_threads(nth)
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    vo_ctx *cx = ctx_new(st);
+    double esum = 0.0;
+#pragma omp for schedule(dynamic, 16)
+    for (long long task = 0; task < ntasks; ++task) {
+      int ijorb, klorb, io, jo, ko, lo;
+      xm_dtriang(1 + task, &ijorb, &klorb);
+      xm_dtriang(ijorb, &io, &jo);
+      xm_dtriang(klorb, &ko, &lo);
+      if ((io == jo && io <= nnd) || (ko == lo && ko <= nnd)) continue;
+      int erep_sig = st->schwarz[indx(io, ko)] * st->schwarz[indx(jo, lo)] > itol;
+      int x_sig = st->schwarz[indx(io, lo)] * st->schwarz[indx(jo, ko)] > itol;
+      double xint = 0.0, eint = 0.0;
+      if (erep_sig || x_sig) {
+        if (io == jo && ko == lo) {
+          eint = st->schwarz[indx(io, ko)] * st->schwarz[indx(io, ko)];
+          xint = eint;
+        } else {
+          int ie = io > nnd ? 2 * io - nnd - 1 : io;
+          int je = jo > nnd ? 2 * jo - nnd - 1 : jo;
+          int ke = ko > nnd ? 2 * ko - nnd - 1 : ko;
+          int le = lo > nnd ? 2 * lo - nnd - 1 : lo;
+          if (erep_sig) {
+            int2e(cx, st->bra[ie], st->ket[ke], st->bra[je], st->ket[le]);
+            eint = cx->gint;
+          }
+          if (x_sig) {
+            if (erep_sig && st->ket[le] == st->ket[ke]) {
+              xint = cx->gint;
+            } else {
+              int2e(cx, st->bra[ie], st->ket[le], st->bra[je], st->ket[ke]);
+              xint = cx->gint;
+            }
+          }
+        }
+      }
+      erep_sig = fabs(eint) > itol;
+      x_sig = fabs(xint) > itol;
+      double esum_t = 0.0, xsum_t = 0.0;
+      if (erep_sig || x_sig) {
+        int id = io > nnd, jd = jo > nnd, kd = ko > nnd, ld = lo > nnd;
+        int iso = id ? 2 : 1, jso = jd ? 2 : 1, kso = kd ? 2 : 1, lso = ld ? 2 : 1;
+        for (int is = 1; is <= iso; ++is) {
+          int i = id ? 2 * io - nnd + is - 2 : io;
+          for (int js = 1; js <= jso; ++js) {
+            int j = jd ? 2 * jo - nnd + js - 2 : jo;
+            if (!(j < i)) continue;
+            for (int ks = 1; ks <= kso; ++ks) {
+              int k = kd ? 2 * ko - nnd + ks - 2 : ko;
+              for (int ls = 1; ls <= lso; ++ls) {
+                int l = ld ? 2 * lo - nnd + ls - 2 : lo;
+                if (!(l < k)) continue;
+                int ik0 = id && kd && (i % 2) != (k % 2);
+                int jl0 = jd && ld && (j % 2) != (l % 2);
+                int ce = !(ik0 || jl0);
+                int il0 = id && ld && (i % 2) != (l % 2);
+                int jk0 = jd && kd && (j % 2) != (k % 2);
+                int cxx = !(il0 || jk0);
+                if ((ce && erep_sig) || (cxx && x_sig)) {
+                  cx->dme_b[1] = i;
+                  cx->dme_k[1] = k;
+                  cx->dme_b[2] = j;
+                  cx->dme_k[2] = l;
+                  double dd = 0.0, xd = 0.0;
+                  density(cx, 2, &dd, &xd, erep_sig, x_sig);
+                  cx->ndens2++;
+                  if (erep_sig) esum_t += dd * eint;
+                  if (x_sig) xsum_t += xd * xint;
+                }
+              }
+            }
+          }
+        }
+      }
+      if (!(ko == io && lo == jo)) {
+        esum_t *= 2.0;
+        xsum_t *= 2.0;
+      }
+      esum += esum_t - xsum_t;
+    }
+    part[tid] = esum;
+    pcount[tid] = cx->ndens2;
+    ctx_free(cx);
+  }
+  double e2 = 0.0;
+  for (int t = 0; t < nth; ++t) {
+    e2 += part[t];
+    res->ndens2 += pcount[t];
+  }
+  free(part);
+  free(pcount);
+  energy += e2;
+  res->e2 = e2;
+  res->wfnorm = wfnorm;
+  /* guess_energy tail (valence.F90:342-344) */
+  res->energy = energy / wfnorm + nre;
+  ctx_free(c0);
+  g_last_state = st;
+  return 0;
+}
+
+/* helpers for tests: orbital integrals with the normalised weights left by
+ * the last vo_guess_energy on this input */
+static vo_state *state_for(vo_input *in) {
+  if (g_last_state && g_last_state->in == in) return g_last_state;
+  return NULL;
+}
+
+double vo_int2e(vo_input *in, int io, int ko, int jo, int lo) {
+  vo_state *st = state_for(in);
+  if (!st) return NAN;
+  vo_ctx *cx = ctx_new(st);
+  int2e(cx, io, ko, jo, lo);
+  double g = cx->gint;
+  ctx_free(cx);
+  return g;
+}
+
+double vo_ovint(vo_input *in, int io, int jo) {
+  vo_state *st = state_for(in);
+  if (!st) return NAN;
+  vo_ctx *cx = ctx_new(st);
+  ovint(cx, io, jo);
+  double g = cx->sint;
+  ctx_free(cx);
+  return g;
+}
+
+double vo_int1e(vo_input *in, int io, int jo) {
+  vo_state *st = state_for(in);
+  if (!st) return NAN;
+  vo_ctx *cx = ctx_new(st);
+  int1e(cx, io, jo);
+  double g = cx->hint;
+  ctx_free(cx);
+  return g;
+}
+
+int vo_num_global_shells(vo_input *in) {
+  vo_state *st = state_for(in);
+  return st ? st->ngsh : -1;
+}
+
+void vo_global_shell(vo_input *in, int g, int *atom, int *shell) {
+  vo_state *st = state_for(in);
+  *atom = -1;
+  *shell = -1;
+  if (!st) return;
+  for (int a = 1; a <= in->natom; ++a) {
+    int n = in->num_shell_atom[in->atom_t[a - 1] - 1];
+    if (g >= st->gfirst[a] && g < st->gfirst[a] + n) {
+      *atom = a;
+      *shell = g - st->gfirst[a];
+    }
+  }
+}
+
+void vo_ao_eri_block(vo_input *in, int ga, int gb, int gc, int gd, double *out) {
+  vo_state *st = state_for(in);
+  if (!st) return;
+  eri_block(st, ga, gb, gc, gd, out);
+}
