@@ -1,0 +1,162 @@
+/*
+ * vsvb_gpu.h -- C ABI of the GB300 (sm_103a) VSVB energy hot path.
+ *
+ * Drop-in boundary.  In VALENCE (VALENCE-software/VALENCE) the guess energy
+ * is
+ *     call wfndet                                           valence.F90:337
+ *     call schwarz_ints( num_spatial_orbs, num_non_docc )   valence.F90:339
+ *     call vsvb_energy( 0, num_non_docc, num_spatial_orbs,  valence.F90:341
+ *                       energy, wfnorm, .false., .true. )
+ *     call xm_equalize_scalar( energy/wfnorm )              valence.F90:342-343
+ *     energy = energy/wfnorm + enucrep                      valence.F90:344
+ * with the integrals from simint (int2e valence.F90:3184-3438, int1e
+ * :3022-3176, ovint :2891-3012) and the cofactor densities from density ..
+ * det .. givens_single (valence.F90:1535-2144, givens.F90:230-262).
+ * vsvb_gpu_energy replaces that whole block: one call computes the orbital
+ * normalisation (normal, valence.F90:2157-2182), the overlap/one-electron
+ * orbital integrals, the Schwarz table, every screened orbital-quartet ERI and
+ * its contraction with the spin-coupled cofactor densities, and returns the
+ * same energy/wfnorm pair.  The Fortran side binds these entry points with
+ * ISO_C_BINDING; nothing here takes a torch type.
+ *
+ * Conventions: all arrays are plain host pointers unless a name ends in
+ * _dev.  Index arrays keep the reference's 1-based Fortran values exactly as
+ * the module arrays hold them (integrals_module.F90:27-63,
+ * density_module.F90:8-9).  Every entry point returns a vsvb_status; none
+ * aborts, exits or traps.  A handle is not thread-safe; use one per host
+ * thread.  The GPU path ignores MPI rank/size: run it on one rank only (the
+ * reference's round-robin split, valence.F90:1158-1163, would otherwise be
+ * summed twice by xm_equalize).
+ */
+#ifndef VSVB_GPU_H
+#define VSVB_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum vsvb_status {
+  VSVB_OK = 0,
+  VSVB_ERR_INPUT = 1,       /* malformed input / inconsistent dimensions */
+  VSVB_ERR_UNSUPPORTED = 2, /* e.g. angular momentum above d on the GPU */
+  VSVB_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  VSVB_ERR_SINGULAR = 4,    /* gradient requested through a singular determinant pair */
+  VSVB_ERR_NOMEM = 5,
+  VSVB_ERR_TIMEOUT = 6,     /* a bounded device-side wait gave up */
+  VSVB_ERR_NOT_NORMALISABLE = 7 /* an orbital has non-positive self-overlap */
+} vsvb_status;
+
+/* Precision modes of the ERI contraction. */
+typedef enum vsvb_precision {
+  VSVB_FP64 = 0,  /* every shell quartet in FP64 */
+  VSVB_MIXED = 1  /* quartets whose Schwarz bound is below mixed_threshold in FP32 */
+} vsvb_precision;
+
+/*
+ * System description: the reference's module arrays, borrowed for the
+ * duration of vsvb_gpu_create.  Mirrors xm_getdims/xm_input
+ * (xm_module.F90:25-335): the 15 dimension integers of input line A, the
+ * density/integral tolerance exponents of line B, the geometry (bohr), the
+ * basis per atom type, the spin couplings and the orbital expansions.
+ */
+typedef struct vsvb_system_desc {
+  int natom, natom_t, npair, nunpd, ndocc, totlen, xpmax, nspinc;
+  int num_sh, num_pr, nang, ndf, nxorb, mxctr;
+  int ntol_d, ntol_i;             /* dtol = 10^-ntol_d, itol = 10^-ntol_i */
+  const int *atom_t;              /* [natom], 1-based type */
+  const double *coords;           /* [3*natom], bohr, coords(1:3, i) */
+  const double *nuc_charge;       /* [natom_t] */
+  const int *map_atom2shell;      /* [natom_t], 1-based */
+  const int *num_shell_atom;      /* [natom_t] */
+  const int *map_shell2prim;      /* [num_sh+1], 1-based */
+  const int *ang_mom;             /* [num_sh] */
+  const double *exponent;         /* [num_pr] */
+  const double *con_coeff;        /* [num_pr], as read (before norm_prim) */
+  const int *pair_sc;             /* [npair*2*max(nspinc,1)], pair_sc(k,s,isc) column-major */
+  const double *coeff_sc;         /* [max(nspinc,1)] */
+  const int *orbas_atnum;         /* [norbs] */
+  const int *orbas_atset;         /* [mxctr*norbs], orbas_atset(k,i) column-major */
+  const int *map_orbs;            /* [norbs+1], 1-based */
+  const int *xpset;               /* [totlen] */
+  const double *coeff;            /* [totlen] raw orbital weights */
+} vsvb_system_desc;
+
+typedef struct vsvb_options {
+  int precision;          /* vsvb_precision */
+  double mixed_threshold; /* Schwarz bound below which a quartet runs in FP32 (default 1e-6) */
+  double ao_screen;       /* AO shell-quartet Schwarz screen (default 1e-15) */
+  int device;             /* CUDA device ordinal (default 0) */
+} vsvb_options;
+
+typedef struct vsvb_energy_result {
+  double energy;   /* e_num/wfnorm + enucrep (valence.F90:344) */
+  double e_num;    /* one- plus two-electron numerator */
+  double e1, e2;   /* its parts */
+  double wfnorm;   /* valence.F90:1106 */
+  double enucrep;  /* tools_module.F90:19-40 */
+  double err_est;  /* mixed path: bound on |E_mixed - E_fp64| from the FP32 quartets; 0 on FP64 */
+  long long n_quartets_fp64, n_quartets_fp32; /* AO shell quartets evaluated */
+  long long n_tasks;                           /* orbital-quartet tasks (valence.F90:1153-1157) */
+  int n_singular_pairs;                        /* determinant pairs on the exact-minor path */
+} vsvb_energy_result;
+
+typedef struct vsvb_gpu vsvb_gpu;
+
+void vsvb_default_options(vsvb_options *opt);
+
+/* Parse a VALENCE input file (xm_module.F90:25-335 record semantics) into a
+ * description that owns its arrays; free it with vsvb_free_desc.  Coordinates
+ * are converted to bohr (tools_module.F90:6-17). */
+int vsvb_read_input(const char *path, vsvb_system_desc **desc, char *err, int errlen);
+void vsvb_free_desc(vsvb_system_desc *desc);
+
+/* Build a handle: normalises primitives (norm_prim, valence.F90:2264-2305),
+ * builds the shell-pair tables, AO one-electron matrices, Schwarz bounds and
+ * quartet schedules on the GPU.  Replaces the set-up half of
+ * calculate_vsvb_energy (valence.F90:70-182). */
+int vsvb_gpu_create(const vsvb_system_desc *desc, const vsvb_options *opt, vsvb_gpu **out);
+void vsvb_gpu_destroy(vsvb_gpu *h);
+const char *vsvb_gpu_last_error(const vsvb_gpu *h);
+
+/* Guess energy for the given raw orbital weights (coeff, totlen host doubles;
+ * NULL = the weights given at create).  Replaces valence.F90:337-344. */
+int vsvb_gpu_energy(vsvb_gpu *h, const double *coeff, vsvb_energy_result *out);
+
+/* Energy and its gradient with respect to the raw weights
+ * (grad[totlen], host).  No counterpart exists in the reference, whose
+ * optimiser (first_order_opt, valence.F90:527-844) diagonalises per-orbital
+ * H/S matrices instead; this is the adjoint that a gradient optimiser
+ * consumes.  The backward pass recomputes the ERIs. */
+int vsvb_gpu_energy_grad(vsvb_gpu *h, const double *coeff, vsvb_energy_result *out, double *grad);
+
+/* Same two calls with the weights/gradient already in device memory
+ * (coeff_dev, grad_dev: totlen doubles on this handle's device); they enqueue
+ * on the handle's stream and synchronise before returning. */
+int vsvb_gpu_energy_device(vsvb_gpu *h, const double *coeff_dev, vsvb_energy_result *out);
+int vsvb_gpu_energy_grad_device(vsvb_gpu *h, const double *coeff_dev, vsvb_energy_result *out, double *grad_dev);
+
+/* Batched energies+gradients of independent molecules (one handle each) in
+ * one call: all handles must live on the same device.  weights[i] / grads[i]
+ * are host arrays of handle i's totlen (grads may be NULL for energy only). */
+int vsvb_gpu_batch_energy_grad(vsvb_gpu *const *handles, int n, const double *const *weights,
+                               vsvb_energy_result *results, double *const *grads);
+
+/* Sizes of a handle (for bindings). */
+int vsvb_gpu_totlen(const vsvb_gpu *h);
+int vsvb_gpu_num_orbitals(const vsvb_gpu *h);
+
+/* Diagnostics used by the parity tests: copy the orbital-pair ERI matrix
+ * T[p*np+q] = (i k | j l) for pairs p=(i,k), q=(j,l) (0-based, i>=k,
+ * index i*(i+1)/2+k) of the last evaluation, np = n(n+1)/2, n = spatial
+ * orbitals.  Returns np, or a negative vsvb_status. */
+int vsvb_gpu_debug_orbital_eri(vsvb_gpu *h, double *out, size_t cap);
+/* Orbital overlap and core-Hamiltonian matrices of the last evaluation
+ * (n x n, row-major). */
+int vsvb_gpu_debug_orbital_1e(vsvb_gpu *h, double *s, double *hcore, size_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,12 @@
+"""GB300 (sm_103a) implementation of VALENCE's VSVB energy hot path.
+
+The compute lives in libvsvb_gb300.so (C ABI, include/vsvb_gpu.h); this
+package is the thin Python host mirroring the reference's API
+(valence_api.F90: initialize / calculate_energy / finalize) plus a
+torch.autograd.Function for the weight gradient.
+"""
+from .api import (VSVBError, System, Options, FP64, MIXED, valence_api_initialize,
+                  valence_api_calculate_energy, valence_api_finalize, VSVBEnergy, library_path)
+
+__all__ = ["VSVBError", "System", "Options", "FP64", "MIXED", "valence_api_initialize",
+           "valence_api_calculate_energy", "valence_api_finalize", "VSVBEnergy", "library_path"]

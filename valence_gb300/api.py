@@ -1,0 +1,276 @@
+"""Python host for libvsvb_gb300.so.
+
+Mirrors VALENCE's library API (src/valence_api.F90):
+    valence_api_initialize(info, call_mpi_init, comm)   valence_api.F90:9-35
+    valence_api_calculate_energy(x, v)                  valence_api.F90:37-108
+    valence_api_finalize(call_mpi_finalize)             valence_api.F90:114-134
+with the same meaning: initialise from an input file, then energies for
+Cartesian coordinates x (Angstrom, 3*natom) in hartree.  The reference reads
+the input file named by argv(1) (valence_initialize_module.F90:49-53); here the
+path is an argument.  Errors raise VSVBError (the reference stops through
+xm_abort).  There is no CPU path: without the built library every entry point
+raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+FP64 = 0
+MIXED = 1
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def library_path():
+    return os.path.join(_HERE, "_build", "libvsvb_gb300.so")
+
+
+class VSVBError(RuntimeError):
+    pass
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("natom", "natom_t", "npair", "nunpd", "ndocc", "totlen", "xpmax",
+                                             "nspinc", "num_sh", "num_pr", "nang", "ndf", "nxorb", "mxctr",
+                                             "ntol_d", "ntol_i")] + [
+        ("atom_t", ctypes.POINTER(ctypes.c_int)), ("coords", ctypes.POINTER(ctypes.c_double)),
+        ("nuc_charge", ctypes.POINTER(ctypes.c_double)), ("map_atom2shell", ctypes.POINTER(ctypes.c_int)),
+        ("num_shell_atom", ctypes.POINTER(ctypes.c_int)), ("map_shell2prim", ctypes.POINTER(ctypes.c_int)),
+        ("ang_mom", ctypes.POINTER(ctypes.c_int)), ("exponent", ctypes.POINTER(ctypes.c_double)),
+        ("con_coeff", ctypes.POINTER(ctypes.c_double)), ("pair_sc", ctypes.POINTER(ctypes.c_int)),
+        ("coeff_sc", ctypes.POINTER(ctypes.c_double)), ("orbas_atnum", ctypes.POINTER(ctypes.c_int)),
+        ("orbas_atset", ctypes.POINTER(ctypes.c_int)), ("map_orbs", ctypes.POINTER(ctypes.c_int)),
+        ("xpset", ctypes.POINTER(ctypes.c_int)), ("coeff", ctypes.POINTER(ctypes.c_double))]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("mixed_threshold", ctypes.c_double), ("ao_screen", ctypes.c_double),
+                ("device", ctypes.c_int)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("energy", ctypes.c_double), ("e_num", ctypes.c_double), ("e1", ctypes.c_double),
+                ("e2", ctypes.c_double), ("wfnorm", ctypes.c_double), ("enucrep", ctypes.c_double),
+                ("err_est", ctypes.c_double), ("n_quartets_fp64", ctypes.c_longlong),
+                ("n_quartets_fp32", ctypes.c_longlong), ("n_tasks", ctypes.c_longlong),
+                ("n_singular_pairs", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        p = library_path()
+        if not os.path.exists(p):
+            raise VSVBError("libvsvb_gb300.so is not built (run __graft_entry__.build())")
+        L = ctypes.CDLL(p)
+        P, D, I = ctypes.POINTER, ctypes.c_double, ctypes.c_int
+        L.vsvb_read_input.argtypes = [ctypes.c_char_p, P(P(Desc)), ctypes.c_char_p, I]
+        L.vsvb_free_desc.argtypes = [P(Desc)]
+        L.vsvb_default_options.argtypes = [P(Options)]
+        L.vsvb_gpu_create.argtypes = [P(Desc), P(Options), P(ctypes.c_void_p)]
+        L.vsvb_gpu_destroy.argtypes = [ctypes.c_void_p]
+        L.vsvb_gpu_last_error.argtypes = [ctypes.c_void_p]
+        L.vsvb_gpu_last_error.restype = ctypes.c_char_p
+        L.vsvb_gpu_energy.argtypes = [ctypes.c_void_p, P(D), P(Result)]
+        L.vsvb_gpu_energy_grad.argtypes = [ctypes.c_void_p, P(D), P(Result), P(D)]
+        L.vsvb_gpu_energy_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, P(Result)]
+        L.vsvb_gpu_energy_grad_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, P(Result), ctypes.c_void_p]
+        L.vsvb_gpu_totlen.argtypes = [ctypes.c_void_p]
+        L.vsvb_gpu_num_orbitals.argtypes = [ctypes.c_void_p]
+        L.vsvb_gpu_debug_orbital_eri.argtypes = [ctypes.c_void_p, P(D), ctypes.c_size_t]
+        L.vsvb_gpu_debug_orbital_1e.argtypes = [ctypes.c_void_p, P(D), P(D), ctypes.c_size_t]
+        L.vsvb_gpu_batch_energy_grad.argtypes = [P(ctypes.c_void_p), I, P(P(D)), P(Result), P(P(D))]
+        _LIB = L
+    return _LIB
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def read_input(path):
+    """Parse a VALENCE input file into a description owned by the library."""
+    d = ctypes.POINTER(Desc)()
+    err = ctypes.create_string_buffer(256)
+    rc = lib().vsvb_read_input(os.fsencode(path), ctypes.byref(d), err, 256)
+    if rc:
+        raise VSVBError(f"input error ({rc}): {err.value.decode()}")
+    return d
+
+
+def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0):
+    o = Options()
+    lib().vsvb_default_options(ctypes.byref(o))
+    o.precision = precision
+    o.mixed_threshold = mixed_threshold
+    o.ao_screen = ao_screen
+    o.device = device
+    return o
+
+
+class System:
+    """One molecule on the GPU: a parsed input plus a device handle."""
+
+    def __init__(self, path, precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, coords_angstrom=None):
+        self.path = path
+        self._desc = read_input(path)
+        d = self._desc.contents
+        self.natom = d.natom
+        self.totlen = d.totlen
+        self.coeff0 = np.ctypeslib.as_array(d.coeff, shape=(d.totlen,)).copy()
+        self._coords_bohr = np.ctypeslib.as_array(d.coords, shape=(3 * d.natom,))
+        if coords_angstrom is not None:
+            self._coords_bohr[:] = np.asarray(coords_angstrom, dtype=np.float64).ravel() * 1.889725987722
+        self.opt = make_options(precision, mixed_threshold, ao_screen, device)
+        self._h = ctypes.c_void_p()
+        rc = lib().vsvb_gpu_create(self._desc, ctypes.byref(self.opt), ctypes.byref(self._h))
+        if rc:
+            msg = lib().vsvb_gpu_last_error(self._h).decode() if self._h else ""
+            self.close()
+            raise VSVBError(f"vsvb_gpu_create failed ({rc}): {msg}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().vsvb_gpu_destroy(self._h)
+            self._h = None
+        if getattr(self, "_desc", None):
+            lib().vsvb_free_desc(self._desc)
+            self._desc = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc:
+            raise VSVBError(f"{what} failed ({rc}): {lib().vsvb_gpu_last_error(self._h).decode()}")
+
+    def energy(self, coeff=None):
+        r = Result()
+        c = None if coeff is None else np.ascontiguousarray(coeff, dtype=np.float64)
+        self._check(lib().vsvb_gpu_energy(self._h, None if c is None else _dptr(c), ctypes.byref(r)), "energy")
+        return r.as_dict()
+
+    def energy_grad(self, coeff=None):
+        r = Result()
+        c = None if coeff is None else np.ascontiguousarray(coeff, dtype=np.float64)
+        g = np.zeros(self.totlen)
+        self._check(lib().vsvb_gpu_energy_grad(self._h, None if c is None else _dptr(c), ctypes.byref(r), _dptr(g)),
+                    "energy_grad")
+        return r.as_dict(), g
+
+    def energy_device(self, coeff_ptr):
+        """Energy with the weights already in device memory (a raw pointer)."""
+        r = Result()
+        self._check(lib().vsvb_gpu_energy_device(self._h, ctypes.c_void_p(coeff_ptr), ctypes.byref(r)), "energy")
+        return r.as_dict()
+
+    def energy_grad_device(self, coeff_ptr, grad_ptr):
+        r = Result()
+        self._check(lib().vsvb_gpu_energy_grad_device(self._h, ctypes.c_void_p(coeff_ptr), ctypes.byref(r),
+                                                      ctypes.c_void_p(grad_ptr)), "energy_grad")
+        return r.as_dict()
+
+    def orbital_eri(self):
+        n = lib().vsvb_gpu_num_orbitals(self._h)
+        np_ = n * (n + 1) // 2
+        out = np.zeros(np_ * np_)
+        rc = lib().vsvb_gpu_debug_orbital_eri(self._h, _dptr(out), out.size)
+        if rc < 0:
+            raise VSVBError("debug_orbital_eri failed")
+        return out.reshape(np_, np_)
+
+    def orbital_1e(self):
+        n = lib().vsvb_gpu_num_orbitals(self._h)
+        s = np.zeros(n * n)
+        h = np.zeros(n * n)
+        rc = lib().vsvb_gpu_debug_orbital_1e(self._h, _dptr(s), _dptr(h), n * n)
+        if rc < 0:
+            raise VSVBError("debug_orbital_1e failed")
+        return s.reshape(n, n), h.reshape(n, n)
+
+
+def batch_energy_grad(systems, weights=None, with_grad=True):
+    """Energies (and gradients) of independent molecules in one library call."""
+    n = len(systems)
+    hs = (ctypes.c_void_p * n)(*[s._h for s in systems])
+    ws = [np.ascontiguousarray(w if w is not None else s.coeff0, dtype=np.float64)
+          for s, w in zip(systems, weights or [None] * n)]
+    wp = (ctypes.POINTER(ctypes.c_double) * n)(*[_dptr(w) for w in ws])
+    res = (Result * n)()
+    grads = [np.zeros(s.totlen) for s in systems] if with_grad else None
+    gp = (ctypes.POINTER(ctypes.c_double) * n)(*[_dptr(g) for g in grads]) if with_grad else None
+    rc = lib().vsvb_gpu_batch_energy_grad(hs, n, wp, res, gp)
+    if rc:
+        raise VSVBError(f"batch failed ({rc}): {lib().vsvb_gpu_last_error(systems[0]._h).decode()}")
+    return [r.as_dict() for r in res], grads
+
+
+# --- reference-shaped API ---------------------------------------------------
+
+_STATE = {}
+
+
+def valence_api_initialize(input_path, precision=FP64, mixed_threshold=1e-6, device=0):
+    """Counterpart of valence_api_initialize (valence_api.F90:9-35): read the
+    input once; returns info = 0 on success (the reference always returns 0)."""
+    _STATE.clear()
+    _STATE.update(path=input_path, precision=precision, mixed_threshold=mixed_threshold, device=device, sys=None,
+                  coords=None)
+    return 0
+
+
+def valence_api_calculate_energy(x):
+    """Counterpart of valence_api_calculate_energy (valence_api.F90:37-108):
+    x = 3*natom Cartesian coordinates in Angstrom; returns the guess energy in
+    hartree (energy/wfnorm + enucrep, valence.F90:344)."""
+    if "path" not in _STATE:
+        raise VSVBError("valence_api_initialize has not been called")
+    x = np.asarray(x, dtype=np.float64).ravel()
+    s = _STATE.get("sys")
+    if s is None or _STATE.get("coords") is None or not np.array_equal(_STATE["coords"], x):
+        if s is not None:
+            s.close()
+        s = System(_STATE["path"], precision=_STATE["precision"], mixed_threshold=_STATE["mixed_threshold"],
+                   device=_STATE["device"], coords_angstrom=x)
+        _STATE["sys"], _STATE["coords"] = s, x.copy()
+    return s.energy()["energy"]
+
+
+def valence_api_finalize():
+    """Counterpart of valence_api_finalize (valence_api.F90:114-134)."""
+    s = _STATE.get("sys")
+    if s is not None:
+        s.close()
+    _STATE.clear()
+
+
+# --- torch binding ----------------------------------------------------------
+
+try:
+    import torch
+
+    class VSVBEnergy(torch.autograd.Function):
+        """E(weights) with dE/dweights from the GPU adjoint (ERIs recomputed in
+        the backward pass).  weights: 1-D float64 tensor of length totlen."""
+
+        @staticmethod
+        def forward(ctx, weights, system):
+            w = weights.detach().to("cpu", torch.float64).contiguous().numpy()
+            r, g = system.energy_grad(w)
+            ctx.save_for_backward(torch.from_numpy(g).to(weights.device))
+            return torch.tensor(r["energy"], dtype=torch.float64, device=weights.device)
+
+        @staticmethod
+        def backward(ctx, gout):
+            (g,) = ctx.saved_tensors
+            return gout * g, None
+except ImportError:  # pragma: no cover
+    VSVBEnergy = None

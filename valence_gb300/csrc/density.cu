@@ -1,0 +1,665 @@
+/*
+ * density.cu -- nonorthogonal cofactor densities and the VSVB energy
+ * assembly (valence.F90:1010-1434 with density/density_sc/dbra/dket/det,
+ * :1535-2056, and givdr/givens_single, :2067-2144, givens.F90:230-262).
+ *
+ * The reference re-factorises a struck overlap matrix with Givens rotations
+ * for every (orbital quartet x spin term x determinant pair).  Here every
+ * determinant pair q of the spin-coupled expansion (dbra x dket over the
+ * 2^npair alpha/beta exchanges of each coupling pair, weight
+ * coeff_sc(isc) coeff_sc(jsc)) is factorised once (Gauss-Jordan with
+ * partial pivoting per spin block), and any struck determinant follows from
+ * Jacobi's identity:
+ *   det(A with row r -> e_c)               = det A * T[c][r]
+ *   det(A with rows r1 -> e_c1, r2 -> e_c2) = det A * (T[c1][r1] T[c2][r2]
+ *                                                      - T[c1][r2] T[c2][r1])
+ * with T = A^-1.  Blocks whose pivots fall below 1e-7 of their largest entry
+ * (exact rank deficiency from molecular symmetry, e.g. pi pairs) take the
+ * exact path: the struck matrix is built and its determinant taken by LU,
+ * which is what the reference's givdr computes.
+ *
+ * The task loop keeps the reference's arithmetic: the same triangular task
+ * enumeration (xm_dtriang8, xm_module.F90:969-991), the Schwarz screens on
+ * the orbital-pair table (:1189-1190), the post-hoc |ERI| > itol screen
+ * (:1286-1287), the DOCC spin-parity skips (:1352-1375), the sign rule of
+ * det() for the exchanged density (:2041-2054) and the factor 2 of the
+ * ijkl symmetry (:1420-1428).  Grid: (determinant pair, task split); each
+ * thread walks tasks, partial sums are reduced in a fixed order.
+ *
+ * With GRAD set the same walk also accumulates the adjoints: dE/dT on the
+ * orbital-pair ERI matrix, dE/dS_orb and dE/dh_orb directly, and per
+ * determinant pair the quantities that give dE/dA for each spin block:
+ *   dv/dA = v T^T - det_a det_b J_other T^T (dJ/dT) T^T.
+ */
+#include <cuda_runtime.h>
+
+#include "density.cuh"
+
+namespace {
+
+__device__ __forceinline__ int spat(const DetCtx &d, int s) { return s < d.ds.nnd ? s : d.ds.nnd + (s - d.ds.nnd) / 2; }
+
+__device__ __forceinline__ void slot_loc(const DetCtx &d, int sc, unsigned bits, int s, int &spin, int &pos) {
+  const int np = d.ds.npair;
+  if (s < 2 * np) {
+    int k = d.slot_pair[sc * 2 * np + s];
+    int wh = d.slot_which[sc * 2 * np + s];
+    spin = wh ^ ((bits >> k) & 1);
+    pos = k;
+  } else if (s < d.ds.nnd) {
+    spin = 0;
+    pos = np + (s - 2 * np);
+  } else {
+    int dd = s - d.ds.nnd;
+    if ((dd & 1) == 0) {
+      spin = 0;
+      pos = np + d.ds.nunpd + dd / 2;
+    } else {
+      spin = 1;
+      pos = np + dd / 2;
+    }
+  }
+}
+
+__device__ __forceinline__ int pos_slot(const DetCtx &d, int sc, unsigned bits, int spin, int pos) {
+  const int np = d.ds.npair;
+  if (pos < np) {
+    int bit = (bits >> pos) & 1;
+    return d.pair_slot[(sc * np + pos) * 2 + (spin ^ bit)];
+  }
+  if (spin == 0) {
+    if (pos < np + d.ds.nunpd) return 2 * np + (pos - np);
+    return d.ds.nnd + 2 * (pos - np - d.ds.nunpd);
+  }
+  return d.ds.nnd + 2 * (pos - np) + 1;
+}
+
+struct QInfo {
+  int isc, jsc;
+  unsigned bb, kb;
+  double w;
+};
+
+__device__ __forceinline__ QInfo decode_q(const DetCtx &d, long long q) {
+  QInfo r;
+  const int np = d.ds.npair;
+  const unsigned mask = np > 0 ? ((1u << np) - 1u) : 0u;
+  r.kb = (unsigned)(q & mask);
+  r.bb = (unsigned)((q >> np) & mask);
+  long long sp = q >> (2 * np);
+  r.isc = (int)(sp / d.ds.nsc);
+  r.jsc = (int)(sp % d.ds.nsc);
+  r.w = d.coeff_sc[r.isc] * d.coeff_sc[r.jsc];
+  return r;
+}
+
+/* exact determinant of spin block sp of pair q with up to two strikes, by LU
+ * with partial pivoting on the struck matrix (n <= VSVB_MAXN) */
+__device__ double struck_det_exact(const DetCtx &d, const QInfo &qi, int sp, int ns, const int *rr, const int *cc) {
+  const int n = sp == 0 ? d.ds.nalpha : d.ds.nbeta;
+  double M[VSVB_MAXN * VSVB_MAXN];
+  for (int r = 0; r < n; ++r) {
+    int sb = spat(d, pos_slot(d, qi.isc, qi.bb, sp, r));
+    for (int c = 0; c < n; ++c) {
+      int sk = spat(d, pos_slot(d, qi.jsc, qi.kb, sp, c));
+      M[r * n + c] = d.So[sb * d.ds.nsp + sk];
+    }
+  }
+  for (int t = 0; t < ns; ++t) {
+    for (int i = 0; i < n; ++i) {
+      M[rr[t] * n + i] = 0.0;
+      M[i * n + cc[t]] = 0.0;
+    }
+    M[rr[t] * n + cc[t]] = 1.0;
+  }
+  double det = 1.0;
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    double mx = fabs(M[k * n + k]);
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(M[i * n + k]) > mx) {
+        mx = fabs(M[i * n + k]);
+        p = i;
+      }
+    if (mx == 0.0) return 0.0;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) {
+        double t = M[k * n + j];
+        M[k * n + j] = M[p * n + j];
+        M[p * n + j] = t;
+      }
+      det = -det;
+    }
+    double piv = M[k * n + k];
+    det *= piv;
+    for (int i = k + 1; i < n; ++i) {
+      double f = M[i * n + k] / piv;
+      for (int j = k + 1; j < n; ++j) M[i * n + j] -= f * M[k * n + j];
+    }
+  }
+  return det;
+}
+
+struct Cof {
+  bool ok;        /* spin integration non-zero */
+  double v;       /* w * det_a * det_b * J_a * J_b */
+  int na_s, nb_s; /* strikes per spin */
+  int ra[2], ca[2], rb[2], cb[2];
+  double Ja, Jb;  /* reduced factors */
+};
+
+/* cofactor of determinant pair q for up to two (bra slot, ket slot) strikes */
+__device__ Cof cofactor(const DetCtx &d, long long q, const QInfo &qi, int nst, const int *sb, const int *sk,
+                        int *status) {
+  Cof c;
+  c.ok = false;
+  c.v = 0.0;
+  c.na_s = c.nb_s = 0;
+  c.Ja = c.Jb = 1.0;
+  for (int t = 0; t < nst; ++t) {
+    int s1, p1, s2, p2;
+    slot_loc(d, qi.isc, qi.bb, sb[t], s1, p1);
+    slot_loc(d, qi.jsc, qi.kb, sk[t], s2, p2);
+    if (s1 != s2) return c;
+    if (s1 == 0) {
+      c.ra[c.na_s] = p1;
+      c.ca[c.na_s] = p2;
+      c.na_s++;
+    } else {
+      c.rb[c.nb_s] = p1;
+      c.cb[c.nb_s] = p2;
+      c.nb_s++;
+    }
+  }
+  c.ok = true;
+  const int na = d.ds.nalpha, nb = d.ds.nbeta;
+  const int sing = d.sing[q];
+  double fa, fb;
+  if ((sing & 1) && c.na_s > 0) {
+    fa = struck_det_exact(d, qi, 0, c.na_s, c.ra, c.ca);
+    c.Ja = 0.0;
+    if (status) atomicOr(status, 2);
+  } else {
+    const double *Ta = d.Ta + (size_t)q * na * na;
+    if (c.na_s == 1) c.Ja = Ta[c.ca[0] * na + c.ra[0]];
+    else if (c.na_s == 2)
+      c.Ja = Ta[c.ca[0] * na + c.ra[0]] * Ta[c.ca[1] * na + c.ra[1]] - Ta[c.ca[0] * na + c.ra[1]] * Ta[c.ca[1] * na + c.ra[0]];
+    fa = d.det_a[q] * c.Ja;
+  }
+  if ((sing & 2) && c.nb_s > 0) {
+    fb = struck_det_exact(d, qi, 1, c.nb_s, c.rb, c.cb);
+    c.Jb = 0.0;
+    if (status) atomicOr(status, 2);
+  } else {
+    const double *Tb = d.Tb + (size_t)q * nb * nb;
+    if (c.nb_s == 1) c.Jb = Tb[c.cb[0] * nb + c.rb[0]];
+    else if (c.nb_s == 2)
+      c.Jb = Tb[c.cb[0] * nb + c.rb[0]] * Tb[c.cb[1] * nb + c.rb[1]] - Tb[c.cb[0] * nb + c.rb[1]] * Tb[c.cb[1] * nb + c.rb[0]];
+    fb = d.det_b[q] * c.Jb;
+  }
+  c.v = qi.w * fa * fb;
+  return c;
+}
+
+/* dJ/dT accumulation for one cofactor with coefficient coef on v */
+__device__ void accum_G(const DetCtx &d, long long q, const QInfo &qi, const Cof &c, double coef, double *Ga, double *Gb,
+                        int lda, int ldb) {
+  if (!c.ok || coef == 0.0) return;
+  const int na = d.ds.nalpha, nb = d.ds.nbeta;
+  const double dd = qi.w * d.det_a[q] * d.det_b[q];
+  if (c.na_s > 0) {
+    const double *Ta = d.Ta + (size_t)q * na * na;
+    const double f = coef * dd * c.Jb;
+    if (c.na_s == 1) {
+      atomicAdd(Ga + c.ca[0] * lda + c.ra[0], f);
+    } else {
+      atomicAdd(Ga + c.ca[0] * lda + c.ra[0], f * Ta[c.ca[1] * na + c.ra[1]]);
+      atomicAdd(Ga + c.ca[1] * lda + c.ra[1], f * Ta[c.ca[0] * na + c.ra[0]]);
+      atomicAdd(Ga + c.ca[0] * lda + c.ra[1], -f * Ta[c.ca[1] * na + c.ra[0]]);
+      atomicAdd(Ga + c.ca[1] * lda + c.ra[0], -f * Ta[c.ca[0] * na + c.ra[1]]);
+    }
+  }
+  if (c.nb_s > 0) {
+    const double *Tb = d.Tb + (size_t)q * nb * nb;
+    const double f = coef * dd * c.Ja;
+    if (c.nb_s == 1) {
+      atomicAdd(Gb + c.cb[0] * ldb + c.rb[0], f);
+    } else {
+      atomicAdd(Gb + c.cb[0] * ldb + c.rb[0], f * Tb[c.cb[1] * nb + c.rb[1]]);
+      atomicAdd(Gb + c.cb[1] * ldb + c.rb[1], f * Tb[c.cb[0] * nb + c.rb[0]]);
+      atomicAdd(Gb + c.cb[0] * ldb + c.rb[1], -f * Tb[c.cb[1] * nb + c.rb[0]]);
+      atomicAdd(Gb + c.cb[1] * ldb + c.rb[0], -f * Tb[c.cb[0] * nb + c.rb[1]]);
+    }
+  }
+}
+
+__device__ double block_sum_d(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    red[0] = s;
+  }
+  __syncthreads();
+  s = red[0];
+  __syncthreads();
+  return s;
+}
+
+__device__ __forceinline__ int opidx(int i, int k) { return i >= k ? i * (i + 1) / 2 + k : k * (k + 1) / 2 + i; }
+
+/* xm_dtriang / xm_dtriang8: 1-based triangular index -> (i, j), j <= i */
+__device__ __forceinline__ void dtriang(long long ij, int &i, int &j) {
+  long long ii = (long long)sqrt((double)(2 * ij));
+  while ((ii * ii + ii) / 2 < ij) ++ii;
+  while (ii > 1 && ((ii - 1) * (ii - 1) + (ii - 1)) / 2 >= ij) --ii;
+  i = (int)ii;
+  j = (int)(ij - (ii * ii - ii) / 2);
+}
+
+}  // namespace
+
+/* ---- determinant pairs: one block per q, Gauss-Jordan per spin block ---- */
+__global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
+  __shared__ double red[8];
+  __shared__ int redi[8];
+  __shared__ double sdet;
+  __shared__ int ssing, spiv;
+  const long long q = blockIdx.x;
+  const QInfo qi = decode_q(d, q);
+  double *W = scratch + (size_t)blockIdx.x * ld_scratch;
+  for (int sp = 0; sp < 2; ++sp) {
+    const int n = sp == 0 ? d.ds.nalpha : d.ds.nbeta;
+    double *Tout = (sp == 0 ? d.Ta : d.Tb) + (size_t)q * n * n;
+    if (n == 0) {
+      if (threadIdx.x == 0) (sp == 0 ? d.det_a : d.det_b)[q] = 1.0;
+      continue;
+    }
+    const int n2 = 2 * n;
+    /* W = [A | I] */
+    double mx = 0.0;
+    for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
+      int r = t / n2, c = t - r * n2;
+      double v;
+      if (c < n) {
+        int sb = spat(d, pos_slot(d, qi.isc, qi.bb, sp, r));
+        int sk = spat(d, pos_slot(d, qi.jsc, qi.kb, sp, c));
+        v = d.So[sb * d.ds.nsp + sk];
+        mx = fmax(mx, fabs(v));
+      } else {
+        v = (c - n == r) ? 1.0 : 0.0;
+      }
+      W[t] = v;
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+      red[0] = m;
+      sdet = 1.0;
+      ssing = 0;
+    }
+    __syncthreads();
+    const double amax = red[0];
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+      /* pivot search */
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
+        double v = fabs(W[i * n2 + k]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if ((threadIdx.x & 31) == 0) {
+        red[threadIdx.x >> 5] = best;
+        redi[threadIdx.x >> 5] = bi;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double b = -1.0;
+        int p = k;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+          if (red[w] > b || (red[w] == b && redi[w] < p)) {
+            b = red[w];
+            p = redi[w];
+          }
+        spiv = p;
+        if (!(b > 1e-7 * amax)) ssing = 1;
+      }
+      __syncthreads();
+      if (ssing) break;
+      const int p = spiv;
+      if (p != k) {
+        for (int j = threadIdx.x; j < n2; j += blockDim.x) {
+          double t = W[k * n2 + j];
+          W[k * n2 + j] = W[p * n2 + j];
+          W[p * n2 + j] = t;
+        }
+      }
+      __syncthreads();
+      const double piv = W[k * n2 + k];
+      if (threadIdx.x == 0) sdet *= (p != k ? -piv : piv);
+      __syncthreads();
+      for (int j = threadIdx.x; j < n2; j += blockDim.x) W[k * n2 + j] /= piv;
+      __syncthreads();
+      for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
+        int i = t / n2, j = t - i * n2;
+        if (i != k && j != k) W[t] -= W[i * n2 + k] * W[k * n2 + j];
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (i != k) W[i * n2 + k] = 0.0;
+      __syncthreads();
+    }
+    if (ssing) {
+      /* exact-minor path: the unstruck determinant by LU on a fresh copy */
+      if (threadIdx.x == 0) {
+        double det = 1.0;
+        double *M = W;
+        for (int r = 0; r < n; ++r)
+          for (int c = 0; c < n; ++c) {
+            int sb = spat(d, pos_slot(d, qi.isc, qi.bb, sp, r));
+            int sk = spat(d, pos_slot(d, qi.jsc, qi.kb, sp, c));
+            M[r * n + c] = d.So[sb * d.ds.nsp + sk];
+          }
+        for (int k = 0; k < n && det != 0.0; ++k) {
+          int p = k;
+          double m = fabs(M[k * n + k]);
+          for (int i = k + 1; i < n; ++i)
+            if (fabs(M[i * n + k]) > m) {
+              m = fabs(M[i * n + k]);
+              p = i;
+            }
+          if (m == 0.0) {
+            det = 0.0;
+            break;
+          }
+          if (p != k) {
+            for (int j = 0; j < n; ++j) {
+              double t = M[k * n + j];
+              M[k * n + j] = M[p * n + j];
+              M[p * n + j] = t;
+            }
+            det = -det;
+          }
+          det *= M[k * n + k];
+          for (int i = k + 1; i < n; ++i) {
+            double f = M[i * n + k] / M[k * n + k];
+            for (int j = k + 1; j < n; ++j) M[i * n + j] -= f * M[k * n + j];
+          }
+        }
+        (sp == 0 ? d.det_a : d.det_b)[q] = det;
+        atomicOr(&d.sing[q], 1 << sp);
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < n * n; t += blockDim.x) Tout[t] = 0.0;
+    } else {
+      for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        int r = t / n, c = t - r * n;
+        Tout[t] = W[r * n2 + n + c];
+      }
+      if (threadIdx.x == 0) (sp == 0 ? d.det_a : d.det_b)[q] = sdet;
+    }
+    __syncthreads();
+  }
+}
+
+/* ---- energy (and adjoint) assembly: grid (nq, nsplit) ---- */
+template <bool GRAD>
+__global__ void assemble_kernel(DetCtx d, AsmArgs a) {
+  __shared__ double red[8];
+  extern __shared__ double gsh[];
+  const long long q = blockIdx.x;
+  const int split = blockIdx.y, nsplit = gridDim.y;
+  const QInfo qi = decode_q(d, q);
+  const int nelec = d.ds.nelec, nnd = d.ds.nnd, nsp = d.ds.nsp;
+  const int na = d.ds.nalpha, nb = d.ds.nbeta;
+  double *Ga = nullptr, *Gb = nullptr;
+  int lda = na, ldb = nb;
+  if (GRAD) {
+    if (a.g_in_smem) {
+      Ga = gsh;
+      Gb = gsh + na * na;
+      for (int t = threadIdx.x; t < na * na + nb * nb; t += blockDim.x) gsh[t] = 0.0;
+      __syncthreads();
+    } else {
+      Ga = a.Gglob + (size_t)q * (na * na + nb * nb);
+      Gb = Ga + na * na;
+    }
+  }
+  double e1 = 0.0, wf = 0.0, e2 = 0.0, vtot = 0.0;
+  const long long stride = (long long)nsplit * blockDim.x;
+  /* one-electron part (valence.F90:1072-1101) */
+  for (long long t = (long long)split * blockDim.x + threadIdx.x; t < (long long)nelec * nelec; t += stride) {
+    const int i = (int)(t / nelec), j = (int)(t % nelec);
+    const bool idocc = i >= nnd, jdocc = j >= nnd;
+    /* 1-based parity as in the reference: slots i+1, j+1 */
+    if (idocc && jdocc && ((i + 1) & 1) != ((j + 1) & 1)) continue;
+    int sb[1] = {i}, sk[1] = {j};
+    Cof c = cofactor(d, q, qi, 1, sb, sk, a.status);
+    if (!c.ok) continue;
+    const int si = spat(d, i), sj = spat(d, j);
+    const double h = d.Ho[si * nsp + sj], s = d.So[si * nsp + sj];
+    e1 += h * c.v;
+    wf += s * c.v;
+    if (GRAD) {
+      const double coef = h * a.inv_w + a.dw_coef * s;
+      vtot += coef * c.v;
+      accum_G(d, q, qi, c, coef, Ga, Gb, lda, ldb);
+      atomicAdd(a.Hbar + si * nsp + sj, c.v * a.inv_w);
+      atomicAdd(a.Sbar + si * nsp + sj, c.v * a.dw_coef);
+    }
+  }
+  /* two-electron tasks (valence.F90:1153-1433) */
+  const int np = a.np;
+  const double itol = a.itol;
+  for (long long task = (long long)split * blockDim.x + threadIdx.x; task < a.ntasks; task += stride) {
+    int ijorb, klorb, io, jo, ko, lo;
+    dtriang(task + 1, ijorb, klorb);
+    dtriang(ijorb, io, jo);
+    dtriang(klorb, ko, lo);
+    --io;
+    --jo;
+    --ko;
+    --lo; /* 0-based orbitals */
+    if ((io == jo && io < nnd) || (ko == lo && ko < nnd)) continue;
+    const int pik = opidx(io, ko), pjl = opidx(jo, lo), pil = opidx(io, lo), pjk = opidx(jo, ko);
+    const double sik = sqrt(fmax(a.T[(size_t)pik * np + pik], 0.0)), sjl = sqrt(fmax(a.T[(size_t)pjl * np + pjl], 0.0));
+    const double sil = sqrt(fmax(a.T[(size_t)pil * np + pil], 0.0)), sjk = sqrt(fmax(a.T[(size_t)pjk * np + pjk], 0.0));
+    bool es = sik * sjl > itol, xs = sil * sjk > itol;
+    double eint = 0.0, xint = 0.0;
+    const bool diag = io == jo && ko == lo;
+    if (es || xs) {
+      if (diag) {
+        eint = sik * sik;
+        xint = eint;
+      } else {
+        if (es) eint = a.T[(size_t)pik * np + pjl];
+        if (xs) xint = a.T[(size_t)pil * np + pjk];
+      }
+    }
+    es = fabs(eint) > itol;
+    xs = fabs(xint) > itol;
+    if (!(es || xs)) continue;
+    const double fac = (ko == io && lo == jo) ? 1.0 : 2.0;
+    const bool id = io >= nnd, jd = jo >= nnd, kd = ko >= nnd, ld = lo >= nnd;
+    const int iso = id ? 2 : 1, jso = jd ? 2 : 1, kso = kd ? 2 : 1, lso = ld ? 2 : 1;
+    double esum = 0.0, xsum = 0.0, dsum_e = 0.0, dsum_x = 0.0;
+    for (int is = 0; is < iso; ++is) {
+      /* 0-based slot; 1-based formula 2*io - nnd + is - 2 with 1-based io */
+      const int i = id ? 2 * (io + 1) - nnd + (is + 1) - 2 - 1 : io;
+      for (int js = 0; js < jso; ++js) {
+        const int j = jd ? 2 * (jo + 1) - nnd + (js + 1) - 2 - 1 : jo;
+        if (!(j < i)) continue;
+        for (int ks = 0; ks < kso; ++ks) {
+          const int k = kd ? 2 * (ko + 1) - nnd + (ks + 1) - 2 - 1 : ko;
+          for (int ls = 0; ls < lso; ++ls) {
+            const int l = ld ? 2 * (lo + 1) - nnd + (ls + 1) - 2 - 1 : lo;
+            if (!(l < k)) continue;
+            /* 1-based parity for the DOCC spin integration */
+            const bool ik0 = id && kd && ((i + 1) & 1) != ((k + 1) & 1);
+            const bool jl0 = jd && ld && ((j + 1) & 1) != ((l + 1) & 1);
+            const bool il0 = id && ld && ((i + 1) & 1) != ((l + 1) & 1);
+            const bool jk0 = jd && kd && ((j + 1) & 1) != ((k + 1) & 1);
+            const bool ce = !(ik0 || jl0), cx = !(il0 || jk0);
+            if (!((ce && es) || (cx && xs))) continue;
+            Cof ce_c, cx_c;
+            ce_c.ok = false;
+            cx_c.ok = false;
+            if (es) {
+              int sb[2] = {i, j}, sk[2] = {k, l};
+              ce_c = cofactor(d, q, qi, 2, sb, sk, a.status);
+            }
+            if (xs) {
+              int sb[2] = {i, j}, sk[2] = {l, k};
+              cx_c = cofactor(d, q, qi, 2, sb, sk, a.status);
+            }
+            double dd = 0.0, xd = 0.0;
+            if (es && ce_c.ok) dd = ce_c.v;
+            if (xs && cx_c.ok) xd = (es && ce_c.ok) ? ce_c.v : -cx_c.v;
+            if (es) {
+              esum += dd * eint;
+              dsum_e += dd;
+            }
+            if (xs) {
+              xsum += xd * xint;
+              dsum_x += xd;
+            }
+            if (GRAD) {
+              /* coefficients of the two cofactors in fac*(dd*eint - xd*xint)/W */
+              double cve = 0.0, cvx = 0.0;
+              if (es && ce_c.ok) {
+                cve = eint;
+                if (xs && cx_c.ok) cve -= xint;
+              } else if (xs && cx_c.ok) {
+                cvx = xint;
+              }
+              cve *= fac * a.inv_w;
+              cvx *= fac * a.inv_w;
+              if (ce_c.ok && cve != 0.0) {
+                vtot += cve * ce_c.v;
+                accum_G(d, q, qi, ce_c, cve, Ga, Gb, lda, ldb);
+              }
+              if (cx_c.ok && cvx != 0.0) {
+                vtot += cvx * cx_c.v;
+                accum_G(d, q, qi, cx_c, cvx, Ga, Gb, lda, ldb);
+              }
+            }
+          }
+        }
+      }
+    }
+    e2 += fac * (esum - xsum);
+    if (GRAD) {
+      const double ge = fac * a.inv_w * dsum_e, gx = -fac * a.inv_w * dsum_x;
+      if (diag) {
+        if (es || xs) atomicAdd(a.Tbar + (size_t)pik * np + pik, (es ? ge : 0.0) + (xs ? gx : 0.0));
+      } else {
+        if (es && ge != 0.0) atomicAdd(a.Tbar + (size_t)pik * np + pjl, ge);
+        if (xs && gx != 0.0) atomicAdd(a.Tbar + (size_t)pil * np + pjk, gx);
+      }
+    }
+  }
+  e1 = block_sum_d(e1, red);
+  wf = block_sum_d(wf, red);
+  e2 = block_sum_d(e2, red);
+  const size_t slot = (size_t)q * nsplit + split;
+  if (GRAD) {
+    vtot = block_sum_d(vtot, red);
+    if (threadIdx.x == 0) a.vtot[slot] = vtot;
+    if (a.g_in_smem) {
+      __syncthreads();
+      double *Gq = a.Gglob + (size_t)q * (na * na + nb * nb);
+      for (int t = threadIdx.x; t < na * na + nb * nb; t += blockDim.x)
+        if (gsh[t] != 0.0) atomicAdd(Gq + t, gsh[t]);
+    }
+  } else if (threadIdx.x == 0) {
+    a.part_e1[slot] = e1;
+    a.part_wf[slot] = wf;
+    a.part_e2[slot] = e2;
+  }
+}
+
+/* fixed-order reduction of the partial sums (one block) */
+__global__ void energy_reduce_kernel(AsmArgs a, long long nslot, int nelec, double enuc, double *out) {
+  __shared__ double red[8];
+  double e1 = 0.0, wf = 0.0, e2 = 0.0;
+  for (long long t = threadIdx.x; t < nslot; t += blockDim.x) {
+    e1 += a.part_e1[t];
+    wf += a.part_wf[t];
+    e2 += a.part_e2[t];
+  }
+  e1 = block_sum_d(e1, red);
+  wf = block_sum_d(wf, red);
+  e2 = block_sum_d(e2, red);
+  if (threadIdx.x == 0) {
+    double w = wf / (double)nelec;
+    out[0] = (e1 + e2) / w + enuc; /* energy */
+    out[1] = e1 + e2;
+    out[2] = e1;
+    out[3] = e2;
+    out[4] = w;
+  }
+}
+
+/* per determinant pair: dE/dA = vtot T^T - T^T G T^T for each spin block,
+ * scattered onto dE/dS_orb */
+__global__ void detpair_adjoint_kernel(DetCtx d, AsmArgs a, int nsplit) {
+  __shared__ double red[8];
+  const long long q = blockIdx.x;
+  const QInfo qi = decode_q(d, q);
+  double vt = 0.0;
+  for (int s = threadIdx.x; s < nsplit; s += blockDim.x) vt += a.vtot[(size_t)q * nsplit + s];
+  vt = block_sum_d(vt, red);
+  const int na = d.ds.nalpha, nb = d.ds.nbeta, nsp = d.ds.nsp;
+  const double *Gq = a.Gglob + (size_t)q * (na * na + nb * nb);
+  for (int sp = 0; sp < 2; ++sp) {
+    const int n = sp == 0 ? na : nb;
+    if (n == 0) continue;
+    const double *T = (sp == 0 ? d.Ta : d.Tb) + (size_t)q * n * n;
+    const double *G = Gq + (sp == 0 ? 0 : na * na);
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      const int ar = t / n, bc = t - ar * n; /* dE/dA[ar][bc] */
+      /* (T^T G T^T)[ar][bc] = sum_xy T[x][ar] G[x][y] T[bc][y] */
+      double s = 0.0;
+      for (int x = 0; x < n; ++x) {
+        const double tx = T[x * n + ar];
+        if (tx == 0.0) continue;
+        double inner = 0.0;
+        for (int y = 0; y < n; ++y) inner += G[x * n + y] * T[bc * n + y];
+        s += tx * inner;
+      }
+      const double abar = vt * T[bc * n + ar] - s;
+      const int sb = spat(d, pos_slot(d, qi.isc, qi.bb, sp, ar));
+      const int sk = spat(d, pos_slot(d, qi.jsc, qi.kb, sp, bc));
+      atomicAdd(a.Sbar + sb * nsp + sk, abar);
+    }
+  }
+}
+
+cudaError_t launch_assemble(bool grad, dim3 grid, int threads, size_t smem, cudaStream_t st, const DetCtx &d,
+                            const AsmArgs &a) {
+  if (grad) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(assemble_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    assemble_kernel<true><<<grid, threads, smem, st>>>(d, a);
+  } else {
+    assemble_kernel<false><<<grid, threads, smem, st>>>(d, a);
+  }
+  return cudaGetLastError();
+}

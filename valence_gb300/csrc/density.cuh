@@ -1,0 +1,40 @@
+/* density.cuh -- launch interface of the determinant-pair / assembly kernels. */
+#ifndef VSVB_DENSITY_CUH
+#define VSVB_DENSITY_CUH
+#include <cuda_runtime.h>
+
+#include "vsvb_internal.h"
+
+struct DetCtx {
+  DetSetup ds;
+  const int *pair_slot;   /* [nsc][npair][2]: 0-based slots of pair_sc(k,1|2,isc) */
+  const int *slot_pair;   /* [nsc][2*npair]: pair index of each coupled slot */
+  const int *slot_which;  /* [nsc][2*npair]: 0 if the slot is pair_sc(k,1), 1 if (k,2) */
+  const double *coeff_sc; /* [nsc] (1.0 when nspinc == 0) */
+  const double *So, *Ho;  /* nsp x nsp orbital overlap / core Hamiltonian */
+  double *det_a, *det_b;  /* [nq] */
+  double *Ta, *Tb;        /* [nq][n*n] inverses (zero on the exact-minor path) */
+  int *sing;              /* [nq] bit0 alpha, bit1 beta on the exact-minor path */
+};
+
+struct AsmArgs {
+  const double *T;  /* np x np orbital-pair ERIs */
+  int np;
+  double itol;
+  long long ntasks;
+  double *part_e1, *part_wf, *part_e2; /* [nq * nsplit] */
+  int *status;
+  /* adjoint pass */
+  double inv_w, dw_coef;  /* 1/W and -E_num/(W^2 nelec) */
+  double *Tbar, *Sbar, *Hbar;
+  double *vtot;            /* [nq * nsplit] */
+  double *Gglob;           /* [nq][na*na + nb*nb] */
+  int g_in_smem;
+};
+
+__global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch);
+cudaError_t launch_assemble(bool grad, dim3 grid, int threads, size_t smem, cudaStream_t st, const DetCtx &d,
+                            const AsmArgs &a);
+__global__ void energy_reduce_kernel(AsmArgs a, long long nslot, int nelec, double enuc, double *out);
+__global__ void detpair_adjoint_kernel(DetCtx d, AsmArgs a, int nsplit);
+#endif

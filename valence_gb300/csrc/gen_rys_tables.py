@@ -134,7 +134,7 @@ def main():
     lines.append("static const int rys_table_offset[RYS_NMAX] = {" + ", ".join(str(o) for o in offs) + "};")
     lines.append(f"static const double rys_table_data[{len(data)}] = {{")
     for i in range(0, len(data), 4):
-        lines.append("  " + ", ".join(mp.nstr(v, 21, strip_zeros=False, min_fixed=-1, max_fixed=-1) for v in data[i:i + 4]) + ",")
+        lines.append("  " + ", ".join(repr(float(v)) for v in data[i:i + 4]) + ",")
     lines.append("};")
     hx, hw = [], []
     for n in range(1, NMAX + 1):
@@ -143,11 +143,11 @@ def main():
         hw.append(W + [mp.mpf(0)] * (NMAX - n))
     lines.append("static const double rys_asym_x[RYS_NMAX][RYS_NMAX] = {")
     for row in hx:
-        lines.append("  {" + ", ".join(mp.nstr(v, 21) for v in row) + "},")
+        lines.append("  {" + ", ".join(repr(float(v)) for v in row) + "},")
     lines.append("};")
     lines.append("static const double rys_asym_w[RYS_NMAX][RYS_NMAX] = {")
     for row in hw:
-        lines.append("  {" + ", ".join(mp.nstr(v, 21) for v in row) + "},")
+        lines.append("  {" + ", ".join(repr(float(v)) for v in row) + "},")
     lines.append("};")
     with open(os.path.join(here, "rys_tables.inc"), "w") as f:
         f.write("\n".join(lines) + "\n")

@@ -1,0 +1,899 @@
+/*
+ * handle.cu -- the C ABI (include/vsvb_gpu.h): handle set-up and the energy /
+ * gradient pipelines on one CUDA stream.
+ *
+ * Set-up mirrors calculate_vsvb_energy (valence.F90:70-182): norm_prim per
+ * shell (:2264-2305), CCA component factors angn (:2337-2421), nuclear
+ * repulsion (tools_module.F90:19-40), then builds what the GPU kernels need:
+ * global shells, the orbital basis sets (OBS) with their weight scatter
+ * terms (ovint/int1e/int2e scatter, :2919-2947; ndf2obs, :2191-2247),
+ * unique shell pairs with primitive-pair data and the orbital pairs that
+ * touch them, AO one-electron matrices, AO Schwarz bounds and a quartet
+ * schedule sorted by angular-momentum class (and by precision on the mixed
+ * path), and the spin-coupling maps of dbra/dket (:1648-1870).
+ *
+ * Evaluation (guess_energy, :309-345, with vsvb_energy, :1010-1434):
+ *   ndf_norm, orb_norm -> orb_1e -> xtab -> eri (per class) -> detpair ->
+ *   assemble -> energy_reduce,
+ * and for the gradient a second walk of the same tasks (assemble<GRAD>),
+ * the determinant-pair adjoint, the ERI adjoint (ERIs recomputed) and the
+ * chain back through the X tables, the orbital integrals and normal().
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "../../include/vsvb_gpu.h"
+#include "density.cuh"
+#include "eri.cuh"
+#include "onee.cuh"
+#include "vsvb_internal.h"
+
+#include "rys_tables.inc"
+
+namespace {
+
+template <typename T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    free();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(&p, sizeof(T) * count);
+  }
+  cudaError_t upload(const std::vector<T> &v) {
+    cudaError_t e = alloc(v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { free(); }
+};
+
+int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; } /* la >= lb */
+
+double dblfac(int n) {
+  double d = 1.0;
+  for (int i = 3; i <= n; i += 2) d *= (double)i;
+  return d;
+}
+
+}  // namespace
+
+struct vsvb_gpu {
+  vsvb_options opt;
+  std::string err;
+  int dev = 0, nsm = 152;
+  cudaStream_t st = nullptr;
+  /* dims */
+  int natom = 0, nsh = 0, nao = 0, norb_all = 0, nsp = 0, ndf = 0, totlen = 0, maxobs = 0, np = 0;
+  DetSetup ds{};
+  double enuc = 0.0, dtol = 0.0, itol = 0.0;
+  long long ntasks = 0;
+  int nsplit = 1;
+  std::vector<double> coeff0;
+  /* schedules: [prec][cp][cq] */
+  std::vector<int2> work_h[2][6][6];
+  DBuf<int2> work_d[2][6][6];
+  long long nq_fp64 = 0, nq_fp32 = 0;
+  double err_bound = 0.0; /* sum over FP32 quartets of the Schwarz bound (scaled later) */
+  /* device data */
+  DBuf<GShell> shells;
+  DBuf<double> exps, coefs, angn, charge, axyz, rys;
+  DBuf<double> S_ao, H_ao;
+  DBuf<ShellPair> pairs;
+  DBuf<PrimPair> prims;
+  DBuf<int> pair_opid;
+  DBuf<XTerm> xterms;
+  DBuf<long long> xelem0;
+  long long nxelem = 0;
+  int nxterm = 0;
+  DBuf<int> obs_n, obs_ao, term0, term_slot, term_j, term_m, term_f, ndf_orb;
+  DBuf<double> coeff_d, ndf_scale, orb_scale, Craw, C, So, Ho, xtab, T, qmax;
+  DBuf<int> pair_slot, slot_pair, slot_which, sing, status;
+  DBuf<double> coeff_sc, det_a, det_b, Ta, Tb, scratch;
+  int ld_scratch = 0;
+  DBuf<double> part_e1, part_wf, part_e2, result;
+  /* adjoint */
+  DBuf<double> Tbar, Sbar, Hbar, xbar, Cbar, vtot, Gglob, coeff_bar;
+  bool grad_ready = false;
+  int last_singular = 0;
+};
+
+namespace {
+
+int cuda_fail(vsvb_gpu *h, cudaError_t e, const char *what) {
+  h->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return VSVB_ERR_CUDA;
+}
+
+#define CK(call, what)                              \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, what); \
+  } while (0)
+
+OrbArgs orb_args(vsvb_gpu *h) {
+  OrbArgs a{};
+  a.norb_all = h->norb_all;
+  a.maxobs = h->maxobs;
+  a.nao = h->nao;
+  a.obs_n = h->obs_n.p;
+  a.obs_ao = h->obs_ao.p;
+  a.term0 = h->term0.p;
+  a.term_slot = h->term_slot.p;
+  a.term_j = h->term_j.p;
+  a.term_m = h->term_m.p;
+  a.term_f = h->term_f.p;
+  a.ndf_orb = h->ndf_orb.p;
+  a.coeff = h->coeff_d.p;
+  a.S = h->S_ao.p;
+  a.H = h->H_ao.p;
+  a.ndf_scale = h->ndf_scale.p;
+  a.orb_scale = h->orb_scale.p;
+  a.Craw = h->Craw.p;
+  a.C = h->C.p;
+  a.status = h->status.p;
+  return a;
+}
+
+XtabArgs xtab_args(vsvb_gpu *h) {
+  XtabArgs x{};
+  x.terms = h->xterms.p;
+  x.elem0 = h->xelem0.p;
+  x.nterm = h->nxterm;
+  x.nelem = h->nxelem;
+  x.C = h->C.p;
+  x.maxobs = h->maxobs;
+  x.angn = h->angn.p;
+  x.dtol = h->dtol;
+  x.xtab = h->xtab.p;
+  return x;
+}
+
+EriArgs eri_args(vsvb_gpu *h) {
+  EriArgs a{};
+  a.pairs = h->pairs.p;
+  a.prims = h->prims.p;
+  a.rys = h->rys.p;
+  a.pair_opid = h->pair_opid.p;
+  a.xtab = h->xtab.p;
+  a.T = h->T.p;
+  a.np = h->np;
+  a.qmax_out = h->qmax.p;
+  a.Tbar = h->Tbar.p;
+  a.xbar = h->xbar.p;
+  return a;
+}
+
+DetCtx det_ctx(vsvb_gpu *h) {
+  DetCtx d{};
+  d.ds = h->ds;
+  d.pair_slot = h->pair_slot.p;
+  d.slot_pair = h->slot_pair.p;
+  d.slot_which = h->slot_which.p;
+  d.coeff_sc = h->coeff_sc.p;
+  d.So = h->So.p;
+  d.Ho = h->Ho.p;
+  d.det_a = h->det_a.p;
+  d.det_b = h->det_b.p;
+  d.Ta = h->Ta.p;
+  d.Tb = h->Tb.p;
+  d.sing = h->sing.p;
+  return d;
+}
+
+AsmArgs asm_args(vsvb_gpu *h) {
+  AsmArgs a{};
+  a.T = h->T.p;
+  a.np = h->np;
+  a.itol = h->itol;
+  a.ntasks = h->ntasks;
+  a.part_e1 = h->part_e1.p;
+  a.part_wf = h->part_wf.p;
+  a.part_e2 = h->part_e2.p;
+  a.status = nullptr;
+  a.Tbar = h->Tbar.p;
+  a.Sbar = h->Sbar.p;
+  a.Hbar = h->Hbar.p;
+  a.vtot = h->vtot.p;
+  a.Gglob = h->Gglob.p;
+  int na = h->ds.nalpha, nb = h->ds.nbeta;
+  a.g_in_smem = (size_t)(na * na + nb * nb) * sizeof(double) <= 40 * 1024;
+  return a;
+}
+
+/* ---------------- set-up ---------------- */
+
+int build(vsvb_gpu *h, const vsvb_system_desc *d) {
+  if (d->npair > 0 && d->nspinc < 1) {
+    h->err = "no spin couplings;";
+    return VSVB_ERR_INPUT;
+  }
+  for (int s = 0; s < d->num_sh; ++s)
+    if (d->ang_mom[s] < 0 || d->ang_mom[s] > VSVB_LMAX) {
+      h->err = "angular momentum above d is not supported on the GPU path";
+      return VSVB_ERR_UNSUPPORTED;
+    }
+  if (d->npair > 15) {
+    h->err = "more than 15 spin-coupled pairs";
+    return VSVB_ERR_UNSUPPORTED;
+  }
+  CK(cudaSetDevice(h->dev), "cudaSetDevice");
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, h->dev), "cudaGetDeviceProperties");
+  h->nsm = prop.multiProcessorCount;
+  CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking), "cudaStreamCreate");
+
+  const int norbs = 2 * d->npair + d->nunpd + d->ndocc + d->ndf;
+  h->natom = d->natom;
+  h->ndf = d->ndf;
+  h->norb_all = norbs;
+  h->nsp = 2 * d->npair + d->nunpd + d->ndocc;
+  h->totlen = d->totlen;
+  h->dtol = std::pow(10.0, -(double)d->ntol_d);
+  h->itol = std::pow(10.0, -(double)d->ntol_i);
+  h->coeff0.assign(d->coeff, d->coeff + d->totlen);
+
+  /* norm_prim (valence.F90:2264-2305) */
+  std::vector<double> cc(d->num_pr);
+  const double pi32 = std::pow(std::acos(-1.0), 1.5);
+  for (int s = 0; s < d->num_sh; ++s) {
+    int l = d->ang_mom[s], k0 = d->map_shell2prim[s] - 1, n = d->map_shell2prim[s + 1] - d->map_shell2prim[s];
+    double fac = pi32 * dblfac(2 * l - 1) * std::pow(2.0, -l), fax = -1.5 - l;
+    for (int i = 0; i < n; ++i) cc[k0 + i] = d->con_coeff[k0 + i] * std::pow(fac * std::pow(2.0 * d->exponent[k0 + i], fax), -0.5);
+    double sovl = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) sovl += fac * cc[k0 + i] * cc[k0 + j] * std::pow(d->exponent[k0 + i] + d->exponent[k0 + j], fax);
+    sovl = std::pow(sovl, -0.5);
+    for (int i = 0; i < n; ++i) cc[k0 + i] *= sovl;
+  }
+  /* angn per component in CCA order (setangn, valence.F90:2395-2421) */
+  auto angn_of = [](int l, int k) {
+    int n = 0;
+    for (int i = 0; i <= l; ++i)
+      for (int j = 0; j <= i; ++j) {
+        if (n == k) {
+          int x = l - i, y = i - j, z = j;
+          return std::sqrt(dblfac(2 * l - 1) / (dblfac(2 * x - 1) * dblfac(2 * y - 1) * dblfac(2 * z - 1)));
+        }
+        ++n;
+      }
+    return 1.0;
+  };
+  /* global shells */
+  std::vector<GShell> sh;
+  std::vector<int> first_sh(d->natom + 1);
+  std::vector<double> angn;
+  int ao = 0;
+  for (int a = 0; a < d->natom; ++a) {
+    first_sh[a] = (int)sh.size();
+    int t = d->atom_t[a] - 1;
+    for (int s = 0; s < d->num_shell_atom[t]; ++s) {
+      int gs = d->map_atom2shell[t] - 1 + s;
+      GShell g{};
+      g.l = d->ang_mom[gs];
+      g.nprim = d->map_shell2prim[gs + 1] - d->map_shell2prim[gs];
+      g.prim0 = d->map_shell2prim[gs] - 1;
+      g.atom = a;
+      g.ao0 = ao;
+      for (int k = 0; k < 3; ++k) g.xyz[k] = d->coords[3 * a + k];
+      for (int k = 0; k < ncart(g.l); ++k) angn.push_back(angn_of(g.l, k));
+      ao += ncart(g.l);
+      sh.push_back(g);
+    }
+  }
+  first_sh[d->natom] = (int)sh.size();
+  h->nsh = (int)sh.size();
+  h->nao = ao;
+  /* nuclear repulsion */
+  h->enuc = 0.0;
+  for (int i = 1; i < d->natom; ++i)
+    for (int j = 0; j < i; ++j) {
+      double zij = d->nuc_charge[d->atom_t[i] - 1] * d->nuc_charge[d->atom_t[j] - 1];
+      if (std::fabs(zij) > 1e-12) {
+        double r2 = 0.0;
+        for (int k = 0; k < 3; ++k) r2 += std::pow(d->coords[3 * i + k] - d->coords[3 * j + k], 2);
+        if (r2 > 1e-5) h->enuc += zij * std::pow(r2, -0.5);
+      }
+    }
+  /* orbital basis sets */
+  std::vector<std::vector<int>> obs(norbs);
+  std::vector<std::vector<int>> slot_of_shell(norbs, std::vector<int>(h->nsh, -1));
+  std::vector<std::vector<int>> orb_atoms(norbs);
+  for (int o = 0; o < norbs; ++o) {
+    for (int k = 0; k < d->orbas_atnum[o]; ++k) {
+      int a = d->orbas_atset[k + (size_t)d->mxctr * o] - 1;
+      if (a < 0 || a >= d->natom) {
+        h->err = "orbital on a non-existent atom";
+        return VSVB_ERR_INPUT;
+      }
+      orb_atoms[o].push_back(a);
+      for (int g = first_sh[a]; g < first_sh[a + 1]; ++g) {
+        if (slot_of_shell[o][g] < 0) slot_of_shell[o][g] = (int)obs[o].size();
+        for (int c = 0; c < ncart(sh[g].l); ++c) obs[o].push_back(sh[g].ao0 + c);
+      }
+    }
+    h->maxobs = std::max(h->maxobs, (int)obs[o].size());
+  }
+  /* weight scatter terms */
+  std::vector<int> term0(norbs + 1, 0), tslot, tj, tm, tf, ndf_orb;
+  const int nfirst_ndf = norbs - d->ndf;
+  for (int f = 0; f < d->ndf; ++f) ndf_orb.push_back(nfirst_ndf + f);
+  for (int o = 0; o < norbs; ++o) {
+    term0[o] = (int)tslot.size();
+    for (int j = d->map_orbs[o] - 1; j < d->map_orbs[o + 1] - 1; ++j) {
+      int xp = d->xpset[j];
+      if (xp >= 1) {
+        if (xp > (int)obs[o].size()) {
+          h->err = "weight address outside its orbital basis set";
+          return VSVB_ERR_INPUT;
+        }
+        tslot.push_back(xp - 1);
+        tj.push_back(j);
+        tm.push_back(-1);
+        tf.push_back(-1);
+      } else {
+        if (o >= nfirst_ndf) {
+          h->err = "a derived basis function refers to another one";
+          return VSVB_ERR_INPUT;
+        }
+        int indf = xp + norbs - 1; /* 0-based orbital index of the NDF */
+        if (indf < nfirst_ndf || indf >= norbs) {
+          h->err = "bad derived-basis-function reference";
+          return VSVB_ERR_INPUT;
+        }
+        /* ndf2obs: NDF atom AO ranges, then the matching orbital atom offsets */
+        std::vector<int> beg, end, target;
+        int ib = 0;
+        for (int a : orb_atoms[indf]) {
+          beg.push_back(ib + 1);
+          for (int g = first_sh[a]; g < first_sh[a + 1]; ++g) ib += ncart(sh[g].l);
+          end.push_back(ib);
+        }
+        target.assign(orb_atoms[indf].size(), 0);
+        int ob = 1;
+        for (int a : orb_atoms[o]) {
+          for (size_t jat = 0; jat < orb_atoms[indf].size(); ++jat)
+            if (orb_atoms[indf][jat] == a) target[jat] = ob;
+          for (int g = first_sh[a]; g < first_sh[a + 1]; ++g) ob += ncart(sh[g].l);
+        }
+        int shift = 0;
+        for (int m = d->map_orbs[indf] - 1; m < d->map_orbs[indf + 1] - 1; ++m) {
+          int xm = d->xpset[m];
+          for (size_t ia = 0; ia < orb_atoms[indf].size(); ++ia)
+            if (xm >= beg[ia] && xm <= end[ia]) shift = target[ia] - beg[ia];
+          int slot = xm + shift - 1;
+          if (slot < 0 || slot >= (int)obs[o].size()) {
+            h->err = "derived basis function outside the orbital basis set";
+            return VSVB_ERR_INPUT;
+          }
+          tslot.push_back(slot);
+          tj.push_back(j);
+          tm.push_back(m);
+          tf.push_back(indf - nfirst_ndf);
+        }
+      }
+    }
+  }
+  term0[norbs] = (int)tslot.size();
+  std::vector<int> obs_n(norbs), obs_ao((size_t)norbs * std::max(h->maxobs, 1), 0);
+  for (int o = 0; o < norbs; ++o) {
+    obs_n[o] = (int)obs[o].size();
+    for (size_t k = 0; k < obs[o].size(); ++k) obs_ao[(size_t)o * h->maxobs + k] = obs[o][k];
+  }
+  /* device uploads for the one-electron stage */
+  std::vector<double> charge(d->natom), axyz(3 * d->natom);
+  for (int a = 0; a < d->natom; ++a) {
+    charge[a] = d->nuc_charge[d->atom_t[a] - 1];
+    for (int k = 0; k < 3; ++k) axyz[3 * a + k] = d->coords[3 * a + k];
+  }
+  CK(h->shells.upload(sh), "upload shells");
+  CK(h->exps.upload(std::vector<double>(d->exponent, d->exponent + d->num_pr)), "upload exps");
+  CK(h->coefs.upload(cc), "upload coefs");
+  CK(h->angn.upload(angn), "upload angn");
+  CK(h->charge.upload(charge), "upload charge");
+  CK(h->axyz.upload(axyz), "upload xyz");
+  CK(h->S_ao.alloc((size_t)h->nao * h->nao), "alloc S");
+  CK(h->H_ao.alloc((size_t)h->nao * h->nao), "alloc H");
+  {
+    Ao1eArgs a{};
+    a.shells = h->shells.p;
+    a.nshell = h->nsh;
+    a.nao = h->nao;
+    a.natom = d->natom;
+    a.exps = h->exps.p;
+    a.coefs = h->coefs.p;
+    a.angn = h->angn.p;
+    a.charge = h->charge.p;
+    a.atom_xyz = h->axyz.p;
+    a.S = h->S_ao.p;
+    a.H = h->H_ao.p;
+    int npairs = h->nsh * (h->nsh + 1) / 2;
+    ao_1e_kernel<<<(npairs + 63) / 64, 64, 0, h->st>>>(a);
+    CK(cudaGetLastError(), "ao_1e_kernel");
+  }
+  CK(h->obs_n.upload(obs_n), "upload obs");
+  CK(h->obs_ao.upload(obs_ao), "upload obs");
+  CK(h->term0.upload(term0), "upload terms");
+  CK(h->term_slot.upload(tslot), "upload terms");
+  CK(h->term_j.upload(tj), "upload terms");
+  CK(h->term_m.upload(tm), "upload terms");
+  CK(h->term_f.upload(tf), "upload terms");
+  CK(h->ndf_orb.upload(ndf_orb), "upload ndf");
+
+  /* shell pairs, orbital pairs, X terms */
+  const int nsp = h->nsp;
+  h->np = nsp * (nsp + 1) / 2;
+  std::vector<std::vector<int>> orbs_on_atom(d->natom);
+  for (int o = 0; o < nsp; ++o)
+    for (int a : orb_atoms[o])
+      if (orbs_on_atom[a].empty() || orbs_on_atom[a].back() != o) orbs_on_atom[a].push_back(o);
+  std::vector<ShellPair> pairs;
+  std::vector<PrimPair> prims;
+  std::vector<int> opid;
+  std::vector<XTerm> xterms;
+  std::vector<long long> xelem0;
+  long long nx = 0;
+  for (int A0 = 0; A0 < h->nsh; ++A0)
+    for (int B0 = 0; B0 <= A0; ++B0) {
+      int A = A0, B = B0;
+      if (sh[A].l < sh[B].l) std::swap(A, B);
+      /* orbital pairs touching (A,B) */
+      std::set<std::pair<int, int>> ops;
+      for (int i : orbs_on_atom[sh[A].atom])
+        for (int k : orbs_on_atom[sh[B].atom]) ops.insert({std::max(i, k), std::min(i, k)});
+      if (ops.empty()) continue;
+      ShellPair P{};
+      P.shA = A;
+      P.shB = B;
+      P.cls = pair_class(sh[A].l, sh[B].l);
+      P.prim0 = (int)prims.size();
+      for (int k = 0; k < 3; ++k) {
+        P.A[k] = sh[A].xyz[k];
+        P.B[k] = sh[B].xyz[k];
+      }
+      double ab2 = 0.0;
+      for (int k = 0; k < 3; ++k) ab2 += (P.A[k] - P.B[k]) * (P.A[k] - P.B[k]);
+      for (int ia = 0; ia < sh[A].nprim; ++ia)
+        for (int ib = 0; ib < sh[B].nprim; ++ib) {
+          double al = d->exponent[sh[A].prim0 + ia], be = d->exponent[sh[B].prim0 + ib];
+          double p = al + be;
+          double K = cc[sh[A].prim0 + ia] * cc[sh[B].prim0 + ib] * std::exp(-al * be / p * ab2);
+          if (std::fabs(K) < 1e-24) continue;
+          PrimPair pp{};
+          for (int k = 0; k < 3; ++k) pp.P[k] = (al * P.A[k] + be * P.B[k]) / p;
+          pp.p = p;
+          pp.K = K;
+          prims.push_back(pp);
+        }
+      P.nprim = (int)prims.size() - P.prim0;
+      if (P.nprim == 0) continue;
+      P.op0 = (int)opid.size();
+      P.nop = (int)ops.size();
+      P.x0 = (int)nx;
+      for (auto &ik : ops) {
+        int i = ik.first, k = ik.second;
+        opid.push_back(i * (i + 1) / 2 + k);
+        XTerm t{};
+        t.oi = i;
+        t.ok = k;
+        t.la = sh[A].l;
+        t.lb = sh[B].l;
+        t.sAi = slot_of_shell[i][A];
+        t.sBi = slot_of_shell[i][B];
+        t.sAk = slot_of_shell[k][A];
+        t.sBk = slot_of_shell[k][B];
+        t.aoA = sh[A].ao0;
+        t.aoB = sh[B].ao0;
+        t.same_shell = A == B;
+        xterms.push_back(t);
+        xelem0.push_back(nx);
+        nx += ncart(sh[A].l) * ncart(sh[B].l);
+      }
+      pairs.push_back(P);
+    }
+  if (nx > (long long)0x7fffffff) {
+    h->err = "weight tables exceed 2^31 elements";
+    return VSVB_ERR_UNSUPPORTED;
+  }
+  h->nxelem = nx;
+  h->nxterm = (int)xterms.size();
+  CK(h->pairs.upload(pairs), "upload pairs");
+  CK(h->prims.upload(prims), "upload prims");
+  CK(h->pair_opid.upload(opid), "upload opid");
+  CK(h->xterms.upload(xterms), "upload xterms");
+  CK(h->xelem0.upload(xelem0), "upload xelem0");
+  CK(h->xtab.alloc(std::max<long long>(nx, 1)), "alloc xtab");
+  CK(h->qmax.alloc(std::max<size_t>(pairs.size(), 1)), "alloc qmax");
+  CK(h->T.alloc(std::max<size_t>((size_t)h->np * h->np, 1)), "alloc T");
+  /* Rys tables */
+  CK(h->rys.upload(std::vector<double>(rys_table_data, rys_table_data + sizeof(rys_table_data) / sizeof(double))),
+     "upload rys");
+  if (eri_set_tables(rys_table_offset, &rys_asym_x[0][0], &rys_asym_w[0][0])) {
+    h->err = "cannot set Rys constant tables";
+    return VSVB_ERR_CUDA;
+  }
+  /* Schwarz bounds (diagonal quartets) */
+  {
+    std::vector<int2> diag[6];
+    for (size_t p = 0; p < pairs.size(); ++p) diag[pairs[p].cls].push_back(make_int2((int)p, (int)p));
+    EriArgs ea = eri_args(h);
+    DBuf<int2> wd[6];
+    for (int c = 0; c < 6; ++c) {
+      if (diag[c].empty()) continue;
+      CK(wd[c].upload(diag[c]), "upload diag");
+      if (eri_launch(1, 0, c, c, ea, wd[c].p, (int)diag[c].size(), h->nsm, h->st)) {
+        h->err = "Schwarz kernel launch failed";
+        return VSVB_ERR_CUDA;
+      }
+    }
+    std::vector<double> q(pairs.size());
+    CK(cudaStreamSynchronize(h->st), "schwarz sync");
+    if (!pairs.empty()) CK(cudaMemcpy(q.data(), h->qmax.p, sizeof(double) * q.size(), cudaMemcpyDeviceToHost), "qmax");
+    for (size_t p = 0; p < pairs.size(); ++p) pairs[p].qmax = q[p];
+    CK(h->pairs.upload(pairs), "upload pairs");
+  }
+  /* quartet schedule */
+  const bool mixed = h->opt.precision == VSVB_MIXED;
+  h->err_bound = 0.0;
+  for (size_t P = 0; P < pairs.size(); ++P)
+    for (size_t Q = 0; Q <= P; ++Q) {
+      double b = pairs[P].qmax * pairs[Q].qmax;
+      if (b < h->opt.ao_screen) continue;
+      int a = (int)P, c = (int)Q;
+      if (pairs[a].cls < pairs[c].cls) std::swap(a, c);
+      int prec = (mixed && b < h->opt.mixed_threshold) ? 1 : 0;
+      if (prec) {
+        h->nq_fp32++;
+        h->err_bound += b;
+      } else {
+        h->nq_fp64++;
+      }
+      h->work_h[prec][pairs[a].cls][pairs[c].cls].push_back(make_int2(a, c));
+    }
+  for (int p = 0; p < 2; ++p)
+    for (int a = 0; a < 6; ++a)
+      for (int c = 0; c < 6; ++c)
+        if (!h->work_h[p][a][c].empty()) CK(h->work_d[p][a][c].upload(h->work_h[p][a][c]), "upload work");
+
+  /* determinant pairs */
+  DetSetup &ds = h->ds;
+  ds.npair = d->npair;
+  ds.nunpd = d->nunpd;
+  ds.ndocc = d->ndocc;
+  ds.nelec = 2 * d->npair + 2 * d->ndocc + d->nunpd;
+  ds.nalpha = d->npair + d->nunpd + d->ndocc;
+  ds.nbeta = d->npair + d->ndocc;
+  ds.nnd = 2 * d->npair + d->nunpd;
+  ds.nsp = nsp;
+  ds.nsc = d->nspinc > 0 ? d->nspinc : 1;
+  ds.nq = (long long)ds.nsc * ds.nsc << (2 * d->npair);
+  std::vector<int> pslot((size_t)ds.nsc * d->npair * 2), spair((size_t)ds.nsc * 2 * d->npair, -1),
+      swhich((size_t)ds.nsc * 2 * d->npair, -1);
+  std::vector<double> csc(ds.nsc, 1.0);
+  for (int isc = 0; isc < ds.nsc; ++isc) {
+    if (d->nspinc > 0) csc[isc] = d->coeff_sc[isc];
+    for (int k = 0; k < d->npair; ++k)
+      for (int s = 0; s < 2; ++s) {
+        int slot = d->pair_sc[k + d->npair * (s + 2 * isc)] - 1;
+        if (slot < 0 || slot >= 2 * d->npair) {
+          h->err = "spin-coupling pair outside the coupled orbitals";
+          return VSVB_ERR_INPUT;
+        }
+        pslot[(isc * d->npair + k) * 2 + s] = slot;
+        spair[isc * 2 * d->npair + slot] = k;
+        swhich[isc * 2 * d->npair + slot] = s;
+      }
+    for (int s = 0; s < 2 * d->npair; ++s)
+      if (spair[isc * 2 * d->npair + s] < 0) {
+        h->err = "spin coupling does not cover every coupled orbital";
+        return VSVB_ERR_INPUT;
+      }
+  }
+  CK(h->pair_slot.upload(pslot.empty() ? std::vector<int>(1, 0) : pslot), "upload sc");
+  CK(h->slot_pair.upload(spair.empty() ? std::vector<int>(1, 0) : spair), "upload sc");
+  CK(h->slot_which.upload(swhich.empty() ? std::vector<int>(1, 0) : swhich), "upload sc");
+  CK(h->coeff_sc.upload(csc), "upload coeff_sc");
+  const long long nq = ds.nq;
+  const int na = ds.nalpha, nb = ds.nbeta;
+  CK(h->det_a.alloc(nq), "alloc det");
+  CK(h->det_b.alloc(nq), "alloc det");
+  CK(h->Ta.alloc(std::max<long long>(nq * na * na, 1)), "alloc Ta");
+  CK(h->Tb.alloc(std::max<long long>(nq * nb * nb, 1)), "alloc Tb");
+  CK(h->sing.alloc(nq), "alloc sing");
+  h->ld_scratch = 2 * std::max(na, nb) * std::max(std::max(na, nb), 1);
+  CK(h->scratch.alloc(std::max<long long>(nq * h->ld_scratch, 1)), "alloc scratch");
+  long long ntij = (long long)nsp * (nsp + 1) / 2;
+  h->ntasks = ntij * (ntij + 1) / 2;
+  long long work = std::max<long long>(h->ntasks, (long long)ds.nelec * ds.nelec);
+  long long want = (2LL * h->nsm + nq - 1) / nq;
+  long long maxs = (work + 127) / 128;
+  h->nsplit = (int)std::max<long long>(1, std::min(want, maxs));
+  size_t nslot = (size_t)nq * h->nsplit;
+  CK(h->part_e1.alloc(nslot), "alloc parts");
+  CK(h->part_wf.alloc(nslot), "alloc parts");
+  CK(h->part_e2.alloc(nslot), "alloc parts");
+  CK(h->result.alloc(8), "alloc result");
+  CK(h->status.alloc(1), "alloc status");
+  /* per-evaluation orbital buffers */
+  CK(h->coeff_d.alloc(h->totlen), "alloc coeff");
+  CK(h->ndf_scale.alloc(std::max(h->ndf, 1)), "alloc ndf");
+  CK(h->orb_scale.alloc(norbs), "alloc scale");
+  CK(h->Craw.alloc((size_t)norbs * h->maxobs), "alloc C");
+  CK(h->C.alloc((size_t)norbs * h->maxobs), "alloc C");
+  CK(h->So.alloc((size_t)nsp * nsp), "alloc So");
+  CK(h->Ho.alloc((size_t)nsp * nsp), "alloc Ho");
+  CK(cudaStreamSynchronize(h->st), "set-up sync");
+  return VSVB_OK;
+}
+
+int alloc_grad(vsvb_gpu *h) {
+  if (h->grad_ready) return VSVB_OK;
+  const long long nq = h->ds.nq;
+  const int na = h->ds.nalpha, nb = h->ds.nbeta;
+  CK(h->Tbar.alloc(std::max<size_t>((size_t)h->np * h->np, 1)), "alloc Tbar");
+  CK(h->Sbar.alloc((size_t)h->nsp * h->nsp), "alloc Sbar");
+  CK(h->Hbar.alloc((size_t)h->nsp * h->nsp), "alloc Hbar");
+  CK(h->xbar.alloc(std::max<long long>(h->nxelem, 1)), "alloc xbar");
+  CK(h->Cbar.alloc((size_t)h->norb_all * h->maxobs), "alloc Cbar");
+  CK(h->vtot.alloc((size_t)nq * h->nsplit), "alloc vtot");
+  CK(h->Gglob.alloc(std::max<long long>(nq * (na * na + nb * nb), 1)), "alloc G");
+  CK(h->coeff_bar.alloc(h->totlen), "alloc coeff_bar");
+  h->grad_ready = true;
+  return VSVB_OK;
+}
+
+/* forward pass on coeff_d; leaves E in result[0..4] (device) */
+int forward(vsvb_gpu *h) {
+  cudaStream_t st = h->st;
+  CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), st), "memset status");
+  OrbArgs oa = orb_args(h);
+  size_t osh = sizeof(double) * std::max(h->maxobs, 1);
+  if (h->ndf > 0) {
+    ndf_norm_kernel<<<h->ndf, 128, osh, st>>>(oa);
+    CK(cudaGetLastError(), "ndf_norm");
+  }
+  orb_norm_kernel<<<h->nsp, 128, osh, st>>>(oa);
+  CK(cudaGetLastError(), "orb_norm");
+  orb_1e_kernel<<<dim3(h->nsp, h->nsp), 128, 0, st>>>(oa, h->So.p, h->Ho.p);
+  CK(cudaGetLastError(), "orb_1e");
+  if (h->nxelem > 0) {
+    XtabArgs xa = xtab_args(h);
+    xtab_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa);
+    CK(cudaGetLastError(), "xtab");
+  }
+  CK(cudaMemsetAsync(h->T.p, 0, sizeof(double) * h->T.n, st), "memset T");
+  EriArgs ea = eri_args(h);
+  for (int p = 0; p < 2; ++p)
+    for (int a = 0; a < 6; ++a)
+      for (int c = 0; c <= a; ++c) {
+        int n = (int)h->work_h[p][a][c].size();
+        if (!n) continue;
+        if (eri_launch(0, p, a, c, ea, h->work_d[p][a][c].p, n, h->nsm, st)) {
+          h->err = "ERI kernel launch failed";
+          return VSVB_ERR_CUDA;
+        }
+      }
+  CK(cudaMemsetAsync(h->sing.p, 0, sizeof(int) * h->sing.n, st), "memset sing");
+  DetCtx dc = det_ctx(h);
+  detpair_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, h->scratch.p, h->ld_scratch);
+  CK(cudaGetLastError(), "detpair");
+  AsmArgs aa = asm_args(h);
+  CK(launch_assemble(false, dim3((unsigned)h->ds.nq, h->nsplit), 128, 0, st, dc, aa), "assemble");
+  energy_reduce_kernel<<<1, 256, 0, st>>>(aa, h->ds.nq * h->nsplit, h->ds.nelec, h->enuc, h->result.p);
+  CK(cudaGetLastError(), "reduce");
+  return VSVB_OK;
+}
+
+int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
+  double r[5];
+  int status = 0;
+  CK(cudaMemcpyAsync(r, h->result.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, h->st), "copy result");
+  CK(cudaMemcpyAsync(&status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->st), "copy status");
+  CK(cudaStreamSynchronize(h->st), "sync");
+  if (status & 1) {
+    h->err = "an orbital has non-positive self-overlap";
+    return VSVB_ERR_NOT_NORMALISABLE;
+  }
+  if (out) {
+    std::memset(out, 0, sizeof(*out));
+    out->energy = r[0];
+    out->e_num = r[1];
+    out->e1 = r[2];
+    out->e2 = r[3];
+    out->wfnorm = r[4];
+    out->enucrep = h->enuc;
+    out->n_quartets_fp64 = h->nq_fp64;
+    out->n_quartets_fp32 = h->nq_fp32;
+    out->n_tasks = h->ntasks;
+  }
+  return VSVB_OK;
+}
+
+int backward(vsvb_gpu *h, double e_num, double w) {
+  if (h->ndf > 0) {
+    h->err = "gradient through derived basis functions is not implemented";
+    return VSVB_ERR_UNSUPPORTED;
+  }
+  int rc = alloc_grad(h);
+  if (rc) return rc;
+  cudaStream_t st = h->st;
+  const int na = h->ds.nalpha, nb = h->ds.nbeta;
+  CK(cudaMemsetAsync(h->Tbar.p, 0, sizeof(double) * h->Tbar.n, st), "memset");
+  CK(cudaMemsetAsync(h->Sbar.p, 0, sizeof(double) * h->Sbar.n, st), "memset");
+  CK(cudaMemsetAsync(h->Hbar.p, 0, sizeof(double) * h->Hbar.n, st), "memset");
+  CK(cudaMemsetAsync(h->xbar.p, 0, sizeof(double) * h->xbar.n, st), "memset");
+  CK(cudaMemsetAsync(h->Cbar.p, 0, sizeof(double) * h->Cbar.n, st), "memset");
+  CK(cudaMemsetAsync(h->Gglob.p, 0, sizeof(double) * h->Gglob.n, st), "memset");
+  CK(cudaMemsetAsync(h->coeff_bar.p, 0, sizeof(double) * h->coeff_bar.n, st), "memset");
+  DetCtx dc = det_ctx(h);
+  AsmArgs aa = asm_args(h);
+  aa.status = h->status.p;
+  aa.inv_w = 1.0 / w;
+  aa.dw_coef = -e_num / (w * w * (double)h->ds.nelec);
+  size_t gsh = aa.g_in_smem ? sizeof(double) * (size_t)(na * na + nb * nb) : 0;
+  CK(launch_assemble(true, dim3((unsigned)h->ds.nq, h->nsplit), 128, gsh, st, dc, aa), "assemble grad");
+  detpair_adjoint_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, aa, h->nsplit);
+  CK(cudaGetLastError(), "detpair adjoint");
+  EriArgs ea = eri_args(h);
+  for (int p = 0; p < 2; ++p)
+    for (int a = 0; a < 6; ++a)
+      for (int c = 0; c <= a; ++c) {
+        int n = (int)h->work_h[p][a][c].size();
+        if (!n) continue;
+        if (eri_launch(2, p, a, c, ea, h->work_d[p][a][c].p, n, h->nsm, st)) {
+          h->err = "ERI adjoint launch failed";
+          return VSVB_ERR_CUDA;
+        }
+      }
+  if (h->nxelem > 0) {
+    XtabArgs xa = xtab_args(h);
+    xtab_adjoint_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa, h->xbar.p, h->Cbar.p);
+    CK(cudaGetLastError(), "xtab adjoint");
+  }
+  OrbArgs oa = orb_args(h);
+  orb_1e_adjoint_kernel<<<h->nsp, 128, 0, st>>>(oa, h->Sbar.p, h->Hbar.p, h->nsp, h->Cbar.p);
+  CK(cudaGetLastError(), "orb_1e adjoint");
+  orb_norm_adjoint_kernel<<<h->nsp, 128, sizeof(double) * std::max(h->maxobs, 1), st>>>(oa, h->Cbar.p,
+                                                                                     h->coeff_bar.p);
+  CK(cudaGetLastError(), "orb_norm adjoint");
+  return VSVB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void vsvb_default_options(vsvb_options *o) {
+  if (!o) return;
+  o->precision = VSVB_FP64;
+  o->mixed_threshold = 1e-6;
+  o->ao_screen = 1e-15;
+  o->device = 0;
+}
+
+int vsvb_gpu_create(const vsvb_system_desc *d, const vsvb_options *opt, vsvb_gpu **out) {
+  if (!d || !out) return VSVB_ERR_INPUT;
+  *out = nullptr;
+  auto *h = new vsvb_gpu();
+  vsvb_default_options(&h->opt);
+  if (opt) h->opt = *opt;
+  h->dev = h->opt.device;
+  int rc = build(h, d);
+  *out = h;
+  return rc;
+}
+
+void vsvb_gpu_destroy(vsvb_gpu *h) {
+  if (!h) return;
+  cudaSetDevice(h->dev);
+  if (h->st) cudaStreamSynchronize(h->st);
+  cudaStream_t st = h->st;
+  delete h;
+  if (st) cudaStreamDestroy(st);
+}
+
+const char *vsvb_gpu_last_error(const vsvb_gpu *h) { return h ? h->err.c_str() : "null handle"; }
+
+int vsvb_gpu_totlen(const vsvb_gpu *h) { return h ? h->totlen : -1; }
+int vsvb_gpu_num_orbitals(const vsvb_gpu *h) { return h ? h->nsp : -1; }
+
+int vsvb_gpu_energy_device(vsvb_gpu *h, const double *coeff_dev, vsvb_energy_result *out) {
+  if (!h) return VSVB_ERR_INPUT;
+  CK(cudaSetDevice(h->dev), "cudaSetDevice");
+  CK(cudaMemcpyAsync(h->coeff_d.p, coeff_dev, sizeof(double) * h->totlen, cudaMemcpyDeviceToDevice, h->st), "copy coeff");
+  int rc = forward(h);
+  if (rc) return rc;
+  return finish_result(h, out);
+}
+
+int vsvb_gpu_energy(vsvb_gpu *h, const double *coeff, vsvb_energy_result *out) {
+  if (!h) return VSVB_ERR_INPUT;
+  CK(cudaSetDevice(h->dev), "cudaSetDevice");
+  const double *src = coeff ? coeff : h->coeff0.data();
+  CK(cudaMemcpyAsync(h->coeff_d.p, src, sizeof(double) * h->totlen, cudaMemcpyHostToDevice, h->st), "copy coeff");
+  int rc = forward(h);
+  if (rc) return rc;
+  return finish_result(h, out);
+}
+
+static int energy_grad_common(vsvb_gpu *h, vsvb_energy_result *out, double *grad, bool grad_on_device) {
+  int rc = forward(h);
+  if (rc) return rc;
+  vsvb_energy_result r;
+  rc = finish_result(h, &r);
+  if (rc) return rc;
+  rc = backward(h, r.e_num, r.wfnorm);
+  if (rc) return rc;
+  int status = 0;
+  CK(cudaMemcpyAsync(&status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->st), "status");
+  CK(cudaMemcpyAsync(grad, h->coeff_bar.p, sizeof(double) * h->totlen,
+                     grad_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->st),
+     "copy grad");
+  CK(cudaStreamSynchronize(h->st), "sync");
+  if (status & 2) {
+    h->err = "gradient through a singular determinant pair is not implemented";
+    return VSVB_ERR_SINGULAR;
+  }
+  if (out) *out = r;
+  return VSVB_OK;
+}
+
+int vsvb_gpu_energy_grad(vsvb_gpu *h, const double *coeff, vsvb_energy_result *out, double *grad) {
+  if (!h || !grad) return VSVB_ERR_INPUT;
+  CK(cudaSetDevice(h->dev), "cudaSetDevice");
+  const double *src = coeff ? coeff : h->coeff0.data();
+  CK(cudaMemcpyAsync(h->coeff_d.p, src, sizeof(double) * h->totlen, cudaMemcpyHostToDevice, h->st), "copy coeff");
+  return energy_grad_common(h, out, grad, false);
+}
+
+int vsvb_gpu_energy_grad_device(vsvb_gpu *h, const double *coeff_dev, vsvb_energy_result *out, double *grad_dev) {
+  if (!h || !grad_dev) return VSVB_ERR_INPUT;
+  CK(cudaSetDevice(h->dev), "cudaSetDevice");
+  CK(cudaMemcpyAsync(h->coeff_d.p, coeff_dev, sizeof(double) * h->totlen, cudaMemcpyDeviceToDevice, h->st), "copy coeff");
+  return energy_grad_common(h, out, grad_dev, true);
+}
+
+int vsvb_gpu_batch_energy_grad(vsvb_gpu *const *hs, int n, const double *const *weights, vsvb_energy_result *res,
+                               double *const *grads) {
+  for (int i = 0; i < n; ++i) {
+    int rc = grads ? vsvb_gpu_energy_grad(hs[i], weights ? weights[i] : nullptr, res ? &res[i] : nullptr, grads[i])
+                   : vsvb_gpu_energy(hs[i], weights ? weights[i] : nullptr, res ? &res[i] : nullptr);
+    if (rc) return rc;
+  }
+  return VSVB_OK;
+}
+
+int vsvb_gpu_debug_orbital_eri(vsvb_gpu *h, double *out, size_t cap) {
+  if (!h) return -VSVB_ERR_INPUT;
+  size_t n = (size_t)h->np * h->np;
+  if (cap < n) return -VSVB_ERR_INPUT;
+  if (cudaMemcpy(out, h->T.p, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return -VSVB_ERR_CUDA;
+  return h->np;
+}
+
+int vsvb_gpu_debug_orbital_1e(vsvb_gpu *h, double *s, double *hc, size_t cap) {
+  if (!h) return -VSVB_ERR_INPUT;
+  size_t n = (size_t)h->nsp * h->nsp;
+  if (cap < n) return -VSVB_ERR_INPUT;
+  if (cudaMemcpy(s, h->So.p, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return -VSVB_ERR_CUDA;
+  if (cudaMemcpy(hc, h->Ho.p, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return -VSVB_ERR_CUDA;
+  return h->nsp;
+}
+
+}  /* extern "C" */

@@ -1,0 +1,67 @@
+/*
+ * vsvb_internal.h -- device data layout of the GB300 VSVB energy path.
+ *
+ * HBM layout (all per handle, built once by vsvb_gpu_create unless noted):
+ *   shells      GShell[nshell]       global Cartesian shells (atom-ordered)
+ *   prims       PrimPair[nprimpair]  primitive pairs of every kept shell pair
+ *   pairs       ShellPair[npair]     unique shell pairs (A>=B), first shell has
+ *                                    the higher angular momentum
+ *   pair_ops    int[]                orbital pairs (i,k) touching each shell pair
+ *   xtab        double[]             per evaluation: X_op(a,b) = angn_a angn_b
+ *                                    (C_i(a) C_k(b) + C_k(a) C_i(b)) on that pair
+ *   work        int2[] per class     screened shell-quartet schedule
+ *   S_ao,H_ao   double[nao*nao]      AO overlap and core Hamiltonian
+ *   C_obs       double[norb*maxobs]  per evaluation: normalised orbital weights
+ *   T           double[np*np]        per evaluation: orbital-pair ERIs
+ *                                    (i k | j l), np = n(n+1)/2
+ *   det data    per determinant pair q: det, inverse (n x n) per spin
+ */
+#ifndef VSVB_INTERNAL_H
+#define VSVB_INTERNAL_H
+
+#include <cstdint>
+
+#define VSVB_LMAX 2     /* highest angular momentum on the GPU */
+#define VSVB_NCLS 6     /* shell-pair classes (la>=lb): 00 10 11 20 21 22 */
+#define VSVB_MAXN 32    /* largest spin block handled by the exact-minor path */
+
+struct GShell {
+  int l, nprim, prim0, atom; /* prim0 indexes the global exponent/coef arrays */
+  int ao0;                   /* first global AO (Cartesian) function */
+  int pad;
+  double xyz[3];
+};
+
+struct PrimPair {
+  double P[3];
+  double p;   /* alpha + beta */
+  double K;   /* c_a c_b exp(-alpha beta / p |AB|^2) */
+  double pad;
+};
+
+struct ShellPair {
+  int shA, shB;      /* global shells; l(shA) >= l(shB) */
+  int cls;           /* pair class 0..5 */
+  int prim0, nprim;  /* into prims */
+  int op0, nop;      /* into pair_ops / orbital-pair lists */
+  int x0;            /* into xtab: nop * n_a * n_b doubles */
+  double A[3], B[3];
+  double qmax;       /* sqrt(max (ab|ab)) */
+  double pad;
+};
+
+/* one orbital-pair term of a shell pair: orbital i on shell A, k on shell B
+ * (or the reverse), flattened for the X-table kernel */
+struct PairOp {
+  int op;       /* global orbital-pair index i*(i+1)/2+k, i>=k */
+  int oi, ok;   /* orbitals (0-based) */
+  int pad;
+};
+
+struct DetSetup {
+  int nelec, nalpha, nbeta, npair, nunpd, ndocc, nnd, nsp;
+  int nsc;          /* number of spin couplings used (>=1) */
+  long long nq;     /* determinant pairs */
+};
+
+#endif
