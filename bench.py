@@ -1,0 +1,287 @@
+"""Benchmark: VSVB energy+gradient evaluations per second on one GB300.
+
+Workload (default): the spin-coupled C/H chain -- 8 atoms alternating Z=6/1
+at 1.1 A, 4 Rumer-coupled pairs (16 determinants per side, 256 determinant
+pairs) + 8 DOCC, s/p/d basis of 104 Cartesian functions, 3-6 primitives per
+shell; seeded synthetic weights (valence_gb300.configs.ch_chain, seed 2).
+A step is one energy + adjoint gradient with respect to all 416 orbital
+weights.  The headline value uses the mixed path (FP32 for shell quartets
+whose Schwarz bound is below 1e-6, FP64 elsewhere); the plain FP64 path is
+timed beside it and |dE| between them is reported.
+
+  value          device-resident weights (vsvb_gpu_energy_grad_device)
+  e2e            public host API (vsvb_gpu_energy_grad): pinned host weights
+                 copied in and the energy + gradient copied out every step
+  roofline       dominant ERI class launch: algorithmic FLOPs / its CUDA-event
+                 time against the FP64 or FP32 FMA rate measured on this
+                 device by vsvb_gpu_fma_peak (MEASURED_PEAKS.json carries only
+                 HBM and bf16 figures)
+  cpu_baseline   the CPU oracle (a literal C restatement of the reference,
+                 energy only -- the reference has no gradient) on all host
+                 cores, one full evaluation
+
+--impl reference times that CPU restatement on the same workload and prints
+the same metric (energy evaluations per second).
+Multi-GPU (torchrun): independent replicas, one per rank ("weak" scaling);
+the path needs no collective.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "VSVB energy+grad evals/s, mixed vs plain FP64 on 1 GB300 at |ΔE|<=1e-6 Eh"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ch_chain")
+    ap.add_argument("--mixed-threshold", type=float, default=1e-6)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def _workload(name, d):
+    from valence_gb300 import configs
+    return configs.WORKLOADS[name](os.path.join(d, name + ".inp"))
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.lines = []
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for ln in self.p.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _oracle_energy_time(path, nthreads):
+    """One full CPU-oracle energy evaluation (literal restatement of the
+    reference) with nthreads host threads; returns seconds."""
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    exe = os.path.join(ROOT, "oracle", "_build", "vsvb_oracle")
+    t = time.perf_counter()
+    out = subprocess.run([exe, path, str(nthreads)], capture_output=True, text=True, check=True).stdout
+    dt = time.perf_counter() - t
+    e = float([ln for ln in out.splitlines() if "guess energy" in ln][0].split()[2])
+    return dt, e
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    steps = max(1, min(a.steps, 3))
+    with tempfile.TemporaryDirectory() as d:
+        path = _workload(a.workload, d)
+        times = []
+        for _ in range(steps):
+            dt, e = _oracle_energy_time(path, cores)
+            times.append(dt)
+    v = 1.0 / statistics.mean(times)
+    sample = (f"{steps} full energy evaluation(s) of the {a.workload} workload by the CPU oracle "
+              f"(literal C restatement of valence.F90's guess energy with cached AO shell-quartet blocks; "
+              f"energy only, the reference has no gradient); steps capped at 3")
+    print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world,
+                      "steps": steps, "warmup": 0, "ms_per_step": 1e3 * statistics.mean(times),
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic", "config": {"workload": a.workload, "seed": 2},
+                      "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
+                                       "sample": sample},
+                      "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def run_ours(a, rank, world):
+    import numpy as np
+    import torch
+
+    import valence_gb300 as vg
+    from valence_gb300 import api
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 126 MB L2
+
+    with tempfile.TemporaryDirectory() as d:
+        path = _workload(a.workload, d)
+        s64 = vg.System(path, precision=vg.FP64, device=dev)
+        smx = vg.System(path, precision=vg.MIXED, mixed_threshold=a.mixed_threshold, device=dev)
+    n = s64.totlen
+    w_dev = torch.from_numpy(s64.coeff0.copy()).to("cuda")
+    g_dev = torch.zeros(n, dtype=torch.float64, device="cuda")
+    w_pin = torch.from_numpy(s64.coeff0.copy()).pin_memory()
+    g_pin = torch.zeros(n, dtype=torch.float64).pin_memory()
+    for s in (s64, smx):
+        s.set_stream(stream.cuda_stream)
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        ms, launches, last = [], 0, None
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            last = fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            launches += last["n_kernel_launches"]
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        return ms, launches, last
+
+    dev_step = lambda s: (lambda: s.energy_grad_device(w_dev.data_ptr(), g_dev.data_ptr()))
+
+    def host_step(s):
+        def f():
+            r = api.Result()
+            rc = api.lib().vsvb_gpu_energy_grad(s._h, w_pin.numpy().ctypes.data_as(api.ctypes.POINTER(api.ctypes.c_double)),
+                                                api.ctypes.byref(r),
+                                                g_pin.numpy().ctypes.data_as(api.ctypes.POINTER(api.ctypes.c_double)))
+            if rc:
+                raise api.VSVBError(api.lib().vsvb_gpu_last_error(s._h).decode())
+            return r.as_dict()
+        return f
+
+    clk = Clocks(dev)
+    clk.start()
+    ms_mx, launches_mx, r_mx = timed(dev_step(smx), a.steps, a.warmup)
+    clocks = clk.stop()
+    ms_64, _, r_64 = timed(dev_step(s64), a.steps, a.warmup)
+    ms_e2e, _, r_e2e = timed(host_step(smx), a.steps, a.warmup)
+
+    def agg(ms):
+        t = torch.tensor([sum(ms)], dtype=torch.float64, device="cuda")
+        if world > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return t.item()
+
+    t_mx, t_64, t_e2e = agg(ms_mx), agg(ms_64), agg(ms_e2e)
+    value = world * a.steps / (t_mx * 1e-3)
+    v64 = world * a.steps / (t_64 * 1e-3)
+    ve2e = world * a.steps / (t_e2e * 1e-3)
+    dE = abs(r_mx["energy"] - r_64["energy"])
+
+    if rank != 0:
+        return
+    # roofline of the dominant ERI launch of the headline (mixed) run
+    fp64_peak, fp32_peak = api.fma_peak(dev)
+    prof = smx.eri_profile()
+    prof.sort(key=lambda x: -x["ms"])
+    top = prof[0]
+    prec = "fp32" if top["cls"] >= 100 else "fp64"
+    peak = fp32_peak if prec == "fp32" else fp64_peak
+    achieved = top["flops"] / (top["ms"] * 1e-3)
+    eri_total_ms = sum(x["ms"] for x in prof)
+    roofline = {"bound": prec + "_pipe", "kernel": f"eri_kernel class {top['cls']:03d} ({prec})",
+                "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": None, "share_of_eri_pass": top["ms"] / eri_total_ms,
+                "peak_source": "measured on this device by vsvb_gpu_fma_peak (FMA chain kernel)",
+                "fp64_peak_tflops": fp64_peak / 1e12, "fp32_peak_tflops": fp32_peak / 1e12}
+    cpu = None
+    if world == 1 and not a.no_cpu_baseline:
+        with tempfile.TemporaryDirectory() as d:
+            path = _workload(a.workload, d)
+            cores = os.cpu_count() or 1
+            dt, e_cpu = _oracle_energy_time(path, cores)
+        cpu = {"value": 1.0 / dt, "unit": "evals/s", "cores": cores, "kind": "port",
+               "sample": "one full energy evaluation of the same workload by the CPU oracle (literal C restatement "
+                         "of valence.F90, cached AO blocks); energy only -- the reference has no gradient",
+               "dE_vs_gpu_fp64": abs(e_cpu - r_64["energy"])}
+    nq = r_mx["n_quartets_fp64"] + r_mx["n_quartets_fp32"]
+    out = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": t_mx / a.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64+f32 (Schwarz-split)", "data": "synthetic",
+           "config": {"workload": a.workload, "seed": 2, "atoms": 8, "functions": 104, "coupled_pairs": 4,
+                      "docc": 8, "determinant_pairs": 256, "weights": n, "mixed_threshold": a.mixed_threshold,
+                      "l2": "flushed (256 MB write) between timed steps", "replicas": world},
+           "fp64": {"value": v64, "unit": "evals/s", "ms_per_step": t_64 / a.steps},
+           "mixed_over_fp64": value / v64, "abs_dE_mixed_vs_fp64": dE, "energy_fp64": r_64["energy"],
+           "quartets": {"fp64": r_mx["n_quartets_fp64"], "fp32": r_mx["n_quartets_fp32"], "total": nq},
+           "e2e": {"value": ve2e, "unit": "evals/s", "h2d_bytes_per_step": 8 * n,
+                   "d2h_bytes_per_step": 8 * n + 5 * 8 + 2 * 4},
+           "gpu_launches": launches_mx, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks}
+    print(json.dumps(out))
+
+
+def main():
+    a = _args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if a.impl == "ours" else "gloo")
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+    else:
+        run_ours(a, rank, world)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -100,6 +100,7 @@ typedef struct vsvb_energy_result {
   long long n_quartets_fp64, n_quartets_fp32; /* AO shell quartets evaluated */
   long long n_tasks;                           /* orbital-quartet tasks (valence.F90:1153-1157) */
   int n_singular_pairs;                        /* determinant pairs on the exact-minor path */
+  int n_kernel_launches;                       /* kernels this call enqueued */
 } vsvb_energy_result;
 
 typedef struct vsvb_gpu vsvb_gpu;
@@ -142,6 +143,23 @@ int vsvb_gpu_energy_grad_device(vsvb_gpu *h, const double *coeff_dev, vsvb_energ
  * are host arrays of handle i's totlen (grads may be NULL for energy only). */
 int vsvb_gpu_batch_energy_grad(vsvb_gpu *const *handles, int n, const double *const *weights,
                                vsvb_energy_result *results, double *const *grads);
+
+/* Run the handle's work on a caller-owned stream (a cudaStream_t passed as
+ * void*; NULL restores the handle's own stream).  Lets a host time calls with
+ * CUDA events on the stream the kernels are launched on. */
+int vsvb_gpu_set_stream(vsvb_gpu *h, void *stream);
+
+/* Diagnostics for roofline reporting: run the forward ERI pass once with a
+ * CUDA event pair around every class launch.  Per launch i (up to cap):
+ * ms[i] its duration, flops[i] its algorithmic FLOP count (Rys roots, 2D
+ * tables, component sums and the orbital-pair transform, counted per
+ * primitive quartet / shell quartet), cls[i] = 100*prec + 10*bra + ket.
+ * Returns the number of launches or a negative status. */
+int vsvb_gpu_eri_profile(vsvb_gpu *h, double *ms, double *flops, int *cls, int cap);
+
+/* Measured FP64 and FP32 FMA throughput of this device in FLOP/s (a dependent
+ * FMA chain kernel sized to fill every SM), for roofline denominators. */
+int vsvb_gpu_fma_peak(int device, double *fp64_flops, double *fp32_flops);
 
 /* Sizes of a handle (for bindings). */
 int vsvb_gpu_totlen(const vsvb_gpu *h);

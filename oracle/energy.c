@@ -933,6 +933,18 @@ static vo_state *state_new(vo_input *in) {
   return st;
 }
 
+static long long g_task_stride = 1;
+
+/* Timing aid for the CPU baseline: only every stride-th 2e task is evaluated
+ * (the others are skipped), so a bounded sample of the reference's task list
+ * can be timed and the full cost extrapolated.  stride = 1 is the full run. */
+int vo_guess_energy_sampled(vo_input *in, vo_result *res, int nthreads, long long stride) {
+  g_task_stride = stride > 0 ? stride : 1;
+  int rc = vo_guess_energy(in, res, nthreads);
+  g_task_stride = 1;
+  return rc;
+}
+
 int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
   memset(res, 0, sizeof(*res));
   if (g_last_state) {
@@ -993,33 +1005,74 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
       A2(st->wdet, nelec, i, j) = c0->sint;
       A2(st->wdet, nelec, j, i) = c0->sint;
     }
-  /* schwarz_ints (valence.F90:1489-1523) */
+  /* schwarz_ints (valence.F90:1489-1523); the pairs are independent, so
+   * they are spread over threads like the reference spreads them over ranks
+   * (:1509-1520) */
   int nsp = st->nsp;
-  for (int i = 1; i <= nsp; ++i)
-    for (int j = 1; j <= i; ++j) {
-      int ie = i > nnd ? 2 * i - nnd : i;
-      int je = j > nnd ? 2 * j - nnd : j;
-      int2e(c0, st->bra[ie], st->ket[je], st->bra[ie], st->ket[je]);
-      st->schwarz[indx(i, j)] = sqrt(c0->gint);
+  int nth = 1;
+#ifdef _OPENMP
+  nth = nthreads > 0 ? nthreads : omp_get_max_threads();
+#endif
+  {
+    long long npairs = ((long long)nsp * nsp + nsp) / 2;
+#pragma omp parallel num_threads(nth)
+    {
+      vo_ctx *cx = ctx_new(st);
+#pragma omp for schedule(dynamic, 1)
+      for (long long t = 0; t < npairs; ++t) {
+        int i, j;
+        long long ii = (long long)sqrt((double)(2 * (t + 1)));
+        while ((ii * ii + ii) / 2 < t + 1) ii++;
+        i = (int)ii;
+        j = (int)(t + 1 - (ii * ii - ii) / 2);
+        int ie = i > nnd ? 2 * i - nnd : i;
+        int je = j > nnd ? 2 * j - nnd : j;
+        int2e(cx, st->bra[ie], st->ket[je], st->bra[ie], st->ket[je]);
+        st->schwarz[indx(i, j)] = sqrt(cx->gint);
+      }
+      ctx_free(cx);
     }
+  }
   /* vsvb_energy (valence.F90:1010-1434), iorb=0, spinav=.false.,
    * ijkl symmetry enabled */
   state_setup_docc_un(st, c0);
   double energy = 0.0, wfnorm = 0.0;
-  for (int i = 1; i <= nelec; ++i) {
-    int i_docc = i > nnd;
-    for (int j = 1; j <= nelec; ++j) {
-      int j_docc = j > nnd;
-      if (i_docc && j_docc && (i % 2) != (j % 2)) continue;
-      ovint(c0, st->bra[i], st->ket[j]);
-      int1e(c0, st->bra[i], st->ket[j]);
-      c0->dme_b[1] = i;
-      c0->dme_k[1] = j;
-      double d1 = 0.0, dummy = 0.0;
-      density(c0, 1, &d1, &dummy, 1, 0);
-      wfnorm += c0->sint * d1;
-      energy += c0->hint * d1;
+  {
+    /* one-electron loop (valence.F90:1072-1101), spread over threads with
+     * per-thread partial sums added in thread order */
+    double *pe = (double *)calloc(nth, sizeof(double)), *pw = (double *)calloc(nth, sizeof(double));
+#pragma omp parallel num_threads(nth)
+    {
+      int tid = 0;
+#ifdef _OPENMP
+      tid = omp_get_thread_num();
+#endif
+      vo_ctx *cx = ctx_new(st);
+      double le = 0.0, lw = 0.0;
+#pragma omp for schedule(dynamic, 1)
+      for (int t = 0; t < nelec * nelec; ++t) {
+        int i = t / nelec + 1, j = t % nelec + 1;
+        int i_docc = i > nnd, j_docc = j > nnd;
+        if (i_docc && j_docc && (i % 2) != (j % 2)) continue;
+        ovint(cx, st->bra[i], st->ket[j]);
+        int1e(cx, st->bra[i], st->ket[j]);
+        cx->dme_b[1] = i;
+        cx->dme_k[1] = j;
+        double d1 = 0.0, dummy = 0.0;
+        density(cx, 1, &d1, &dummy, 1, 0);
+        lw += cx->sint * d1;
+        le += cx->hint * d1;
+      }
+      pe[tid] = le;
+      pw[tid] = lw;
+      ctx_free(cx);
     }
+    for (int t = 0; t < nth; ++t) {
+      energy += pe[t];
+      wfnorm += pw[t];
+    }
+    free(pe);
+    free(pw);
   }
   wfnorm /= (double)nelec;
   res->e1 = energy;
@@ -1027,10 +1080,6 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
   long long ntasks = (ntij * ntij + ntij) / 2;
   res->ntasks = ntasks;
   double itol = in->itol;
-  int nth = 1;
-#ifdef _OPENMP
-  nth = nthreads > 0 ? nthreads : omp_get_max_threads();
-#endif
   double *part = (double *)calloc(nth, sizeof(double));
   long long *pcount = (long long *)calloc(nth, sizeof(long long));
 #pragma omp parallel num_threads(nth)
@@ -1043,6 +1092,7 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
     double esum = 0.0;
 #pragma omp for schedule(dynamic, 16)
     for (long long task = 0; task < ntasks; ++task) {
+      if (g_task_stride > 1 && task % g_task_stride) continue;
       int ijorb, klorb, io, jo, ko, lo;
       xm_dtriang(1 + task, &ijorb, &klorb);
       xm_dtriang(ijorb, &io, &jo);

@@ -91,6 +91,9 @@ typedef struct vo_result {
 
 /* Literal guess energy (valence.F90:309-345). nthreads<=0: OpenMP default. */
 int vo_guess_energy(vo_input *in, vo_result *res, int nthreads);
+/* Same with only every stride-th two-electron task evaluated (CPU-baseline
+ * timing on a bounded sample; the energy is then not the full energy). */
+int vo_guess_energy_sampled(vo_input *in, vo_result *res, int nthreads, long long stride);
 
 /* Orbital-level integrals after vo_guess_energy's normalisation:
  * (io ko | jo lo) over the screened LCAO weights (1-based orbitals). */

@@ -36,6 +36,8 @@ def lib():
         _lib.vo_int1e.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         _lib.vo_int1e.restype = ctypes.c_double
         _lib.vo_boys.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+        _lib.vo_guess_energy_sampled.argtypes = [ctypes.c_void_p, ctypes.POINTER(VoResult), ctypes.c_int,
+                                                 ctypes.c_longlong]
     return _lib
 
 
@@ -64,6 +66,11 @@ class Oracle:
     def guess_energy(self, nthreads=0):
         r = VoResult()
         lib().vo_guess_energy(self.h, ctypes.byref(r), nthreads)
+        return r
+
+    def guess_energy_sampled(self, nthreads=0, stride=1):
+        r = VoResult()
+        lib().vo_guess_energy_sampled(self.h, ctypes.byref(r), nthreads, stride)
         return r
 
     def int2e(self, io, ko, jo, lo):

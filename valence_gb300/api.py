@@ -55,7 +55,7 @@ class Result(ctypes.Structure):
                 ("e2", ctypes.c_double), ("wfnorm", ctypes.c_double), ("enucrep", ctypes.c_double),
                 ("err_est", ctypes.c_double), ("n_quartets_fp64", ctypes.c_longlong),
                 ("n_quartets_fp32", ctypes.c_longlong), ("n_tasks", ctypes.c_longlong),
-                ("n_singular_pairs", ctypes.c_int)]
+                ("n_singular_pairs", ctypes.c_int), ("n_kernel_launches", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -85,6 +85,9 @@ def lib():
         L.vsvb_gpu_debug_orbital_eri.argtypes = [ctypes.c_void_p, P(D), ctypes.c_size_t]
         L.vsvb_gpu_debug_orbital_1e.argtypes = [ctypes.c_void_p, P(D), P(D), ctypes.c_size_t]
         L.vsvb_gpu_batch_energy_grad.argtypes = [P(ctypes.c_void_p), I, P(P(D)), P(Result), P(P(D))]
+        L.vsvb_gpu_set_stream.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.vsvb_gpu_eri_profile.argtypes = [ctypes.c_void_p, P(D), P(D), P(I), I]
+        L.vsvb_gpu_fma_peak.argtypes = [I, P(D), P(D)]
         _LIB = L
     return _LIB
 
@@ -178,6 +181,21 @@ class System:
                                                       ctypes.c_void_p(grad_ptr)), "energy_grad")
         return r.as_dict()
 
+    def set_stream(self, stream_ptr):
+        """Enqueue this system's work on a caller-owned CUDA stream (an int
+        cudaStream_t, e.g. torch.cuda.current_stream().cuda_stream; 0 restores
+        the handle's own stream)."""
+        self._check(lib().vsvb_gpu_set_stream(self._h, ctypes.c_void_p(stream_ptr or None)), "set_stream")
+
+    def eri_profile(self, cap=128):
+        ms = np.zeros(cap)
+        fl = np.zeros(cap)
+        cl = np.zeros(cap, dtype=np.int32)
+        n = lib().vsvb_gpu_eri_profile(self._h, _dptr(ms), _dptr(fl), cl.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), cap)
+        if n < 0:
+            raise VSVBError("eri_profile failed")
+        return [dict(cls=int(cl[i]), ms=float(ms[i]), flops=float(fl[i])) for i in range(n)]
+
     def orbital_eri(self):
         n = lib().vsvb_gpu_num_orbitals(self._h)
         np_ = n * (n + 1) // 2
@@ -211,6 +229,14 @@ def batch_energy_grad(systems, weights=None, with_grad=True):
     if rc:
         raise VSVBError(f"batch failed ({rc}): {lib().vsvb_gpu_last_error(systems[0]._h).decode()}")
     return [r.as_dict() for r in res], grads
+
+
+def fma_peak(device=0):
+    """Measured FP64 and FP32 FMA throughput (FLOP/s) of the device."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    if lib().vsvb_gpu_fma_peak(device, ctypes.byref(a), ctypes.byref(b)):
+        raise VSVBError("fma_peak failed")
+    return a.value, b.value
 
 
 # --- reference-shaped API ---------------------------------------------------

@@ -410,6 +410,25 @@ int dispatch(int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cu
 
 }  // namespace
 
+/* algorithmic FLOPs of one shell quartet of class (cp, cq) in this
+ * formulation: per primitive quartet the n_r roots (two 12-term Clenshaw sums
+ * each), the 3 n_r 2D tables (recurrence + transfers) and the component sums
+ * (3 flops per component and root); per quartet the two transform GEMVs. */
+double eri_flops(int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ) {
+  static const int la_[6] = {0, 1, 1, 2, 2, 2}, lb_[6] = {0, 0, 1, 0, 1, 2};
+  int la = la_[cp], lb = lb_[cp], lc = la_[cq], ld = lb_[cq];
+  auto nc = [](int l) { return (l + 1) * (l + 2) / 2; };
+  int nab = nc(la) * nc(lb), ncd = nc(lc) * nc(ld), ncomp = nab * ncd;
+  int nr = (la + lb + lc + ld) / 2 + 1;
+  int n2d = (la + 1) * (lb + 1) * (lc + 1) * (ld + 1);
+  double roots = nr * 2.0 * 24.0;
+  double twod = 3.0 * nr * (5.0 * (la + lb + 1) * (lc + ld + 1) + 2.0 * n2d);
+  double comp = 3.0 * nr * (double)ncomp;
+  double prim = 30.0 + roots + twod + comp;
+  double tr = 2.0 * nopQ * (double)nab * ncd + 2.0 * nopP * (double)nopQ * nab;
+  return (double)nprimP * nprimQ * prim + tr;
+}
+
 int eri_set_tables(const int *off, const double *ax, const double *aw) {
   if (cudaMemcpyToSymbol(c_rys_off, off, sizeof(int) * 5) != cudaSuccess) return 1;
   if (cudaMemcpyToSymbol(c_rys_ax, ax, sizeof(double) * 25) != cudaSuccess) return 1;

@@ -21,5 +21,6 @@ struct EriArgs {
 /* cp >= cq are pair classes 0..5; mode 0 forward, 1 Schwarz, 2 adjoint. */
 int eri_launch(int mode, int fp32, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int nsm,
                cudaStream_t st);
+double eri_flops(int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ);
 int eri_set_tables(const int *off, const double *ax, const double *aw);
 #endif

@@ -78,7 +78,9 @@ struct vsvb_gpu {
   vsvb_options opt;
   std::string err;
   int dev = 0, nsm = 152;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;     /* stream in use */
+  cudaStream_t own_st = nullptr; /* the handle's own stream */
+  int launches = 0;              /* kernels enqueued by the current call */
   /* dims */
   int natom = 0, nsh = 0, nao = 0, norb_all = 0, nsp = 0, ndf = 0, totlen = 0, maxobs = 0, np = 0;
   DetSetup ds{};
@@ -237,7 +239,8 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   cudaDeviceProp prop;
   CK(cudaGetDeviceProperties(&prop, h->dev), "cudaGetDeviceProperties");
   h->nsm = prop.multiProcessorCount;
-  CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking), "cudaStreamCreate");
+  CK(cudaStreamCreateWithFlags(&h->own_st, cudaStreamNonBlocking), "cudaStreamCreate");
+  h->st = h->own_st;
 
   const int norbs = 2 * d->npair + d->nunpd + d->ndocc + d->ndf;
   h->natom = d->natom;
@@ -661,21 +664,25 @@ int alloc_grad(vsvb_gpu *h) {
 /* forward pass on coeff_d; leaves E in result[0..4] (device) */
 int forward(vsvb_gpu *h) {
   cudaStream_t st = h->st;
+  h->launches = 0;
   CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), st), "memset status");
   OrbArgs oa = orb_args(h);
   size_t osh = sizeof(double) * std::max(h->maxobs, 1);
   if (h->ndf > 0) {
     ndf_norm_kernel<<<h->ndf, 128, osh, st>>>(oa);
     CK(cudaGetLastError(), "ndf_norm");
+    h->launches++;
   }
   orb_norm_kernel<<<h->nsp, 128, osh, st>>>(oa);
   CK(cudaGetLastError(), "orb_norm");
   orb_1e_kernel<<<dim3(h->nsp, h->nsp), 128, 0, st>>>(oa, h->So.p, h->Ho.p);
   CK(cudaGetLastError(), "orb_1e");
+  h->launches += 2;
   if (h->nxelem > 0) {
     XtabArgs xa = xtab_args(h);
     xtab_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa);
     CK(cudaGetLastError(), "xtab");
+    h->launches++;
   }
   CK(cudaMemsetAsync(h->T.p, 0, sizeof(double) * h->T.n, st), "memset T");
   EriArgs ea = eri_args(h);
@@ -688,6 +695,7 @@ int forward(vsvb_gpu *h) {
           h->err = "ERI kernel launch failed";
           return VSVB_ERR_CUDA;
         }
+        h->launches++;
       }
   CK(cudaMemsetAsync(h->sing.p, 0, sizeof(int) * h->sing.n, st), "memset sing");
   DetCtx dc = det_ctx(h);
@@ -697,6 +705,7 @@ int forward(vsvb_gpu *h) {
   CK(launch_assemble(false, dim3((unsigned)h->ds.nq, h->nsplit), 128, 0, st, dc, aa), "assemble");
   energy_reduce_kernel<<<1, 256, 0, st>>>(aa, h->ds.nq * h->nsplit, h->ds.nelec, h->enuc, h->result.p);
   CK(cudaGetLastError(), "reduce");
+  h->launches += 3;
   return VSVB_OK;
 }
 
@@ -721,6 +730,7 @@ int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
     out->n_quartets_fp64 = h->nq_fp64;
     out->n_quartets_fp32 = h->nq_fp32;
     out->n_tasks = h->ntasks;
+    out->n_kernel_launches = h->launches;
   }
   return VSVB_OK;
 }
@@ -760,6 +770,7 @@ int backward(vsvb_gpu *h, double e_num, double w) {
           h->err = "ERI adjoint launch failed";
           return VSVB_ERR_CUDA;
         }
+        h->launches++;
       }
   if (h->nxelem > 0) {
     XtabArgs xa = xtab_args(h);
@@ -772,6 +783,7 @@ int backward(vsvb_gpu *h, double e_num, double w) {
   orb_norm_adjoint_kernel<<<h->nsp, 128, sizeof(double) * std::max(h->maxobs, 1), st>>>(oa, h->Cbar.p,
                                                                                      h->coeff_bar.p);
   CK(cudaGetLastError(), "orb_norm adjoint");
+  h->launches += 5;
   return VSVB_OK;
 }
 
@@ -803,7 +815,7 @@ void vsvb_gpu_destroy(vsvb_gpu *h) {
   if (!h) return;
   cudaSetDevice(h->dev);
   if (h->st) cudaStreamSynchronize(h->st);
-  cudaStream_t st = h->st;
+  cudaStream_t st = h->own_st;
   delete h;
   if (st) cudaStreamDestroy(st);
 }
@@ -841,6 +853,7 @@ static int energy_grad_common(vsvb_gpu *h, vsvb_energy_result *out, double *grad
   rc = backward(h, r.e_num, r.wfnorm);
   if (rc) return rc;
   int status = 0;
+  r.n_kernel_launches = h->launches;
   CK(cudaMemcpyAsync(&status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->st), "status");
   CK(cudaMemcpyAsync(grad, h->coeff_bar.p, sizeof(double) * h->totlen,
                      grad_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->st),
@@ -877,6 +890,51 @@ int vsvb_gpu_batch_energy_grad(vsvb_gpu *const *hs, int n, const double *const *
     if (rc) return rc;
   }
   return VSVB_OK;
+}
+
+int vsvb_gpu_set_stream(vsvb_gpu *h, void *stream) {
+  if (!h) return VSVB_ERR_INPUT;
+  h->st = stream ? static_cast<cudaStream_t>(stream) : h->own_st;
+  return VSVB_OK;
+}
+
+int vsvb_gpu_eri_profile(vsvb_gpu *h, double *ms, double *flops, int *cls, int cap) {
+  if (!h) return -VSVB_ERR_INPUT;
+  if (cudaSetDevice(h->dev) != cudaSuccess) return -VSVB_ERR_CUDA;
+  std::vector<double> P(h->pairs.n);
+  std::vector<ShellPair> pairs(h->pairs.n);
+  if (!pairs.empty() &&
+      cudaMemcpy(pairs.data(), h->pairs.p, sizeof(ShellPair) * pairs.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -VSVB_ERR_CUDA;
+  EriArgs ea = eri_args(h);
+  if (cudaMemsetAsync(h->T.p, 0, sizeof(double) * h->T.n, h->st) != cudaSuccess) return -VSVB_ERR_CUDA;
+  int k = 0;
+  for (int p = 0; p < 2; ++p)
+    for (int a = 0; a < 6; ++a)
+      for (int c = 0; c <= a; ++c) {
+        const auto &w = h->work_h[p][a][c];
+        if (w.empty()) continue;
+        if (k >= cap) return k;
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, h->st);
+        if (eri_launch(0, p, a, c, ea, h->work_d[p][a][c].p, (int)w.size(), h->nsm, h->st)) return -VSVB_ERR_CUDA;
+        cudaEventRecord(e1, h->st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) return -VSVB_ERR_CUDA;
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        double f = 0.0;
+        for (const int2 &q : w)
+          f += eri_flops(a, c, pairs[q.x].nprim, pairs[q.y].nprim, pairs[q.x].nop, pairs[q.y].nop);
+        ms[k] = t;
+        flops[k] = f;
+        cls[k] = 100 * p + 10 * a + c;
+        ++k;
+      }
+  return k;
 }
 
 int vsvb_gpu_debug_orbital_eri(vsvb_gpu *h, double *out, size_t cap) {

@@ -199,6 +199,8 @@ extern "C" int vsvb_read_input(const char *path, vsvb_system_desc **out, char *e
   /* the reference reads only what the shells need; declared counts may be
    * larger (its arrays are allocated from them) */
   o->map_shell2prim[ns - 1] = np;
+  d.num_sh = ns - 1;
+  d.num_pr = np - 1;
   int nsc = d.nspinc > 0 ? d.nspinc : 1;
   o->pair_sc.assign((size_t)2 * d.npair * nsc, 0);
   o->coeff_sc.assign(nsc, 1.0);
