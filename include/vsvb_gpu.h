@@ -88,6 +88,10 @@ typedef struct vsvb_options {
   double mixed_threshold; /* Schwarz bound below which a quartet runs in FP32 (default 1e-6) */
   double ao_screen;       /* AO shell-quartet Schwarz screen (default 1e-15) */
   int device;             /* CUDA device ordinal (default 0) */
+  int grad_mode;          /* 0 (default): one ERI sweep yields T and dE/dX, the adjoint
+                           * weights taken from the unscreened cofactor densities;
+                           * 1: a second sweep recomputes the ERIs against the
+                           * exactly screened dE/dT (valence.F90:1189-1190,1286-1287) */
 } vsvb_options;
 
 typedef struct vsvb_energy_result {

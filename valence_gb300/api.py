@@ -47,7 +47,7 @@ class Desc(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("mixed_threshold", ctypes.c_double), ("ao_screen", ctypes.c_double),
-                ("device", ctypes.c_int)]
+                ("device", ctypes.c_int), ("grad_mode", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -106,20 +106,22 @@ def read_input(path):
     return d
 
 
-def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0):
+def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, grad_mode=0):
     o = Options()
     lib().vsvb_default_options(ctypes.byref(o))
     o.precision = precision
     o.mixed_threshold = mixed_threshold
     o.ao_screen = ao_screen
     o.device = device
+    o.grad_mode = grad_mode
     return o
 
 
 class System:
     """One molecule on the GPU: a parsed input plus a device handle."""
 
-    def __init__(self, path, precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, coords_angstrom=None):
+    def __init__(self, path, precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, coords_angstrom=None,
+                 grad_mode=0):
         self.path = path
         self._desc = read_input(path)
         d = self._desc.contents
@@ -129,7 +131,7 @@ class System:
         self._coords_bohr = np.ctypeslib.as_array(d.coords, shape=(3 * d.natom,))
         if coords_angstrom is not None:
             self._coords_bohr[:] = np.asarray(coords_angstrom, dtype=np.float64).ravel() * 1.889725987722
-        self.opt = make_options(precision, mixed_threshold, ao_screen, device)
+        self.opt = make_options(precision, mixed_threshold, ao_screen, device, grad_mode)
         self._h = ctypes.c_void_p()
         rc = lib().vsvb_gpu_create(self._desc, ctypes.byref(self.opt), ctypes.byref(self._h))
         if rc:

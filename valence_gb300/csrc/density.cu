@@ -421,8 +421,15 @@ __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
 }
 
 /* ---- energy (and adjoint) assembly: grid (nq, nsplit) ---- */
-template <bool GRAD>
+/* MODE 0: energy partial sums (screened as the reference).
+ * MODE 1: adjoint walk: dE/dS_orb, dE/dh_orb, per-pair dJ/dT; dE/dT as well
+ *         unless a.skip_tbar.
+ * MODE 2: unscreened density walk: Tbar += fac*dd at (ik,jl) and -fac*xd at
+ *         (il,jk), unscaled by 1/W, for the single-sweep adjoint. */
+template <int MODE>
 __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
+  constexpr bool GRAD = MODE == 1;
+  constexpr bool DENS = MODE == 2;
   __shared__ double red[8];
   extern __shared__ double gsh[];
   const long long q = blockIdx.x;
@@ -446,7 +453,7 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
   double e1 = 0.0, wf = 0.0, e2 = 0.0, vtot = 0.0;
   const long long stride = (long long)nsplit * blockDim.x;
   /* one-electron part (valence.F90:1072-1101) */
-  for (long long t = (long long)split * blockDim.x + threadIdx.x; t < (long long)nelec * nelec; t += stride) {
+  for (long long t = (long long)split * blockDim.x + threadIdx.x; !DENS && t < (long long)nelec * nelec; t += stride) {
     const int i = (int)(t / nelec), j = (int)(t % nelec);
     const bool idocc = i >= nnd, jdocc = j >= nnd;
     /* 1-based parity as in the reference: slots i+1, j+1 */
@@ -480,23 +487,32 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
     --lo; /* 0-based orbitals */
     if ((io == jo && io < nnd) || (ko == lo && ko < nnd)) continue;
     const int pik = opidx(io, ko), pjl = opidx(jo, lo), pil = opidx(io, lo), pjk = opidx(jo, ko);
-    const double sik = sqrt(fmax(a.T[(size_t)pik * np + pik], 0.0)), sjl = sqrt(fmax(a.T[(size_t)pjl * np + pjl], 0.0));
-    const double sil = sqrt(fmax(a.T[(size_t)pil * np + pil], 0.0)), sjk = sqrt(fmax(a.T[(size_t)pjk * np + pjk], 0.0));
+    double sik = 0.0, sjl = 0.0, sil = 0.0, sjk = 0.0;
+    if (!DENS) {
+      sik = sqrt(fmax(a.T[(size_t)pik * np + pik], 0.0));
+      sjl = sqrt(fmax(a.T[(size_t)pjl * np + pjl], 0.0));
+      sil = sqrt(fmax(a.T[(size_t)pil * np + pil], 0.0));
+      sjk = sqrt(fmax(a.T[(size_t)pjk * np + pjk], 0.0));
+    }
     bool es = sik * sjl > itol, xs = sil * sjk > itol;
     double eint = 0.0, xint = 0.0;
     const bool diag = io == jo && ko == lo;
-    if (es || xs) {
-      if (diag) {
-        eint = sik * sik;
-        xint = eint;
-      } else {
-        if (es) eint = a.T[(size_t)pik * np + pjl];
-        if (xs) xint = a.T[(size_t)pil * np + pjk];
+    if (DENS) {
+      es = xs = true;
+    } else {
+      if (es || xs) {
+        if (diag) {
+          eint = sik * sik;
+          xint = eint;
+        } else {
+          if (es) eint = a.T[(size_t)pik * np + pjl];
+          if (xs) xint = a.T[(size_t)pil * np + pjk];
+        }
       }
+      es = fabs(eint) > itol;
+      xs = fabs(xint) > itol;
+      if (!(es || xs)) continue;
     }
-    es = fabs(eint) > itol;
-    xs = fabs(xint) > itol;
-    if (!(es || xs)) continue;
     const double fac = (ko == io && lo == jo) ? 1.0 : 2.0;
     const bool id = io >= nnd, jd = jo >= nnd, kd = ko >= nnd, ld = lo >= nnd;
     const int iso = id ? 2 : 1, jso = jd ? 2 : 1, kso = kd ? 2 : 1, lso = ld ? 2 : 1;
@@ -566,7 +582,15 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
       }
     }
     e2 += fac * (esum - xsum);
-    if (GRAD) {
+    if (DENS) {
+      if (diag) {
+        atomicAdd(a.Tbar + (size_t)pik * np + pik, fac * (dsum_e - dsum_x));
+      } else {
+        if (dsum_e != 0.0) atomicAdd(a.Tbar + (size_t)pik * np + pjl, fac * dsum_e);
+        if (dsum_x != 0.0) atomicAdd(a.Tbar + (size_t)pil * np + pjk, -fac * dsum_x);
+      }
+    }
+    if (GRAD && !a.skip_tbar) {
       const double ge = fac * a.inv_w * dsum_e, gx = -fac * a.inv_w * dsum_x;
       if (diag) {
         if (es || xs) atomicAdd(a.Tbar + (size_t)pik * np + pik, (es ? ge : 0.0) + (xs ? gx : 0.0));
@@ -589,7 +613,7 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
       for (int t = threadIdx.x; t < na * na + nb * nb; t += blockDim.x)
         if (gsh[t] != 0.0) atomicAdd(Gq + t, gsh[t]);
     }
-  } else if (threadIdx.x == 0) {
+  } else if (!DENS && threadIdx.x == 0) {
     a.part_e1[slot] = e1;
     a.part_wf[slot] = wf;
     a.part_e2[slot] = e2;
@@ -653,13 +677,15 @@ __global__ void detpair_adjoint_kernel(DetCtx d, AsmArgs a, int nsplit) {
   }
 }
 
-cudaError_t launch_assemble(bool grad, dim3 grid, int threads, size_t smem, cudaStream_t st, const DetCtx &d,
+cudaError_t launch_assemble(int mode, dim3 grid, int threads, size_t smem, cudaStream_t st, const DetCtx &d,
                             const AsmArgs &a) {
-  if (grad) {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(assemble_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    assemble_kernel<true><<<grid, threads, smem, st>>>(d, a);
+  if (mode == 1) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(assemble_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    assemble_kernel<1><<<grid, threads, smem, st>>>(d, a);
+  } else if (mode == 2) {
+    assemble_kernel<2><<<grid, threads, 0, st>>>(d, a);
   } else {
-    assemble_kernel<false><<<grid, threads, smem, st>>>(d, a);
+    assemble_kernel<0><<<grid, threads, 0, st>>>(d, a);
   }
   return cudaGetLastError();
 }

@@ -30,10 +30,11 @@ struct AsmArgs {
   double *vtot;            /* [nq * nsplit] */
   double *Gglob;           /* [nq][na*na + nb*nb] */
   int g_in_smem;
+  int skip_tbar; /* adjoint walk without dE/dT (single-sweep mode) */
 };
 
 __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch);
-cudaError_t launch_assemble(bool grad, dim3 grid, int threads, size_t smem, cudaStream_t st, const DetCtx &d,
+cudaError_t launch_assemble(int mode, dim3 grid, int threads, size_t smem, cudaStream_t st, const DetCtx &d,
                             const AsmArgs &a);
 __global__ void energy_reduce_kernel(AsmArgs a, long long nslot, int nelec, double enuc, double *out);
 __global__ void detpair_adjoint_kernel(DetCtx d, AsmArgs a, int nsplit);

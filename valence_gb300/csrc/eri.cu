@@ -67,11 +67,13 @@ __device__ __forceinline__ void rys_root(int n, int r, double T, const double *_
     const double *c = tab + c_rys_off[n - 1] + (size_t)j * (2 * n) * RYS_NCHEB_D;
     double fx = clenshaw12(c + r * RYS_NCHEB_D, t);
     double fw = clenshaw12(c + (n + r) * RYS_NCHEB_D, t);
-    x = fx / (1.0 + T);
-    w = fw * rsqrt(1.0 + T);
+    const double s = rsqrt(1.0 + T);
+    x = fx * s * s;
+    w = fw * s;
   } else {
-    x = c_rys_ax[n - 1][r] / T;
-    w = c_rys_aw[n - 1][r] * rsqrt(T);
+    const double s = rsqrt(T);
+    x = c_rys_ax[n - 1][r] * s * s;
+    w = c_rys_aw[n - 1][r] * s;
   }
 }
 
@@ -140,12 +142,18 @@ struct QuartetShape {
   static constexpr int NAB = NA * NB, NCD = NCc * ND, NCOMP = NAB * NCD;
   static constexpr int NR = (LA + LB + LC + LD) / 2 + 1;
   static constexpr int N2D = (LA + 1) * (LB + 1) * (LC + 1) * (LD + 1);
-  static constexpr int PER_LANE = (NCOMP + 31) / 32;
+  /* primitive quartets processed side by side per warp iteration: each takes
+   * 3*NR lanes for its 2D tables; large blocks keep one slot so that the
+   * per-lane accumulators stay in registers */
+  static constexpr int G0 = 32 / (3 * NR);
+  static constexpr int G = NCOMP >= 200 ? 1 : (G0 < 1 ? 1 : G0);
+  static constexpr int NITEM = G * NCOMP;
+  static constexpr int PER_LANE = (NITEM + 31) / 32;
   static constexpr int JCH = 8; /* ket orbital pairs per transform chunk */
   /* per-warp shared memory in doubles: 2D tables (phase 1) and block + Y
    * chunk (phase 2) share storage */
-  static constexpr int SM_2D = 3 * NR * N2D;
-  static constexpr int SM_TR = NCOMP + JCH * (NAB > NCD ? NAB : NCD);
+  static constexpr int SM_2D = G * 3 * NR * N2D;
+  static constexpr int SM_TR = NCOMP + (NITEM > JCH * (NAB > NCD ? NAB : NCD) ? NITEM : JCH * (NAB > NCD ? NAB : NCD));
   static constexpr int PER_WARP = (SM_2D > SM_TR ? SM_2D : SM_TR);
 };
 
@@ -155,6 +163,7 @@ constexpr int WARPS = 4;
  * MODE 0: forward transform into T.
  * MODE 1: Schwarz diagonal -- pairs[P].qmax = sqrt(max_ab |(ab|ab)|).
  * MODE 2: adjoint -- accumulate dE/dX for both pairs from Tbar.
+ * MODE 3: forward and adjoint from one evaluation of each quartet.
  */
 template <int LA, int LB, int LC, int LD, typename R, int MODE>
 __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int2 *__restrict__ work, int nwork) {
@@ -193,84 +202,111 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
     R acc[S::PER_LANE];
 #pragma unroll
     for (int m = 0; m < S::PER_LANE; ++m) acc[m] = R(0);
-    const double ab[3] = {P.A[0] - P.B[0], P.A[1] - P.B[1], P.A[2] - P.B[2]};
-    const double cdv[3] = {Q.A[0] - Q.B[0], Q.A[1] - Q.B[1], Q.A[2] - Q.B[2]};
+    const int npq = P.nprim * Q.nprim;
+    /* lane roles in phase A: slot g, root r, direction dir */
+    const int g = lane / (3 * S::NR), rem = lane - g * (3 * S::NR);
+    const int r = rem / 3, dir = rem - 3 * (rem / 3);
+    const bool lane_a = g < S::G;
 
-    for (int ip = 0; ip < P.nprim; ++ip) {
-      const PrimPair pp = args.prims[P.prim0 + ip];
-      for (int iq = 0; iq < Q.nprim; ++iq) {
-        const PrimPair qq = args.prims[Q.prim0 + iq];
-        const double p = pp.p, q = qq.p, pq_ = p + q;
-        const double dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
-        const double rho = p * q / pq_;
-        const double Tb = rho * (dx * dx + dy * dy + dz * dz);
-        const double pref = two_pi_25 / (p * q * sqrt(pq_)) * pp.K * qq.K;
-        double xr = 0.0, wr = 0.0;
-        if (lane < S::NR) rys_root(S::NR, lane, Tb, args.rys, xr, wr);
-        const int r = lane / 3, dir = lane - 3 * (lane / 3);
-        const int src = r < S::NR ? r : 0;
-        const double u = __shfl_sync(0xffffffffu, xr, src);
-        const double w = __shfl_sync(0xffffffffu, wr, src);
-        if (lane < 3 * S::NR) {
-          const double Pd = pp.P[dir], Qd = qq.P[dir];
-          const double Ad = P.A[dir], Cd = Q.A[dir];
-          const double b00 = 0.5 * u / pq_;
-          const double b10 = 0.5 / p - 0.5 * q * u / (p * pq_);
-          const double b01 = 0.5 / q - 0.5 * p * u / (q * pq_);
-          const double c00 = (Pd - Ad) - q * u * (Pd - Qd) / pq_;
-          const double d00 = (Qd - Cd) + p * u * (Pd - Qd) / pq_;
-          const double g00 = dir == 2 ? w * pref : 1.0;
-          rys_2d<LA, LB, LC, LD, R>(R(g00), R(c00), R(d00), R(b00), R(b10), R(b01), R(ab[dir]), R(cdv[dir]),
-                                    h2d + (size_t)(dir * S::NR + r) * S::N2D);
+    for (int base = 0; base < npq; base += S::G) {
+      const int pqi = base + g;
+      const bool act = lane_a && pqi < npq;
+      const unsigned amask = __ballot_sync(0xffffffffu, act);
+      double u = 0.0, w = 0.0, ipq = 0.0;
+      if (act) {
+        const int ip = pqi / Q.nprim, iq = pqi - ip * Q.nprim;
+        const PrimPair &pp = args.prims[P.prim0 + ip];
+        const PrimPair &qq = args.prims[Q.prim0 + iq];
+        /* FP64: reciprocal of p+q, Boys argument, Rys root and scaled weight */
+        if (dir == 0) {
+          const double p = pp.p, q = qq.p;
+          ipq = 1.0 / (p + q);
+          const double dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
+          const double Tb = p * q * ipq * (dx * dx + dy * dy + dz * dz);
+          rys_root(S::NR, r, Tb, args.rys, u, w);
+          w *= two_pi_25 * pp.Kp * qq.Kp * sqrt(ipq);
         }
-        __syncwarp();
-        const R *hx = h2d, *hy = h2d + S::NR * S::N2D, *hz = h2d + 2 * S::NR * S::N2D;
+        u = __shfl_sync(amask, u, lane - dir);
+        w = __shfl_sync(amask, w, lane - dir);
+        ipq = __shfl_sync(amask, ipq, lane - dir);
+        /* 2D recurrence coefficients in the kernel's precision */
+        const R uR = R(u), ipqR = R(ipq);
+        const R pR = R(pp.p), qR = R(qq.p), ipR = R(pp.inv_p), iqR = R(qq.inv_p);
+        const R Pd = R(pp.P[dir]), Qd = R(qq.P[dir]);
+        const R PQ = Pd - Qd, uq = uR * ipqR;
+        const R b00 = R(0.5) * uq;
+        const R b10 = R(0.5) * ipR * (R(1) - qR * uq);
+        const R b01 = R(0.5) * iqR * (R(1) - pR * uq);
+        const R c00 = (Pd - R(P.A[dir])) - qR * uq * PQ;
+        const R d00 = (Qd - R(Q.A[dir])) + pR * uq * PQ;
+        const R g00 = dir == 2 ? R(w) : R(1);
+        rys_2d<LA, LB, LC, LD, R>(g00, c00, d00, b00, b10, b01, R(P.A[dir] - P.B[dir]), R(Q.A[dir] - Q.B[dir]),
+                                  h2d + (size_t)((g * 3 + dir) * S::NR + r) * S::N2D);
+      }
+      __syncwarp();
+      const int nact = min(S::G, npq - base);
 #pragma unroll
-        for (int m = 0; m < S::PER_LANE; ++m) {
-          const int c = lane + 32 * m;
-          if (c < S::NCOMP) {
+      for (int m = 0; m < S::PER_LANE; ++m) {
+        const int it = lane + 32 * m;
+        if (it < S::NITEM) {
+          const int gg = it / S::NCOMP, c = it - gg * S::NCOMP;
+          if (gg < nact) {
             const int id = idx[c];
             const int ix = id & 1023, iy = (id >> 10) & 1023, iz = id >> 20;
-            R s = acc[m];
+            const R *hx = h2d + (size_t)(gg * 3 + 0) * S::NR * S::N2D;
+            const R *hy = hx + S::NR * S::N2D, *hz = hy + S::NR * S::N2D;
+            R sacc = acc[m];
 #pragma unroll
             for (int rr = 0; rr < S::NR; ++rr)
-              s += hx[rr * S::N2D + ix] * hy[rr * S::N2D + iy] * hz[rr * S::N2D + iz];
-            acc[m] = s;
+              sacc += hx[rr * S::N2D + ix] * hy[rr * S::N2D + iy] * hz[rr * S::N2D + iz];
+            acc[m] = sacc;
           }
         }
-        __syncwarp();
       }
+      __syncwarp();
     }
 
-    if (MODE == 1) {
-      /* Schwarz: max over diagonal components (ab|ab) */
-      double mx = 0.0;
+    /* stage the block: sum the slots into E[c] (double) */
+    double *E = ws;
+    double *E2 = ws + S::NCOMP;
+    if (S::G == 1) {
 #pragma unroll
       for (int m = 0; m < S::PER_LANE; ++m) {
         const int c = lane + 32 * m;
-        if (c < S::NCOMP && (c / S::NCD) == (c % S::NCD)) mx = fmax(mx, fabs((double)acc[m]));
+        if (c < S::NCOMP) E[c] = (double)acc[m];
       }
+    } else {
+#pragma unroll
+      for (int m = 0; m < S::PER_LANE; ++m) {
+        const int it = lane + 32 * m;
+        if (it < S::NITEM) E2[it] = (double)acc[m];
+      }
+      __syncwarp();
+      for (int c = lane; c < S::NCOMP; c += 32) {
+        double sum = 0.0;
+        for (int gg = 0; gg < S::G; ++gg) sum += E2[gg * S::NCOMP + c];
+        E[c] = sum;
+      }
+    }
+    __syncwarp();
+    if (MODE == 1) {
+      /* Schwarz: max over diagonal components (ab|ab) */
+      double mx = 0.0;
+      for (int c = lane; c < S::NCOMP; c += 32)
+        if ((c / S::NCD) == (c % S::NCD)) mx = fmax(mx, fabs(E[c]));
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
       if (lane == 0) args.qmax_out[pq.x] = sqrt(mx);
+      __syncwarp();
       continue;
     }
-
-    /* stage the block */
-    double *E = ws;
-#pragma unroll
-    for (int m = 0; m < S::PER_LANE; ++m) {
-      const int c = lane + 32 * m;
-      if (c < S::NCOMP) E[c] = (double)acc[m];
-    }
-    __syncwarp();
-    double *Y = ws + S::NCOMP;
+    double *Y = ws + S::NCOMP; /* reuses the slot buffer */
     const double *XP = args.xtab + P.x0;
     const double *XQ = args.xtab + Q.x0;
     const int *opP = args.pair_opid + P.op0;
     const int *opQ = args.pair_opid + Q.op0;
     const bool same = pq.x == pq.y;
-    if (MODE == 0) {
+    if (MODE == 0 || MODE == 3) {
       for (int j0 = 0; j0 < Q.nop; j0 += S::JCH) {
         const int nj = min(S::JCH, Q.nop - j0);
         /* Y[jl][ab] = sum_cd E[ab][cd] X_Q[jl][cd] */
@@ -293,13 +329,13 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
 #pragma unroll
           for (int c = 0; c < S::NAB; ++c) s = fma(__ldg(xp + c), y[c], s);
           const int a = __ldg(opP + ik), b = __ldg(opQ + j0 + jl);
-          atomicAdd(args.T + (size_t)a * args.np + b, s);
-          if (!same) atomicAdd(args.T + (size_t)b * args.np + a, s);
+          atomicAdd(args.T + (size_t)a * args.np + b, same ? 0.5 * s : s);
         }
         __syncwarp();
       }
-    } else {
-      /* MODE 2: adjoint.  With Tbar symmetric and Z(ik,jl) = X_P E X_Q^T,
+    }
+    if (MODE == 2 || MODE == 3) {
+      /* MODE 2/3: adjoint.  With Tbar symmetric and Z(ik,jl) = X_P E X_Q^T,
        * dE/dX_P[ik][ab] += sum_jl W(ik,jl) (E X_Q^T)[ab][jl] and
        * dE/dX_Q[jl][cd] += sum_ik W(ik,jl) (X_P E)[ik][cd], where
        * W = Tbar[ik][jl] (+ Tbar[jl][ik] when the pairs differ). */
@@ -408,7 +444,30 @@ int dispatch(int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cu
   return 2;
 }
 
+__global__ void symmetrize_kernel(double *T, int np) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long n = (long long)np * (np + 1) / 2;
+  if (t >= n) return;
+  long long i = (long long)((sqrt(8.0 * t + 1.0) - 1.0) / 2.0);
+  while ((i + 1) * (i + 2) / 2 <= t) ++i;
+  while (i * (i + 1) / 2 > t) --i;
+  long long j = t - i * (i + 1) / 2;
+  double *a = T + i * np + j, *b = T + j * np + i;
+  double v = *a + *b;
+  if (i == j) v = 2.0 * (*a);
+  *a = v;
+  *b = v;
+}
+
 }  // namespace
+
+/* T = U + U^T after the forward pass (the kernels accumulate one orientation) */
+int eri_symmetrize(double *T, int np, cudaStream_t st) {
+  long long n = (long long)np * (np + 1) / 2;
+  if (n == 0) return 0;
+  symmetrize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(T, np);
+  return cudaGetLastError() != cudaSuccess;
+}
 
 /* algorithmic FLOPs of one shell quartet of class (cp, cq) in this
  * formulation: per primitive quartet the n_r roots (two 12-term Clenshaw sums
@@ -439,6 +498,8 @@ int eri_set_tables(const int *off, const double *ax, const double *aw) {
 int eri_launch(int mode, int fp32, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int nsm,
                cudaStream_t st) {
   if (mode == 1) return dispatch<double, 1>(cp, cq, a, work, nwork, nsm, st);
+  if (mode == 3) return fp32 ? dispatch<float, 3>(cp, cq, a, work, nwork, nsm, st)
+                             : dispatch<double, 3>(cp, cq, a, work, nwork, nsm, st);
   if (mode == 2) return fp32 ? dispatch<float, 2>(cp, cq, a, work, nwork, nsm, st)
                              : dispatch<double, 2>(cp, cq, a, work, nwork, nsm, st);
   return fp32 ? dispatch<float, 0>(cp, cq, a, work, nwork, nsm, st) : dispatch<double, 0>(cp, cq, a, work, nwork, nsm, st);

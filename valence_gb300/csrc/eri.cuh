@@ -22,5 +22,6 @@ struct EriArgs {
 int eri_launch(int mode, int fp32, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int nsm,
                cudaStream_t st);
 double eri_flops(int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ);
+int eri_symmetrize(double *T, int np, cudaStream_t st);
 int eri_set_tables(const int *off, const double *ax, const double *aw);
 #endif

@@ -164,6 +164,7 @@ XtabArgs xtab_args(vsvb_gpu *h) {
   x.angn = h->angn.p;
   x.dtol = h->dtol;
   x.xtab = h->xtab.p;
+  x.xbar_scale = 1.0;
   return x;
 }
 
@@ -481,7 +482,8 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
           PrimPair pp{};
           for (int k = 0; k < 3; ++k) pp.P[k] = (al * P.A[k] + be * P.B[k]) / p;
           pp.p = p;
-          pp.K = K;
+          pp.inv_p = 1.0 / p;
+          pp.Kp = K / p;
           prims.push_back(pp);
         }
       P.nprim = (int)prims.size() - P.prim0;
@@ -661,8 +663,12 @@ int alloc_grad(vsvb_gpu *h) {
   return VSVB_OK;
 }
 
-/* forward pass on coeff_d; leaves E in result[0..4] (device) */
-int forward(vsvb_gpu *h) {
+int alloc_grad(vsvb_gpu *h);
+
+/* forward pass on coeff_d; leaves E in result[0..4] (device).  With fused,
+ * the ERI sweep also accumulates the (unscaled) adjoint dE/dX from the
+ * unscreened cofactor densities. */
+int forward(vsvb_gpu *h, bool fused = false) {
   cudaStream_t st = h->st;
   h->launches = 0;
   CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), st), "memset status");
@@ -684,6 +690,20 @@ int forward(vsvb_gpu *h) {
     CK(cudaGetLastError(), "xtab");
     h->launches++;
   }
+  CK(cudaMemsetAsync(h->sing.p, 0, sizeof(int) * h->sing.n, st), "memset sing");
+  DetCtx dc = det_ctx(h);
+  detpair_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, h->scratch.p, h->ld_scratch);
+  CK(cudaGetLastError(), "detpair");
+  h->launches++;
+  if (fused) {
+    int rc = alloc_grad(h);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(h->Tbar.p, 0, sizeof(double) * h->Tbar.n, st), "memset Tbar");
+    CK(cudaMemsetAsync(h->xbar.p, 0, sizeof(double) * h->xbar.n, st), "memset xbar");
+    AsmArgs ad = asm_args(h);
+    CK(launch_assemble(2, dim3((unsigned)h->ds.nq, h->nsplit), 128, 0, st, dc, ad), "density walk");
+    h->launches++;
+  }
   CK(cudaMemsetAsync(h->T.p, 0, sizeof(double) * h->T.n, st), "memset T");
   EriArgs ea = eri_args(h);
   for (int p = 0; p < 2; ++p)
@@ -691,21 +711,22 @@ int forward(vsvb_gpu *h) {
       for (int c = 0; c <= a; ++c) {
         int n = (int)h->work_h[p][a][c].size();
         if (!n) continue;
-        if (eri_launch(0, p, a, c, ea, h->work_d[p][a][c].p, n, h->nsm, st)) {
+        if (eri_launch(fused ? 3 : 0, p, a, c, ea, h->work_d[p][a][c].p, n, h->nsm, st)) {
           h->err = "ERI kernel launch failed";
           return VSVB_ERR_CUDA;
         }
         h->launches++;
       }
-  CK(cudaMemsetAsync(h->sing.p, 0, sizeof(int) * h->sing.n, st), "memset sing");
-  DetCtx dc = det_ctx(h);
-  detpair_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, h->scratch.p, h->ld_scratch);
-  CK(cudaGetLastError(), "detpair");
+  if (eri_symmetrize(h->T.p, h->np, st)) {
+    h->err = "symmetrize launch failed";
+    return VSVB_ERR_CUDA;
+  }
+  h->launches++;
   AsmArgs aa = asm_args(h);
-  CK(launch_assemble(false, dim3((unsigned)h->ds.nq, h->nsplit), 128, 0, st, dc, aa), "assemble");
+  CK(launch_assemble(0, dim3((unsigned)h->ds.nq, h->nsplit), 128, 0, st, dc, aa), "assemble");
   energy_reduce_kernel<<<1, 256, 0, st>>>(aa, h->ds.nq * h->nsplit, h->ds.nelec, h->enuc, h->result.p);
   CK(cudaGetLastError(), "reduce");
-  h->launches += 3;
+  h->launches += 2;
   return VSVB_OK;
 }
 
@@ -735,7 +756,7 @@ int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
   return VSVB_OK;
 }
 
-int backward(vsvb_gpu *h, double e_num, double w) {
+int backward(vsvb_gpu *h, double e_num, double w, bool fused) {
   if (h->ndf > 0) {
     h->err = "gradient through derived basis functions is not implemented";
     return VSVB_ERR_UNSUPPORTED;
@@ -744,10 +765,12 @@ int backward(vsvb_gpu *h, double e_num, double w) {
   if (rc) return rc;
   cudaStream_t st = h->st;
   const int na = h->ds.nalpha, nb = h->ds.nbeta;
-  CK(cudaMemsetAsync(h->Tbar.p, 0, sizeof(double) * h->Tbar.n, st), "memset");
+  if (!fused) {
+    CK(cudaMemsetAsync(h->Tbar.p, 0, sizeof(double) * h->Tbar.n, st), "memset");
+    CK(cudaMemsetAsync(h->xbar.p, 0, sizeof(double) * h->xbar.n, st), "memset");
+  }
   CK(cudaMemsetAsync(h->Sbar.p, 0, sizeof(double) * h->Sbar.n, st), "memset");
   CK(cudaMemsetAsync(h->Hbar.p, 0, sizeof(double) * h->Hbar.n, st), "memset");
-  CK(cudaMemsetAsync(h->xbar.p, 0, sizeof(double) * h->xbar.n, st), "memset");
   CK(cudaMemsetAsync(h->Cbar.p, 0, sizeof(double) * h->Cbar.n, st), "memset");
   CK(cudaMemsetAsync(h->Gglob.p, 0, sizeof(double) * h->Gglob.n, st), "memset");
   CK(cudaMemsetAsync(h->coeff_bar.p, 0, sizeof(double) * h->coeff_bar.n, st), "memset");
@@ -756,12 +779,13 @@ int backward(vsvb_gpu *h, double e_num, double w) {
   aa.status = h->status.p;
   aa.inv_w = 1.0 / w;
   aa.dw_coef = -e_num / (w * w * (double)h->ds.nelec);
+  aa.skip_tbar = fused ? 1 : 0;
   size_t gsh = aa.g_in_smem ? sizeof(double) * (size_t)(na * na + nb * nb) : 0;
-  CK(launch_assemble(true, dim3((unsigned)h->ds.nq, h->nsplit), 128, gsh, st, dc, aa), "assemble grad");
+  CK(launch_assemble(1, dim3((unsigned)h->ds.nq, h->nsplit), 128, gsh, st, dc, aa), "assemble grad");
   detpair_adjoint_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, aa, h->nsplit);
   CK(cudaGetLastError(), "detpair adjoint");
   EriArgs ea = eri_args(h);
-  for (int p = 0; p < 2; ++p)
+  for (int p = 0; !fused && p < 2; ++p)
     for (int a = 0; a < 6; ++a)
       for (int c = 0; c <= a; ++c) {
         int n = (int)h->work_h[p][a][c].size();
@@ -774,6 +798,7 @@ int backward(vsvb_gpu *h, double e_num, double w) {
       }
   if (h->nxelem > 0) {
     XtabArgs xa = xtab_args(h);
+    if (fused) xa.xbar_scale = 1.0 / w; /* the sweep used the unscaled densities */
     xtab_adjoint_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa, h->xbar.p, h->Cbar.p);
     CK(cudaGetLastError(), "xtab adjoint");
   }
@@ -797,6 +822,7 @@ void vsvb_default_options(vsvb_options *o) {
   o->mixed_threshold = 1e-6;
   o->ao_screen = 1e-15;
   o->device = 0;
+  o->grad_mode = 0;
 }
 
 int vsvb_gpu_create(const vsvb_system_desc *d, const vsvb_options *opt, vsvb_gpu **out) {
@@ -845,12 +871,19 @@ int vsvb_gpu_energy(vsvb_gpu *h, const double *coeff, vsvb_energy_result *out) {
 }
 
 static int energy_grad_common(vsvb_gpu *h, vsvb_energy_result *out, double *grad, bool grad_on_device) {
-  int rc = forward(h);
+  const bool fused = h->opt.grad_mode == 0;
+  if (h->ndf > 0) {
+    h->err = "gradient through derived basis functions is not implemented";
+    return VSVB_ERR_UNSUPPORTED;
+  }
+  int rc = forward(h, fused);
   if (rc) return rc;
+  int nl = h->launches;
   vsvb_energy_result r;
   rc = finish_result(h, &r);
   if (rc) return rc;
-  rc = backward(h, r.e_num, r.wfnorm);
+  rc = backward(h, r.e_num, r.wfnorm, fused);
+  h->launches += nl;
   if (rc) return rc;
   int status = 0;
   r.n_kernel_launches = h->launches;

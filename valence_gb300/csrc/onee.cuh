@@ -50,6 +50,7 @@ struct XtabArgs {
   const double *angn;
   double dtol;
   double *xtab;
+  double xbar_scale; /* adjoint: factor applied to dE/dX */
 };
 
 __global__ void ao_1e_kernel(Ao1eArgs a);

@@ -34,9 +34,9 @@ struct GShell {
 
 struct PrimPair {
   double P[3];
-  double p;   /* alpha + beta */
-  double K;   /* c_a c_b exp(-alpha beta / p |AB|^2) */
-  double pad;
+  double p;      /* alpha + beta */
+  double inv_p;  /* 1 / p */
+  double Kp;     /* c_a c_b exp(-alpha beta / p |AB|^2) / p */
 };
 
 struct ShellPair {
