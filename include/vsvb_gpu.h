@@ -165,6 +165,18 @@ int vsvb_gpu_eri_profile(vsvb_gpu *h, double *ms, double *flops, int *cls, int c
  * FMA chain kernel sized to fill every SM), for roofline denominators. */
 int vsvb_gpu_fma_peak(int device, double *fp64_flops, double *fp32_flops);
 
+/* Batched determinant and inverse of nmat dense n x n matrices (row-major,
+ * device memory, a_dev[nmat*n*n]) by Gauss-Jordan elimination with partial
+ * pivoting: the factorisation applied to every spin block of every
+ * determinant pair, replacing givdr/givens_single (valence.F90:2067-2144,
+ * givens.F90:230-262).  Outputs (device): det_dev[nmat], inv_dev[nmat*n*n]
+ * (row-major inverse), sing_dev[nmat] = 1 when a pivot falls below 1e-7 of
+ * the matrix's largest entry (the determinant then comes from LU and the
+ * inverse is zero).  Enqueues on stream (a cudaStream_t, NULL = default)
+ * and synchronises it.  Allocates n x 2n doubles of scratch per matrix. */
+int vsvb_det_factor(const double *a_dev, int n, int nmat, double *det_dev, double *inv_dev, int *sing_dev,
+                    void *stream);
+
 /* Sizes of a handle (for bindings). */
 int vsvb_gpu_totlen(const vsvb_gpu *h);
 int vsvb_gpu_num_orbitals(const vsvb_gpu *h);

@@ -88,6 +88,8 @@ def lib():
         L.vsvb_gpu_set_stream.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.vsvb_gpu_eri_profile.argtypes = [ctypes.c_void_p, P(D), P(D), P(I), I]
         L.vsvb_gpu_fma_peak.argtypes = [I, P(D), P(D)]
+        L.vsvb_det_factor.argtypes = [ctypes.c_void_p, I, I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p]
         _LIB = L
     return _LIB
 
@@ -231,6 +233,24 @@ def batch_energy_grad(systems, weights=None, with_grad=True):
     if rc:
         raise VSVBError(f"batch failed ({rc}): {lib().vsvb_gpu_last_error(systems[0]._h).decode()}")
     return [r.as_dict() for r in res], grads
+
+
+def det_factor(a, stream=0):
+    """Determinants and inverses of a batch of square matrices held in a
+    CUDA torch tensor of shape (nmat, n, n), float64.  Returns (det, inv,
+    singular) as CUDA tensors."""
+    import torch
+    a = a.contiguous()
+    nmat, n, _ = a.shape
+    det = torch.empty(nmat, dtype=torch.float64, device=a.device)
+    inv = torch.empty_like(a)
+    sing = torch.empty(nmat, dtype=torch.int32, device=a.device)
+    rc = lib().vsvb_det_factor(ctypes.c_void_p(a.data_ptr()), n, nmat, ctypes.c_void_p(det.data_ptr()),
+                               ctypes.c_void_p(inv.data_ptr()), ctypes.c_void_p(sing.data_ptr()),
+                               ctypes.c_void_p(stream or None))
+    if rc:
+        raise VSVBError(f"vsvb_det_factor failed ({rc})")
+    return det, inv, sing
 
 
 def fma_peak(device=0):

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libvsvb_gb300.so")
-CU = ["eri.cu", "density.cu", "onee.cu", "handle.cu", "peak.cu"]
+CU = ["eri.cu", "density.cu", "onee.cu", "handle.cu", "peak.cu", "detfactor.cu"]
 CPP = ["input.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
