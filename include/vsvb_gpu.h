@@ -45,7 +45,8 @@ typedef enum vsvb_status {
   VSVB_ERR_SINGULAR = 4,    /* gradient requested through a singular determinant pair */
   VSVB_ERR_NOMEM = 5,
   VSVB_ERR_TIMEOUT = 6,     /* a bounded device-side wait gave up */
-  VSVB_ERR_NOT_NORMALISABLE = 7 /* an orbital has non-positive self-overlap */
+  VSVB_ERR_NOT_NORMALISABLE = 7, /* an orbital has non-positive self-overlap */
+  VSVB_ERR_TOO_LARGE = 8          /* request exceeds a fixed-size buffer (vsvb_det_factor_noalloc) */
 } vsvb_status;
 
 /* Precision modes of the ERI contraction. */
@@ -176,6 +177,18 @@ int vsvb_gpu_fma_peak(int device, double *fp64_flops, double *fp32_flops);
  * and synchronises it.  Allocates n x 2n doubles of scratch per matrix. */
 int vsvb_det_factor(const double *a_dev, int n, int nmat, double *det_dev, double *inv_dev, int *sing_dev,
                     void *stream);
+
+/* Same factorisation without any device allocation, for callers that may
+ * not call cudaMalloc (their device memory is owned by another framework's
+ * allocator, or allocation is forbidden in the phase they run in).  Has no
+ * counterpart in the reference.  Scratch is a fixed 4 MiB device array per
+ * device (2*n*n*nmat doubles at most, else VSVB_ERR_TOO_LARGE) held for the
+ * life of the process; the first call on a device resolves that array's
+ * address and should come before any stream capture; concurrent calls share
+ * the array and must not overlap on the GPU.  Arguments and results as
+ * vsvb_det_factor. */
+int vsvb_det_factor_noalloc(const double *a_dev, int n, int nmat, double *det_dev, double *inv_dev, int *sing_dev,
+                            void *stream);
 
 /* Sizes of a handle (for bindings). */
 int vsvb_gpu_totlen(const vsvb_gpu *h);

@@ -90,6 +90,7 @@ def lib():
         L.vsvb_gpu_fma_peak.argtypes = [I, P(D), P(D)]
         L.vsvb_det_factor.argtypes = [ctypes.c_void_p, I, I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_void_p]
+        L.vsvb_det_factor_noalloc.argtypes = L.vsvb_det_factor.argtypes
         _LIB = L
     return _LIB
 

@@ -15,6 +15,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "../../include/vsvb_gpu.h"
 
 namespace {
@@ -186,5 +188,63 @@ extern "C" int vsvb_det_factor(const double *a_dev, int n, int nmat, double *det
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cudaFree(scratch);
+  return e == cudaSuccess ? VSVB_OK : VSVB_ERR_CUDA;
+}
+
+/*
+ * Allocation-free variant.  Some callers cannot call cudaMalloc at the
+ * moment they need a factorisation: a Fortran optimiser that runs inside a
+ * host-side memory budget handed to it by another framework (PyTorch's
+ * caching allocator owns the device pool, and a raw cudaMalloc would grow
+ * or fragment it behind that allocator's back), or code running between
+ * kernels of a larger asynchronous pipeline whose owner forbids device
+ * allocation in that phase.  This entry point takes its scratch from a
+ * fixed file-scope device array instead of allocating.
+ *
+ * Limits and behaviour:
+ *  - the scratch holds VSVB_NOALLOC_SCRATCH_DOUBLES doubles (4 MiB) on every
+ *    device that loads the library, for the life of the process; a call
+ *    needs 2*n*n*nmat of them and is rejected with VSVB_ERR_TOO_LARGE beyond
+ *    that;
+ *  - the first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture;
+ *  - every call shares the one array, which keeps the previous call's
+ *    contents (each call rewrites all the scratch it reads); calls whose
+ *    work overlaps on the GPU race on it, so serialise them (one stream, or
+ *    wait between calls);
+ *  - no cudaMalloc, cudaFree or allocating library routine is called.
+ */
+#define VSVB_NOALLOC_SCRATCH_DOUBLES (1 << 19)
+
+static __device__ __align__(256) double g_noalloc_scratch[VSVB_NOALLOC_SCRATCH_DOUBLES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+double *g_noalloc_addr[kMaxDevices] = {};
+std::mutex g_noalloc_mu;
+}  // namespace
+
+extern "C" int vsvb_det_factor_noalloc(const double *a_dev, int n, int nmat, double *det_dev, double *inv_dev,
+                                       int *sing_dev, void *stream) {
+  if (n < 1 || nmat < 0 || !a_dev || !det_dev || !inv_dev || !sing_dev) return VSVB_ERR_INPUT;
+  if ((double)2 * n * n * (double)nmat > (double)VSVB_NOALLOC_SCRATCH_DOUBLES) return VSVB_ERR_TOO_LARGE;
+  if (nmat == 0) return VSVB_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return VSVB_ERR_CUDA;
+  double *scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void *addr = nullptr;
+      if (cudaGetSymbolAddress(&addr, g_noalloc_scratch) != cudaSuccess || !addr) return VSVB_ERR_CUDA;
+      g_noalloc_addr[dev] = static_cast<double *>(addr);
+    }
+    scratch = g_noalloc_addr[dev];
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  det_factor_kernel<<<nmat, GJ_THREADS, 0, st>>>(a_dev, n, scratch, det_dev, inv_dev, sing_dev);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return e == cudaSuccess ? VSVB_OK : VSVB_ERR_CUDA;
 }
