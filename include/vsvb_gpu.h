@@ -51,8 +51,9 @@ typedef enum vsvb_status {
 
 /* Precision modes of the ERI contraction. */
 typedef enum vsvb_precision {
-  VSVB_FP64 = 0,  /* every shell quartet in FP64 */
-  VSVB_MIXED = 1  /* quartets whose Schwarz bound is below mixed_threshold in FP32 */
+  VSVB_FP64 = 0,      /* every shell quartet in FP64 */
+  VSVB_MIXED = 1,     /* quartets whose Schwarz bound is below mixed_threshold in FP32, the rest in FP64 */
+  VSVB_MIXED_DF64 = 2 /* as VSVB_MIXED, but the rest in double-float (FP32 pairs, ~48-bit) on the FP32 pipes */
 } vsvb_precision;
 
 /*

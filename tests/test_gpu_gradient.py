@@ -98,3 +98,30 @@ def test_mixed_precision_error_bound(vg, tmp_path):
     rm = vg.System(p, precision=vg.MIXED).energy()
     assert rm["n_quartets_fp32"] > 0
     assert abs(rm["energy"] - e64) <= 1e-6
+
+
+def test_double_float_path_matches_fp64(vg, tmp_path):
+    """VSVB_MIXED_DF64 runs the FP64-designated quartets in double-float
+    (FP32 pairs) with double-float Rys roots; with threshold 0 every quartet
+    takes that path and must reproduce FP64 to near FP64 accuracy."""
+    from valence_gb300 import configs
+    p = configs.ch_chain(str(tmp_path / "chain.inp"))
+    r64, g64 = vg.System(p, precision=vg.FP64).energy_grad()
+    rdf, gdf = vg.System(p, precision=vg.MIXED_DF64, mixed_threshold=0.0).energy_grad()
+    assert rdf["n_quartets_fp32"] == 0
+    assert abs(rdf["energy"] - r64["energy"]) < 1e-10 * abs(r64["energy"])
+    assert np.max(np.abs(gdf - g64)) < 1e-9 * max(1.0, np.abs(g64).max())
+    rm, gm = vg.System(p, precision=vg.MIXED_DF64).energy_grad()
+    assert rm["n_quartets_fp32"] > 0
+    assert abs(rm["energy"] - r64["energy"]) <= 1e-6
+
+
+def test_double_float_golden(vg):
+    """A spin-coupled golden case through the double-float path."""
+    import json
+    from tests import oracle_py
+    g = {c["name"]: c for c in oracle_py.goldens()["cases"] if c["suite"] == "testing"}
+    for name in ("h2o-vdz", "c2-pt-vshf-p2", "cu+"):
+        s = vg.System(os.path.join(ROOT, "tests", "golden", g[name]["input"]), precision=vg.MIXED_DF64,
+                      mixed_threshold=0.0)
+        assert abs(s.energy()["energy"] - g[name]["guess_energy"]) < 1e-8, name

@@ -18,6 +18,7 @@ import numpy as np
 
 FP64 = 0
 MIXED = 1
+MIXED_DF64 = 2
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None

@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libvsvb_gb300.so")
-CU = ["eri.cu", "density.cu", "onee.cu", "handle.cu", "peak.cu", "detfactor.cu"]
+CU = ["eri.cu", "eri_f64.cu", "eri_f32.cu", "eri_df64.cu", "density.cu", "onee.cu", "handle.cu", "peak.cu",
+      "detfactor.cu"]
 CPP = ["input.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

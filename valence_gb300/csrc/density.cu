@@ -95,7 +95,7 @@ __device__ __forceinline__ QInfo decode_q(const DetCtx &d, long long q) {
 
 /* exact determinant of spin block sp of pair q with up to two strikes, by LU
  * with partial pivoting on the struck matrix (n <= VSVB_MAXN) */
-__device__ double struck_det_exact(const DetCtx &d, const QInfo &qi, int sp, int ns, const int *rr, const int *cc) {
+__device__ __noinline__ double struck_det_exact(const DetCtx &d, const QInfo &qi, int sp, int ns, const int *rr, const int *cc) {
   const int n = sp == 0 ? d.ds.nalpha : d.ds.nbeta;
   double M[VSVB_MAXN * VSVB_MAXN];
   for (int r = 0; r < n; ++r) {

@@ -5,10 +5,21 @@
 
 #include "vsvb_internal.h"
 
+struct RysConst {
+  int off[5];            /* offset of each rule's Chebyshev block in the table */
+  double ax[5][5];       /* large-T limit: x_i = ax / T */
+  double aw[5][5];       /*                w_i = aw / sqrt(T) */
+  float2 axf[5][5], awf[5][5]; /* the same as (hi, lo) FP32 pairs */
+};
+
 struct EriArgs {
+  RysConst rc;
+  const void *prim64, *prim32, *primdf; /* PrimT<double|float|df64> per primitive pair */
+  const void *geom64, *geom32, *geomdf; /* GeomT<...> per shell pair */
   const ShellPair *pairs;
   const PrimPair *prims;
   const double *rys;       /* Chebyshev tables (device) */
+  const float2 *rysdf;     /* the same coefficients as (hi, lo) FP32 pairs */
   const int *pair_opid;    /* orbital-pair index of every pair term */
   const double *xtab;      /* X tables */
   double *T;               /* np x np orbital-pair ERIs (mode 0) */
@@ -18,10 +29,16 @@ struct EriArgs {
   double *xbar;            /* mode 2: dE/dX */
 };
 
-/* cp >= cq are pair classes 0..5; mode 0 forward, 1 Schwarz, 2 adjoint. */
-int eri_launch(int mode, int fp32, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int nsm,
+/* arithmetic kinds of the ERI kernels */
+enum { ERI_F64 = 0, ERI_F32 = 1, ERI_DF64 = 2 };
+
+/* cp >= cq are pair classes 0..5; mode 0 forward, 1 Schwarz (F64 only),
+ * 2 adjoint, 3 forward + adjoint. */
+int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int nsm,
                cudaStream_t st);
+int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
+int eri_dispatch_f32(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
+int eri_dispatch_df64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
 double eri_flops(int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ);
 int eri_symmetrize(double *T, int np, cudaStream_t st);
-int eri_set_tables(const int *off, const double *ax, const double *aw);
 #endif

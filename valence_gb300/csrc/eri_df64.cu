@@ -1,0 +1,11 @@
+/*
+ * eri_df64.cu -- instantiation of the shell-quartet ERI kernels
+ * (eri_impl.cuh) with df64 arithmetic in the 2D tables and component sums.
+ */
+#include "eri_impl.cuh"
+
+int eri_dispatch_df64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st) {
+  if (mode == 0) return dispatch<df64, 0>(cp, cq, a, w, n, nsm, st);
+  if (mode == 3) return dispatch<df64, 3>(cp, cq, a, w, n, nsm, st);
+  return 3;
+}

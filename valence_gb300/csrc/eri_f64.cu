@@ -1,0 +1,13 @@
+/*
+ * eri_f64.cu -- instantiation of the shell-quartet ERI kernels
+ * (eri_impl.cuh) with double arithmetic in the 2D tables and component sums.
+ */
+#include "eri_impl.cuh"
+
+int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st) {
+  if (mode == 0) return dispatch<double, 0>(cp, cq, a, w, n, nsm, st);
+  if (mode == 1) return dispatch<double, 1>(cp, cq, a, w, n, nsm, st);
+  if (mode == 2) return dispatch<double, 2>(cp, cq, a, w, n, nsm, st);
+  if (mode == 3) return dispatch<double, 3>(cp, cq, a, w, n, nsm, st);
+  return 3;
+}

@@ -1,0 +1,684 @@
+/*
+ * eri_impl.cuh -- shell-quartet electron-repulsion integrals fused with the
+ * LCAO-weight contraction of VALENCE's int2e (valence.F90:3184-3438),
+ * templated on the arithmetic of the 2D tables and component sums.
+ *
+ * int2e contracts every shell quartet of four orbital bases with the weight
+ * products dij(ab) dkl(cd) (valence.F90:3372-3412).  Here each unique AO shell
+ * quartet (AB|CD) is evaluated once and transformed straight into the
+ * orbital-pair matrix
+ *     U[(i,k)][(j,l)] += sum_ab sum_cd X_ik(ab) (ab|cd) X_jl(cd),
+ * X_ik(ab) = angn_a angn_b (C_i(a) C_k(b) + C_k(a) C_i(b)); T = U + U^T then
+ * holds every (i k | j l) that vsvb_energy asks int2e for (valence.F90:1256,
+ * 1264) and the Schwarz table (:1516).  No AO integral is written to HBM.
+ *
+ * Integrals: Rys quadrature (Rys, Dupuis & King, J. Comput. Chem. 4, 154
+ * (1983)) with the 2D recurrences for the x, y, z factors and horizontal
+ * transfer to the second centre of each pair; roots and weights come from
+ * project-generated Chebyshev tables (gen_rys_tables.py).
+ *
+ * Work split.  Per primitive quartet, 3*n_r lanes build the x/y/z 2D tables
+ * of the n_r roots in shared memory, then lanes accumulate their share of
+ * the Cartesian components in registers.  Small blocks run G primitive
+ * quartets side by side in one warp (one warp per shell quartet); large
+ * blocks (>= 200 components) put a whole CTA on one shell quartet, its warps
+ * splitting the primitive quartets, so that classes with few quartets still
+ * fill the SMs.  After the primitive loop the block is staged in shared
+ * memory and transformed with the X tables; U is updated with FP64 atomics.
+ *
+ * Arithmetic.  R = double: everything FP64.  R = float or double-float
+ * (df64): the Boys argument T, 1/(p+q) and the prefactor are formed once per
+ * primitive quartet in FP64; the Chebyshev evaluation of the Rys roots and
+ * weights runs in double-float (its small high-order terms in FP32), so the
+ * roots keep FP64-class accuracy (~1e-14) on the FP32 pipes; 2D tables and
+ * component sums run in R.  The transform to U is FP64 in every case.
+ */
+#ifndef VSVB_ERI_IMPL_CUH
+#define VSVB_ERI_IMPL_CUH
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <type_traits>
+
+#include "eri.cuh"
+#include "vsvb_internal.h"
+
+namespace {
+
+/* Cartesian exponents in CCA order, l = 0..2: [l][k][xyz] */
+__constant__ int c_cart[3][6][3] = {
+    {{0, 0, 0}},
+    {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}},
+    {{2, 0, 0}, {1, 1, 0}, {1, 0, 1}, {0, 2, 0}, {0, 1, 1}, {0, 0, 2}}};
+
+constexpr int RYS_NCHEB_D = 12;
+constexpr double RYS_TMAX_D = 64.0;
+constexpr double RYS_H_D = 0.5;
+constexpr int RYS_DF_SPLIT = 5; /* Chebyshev terms >= this index are summed in FP32 */
+
+/* ---- double-float arithmetic -------------------------------------------- */
+
+__device__ __forceinline__ df64 df_quick(float s, float e) {
+  const float r = s + e;
+  return df64(r, e - (r - s));
+}
+__device__ __forceinline__ df64 operator+(df64 a, df64 b) {
+  const float s = a.hi + b.hi;
+  const float v = s - a.hi;
+  float e = (a.hi - (s - v)) + (b.hi - v);
+  e += a.lo + b.lo;
+  return df_quick(s, e);
+}
+__device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
+__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
+__device__ __forceinline__ df64 operator*(df64 a, df64 b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_quick(p, e);
+}
+__device__ __forceinline__ df64 &operator+=(df64 &a, df64 b) {
+  a = a + b;
+  return a;
+}
+
+/* reciprocal, square root and inverse square root in double-float: an
+ * FP32 first guess refined by one Newton step in df64 (~2^-46 relative) */
+__device__ __forceinline__ df64 df_recip(df64 a) {
+  const float r0 = 1.0f / a.hi;
+  const df64 e = df64(1.f) - a * df64(r0);
+  return df64(r0) + df64(r0) * e;
+}
+__device__ __forceinline__ df64 df_sqrt(df64 a) {
+  if (a.hi <= 0.f) return df64(0.f);
+  const float s0 = sqrtf(a.hi);
+  const df64 d = a - df64(s0) * df64(s0);
+  return df64(s0) + d * df64(0.5f / s0);
+}
+__device__ __forceinline__ df64 df_rsqrt(df64 a) { return df_recip(df_sqrt(a)); }
+
+/* acc += x*y*z.  For df64 the accumulator is kept unnormalised (hi, lo) and
+ * the two products skip their intermediate renormalisation. */
+__device__ __forceinline__ void acc3(double &acc, double x, double y, double z) { acc = fma(x * y, z, acc); }
+__device__ __forceinline__ void acc3(float &acc, float x, float y, float z) { acc = fmaf(x * y, z, acc); }
+__device__ __forceinline__ void acc3(df64 &acc, df64 x, df64 y, df64 z) {
+  const float p = x.hi * y.hi;
+  float e = fmaf(x.hi, y.hi, -p);
+  e = fmaf(x.hi, y.lo, e);
+  e = fmaf(x.lo, y.hi, e);
+  const float q = p * z.hi;
+  float f = fmaf(p, z.hi, -q);
+  f = fmaf(p, z.lo, f);
+  f = fmaf(e, z.hi, f);
+  const float s = acc.hi + q;
+  const float v = s - acc.hi;
+  const float err = (acc.hi - (s - v)) + (q - v);
+  acc.lo += err + f;
+  acc.hi = s;
+}
+__device__ __forceinline__ double to_double(double v) { return v; }
+__device__ __forceinline__ double to_double(float v) { return (double)v; }
+__device__ __forceinline__ double to_double(df64 v) { return (double)v.hi + (double)v.lo; }
+
+/* ---- Rys roots ------------------------------------------------------------ */
+
+__device__ __forceinline__ double clenshaw12(const double *__restrict__ c, double t) {
+  double b1 = 0.0, b2 = 0.0;
+#pragma unroll
+  for (int k = RYS_NCHEB_D - 1; k > 0; --k) {
+    double b0 = fma(2.0 * t, b1, c[k] - b2);
+    b2 = b1;
+    b1 = b0;
+  }
+  return fma(t, b1, c[0] - b2);
+}
+
+/* root r of the n-point rule in FP64: x (= t^2) and weight */
+__device__ __forceinline__ void rys_root(int n, int r, double T, const double *__restrict__ tab, const RysConst &rc,
+                                         double &x, double &w) {
+  if (T < RYS_TMAX_D) {
+    int j = (int)(T * (1.0 / RYS_H_D));
+    double t = (T - j * RYS_H_D) * (2.0 / RYS_H_D) - 1.0;
+    const double *c = tab + rc.off[n - 1] + (size_t)j * (2 * n) * RYS_NCHEB_D;
+    double fx = clenshaw12(c + r * RYS_NCHEB_D, t);
+    double fw = clenshaw12(c + (n + r) * RYS_NCHEB_D, t);
+    const double s = rsqrt(1.0 + T);
+    x = fx * s * s;
+    w = fw * s;
+  } else {
+    const double s = rsqrt(T);
+    x = rc.ax[n - 1][r] * s * s;
+    w = rc.aw[n - 1][r] * s;
+  }
+}
+
+/* Chebyshev sum in double-float: the high-order terms (below the FP32 noise
+ * of the result) in FP32, the rest in df64.  c: (hi, lo) coefficient pairs. */
+__device__ __forceinline__ df64 clenshaw12_df(const float2 *__restrict__ c, df64 t) {
+  float b1f = 0.f, b2f = 0.f;
+  const float t2f = 2.f * t.hi;
+#pragma unroll
+  for (int k = RYS_NCHEB_D - 1; k >= RYS_DF_SPLIT; --k) {
+    const float b0 = fmaf(t2f, b1f, c[k].x - b2f);
+    b2f = b1f;
+    b1f = b0;
+  }
+  df64 b1(b1f), b2(b2f);
+  const df64 t2 = t + t;
+#pragma unroll
+  for (int k = RYS_DF_SPLIT - 1; k > 0; --k) {
+    const df64 b0 = t2 * b1 - b2 + df64(c[k].x, c[k].y);
+    b2 = b1;
+    b1 = b0;
+  }
+  return t * b1 - b2 + df64(c[0].x, c[0].y);
+}
+
+/* root r in double-float; interval j, Chebyshev variable t and
+ * s = (1+T)^(-1/2) (or T^(-1/2) beyond the tables) given */
+__device__ __forceinline__ void rys_root_df(int n, int r, int j, bool in_table, df64 t, df64 s,
+                                            const float2 *__restrict__ tab, const RysConst &rc, df64 &x, df64 &w) {
+  if (in_table) {
+    const float2 *c = tab + rc.off[n - 1] + (size_t)j * (2 * n) * RYS_NCHEB_D;
+    const df64 fx = clenshaw12_df(c + r * RYS_NCHEB_D, t);
+    const df64 fw = clenshaw12_df(c + (n + r) * RYS_NCHEB_D, t);
+    x = fx * s * s;
+    w = fw * s;
+  } else {
+    x = df64(rc.axf[n - 1][r].x, rc.axf[n - 1][r].y) * s * s;
+    w = df64(rc.awf[n - 1][r].x, rc.awf[n - 1][r].y) * s;
+  }
+}
+
+__device__ __forceinline__ const PrimT<df64> *args_primdf(const EriArgs &a) {
+  return static_cast<const PrimT<df64> *>(a.primdf);
+}
+
+/* per-precision views of the primitive-pair and pair-geometry arrays */
+template <typename R>
+struct prec_data;
+template <>
+struct prec_data<double> {
+  static __device__ const void *prim(const EriArgs &a) { return a.prim64; }
+  static __device__ const void *geom(const EriArgs &a) { return a.geom64; }
+};
+template <>
+struct prec_data<float> {
+  static __device__ const void *prim(const EriArgs &a) { return a.prim32; }
+  static __device__ const void *geom(const EriArgs &a) { return a.geom32; }
+};
+template <>
+struct prec_data<df64> {
+  static __device__ const void *prim(const EriArgs &a) { return a.primdf; }
+  static __device__ const void *geom(const EriArgs &a) { return a.geomdf; }
+};
+
+template <typename R>
+__device__ __forceinline__ R from_df(df64 v);
+template <>
+__device__ __forceinline__ float from_df<float>(df64 v) {
+  return v.hi + v.lo;
+}
+template <>
+__device__ __forceinline__ df64 from_df<df64>(df64 v) {
+  return v;
+}
+
+template <int L>
+struct NC {
+  static constexpr int v = (L + 1) * (L + 2) / 2;
+};
+
+/* x (or y, z) 2D factor for one root: G(i,k) by the Rys recurrences, then
+ * horizontal transfer to (ia, ib, kc, kd) */
+template <int LA, int LB, int LC, int LD, typename R>
+__device__ __forceinline__ void rys_2d(R g00, R c00, R d00, R b00, R b10, R b01, R ab, R cd, R *__restrict__ out) {
+  constexpr int LAB = LA + LB, LCD = LC + LD;
+  R G[LAB + 1][LCD + 1];
+  G[0][0] = g00;
+#pragma unroll
+  for (int i = 0; i < LAB; ++i) G[i + 1][0] = c00 * G[i][0] + (i > 0 ? R(i) * b10 * G[i > 0 ? i - 1 : 0][0] : R(0));
+#pragma unroll
+  for (int k = 0; k < LCD; ++k) {
+#pragma unroll
+    for (int i = 0; i <= LAB; ++i) {
+      R v = d00 * G[i][k];
+      if (k > 0) v += R(k) * b01 * G[i][k > 0 ? k - 1 : 0];
+      if (i > 0) v += R(i) * b00 * G[i > 0 ? i - 1 : 0][k];
+      G[i][k + 1] = v;
+    }
+  }
+  /* ket transfer: K[i][c][d] = G(i, c+d) reduced to (c,d) */
+  R K[LAB + 1][LC + 1][LD + 1];
+#pragma unroll
+  for (int i = 0; i <= LAB; ++i) {
+    R W[LCD + 1][LD + 1];
+#pragma unroll
+    for (int c = 0; c <= LCD; ++c) W[c][0] = G[i][c];
+#pragma unroll
+    for (int d = 1; d <= LD; ++d)
+#pragma unroll
+      for (int c = 0; c <= LCD - d; ++c) W[c][d] = W[c + 1][d - 1] + cd * W[c][d - 1];
+#pragma unroll
+    for (int c = 0; c <= LC; ++c)
+#pragma unroll
+      for (int d = 0; d <= LD; ++d) K[i][c][d] = W[c][d];
+  }
+  /* bra transfer */
+#pragma unroll
+  for (int c = 0; c <= LC; ++c)
+#pragma unroll
+    for (int d = 0; d <= LD; ++d) {
+      R V[LAB + 1][LB + 1];
+#pragma unroll
+      for (int a = 0; a <= LAB; ++a) V[a][0] = K[a][c][d];
+#pragma unroll
+      for (int b = 1; b <= LB; ++b)
+#pragma unroll
+        for (int a = 0; a <= LAB - b; ++a) V[a][b] = V[a + 1][b - 1] + ab * V[a][b - 1];
+#pragma unroll
+      for (int a = 0; a <= LA; ++a)
+#pragma unroll
+        for (int b = 0; b <= LB; ++b) out[((a * (LB + 1) + b) * (LC + 1) + c) * (LD + 1) + d] = V[a][b];
+    }
+}
+
+constexpr int WARPS = 4;
+
+template <int LA, int LB, int LC, int LD>
+struct QuartetShape {
+  static constexpr int NA = NC<LA>::v, NB = NC<LB>::v, NCc = NC<LC>::v, ND = NC<LD>::v;
+  static constexpr int NAB = NA * NB, NCD = NCc * ND, NCOMP = NAB * NCD;
+  static constexpr int NR = (LA + LB + LC + LD) / 2 + 1;
+  static constexpr int N2D = (LA + 1) * (LB + 1) * (LC + 1) * (LD + 1);
+  /* primitive quartets processed side by side per warp iteration: each takes
+   * 3*NR lanes for its 2D tables; large blocks keep one slot per warp (their
+   * per-lane accumulators must stay in registers) and put the CTA's warps on
+   * one shell quartet instead */
+  static constexpr int G0 = 32 / (3 * NR);
+  static constexpr bool CTA = NCOMP >= 200;
+  static constexpr int G = CTA ? 1 : (G0 < 1 ? 1 : G0);
+  static constexpr int NITEM = G * NCOMP;
+  static constexpr int PER_LANE = (NITEM + 31) / 32;
+  static constexpr int JCH = 8; /* ket orbital pairs per transform chunk */
+  static constexpr int NMAX = NAB > NCD ? NAB : NCD;
+  static constexpr int SM_2D = G * 3 * NR * N2D; /* per warp, doubles */
+  static constexpr int SM_ROOT = 2 * 32 * NR + 32; /* per warp: roots, weights, 1/(p+q) */
+  /* staging: E[NCOMP] + max(slot buffer, transform chunk); per warp in warp
+   * mode, one per CTA in CTA mode */
+  static constexpr int SM_TR = NCOMP + (NITEM > JCH * NMAX ? NITEM : JCH * NMAX);
+  static constexpr int PER_WARP = CTA ? SM_2D + SM_ROOT : (SM_2D + SM_ROOT > SM_TR ? SM_2D + SM_ROOT : SM_TR);
+  static constexpr int SHARED = CTA ? SM_TR : 0;
+};
+
+/*
+ * MODE 0: forward transform into U.
+ * MODE 1: Schwarz diagonal -- qmax_out[P] = sqrt(max_ab |(ab|ab)|).
+ * MODE 2: adjoint -- accumulate dE/dX for both pairs from Tbar.
+ * MODE 3: forward and adjoint from one evaluation of each quartet.
+ */
+template <int LA, int LB, int LC, int LD, typename R, int MODE>
+__global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int2 *__restrict__ work, int nwork) {
+  using S = QuartetShape<LA, LB, LC, LD>;
+  constexpr bool CTA = S::CTA;
+  constexpr bool DFROOT = !std::is_same<R, double>::value;
+  extern __shared__ double smem[];
+  int *idx = reinterpret_cast<int *>(smem);
+  double *wbase = smem + (S::NCOMP + 1) / 2 + 1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *ws = wbase + (size_t)warp * S::PER_WARP;
+  /* staging area: per warp (warp mode) or shared by the CTA */
+  double *stage = CTA ? wbase + (size_t)WARPS * S::PER_WARP : ws;
+  const int tid = CTA ? (int)threadIdx.x : lane;
+  const int nthr = CTA ? (int)blockDim.x : 32;
+
+  for (int c = threadIdx.x; c < S::NCOMP; c += blockDim.x) {
+    int a = c / (S::NB * S::NCD), b = (c / S::NCD) % S::NB, cc = (c / S::ND) % S::NCc, d = c % S::ND;
+    int pw[4][3];
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+      pw[0][t] = c_cart[LA][a][t];
+      pw[1][t] = c_cart[LB][b][t];
+      pw[2][t] = c_cart[LC][cc][t];
+      pw[3][t] = c_cart[LD][d][t];
+    }
+    const int ix = ((pw[0][0] * (LB + 1) + pw[1][0]) * (LC + 1) + pw[2][0]) * (LD + 1) + pw[3][0];
+    const int iy = ((pw[0][1] * (LB + 1) + pw[1][1]) * (LC + 1) + pw[2][1]) * (LD + 1) + pw[3][1];
+    const int iz = ((pw[0][2] * (LB + 1) + pw[1][2]) * (LC + 1) + pw[2][2]) * (LD + 1) + pw[3][2];
+    idx[c] = ix | (iy << 10) | (iz << 20);
+  }
+  __syncthreads();
+
+  R *h2d = reinterpret_cast<R *>(ws);
+  const double two_pi_25 = 34.98683665524972; /* 2 pi^(5/2) */
+  const PrimT<R> *__restrict__ primR = static_cast<const PrimT<R> *>(prec_data<R>::prim(args));
+  const GeomT<R> *__restrict__ geomR = static_cast<const GeomT<R> *>(prec_data<R>::geom(args));
+
+  const int item0 = CTA ? (int)blockIdx.x : (int)blockIdx.x * WARPS + warp;
+  const int istep = CTA ? (int)gridDim.x : (int)gridDim.x * WARPS;
+  for (int item = item0; item < nwork; item += istep) {
+    const int2 pq = work[item];
+    const ShellPair &P = args.pairs[pq.x];
+    const ShellPair &Q = args.pairs[pq.y];
+    R acc[S::PER_LANE];
+#pragma unroll
+    for (int m = 0; m < S::PER_LANE; ++m) acc[m] = R(0);
+    const int npq = P.nprim * Q.nprim;
+    /* lane roles in phase A: slot g, root r, direction dir */
+    const int g = lane / (3 * S::NR), rem = lane - g * (3 * S::NR);
+    const int r = rem / 3, dir = rem - 3 * (rem / 3);
+    const bool lane_a = g < S::G;
+    /* this warp's chunks of 32 primitive quartets */
+    const int cfirst = CTA ? warp * 32 : 0;
+    const int cstep = CTA ? WARPS * 32 : 32;
+    R *rx = reinterpret_cast<R *>(ws + S::SM_2D); /* [32][NR] roots */
+    R *rw = rx + 32 * S::NR;                      /* [32][NR] scaled weights */
+    R *ripq = rw + 32 * S::NR;                    /* [32] 1/(p+q) */
+
+    for (int chunk = cfirst; chunk < npq; chunk += cstep) {
+      /* phase R: one primitive quartet per lane -- Boys argument, 1/(p+q),
+       * prefactor and the n_r Rys roots/weights */
+      {
+        const int pqi = chunk + lane;
+        if (pqi < npq) {
+          const int ip = pqi / Q.nprim, iq = pqi - ip * Q.nprim;
+          if constexpr (!DFROOT) {
+            const PrimPair &pp = args.prims[P.prim0 + ip];
+            const PrimPair &qq = args.prims[Q.prim0 + iq];
+            const double p = pp.p, q = qq.p;
+            const double ipq = 1.0 / (p + q);
+            const double dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
+            const double Tb = p * q * ipq * (dx * dx + dy * dy + dz * dz);
+            const double pref = two_pi_25 * pp.Kp * qq.Kp * sqrt(ipq);
+#pragma unroll
+            for (int rr = 0; rr < S::NR; ++rr) {
+              double u, w;
+              rys_root(S::NR, rr, Tb, args.rys, args.rc, u, w);
+              rx[lane * S::NR + rr] = R(u);
+              rw[lane * S::NR + rr] = R(w * pref);
+            }
+            ripq[lane] = R(ipq);
+          } else {
+            /* double-float throughout: no FP64 instruction on this path */
+            const PrimT<df64> &pp = args_primdf(args)[P.prim0 + ip];
+            const PrimT<df64> &qq = args_primdf(args)[Q.prim0 + iq];
+            const df64 pq = pp.p + qq.p;
+            const df64 ipq = df_recip(pq);
+            const df64 dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
+            const df64 Tb = pp.p * qq.p * ipq * (dx * dx + dy * dy + dz * dz);
+            const df64 pref = df64(34.98683547973633f, 1.1755134e-06f) /* 2 pi^(5/2) */ * pp.Kp * qq.Kp * df_sqrt(ipq);
+            const float Tf = Tb.hi;
+            df64 t(0.f), sc(0.f);
+            int j = 0;
+            if (Tf < (float)RYS_TMAX_D) {
+              j = (int)(Tf * (float)(1.0 / RYS_H_D));
+              /* guard the interval choice against hi-part rounding at its edge */
+              const df64 tj = Tb - df64((float)(j * RYS_H_D));
+              if (tj.hi < 0.f) {
+                --j;
+              } else if (tj.hi >= (float)RYS_H_D) {
+                ++j;
+              }
+              j = max(0, min(j, (int)(RYS_TMAX_D / RYS_H_D) - 1));
+              t = (Tb - df64((float)(j * RYS_H_D))) * df64((float)(2.0 / RYS_H_D)) - df64(1.f);
+              sc = df_rsqrt(Tb + df64(1.f));
+            } else {
+              sc = df_rsqrt(Tb);
+            }
+#pragma unroll
+            for (int rr = 0; rr < S::NR; ++rr) {
+              df64 x, w;
+              rys_root_df(S::NR, rr, j, Tf < (float)RYS_TMAX_D, t, sc, args.rysdf, args.rc, x, w);
+              rx[lane * S::NR + rr] = from_df<R>(x);
+              rw[lane * S::NR + rr] = from_df<R>(w * pref);
+            }
+            ripq[lane] = from_df<R>(ipq);
+          }
+        }
+      }
+      __syncwarp();
+      const int nch = min(32, npq - chunk);
+      for (int sub = 0; sub < nch; sub += S::G) {
+        const int li = sub + g; /* local index of this slot's primitive quartet */
+        const bool act = lane_a && li < nch;
+        if (act) {
+          const int pqi = chunk + li;
+          const int ip = pqi / Q.nprim, iq = pqi - ip * Q.nprim;
+          const R uR = rx[li * S::NR + r], wR = rw[li * S::NR + r], ipqR = ripq[li];
+          /* 2D recurrence coefficients in R, from the primitive-pair and
+           * pair-geometry data stored in R */
+          const PrimT<R> &pr = primR[P.prim0 + ip], &qr = primR[Q.prim0 + iq];
+          const GeomT<R> &gp = geomR[pq.x], &gq = geomR[pq.y];
+          const R Pd = pr.P[dir], Qd = qr.P[dir];
+          const R PQ = Pd - Qd, uq = uR * ipqR;
+          const R b00 = R(0.5f) * uq;
+          const R b10 = R(0.5f) * pr.inv_p * (R(1) - qr.p * uq);
+          const R b01 = R(0.5f) * qr.inv_p * (R(1) - pr.p * uq);
+          const R c00 = (Pd - gp.A[dir]) - qr.p * uq * PQ;
+          const R d00 = (Qd - gq.A[dir]) + pr.p * uq * PQ;
+          const R g00 = dir == 2 ? wR : R(1);
+          rys_2d<LA, LB, LC, LD, R>(g00, c00, d00, b00, b10, b01, gp.AB[dir], gq.AB[dir],
+                                    h2d + (size_t)((g * 3 + dir) * S::NR + r) * S::N2D);
+        }
+        __syncwarp();
+        const int nact = min(S::G, nch - sub);
+#pragma unroll
+        for (int m = 0; m < S::PER_LANE; ++m) {
+          const int it = lane + 32 * m;
+          if (it < S::NITEM) {
+            const int gg = it / S::NCOMP, c = it - gg * S::NCOMP;
+            if (gg < nact) {
+              const int id = idx[c];
+              const int ix = id & 1023, iy = (id >> 10) & 1023, iz = id >> 20;
+              const R *hx = h2d + (size_t)(gg * 3 + 0) * S::NR * S::N2D;
+              const R *hy = hx + S::NR * S::N2D, *hz = hy + S::NR * S::N2D;
+              R sacc = acc[m];
+#pragma unroll
+              for (int rr = 0; rr < S::NR; ++rr)
+                acc3(sacc, hx[rr * S::N2D + ix], hy[rr * S::N2D + iy], hz[rr * S::N2D + iz]);
+              acc[m] = sacc;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
+
+    /* stage the block: E[c] (double) */
+    double *E = stage;
+    if (CTA) {
+      for (int c = tid; c < S::NCOMP; c += nthr) E[c] = 0.0;
+      __syncthreads();
+#pragma unroll
+      for (int m = 0; m < S::PER_LANE; ++m) {
+        const int c = lane + 32 * m;
+        if (c < S::NCOMP) atomicAdd(E + c, to_double(acc[m]));
+      }
+      __syncthreads();
+    } else if (S::G == 1) {
+#pragma unroll
+      for (int m = 0; m < S::PER_LANE; ++m) {
+        const int c = lane + 32 * m;
+        if (c < S::NCOMP) E[c] = to_double(acc[m]);
+      }
+      __syncwarp();
+    } else {
+      double *E2 = stage + S::NCOMP;
+#pragma unroll
+      for (int m = 0; m < S::PER_LANE; ++m) {
+        const int it = lane + 32 * m;
+        if (it < S::NITEM) E2[it] = to_double(acc[m]);
+      }
+      __syncwarp();
+      for (int c = lane; c < S::NCOMP; c += 32) {
+        double sum = 0.0;
+        for (int gg = 0; gg < S::G; ++gg) sum += E2[gg * S::NCOMP + c];
+        E[c] = sum;
+      }
+      __syncwarp();
+    }
+    if (MODE == 1) {
+      /* Schwarz: max over diagonal components (ab|ab), by the first warp */
+      if (!CTA || warp == 0) {
+        double mx = 0.0;
+        for (int c = lane; c < S::NCOMP; c += 32)
+          if ((c / S::NCD) == (c % S::NCD)) mx = fmax(mx, fabs(E[c]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) args.qmax_out[pq.x] = sqrt(mx);
+      }
+      if (CTA) __syncthreads();
+      else __syncwarp();
+      continue;
+    }
+
+    double *Y = stage + S::NCOMP;
+    const double *XP = args.xtab + P.x0;
+    const double *XQ = args.xtab + Q.x0;
+    const int *opP = args.pair_opid + P.op0;
+    const int *opQ = args.pair_opid + Q.op0;
+    const bool same = pq.x == pq.y;
+    auto sync = [&]() {
+      if (CTA) __syncthreads();
+      else __syncwarp();
+    };
+    if (MODE == 0 || MODE == 3) {
+      for (int j0 = 0; j0 < Q.nop; j0 += S::JCH) {
+        const int nj = min(S::JCH, Q.nop - j0);
+        /* Y[jl][ab] = sum_cd E[ab][cd] X_Q[jl][cd] */
+        for (int o = tid; o < nj * S::NAB; o += nthr) {
+          const int jl = o / S::NAB, abi = o - jl * S::NAB;
+          const double *xq = XQ + (size_t)(j0 + jl) * S::NCD;
+          const double *e = E + abi * S::NCD;
+          double s = 0.0;
+#pragma unroll
+          for (int c = 0; c < S::NCD; ++c) s = fma(e[c], __ldg(xq + c), s);
+          Y[o] = s;
+        }
+        sync();
+        /* Z[ik][jl] = sum_ab X_P[ik][ab] Y[jl][ab] -> U (one orientation) */
+        for (int o = tid; o < P.nop * nj; o += nthr) {
+          const int ik = o / nj, jl = o - ik * nj;
+          const double *xp = XP + (size_t)ik * S::NAB;
+          const double *y = Y + jl * S::NAB;
+          double s = 0.0;
+#pragma unroll
+          for (int c = 0; c < S::NAB; ++c) s = fma(__ldg(xp + c), y[c], s);
+          const int a = __ldg(opP + ik), b = __ldg(opQ + j0 + jl);
+          atomicAdd(args.T + (size_t)a * args.np + b, same ? 0.5 * s : s);
+        }
+        sync();
+      }
+    }
+    if (MODE == 2 || MODE == 3) {
+      /* adjoint.  With Z(ik,jl) = X_P E X_Q^T and W = dE/dZ
+       * (Tbar[ik][jl] (+ Tbar[jl][ik] when the pairs differ)):
+       * dX_P[ik][ab] += sum_jl W(ik,jl) (E X_Q^T)[ab][jl] and
+       * dX_Q[jl][cd] += sum_ik W(ik,jl) (X_P E)[ik][cd] */
+      double *XPb = args.xbar + P.x0;
+      double *XQb = args.xbar + Q.x0;
+      for (int j0 = 0; j0 < Q.nop; j0 += S::JCH) {
+        const int nj = min(S::JCH, Q.nop - j0);
+        for (int o = tid; o < nj * S::NAB; o += nthr) {
+          const int jl = o / S::NAB, abi = o - jl * S::NAB;
+          const double *xq = XQ + (size_t)(j0 + jl) * S::NCD;
+          const double *e = E + abi * S::NCD;
+          double s = 0.0;
+#pragma unroll
+          for (int c = 0; c < S::NCD; ++c) s = fma(e[c], __ldg(xq + c), s);
+          Y[o] = s;
+        }
+        sync();
+        for (int o = tid; o < P.nop * S::NAB; o += nthr) {
+          const int ik = o / S::NAB, abi = o - ik * S::NAB;
+          const int a = __ldg(opP + ik);
+          double s = 0.0;
+          for (int jl = 0; jl < nj; ++jl) {
+            const int b = __ldg(opQ + j0 + jl);
+            double wv = args.Tbar[(size_t)a * args.np + b];
+            if (!same) wv += args.Tbar[(size_t)b * args.np + a];
+            s = fma(wv, Y[jl * S::NAB + abi], s);
+          }
+          atomicAdd(XPb + (size_t)ik * S::NAB + abi, s);
+        }
+        sync();
+      }
+      constexpr int ICH = S::JCH;
+      for (int i0 = 0; i0 < P.nop; i0 += ICH) {
+        const int ni = min(ICH, P.nop - i0);
+        for (int o = tid; o < ni * S::NCD; o += nthr) {
+          const int ik = o / S::NCD, cdi = o - ik * S::NCD;
+          const double *xp = XP + (size_t)(i0 + ik) * S::NAB;
+          double s = 0.0;
+#pragma unroll
+          for (int c = 0; c < S::NAB; ++c) s = fma(__ldg(xp + c), E[c * S::NCD + cdi], s);
+          Y[o] = s;
+        }
+        sync();
+        for (int o = tid; o < Q.nop * S::NCD; o += nthr) {
+          const int jl = o / S::NCD, cdi = o - jl * S::NCD;
+          const int b = __ldg(opQ + jl);
+          double s = 0.0;
+          for (int ik = 0; ik < ni; ++ik) {
+            const int a = __ldg(opP + i0 + ik);
+            double wv = args.Tbar[(size_t)a * args.np + b];
+            if (!same) wv += args.Tbar[(size_t)b * args.np + a];
+            s = fma(wv, Y[ik * S::NCD + cdi], s);
+          }
+          atomicAdd(XQb + (size_t)jl * S::NCD + cdi, s);
+        }
+        sync();
+      }
+    }
+    if (CTA) __syncthreads();
+  }
+}
+
+template <int LA, int LB, int LC, int LD, typename R, int MODE>
+int launch_one(const EriArgs &args, const int2 *work, int nwork, int nsm, cudaStream_t st) {
+  if (nwork <= 0) return 0;
+  using S = QuartetShape<LA, LB, LC, LD>;
+  size_t shm = sizeof(double) * ((S::NCOMP + 1) / 2 + 1 + (size_t)WARPS * S::PER_WARP + S::SHARED);
+  auto kfn = eri_kernel<LA, LB, LC, LD, R, MODE>;
+  static bool attr_done = false;
+  if (!attr_done) {
+    if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess) return 1;
+    attr_done = true;
+  }
+  const int per_block = S::CTA ? 1 : WARPS;
+  int blocks = (nwork + per_block - 1) / per_block;
+  int cap = nsm * 16;
+  if (blocks > cap) blocks = cap;
+  kfn<<<blocks, WARPS * 32, shm, st>>>(args, work, nwork);
+  return cudaGetLastError() != cudaSuccess;
+}
+
+/* class id of a pair (la>=lb): 00->0 10->1 11->2 20->3 21->4 22->5 */
+template <int C>
+struct ClsL;
+template <> struct ClsL<0> { static constexpr int a = 0, b = 0; };
+template <> struct ClsL<1> { static constexpr int a = 1, b = 0; };
+template <> struct ClsL<2> { static constexpr int a = 1, b = 1; };
+template <> struct ClsL<3> { static constexpr int a = 2, b = 0; };
+template <> struct ClsL<4> { static constexpr int a = 2, b = 1; };
+template <> struct ClsL<5> { static constexpr int a = 2, b = 2; };
+
+template <int CP, int CQ, typename R, int MODE>
+int launch_cls(const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st) {
+  return launch_one<ClsL<CP>::a, ClsL<CP>::b, ClsL<CQ>::a, ClsL<CQ>::b, R, MODE>(a, w, n, nsm, st);
+}
+
+template <typename R, int MODE>
+int dispatch(int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st) {
+#define CASE(X, Y) \
+  if (cp == X && cq == Y) return launch_cls<X, Y, R, MODE>(a, w, n, nsm, st);
+  CASE(0, 0) CASE(1, 0) CASE(1, 1) CASE(2, 0) CASE(2, 1) CASE(2, 2)
+  CASE(3, 0) CASE(3, 1) CASE(3, 2) CASE(3, 3) CASE(4, 0) CASE(4, 1) CASE(4, 2) CASE(4, 3) CASE(4, 4)
+  CASE(5, 0) CASE(5, 1) CASE(5, 2) CASE(5, 3) CASE(5, 4) CASE(5, 5)
+#undef CASE
+  return 2;
+}
+
+}  // namespace
+#endif

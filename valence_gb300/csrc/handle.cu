@@ -96,9 +96,17 @@ struct vsvb_gpu {
   /* device data */
   DBuf<GShell> shells;
   DBuf<double> exps, coefs, angn, charge, axyz, rys;
+  DBuf<float2> rysdf;
   DBuf<double> S_ao, H_ao;
   DBuf<ShellPair> pairs;
   DBuf<PrimPair> prims;
+  DBuf<PrimT<double>> prim64;
+  DBuf<PrimT<float>> prim32;
+  DBuf<PrimT<df64>> primdf;
+  DBuf<GeomT<double>> geom64;
+  DBuf<GeomT<float>> geom32;
+  DBuf<GeomT<df64>> geomdf;
+  RysConst rc{};
   DBuf<int> pair_opid;
   DBuf<XTerm> xterms;
   DBuf<long long> xelem0;
@@ -170,9 +178,17 @@ XtabArgs xtab_args(vsvb_gpu *h) {
 
 EriArgs eri_args(vsvb_gpu *h) {
   EriArgs a{};
+  a.rc = h->rc;
+  a.prim64 = h->prim64.p;
+  a.prim32 = h->prim32.p;
+  a.primdf = h->primdf.p;
+  a.geom64 = h->geom64.p;
+  a.geom32 = h->geom32.p;
+  a.geomdf = h->geomdf.p;
   a.pairs = h->pairs.p;
   a.prims = h->prims.p;
   a.rys = h->rys.p;
+  a.rysdf = h->rysdf.p;
   a.pair_opid = h->pair_opid.p;
   a.xtab = h->xtab.p;
   a.T = h->T.p;
@@ -218,6 +234,14 @@ AsmArgs asm_args(vsvb_gpu *h) {
   int na = h->ds.nalpha, nb = h->ds.nbeta;
   a.g_in_smem = (size_t)(na * na + nb * nb) * sizeof(double) <= 40 * 1024;
   return a;
+}
+
+/* arithmetic of a schedule: list 1 holds the quartets below the mixed
+ * threshold (FP32); list 0 the rest, in FP64 or, on VSVB_MIXED_DF64, in
+ * double-float */
+int eri_kind(const vsvb_gpu *h, int list) {
+  if (list == 1) return ERI_F32;
+  return h->opt.precision == VSVB_MIXED_DF64 ? ERI_DF64 : ERI_F64;
 }
 
 /* ---------------- set-up ---------------- */
@@ -520,6 +544,47 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   h->nxterm = (int)xterms.size();
   CK(h->pairs.upload(pairs), "upload pairs");
   CK(h->prims.upload(prims), "upload prims");
+  {
+    /* the same primitive-pair and pair data in each kernel arithmetic */
+    std::vector<PrimT<double>> p64(prims.size());
+    std::vector<PrimT<float>> p32(prims.size());
+    std::vector<PrimT<df64>> pdf(prims.size());
+    for (size_t i = 0; i < prims.size(); ++i) {
+      for (int k = 0; k < 3; ++k) {
+        p64[i].P[k] = prims[i].P[k];
+        p32[i].P[k] = (float)prims[i].P[k];
+        pdf[i].P[k] = df64(prims[i].P[k]);
+      }
+      p64[i].p = prims[i].p;
+      p64[i].inv_p = prims[i].inv_p;
+      p64[i].Kp = prims[i].Kp;
+      p32[i].p = (float)prims[i].p;
+      p32[i].inv_p = (float)prims[i].inv_p;
+      p32[i].Kp = (float)prims[i].Kp;
+      pdf[i].p = df64(prims[i].p);
+      pdf[i].inv_p = df64(prims[i].inv_p);
+      pdf[i].Kp = df64(prims[i].Kp);
+    }
+    std::vector<GeomT<double>> g64(pairs.size());
+    std::vector<GeomT<float>> g32(pairs.size());
+    std::vector<GeomT<df64>> gdf(pairs.size());
+    for (size_t i = 0; i < pairs.size(); ++i)
+      for (int k = 0; k < 3; ++k) {
+        const double A = pairs[i].A[k], AB = pairs[i].A[k] - pairs[i].B[k];
+        g64[i].A[k] = A;
+        g64[i].AB[k] = AB;
+        g32[i].A[k] = (float)A;
+        g32[i].AB[k] = (float)AB;
+        gdf[i].A[k] = df64(A);
+        gdf[i].AB[k] = df64(AB);
+      }
+    CK(h->prim64.upload(p64), "upload prim64");
+    CK(h->prim32.upload(p32), "upload prim32");
+    CK(h->primdf.upload(pdf), "upload primdf");
+    CK(h->geom64.upload(g64), "upload geom64");
+    CK(h->geom32.upload(g32), "upload geom32");
+    CK(h->geomdf.upload(gdf), "upload geomdf");
+  }
   CK(h->pair_opid.upload(opid), "upload opid");
   CK(h->xterms.upload(xterms), "upload xterms");
   CK(h->xelem0.upload(xelem0), "upload xelem0");
@@ -529,9 +594,24 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   /* Rys tables */
   CK(h->rys.upload(std::vector<double>(rys_table_data, rys_table_data + sizeof(rys_table_data) / sizeof(double))),
      "upload rys");
-  if (eri_set_tables(rys_table_offset, &rys_asym_x[0][0], &rys_asym_w[0][0])) {
-    h->err = "cannot set Rys constant tables";
-    return VSVB_ERR_CUDA;
+  {
+    const size_t nt = sizeof(rys_table_data) / sizeof(double);
+    std::vector<float2> df(nt);
+    for (size_t i = 0; i < nt; ++i) {
+      const float hi = (float)rys_table_data[i];
+      df[i] = make_float2(hi, (float)(rys_table_data[i] - (double)hi));
+    }
+    CK(h->rysdf.upload(df), "upload rysdf");
+  }
+  for (int k = 0; k < 5; ++k) {
+    h->rc.off[k] = rys_table_offset[k];
+    for (int r = 0; r < 5; ++r) {
+      h->rc.ax[k][r] = rys_asym_x[k][r];
+      h->rc.aw[k][r] = rys_asym_w[k][r];
+      const float axh = (float)rys_asym_x[k][r], awh = (float)rys_asym_w[k][r];
+      h->rc.axf[k][r] = make_float2(axh, (float)(rys_asym_x[k][r] - (double)axh));
+      h->rc.awf[k][r] = make_float2(awh, (float)(rys_asym_w[k][r] - (double)awh));
+    }
   }
   /* Schwarz bounds (diagonal quartets) */
   {
@@ -554,7 +634,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     CK(h->pairs.upload(pairs), "upload pairs");
   }
   /* quartet schedule */
-  const bool mixed = h->opt.precision == VSVB_MIXED;
+  const bool mixed = h->opt.precision == VSVB_MIXED || h->opt.precision == VSVB_MIXED_DF64;
   h->err_bound = 0.0;
   for (size_t P = 0; P < pairs.size(); ++P)
     for (size_t Q = 0; Q <= P; ++Q) {
@@ -711,7 +791,7 @@ int forward(vsvb_gpu *h, bool fused = false) {
       for (int c = 0; c <= a; ++c) {
         int n = (int)h->work_h[p][a][c].size();
         if (!n) continue;
-        if (eri_launch(fused ? 3 : 0, p, a, c, ea, h->work_d[p][a][c].p, n, h->nsm, st)) {
+        if (eri_launch(fused ? 3 : 0, eri_kind(h, p), a, c, ea, h->work_d[p][a][c].p, n, h->nsm, st)) {
           h->err = "ERI kernel launch failed";
           return VSVB_ERR_CUDA;
         }
@@ -790,7 +870,7 @@ int backward(vsvb_gpu *h, double e_num, double w, bool fused) {
       for (int c = 0; c <= a; ++c) {
         int n = (int)h->work_h[p][a][c].size();
         if (!n) continue;
-        if (eri_launch(2, p, a, c, ea, h->work_d[p][a][c].p, n, h->nsm, st)) {
+        if (eri_launch(2, eri_kind(h, p), a, c, ea, h->work_d[p][a][c].p, n, h->nsm, st)) {
           h->err = "ERI adjoint launch failed";
           return VSVB_ERR_CUDA;
         }
@@ -952,7 +1032,8 @@ int vsvb_gpu_eri_profile(vsvb_gpu *h, double *ms, double *flops, int *cls, int c
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         cudaEventRecord(e0, h->st);
-        if (eri_launch(0, p, a, c, ea, h->work_d[p][a][c].p, (int)w.size(), h->nsm, h->st)) return -VSVB_ERR_CUDA;
+        if (eri_launch(0, eri_kind(h, p), a, c, ea, h->work_d[p][a][c].p, (int)w.size(), h->nsm, h->st))
+          return -VSVB_ERR_CUDA;
         cudaEventRecord(e1, h->st);
         if (cudaEventSynchronize(e1) != cudaSuccess) return -VSVB_ERR_CUDA;
         float t = 0.f;
@@ -964,7 +1045,7 @@ int vsvb_gpu_eri_profile(vsvb_gpu *h, double *ms, double *flops, int *cls, int c
           f += eri_flops(a, c, pairs[q.x].nprim, pairs[q.y].nprim, pairs[q.x].nop, pairs[q.y].nop);
         ms[k] = t;
         flops[k] = f;
-        cls[k] = 100 * p + 10 * a + c;
+        cls[k] = 100 * eri_kind(h, p) + 10 * a + c;
         ++k;
       }
   return k;

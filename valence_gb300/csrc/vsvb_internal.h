@@ -39,6 +39,41 @@ struct PrimPair {
   double Kp;     /* c_a c_b exp(-alpha beta / p |AB|^2) / p */
 };
 
+#ifdef __CUDACC__
+#define VSVB_HD __host__ __device__
+#else
+#define VSVB_HD
+#endif
+
+/* double-float: an unevaluated sum hi + lo of two FP32 numbers (about 48
+ * significant bits), used on the mixed path for quartets that need
+ * FP64-class accuracy while running on the FP32 pipes */
+struct df64 {
+  float hi, lo;
+  df64() = default;
+  VSVB_HD df64(float h, float l) : hi(h), lo(l) {}
+  VSVB_HD df64(float h) : hi(h), lo(0.0f) {}
+  VSVB_HD df64(int i) : hi((float)i), lo(0.0f) {}
+  VSVB_HD explicit df64(double d) {
+    hi = (float)d;
+    lo = (float)(d - (double)hi);
+  }
+  VSVB_HD explicit operator double() const { return (double)hi + (double)lo; }
+};
+
+/* primitive-pair and pair-geometry data in the arithmetic type R of a kernel */
+template <typename R>
+struct PrimT {
+  R P[3];
+  R p, inv_p;
+  R Kp; /* c_a c_b exp(-alpha beta / p |AB|^2) / p */
+};
+template <typename R>
+struct GeomT {
+  R A[3];   /* first centre */
+  R AB[3];  /* A - B */
+};
+
 struct ShellPair {
   int shA, shB;      /* global shells; l(shA) >= l(shB) */
   int cls;           /* pair class 0..5 */
