@@ -1,0 +1,149 @@
+"""Host-side checks of the C ABI (no GPU needed).
+
+* the shared library exports every function include/vsvb_gpu.h declares;
+* vsvb_read_input (the product's reader, xm_module.F90:25-335 semantics)
+  agrees with an independent record-by-record parse of every golden input;
+* entry points fail with a status code, never a crash, when no GPU is present
+  or a request is malformed.
+"""
+import ctypes
+import math
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests import oracle_py
+
+ROOT = oracle_py.ROOT
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from valence_gb300 import api, build
+    build.build()
+    return api.lib()
+
+
+def _declared():
+    h = open(os.path.join(ROOT, "include", "vsvb_gpu.h")).read()
+    h = re.sub(r"/\*.*?\*/", "", h, flags=re.S)
+    return sorted(set(re.findall(r"\b(vsvb_[a-z0-9_]+)\s*\(", h)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from valence_gb300 import api
+    out = subprocess.run(["nm", "-D", "--defined-only", api.library_path()], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (vsvb_\w+)", out))
+    names = _declared()
+    assert len(names) >= 15
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+
+
+class _Rec:
+    """independent Fortran list-directed record reader for the check"""
+
+    def __init__(self, path):
+        self.lines = open(path).read().split("\n")
+        self.pos = 0
+
+    def read(self, types):
+        vals = []
+        while len(vals) < len(types):
+            toks = self.lines[self.pos].replace(",", " ").split()
+            self.pos += 1
+            vals += toks[: len(types) - len(vals)]
+        return [t(v.replace("d", "e").replace("D", "e")) for t, v in zip(types, vals)]
+
+
+def _parse(path):
+    r = _Rec(path)
+    d = r.read([int] * 15)
+    natom, natom_t, npair, nunpd, ndocc, totlen = d[:6]
+    nspinc, nset, nxorb, mxctr = d[7], d[12], d[13], d[14]
+    ndf = d[11]
+    tol = r.read([int] * 6 + [float] * 2 + [int] * (2 * nset))
+    atoms = [r.read([int, float, float, float]) for _ in range(natom)]
+    exps, ncoef = [], []
+    for _ in range(natom_t):
+        z, ns = r.read([float, int])
+        for _ in range(ns):
+            l, nc = r.read([int, int])
+            for _ in range(nc):
+                v = r.read([float] if nc == 1 else [float, float])
+                exps.append(v[0])
+    if npair > 0:
+        r.read(([float] if nspinc > 1 else []) * 1 + [int] * (2 * npair)) if nspinc == 1 else \
+            r.read(([float] + [int] * (2 * npair)) * nspinc)
+    if nxorb > 0:
+        r.read([int] * (2 * nxorb))
+    coeff = []
+    for _ in range(2 * npair + nunpd + ndocc + ndf):
+        head = r.read([int])
+        n_at = head[0]
+        r.pos -= 1
+        head = r.read([int] * (n_at + 2))
+        vals = r.read([int, float] * head[-1])
+        coeff += vals[1::2]
+    return dict(natom=natom, ntol_d=tol[1], ntol_i=tol[2], xyz=np.array([a[1:] for a in atoms]).ravel(),
+                exps=np.array(exps), coeff=np.array(coeff))
+
+
+@pytest.mark.parametrize("case", oracle_py.goldens()["cases"],
+                         ids=[f'{c["suite"]}/{c["name"]}' for c in oracle_py.goldens()["cases"]])
+def test_reader_matches_independent_parse(lib, case):
+    from valence_gb300 import api
+    path = os.path.join(oracle_py.GOLDEN, case["input"])
+    d = api.read_input(path).contents
+    ref = _parse(path)
+    assert d.natom == ref["natom"] and d.ntol_d == ref["ntol_d"] and d.ntol_i == ref["ntol_i"]
+    xyz = np.ctypeslib.as_array(d.coords, shape=(3 * d.natom,))
+    assert np.allclose(xyz, ref["xyz"] * 1.889725987722, rtol=0, atol=1e-12)
+    assert d.num_pr == len(ref["exps"])
+    assert np.array_equal(np.ctypeslib.as_array(d.exponent, shape=(d.num_pr,)), ref["exps"])
+    assert d.totlen >= len(ref["coeff"])
+    assert np.array_equal(np.ctypeslib.as_array(d.coeff, shape=(len(ref["coeff"]),)), ref["coeff"])
+
+
+def test_reader_rejects_malformed_input(lib, tmp_path):
+    from valence_gb300 import api
+    p = tmp_path / "bad.inp"
+    p.write_text("1 1 1 0 0 4 4 0 1 1 0 0 0 0 1\n20 10 10 2 2 0 0.0 0.0\n")
+    with pytest.raises(api.VSVBError, match="no spin couplings"):
+        api.read_input(str(p))
+    p.write_text("1 1 0 0 1\n")
+    with pytest.raises(api.VSVBError):
+        api.read_input(str(p))
+    with pytest.raises(api.VSVBError):
+        api.read_input(str(tmp_path / "missing.inp"))
+
+
+def test_no_gpu_errors_are_status_codes(lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from valence_gb300 import api
+    with pytest.raises(api.VSVBError, match="vsvb_gpu_create failed"):
+        api.System(os.path.join(oracle_py.GOLDEN, "cases", "testing", "h"))
+    null = ctypes.c_void_p(1)
+    assert lib.vsvb_det_factor_noalloc(null, 64, 65, null, null, null, None) == 8
+    assert lib.vsvb_det_factor(None, 4, 1, null, null, null, None) == 1
+
+
+def test_bench_reference_arm_two_gloo_ranks():
+    """bench.py under torchrun with 2 ranks (gloo, CPU): rank 0 alone runs the
+    CPU reference arm and prints one JSON line; rank 1 exits cleanly."""
+    import json
+    cmd = ["python", "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
+           "127.0.0.1", "--master-port", "29517", os.path.join(ROOT, "bench.py"), "--impl", "reference",
+           "--workload", "water_vshf", "--steps", "2", "--warmup", "1", "--gpus", "2"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    j = lines[0]
+    assert j["impl"] == "reference" and j["n_gpus"] == 2 and j["value"] > 0
+    assert j["cpu_baseline"]["kind"] == "port"
