@@ -231,7 +231,7 @@ struct NC {
 };
 
 /* x (or y, z) 2D factor for one root: G(i,k) by the Rys recurrences, then
- * horizontal transfer to (ia, ib, kc, kd) */
+ * horizontal transfer to (ia, ib, kc, kd). */
 template <int LA, int LB, int LC, int LD, typename R>
 __device__ __forceinline__ void rys_2d(R g00, R c00, R d00, R b00, R b10, R b01, R ab, R cd, R *__restrict__ out) {
   constexpr int LAB = LA + LB, LCD = LC + LD;
@@ -293,17 +293,20 @@ struct QuartetShape {
   static constexpr int NR = (LA + LB + LC + LD) / 2 + 1;
   static constexpr int N2D = (LA + 1) * (LB + 1) * (LC + 1) * (LD + 1);
   /* primitive quartets processed side by side per warp iteration: each takes
-   * 3*NR lanes for its 2D tables; large blocks keep one slot per warp (their
-   * per-lane accumulators must stay in registers) and put the CTA's warps on
-   * one shell quartet instead */
-  static constexpr int G0 = 32 / (3 * NR);
+   * 3*NR lanes for its 2D tables (G2 slots).  Small blocks keep a separate
+   * accumulator per slot (NITEM = G * NCOMP items spread over the lanes);
+   * large blocks (CTA mode) keep one accumulator per component, summed over
+   * the slots, so that the registers stay bounded, and put the CTA's warps on
+   * one shell quartet */
+  static constexpr int G0 = 32 / (3 * NR) < 1 ? 1 : 32 / (3 * NR);
   static constexpr bool CTA = NCOMP >= 200;
-  static constexpr int G = CTA ? 1 : (G0 < 1 ? 1 : G0);
+  static constexpr int G = CTA ? 1 : G0;
+  static constexpr int G2 = G0;
   static constexpr int NITEM = G * NCOMP;
   static constexpr int PER_LANE = (NITEM + 31) / 32;
   static constexpr int JCH = 8; /* ket orbital pairs per transform chunk */
   static constexpr int NMAX = NAB > NCD ? NAB : NCD;
-  static constexpr int SM_2D = G * 3 * NR * N2D; /* per warp, doubles */
+  static constexpr int SM_2D = G2 * 3 * NR * N2D; /* per warp, doubles */
   static constexpr int SM_ROOT = 2 * 32 * NR + 32; /* per warp: roots, weights, 1/(p+q) */
   /* staging: E[NCOMP] + max(slot buffer, transform chunk); per warp in warp
    * mode, one per CTA in CTA mode */
@@ -365,10 +368,10 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
 #pragma unroll
     for (int m = 0; m < S::PER_LANE; ++m) acc[m] = R(0);
     const int npq = P.nprim * Q.nprim;
-    /* lane roles in phase A: slot g, root r, direction dir */
+    /* lane roles in the 2D phase: slot g, root r, direction dir */
     const int g = lane / (3 * S::NR), rem = lane - g * (3 * S::NR);
     const int r = rem / 3, dir = rem - 3 * (rem / 3);
-    const bool lane_a = g < S::G;
+    const bool lane_a = g < S::G2;
     /* this warp's chunks of 32 primitive quartets */
     const int cfirst = CTA ? warp * 32 : 0;
     const int cstep = CTA ? WARPS * 32 : 32;
@@ -439,7 +442,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
       }
       __syncwarp();
       const int nch = min(32, npq - chunk);
-      for (int sub = 0; sub < nch; sub += S::G) {
+      for (int sub = 0; sub < nch; sub += S::G2) {
         const int li = sub + g; /* local index of this slot's primitive quartet */
         const bool act = lane_a && li < nch;
         if (act) {
@@ -462,7 +465,26 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
                                     h2d + (size_t)((g * 3 + dir) * S::NR + r) * S::N2D);
         }
         __syncwarp();
-        const int nact = min(S::G, nch - sub);
+        const int nact = min(S::G2, nch - sub);
+        if constexpr (CTA) {
+#pragma unroll
+          for (int m = 0; m < S::PER_LANE; ++m) {
+            const int c = lane + 32 * m;
+            if (c < S::NCOMP) {
+              const int id = idx[c];
+              const int ix = id & 1023, iy = (id >> 10) & 1023, iz = id >> 20;
+              R sacc = acc[m];
+              for (int gg = 0; gg < nact; ++gg) {
+                const R *hx = h2d + (size_t)(gg * 3 + 0) * S::NR * S::N2D;
+                const R *hy = hx + S::NR * S::N2D, *hz = hy + S::NR * S::N2D;
+#pragma unroll
+                for (int rr = 0; rr < S::NR; ++rr)
+                  acc3(sacc, hx[rr * S::N2D + ix], hy[rr * S::N2D + iy], hz[rr * S::N2D + iz]);
+              }
+              acc[m] = sacc;
+            }
+          }
+        } else
 #pragma unroll
         for (int m = 0; m < S::PER_LANE; ++m) {
           const int it = lane + 32 * m;

@@ -80,6 +80,10 @@ struct vsvb_gpu {
   int dev = 0, nsm = 152;
   cudaStream_t st = nullptr;     /* stream in use */
   cudaStream_t own_st = nullptr; /* the handle's own stream */
+  static constexpr int NAUX = 6;  /* side streams for concurrent ERI class launches */
+  cudaStream_t aux[NAUX] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[NAUX] = {};
+  std::vector<int> class_order;   /* (prec, a, c) packed, by decreasing work */
   int launches = 0;              /* kernels enqueued by the current call */
   /* dims */
   int natom = 0, nsh = 0, nao = 0, norb_all = 0, nsp = 0, ndf = 0, totlen = 0, maxobs = 0, np = 0;
@@ -266,6 +270,11 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   h->nsm = prop.multiProcessorCount;
   CK(cudaStreamCreateWithFlags(&h->own_st, cudaStreamNonBlocking), "cudaStreamCreate");
   h->st = h->own_st;
+  for (int k = 0; k < vsvb_gpu::NAUX; ++k) {
+    CK(cudaStreamCreateWithFlags(&h->aux[k], cudaStreamNonBlocking), "cudaStreamCreate");
+    CK(cudaEventCreateWithFlags(&h->ev_join[k], cudaEventDisableTiming), "cudaEventCreate");
+  }
+  CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
 
   const int norbs = 2 * d->npair + d->nunpd + d->ndocc + d->ndf;
   h->natom = d->natom;
@@ -651,10 +660,23 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
       }
       h->work_h[prec][pairs[a].cls][pairs[c].cls].push_back(make_int2(a, c));
     }
-  for (int p = 0; p < 2; ++p)
-    for (int a = 0; a < 6; ++a)
-      for (int c = 0; c < 6; ++c)
-        if (!h->work_h[p][a][c].empty()) CK(h->work_d[p][a][c].upload(h->work_h[p][a][c]), "upload work");
+  {
+    std::vector<std::pair<double, int>> cost;
+    for (int p = 0; p < 2; ++p)
+      for (int a = 0; a < 6; ++a)
+        for (int c = 0; c < 6; ++c) {
+          const auto &w = h->work_h[p][a][c];
+          if (w.empty()) continue;
+          CK(h->work_d[p][a][c].upload(w), "upload work");
+          double f = 0.0;
+          for (const int2 &q : w) f += eri_flops(a, c, pairs[q.x].nprim, pairs[q.y].nprim, pairs[q.x].nop, pairs[q.y].nop);
+          cost.push_back({f, p * 100 + a * 10 + c});
+        }
+    std::sort(cost.begin(), cost.end(), [](const std::pair<double, int> &x, const std::pair<double, int> &y) {
+      return x.first > y.first;
+    });
+    for (auto &c : cost) h->class_order.push_back(c.second);
+  }
 
   /* determinant pairs */
   DetSetup &ds = h->ds;
@@ -745,6 +767,31 @@ int alloc_grad(vsvb_gpu *h) {
 
 int alloc_grad(vsvb_gpu *h);
 
+/* one sweep over every class schedule, spread over the side streams (largest
+ * classes first), joined back into the handle's stream */
+int eri_sweep(vsvb_gpu *h, int mode) {
+  cudaStream_t st = h->st;
+  EriArgs ea = eri_args(h);
+  CK(cudaEventRecord(h->ev_fork, st), "event record");
+  for (int k = 0; k < vsvb_gpu::NAUX; ++k) CK(cudaStreamWaitEvent(h->aux[k], h->ev_fork, 0), "stream wait");
+  int i = 0;
+  for (int code : h->class_order) {
+    const int p = code / 100, a = (code / 10) % 10, c = code % 10;
+    const int n = (int)h->work_h[p][a][c].size();
+    if (eri_launch(mode, eri_kind(h, p), a, c, ea, h->work_d[p][a][c].p, n, h->nsm, h->aux[i % vsvb_gpu::NAUX])) {
+      h->err = "ERI kernel launch failed";
+      return VSVB_ERR_CUDA;
+    }
+    h->launches++;
+    ++i;
+  }
+  for (int k = 0; k < vsvb_gpu::NAUX; ++k) {
+    CK(cudaEventRecord(h->ev_join[k], h->aux[k]), "event record");
+    CK(cudaStreamWaitEvent(st, h->ev_join[k], 0), "stream wait");
+  }
+  return VSVB_OK;
+}
+
 /* forward pass on coeff_d; leaves E in result[0..4] (device).  With fused,
  * the ERI sweep also accumulates the (unscaled) adjoint dE/dX from the
  * unscreened cofactor densities. */
@@ -785,18 +832,10 @@ int forward(vsvb_gpu *h, bool fused = false) {
     h->launches++;
   }
   CK(cudaMemsetAsync(h->T.p, 0, sizeof(double) * h->T.n, st), "memset T");
-  EriArgs ea = eri_args(h);
-  for (int p = 0; p < 2; ++p)
-    for (int a = 0; a < 6; ++a)
-      for (int c = 0; c <= a; ++c) {
-        int n = (int)h->work_h[p][a][c].size();
-        if (!n) continue;
-        if (eri_launch(fused ? 3 : 0, eri_kind(h, p), a, c, ea, h->work_d[p][a][c].p, n, h->nsm, st)) {
-          h->err = "ERI kernel launch failed";
-          return VSVB_ERR_CUDA;
-        }
-        h->launches++;
-      }
+  {
+    int rc = eri_sweep(h, fused ? 3 : 0);
+    if (rc) return rc;
+  }
   if (eri_symmetrize(h->T.p, h->np, st)) {
     h->err = "symmetrize launch failed";
     return VSVB_ERR_CUDA;
@@ -864,18 +903,10 @@ int backward(vsvb_gpu *h, double e_num, double w, bool fused) {
   CK(launch_assemble(1, dim3((unsigned)h->ds.nq, h->nsplit), 128, gsh, st, dc, aa), "assemble grad");
   detpair_adjoint_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, aa, h->nsplit);
   CK(cudaGetLastError(), "detpair adjoint");
-  EriArgs ea = eri_args(h);
-  for (int p = 0; !fused && p < 2; ++p)
-    for (int a = 0; a < 6; ++a)
-      for (int c = 0; c <= a; ++c) {
-        int n = (int)h->work_h[p][a][c].size();
-        if (!n) continue;
-        if (eri_launch(2, eri_kind(h, p), a, c, ea, h->work_d[p][a][c].p, n, h->nsm, st)) {
-          h->err = "ERI adjoint launch failed";
-          return VSVB_ERR_CUDA;
-        }
-        h->launches++;
-      }
+  if (!fused) {
+    int rc2 = eri_sweep(h, 2);
+    if (rc2) return rc2;
+  }
   if (h->nxelem > 0) {
     XtabArgs xa = xtab_args(h);
     if (fused) xa.xbar_scale = 1.0 / w; /* the sweep used the unscaled densities */
@@ -922,6 +953,11 @@ void vsvb_gpu_destroy(vsvb_gpu *h) {
   cudaSetDevice(h->dev);
   if (h->st) cudaStreamSynchronize(h->st);
   cudaStream_t st = h->own_st;
+  for (int k = 0; k < vsvb_gpu::NAUX; ++k) {
+    if (h->aux[k]) cudaStreamDestroy(h->aux[k]);
+    if (h->ev_join[k]) cudaEventDestroy(h->ev_join[k]);
+  }
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   delete h;
   if (st) cudaStreamDestroy(st);
 }
