@@ -13,18 +13,14 @@
  * the Schwarz table (:1516).  No AO integral is ever written to HBM.
  *
  * Integrals: Rys quadrature (Rys, Dupuis & King, J. Comput. Chem. 4, 154
- * (1983)) with the 2D recurrences for the x, y, z factors and horizontal
- * transfer to the second centre of each pair; roots and weights come from
- * project-generated Chebyshev tables (gen_rys_tables.py).
- *
- * Work split: one warp per shell quartet.  Per primitive quartet, lanes
- * 0..n_roots-1 evaluate the roots, lanes (root, direction) build the 2D
- * tables in shared memory, then all 32 lanes accumulate their share of the
- * Cartesian components in registers.  After the primitive loop the block is
- * staged in shared memory and transformed with the X tables; the result is
- * added to T with FP64 atomics.  R is the arithmetic type of the 2D tables
- * and the component accumulation (double, or float on the mixed path); the
- * roots, prefactors and the transform stay FP64.
+ * (1983)): per primitive quartet the 2D recurrences G(i, k) for x, y, z give
+ * the (e0|f0) integrals on the bra and ket centres A and C; the horizontal
+ * transfer to B and D (Head-Gordon & Pople, J. Chem. Phys. 89, 5777 (1988))
+ * is linear in the contracted (e0|f0) block, (ab|cd) = M_P (e0|f0) M_Q^T
+ * with M fixed by the pair geometry, so it is folded into the weight tables
+ * (X' = X M, one small product per evaluation) and never runs per
+ * primitive.  Roots and weights come from project-generated Chebyshev tables
+ * (gen_rys_tables.py).  Kernel structure and arithmetic kinds: eri_impl.cuh.
  */
 #include <cuda_runtime.h>
 
@@ -61,20 +57,25 @@ int eri_symmetrize(double *T, int np, cudaStream_t st) {
 
 /* algorithmic FLOPs of one shell quartet of class (cp, cq) in this
  * formulation: per primitive quartet the n_r roots (two 12-term Clenshaw sums
- * each), the 3 n_r 2D tables (recurrence + transfers) and the component sums
- * (3 flops per component and root); per quartet the two transform GEMVs. */
+ * each), the 3 n_r 2D recurrence tables G(i, k) and the (e0|f0) component
+ * sums (3 flops per component and root); per quartet the two transform
+ * GEMVs with the transferred weights X' (ne_P x ne_Q block). */
 double eri_flops(int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ) {
   static const int la_[6] = {0, 1, 1, 2, 2, 2}, lb_[6] = {0, 0, 1, 0, 1, 2};
-  int la = la_[cp], lb = lb_[cp], lc = la_[cq], ld = lb_[cq];
+  const int la = la_[cp], lb = lb_[cp], lc = la_[cq], ld = lb_[cq];
   auto nc = [](int l) { return (l + 1) * (l + 2) / 2; };
-  int nab = nc(la) * nc(lb), ncd = nc(lc) * nc(ld), ncomp = nab * ncd;
-  int nr = (la + lb + lc + ld) / 2 + 1;
-  int n2d = (la + 1) * (lb + 1) * (lc + 1) * (ld + 1);
-  double roots = nr * 2.0 * 24.0;
-  double twod = 3.0 * nr * (5.0 * (la + lb + 1) * (lc + ld + 1) + 2.0 * n2d);
-  double comp = 3.0 * nr * (double)ncomp;
-  double prim = 30.0 + roots + twod + comp;
-  double tr = 2.0 * nopQ * (double)nab * ncd + 2.0 * nopP * (double)nopQ * nab;
+  auto ne = [&](int l0, int l1) {
+    int n = 0;
+    for (int l = l0; l <= l0 + l1; ++l) n += nc(l);
+    return n;
+  };
+  const int nea = ne(la, lb), nec = ne(lc, ld);
+  const int nr = (la + lb + lc + ld) / 2 + 1;
+  const double roots = nr * 2.0 * 24.0;
+  const double twod = 3.0 * nr * 5.0 * (la + lb + 1) * (lc + ld + 1);
+  const double comp = 3.0 * nr * (double)nea * nec;
+  const double prim = 30.0 + roots + twod + comp;
+  const double tr = 2.0 * nopQ * (double)nea * nec + 2.0 * nopP * (double)nopQ * nea;
   return (double)nprimP * nprimQ * prim + tr;
 }
 

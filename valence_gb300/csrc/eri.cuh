@@ -21,12 +21,13 @@ struct EriArgs {
   const double *rys;       /* Chebyshev tables (device) */
   const float2 *rysdf;     /* the same coefficients as (hi, lo) FP32 pairs */
   const int *pair_opid;    /* orbital-pair index of every pair term */
-  const double *xtab;      /* X tables */
+  const double *xtab;      /* transferred weight tables X' = X M (nop x ne per pair) */
+  const double *hrr;       /* per-pair transfer matrices M (n_a n_b x ne) */
   double *T;               /* np x np orbital-pair ERIs (mode 0) */
   int np;
   double *qmax_out;        /* mode 1 */
   const double *Tbar;      /* mode 2: dE/dT */
-  double *xbar;            /* mode 2: dE/dX */
+  double *xbar;            /* mode 2: dE/dX' */
 };
 
 /* arithmetic kinds of the ERI kernels */

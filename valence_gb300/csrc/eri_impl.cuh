@@ -13,24 +13,30 @@
  * 1264) and the Schwarz table (:1516).  No AO integral is written to HBM.
  *
  * Integrals: Rys quadrature (Rys, Dupuis & King, J. Comput. Chem. 4, 154
- * (1983)) with the 2D recurrences for the x, y, z factors and horizontal
- * transfer to the second centre of each pair; roots and weights come from
+ * (1983)); per primitive quartet only the 2D recurrence tables G(i, k) of the
+ * (e0|f0) integrals (e on centre A, |e| = la..la+lb; f on C).  The horizontal
+ * transfer (ab| = sum_e M(ab, e) (e0| depends on the pair geometry alone, so
+ * with X' = X M (xhrr_kernel) the transform reads
+ *     U += X'_P (e0|f0) X'_Q^T
+ * and the transfer costs nothing per primitive.  Roots and weights come from
  * project-generated Chebyshev tables (gen_rys_tables.py).
  *
  * Work split.  Per primitive quartet, 3*n_r lanes build the x/y/z 2D tables
  * of the n_r roots in shared memory, then lanes accumulate their share of
- * the Cartesian components in registers.  Small blocks run G primitive
- * quartets side by side in one warp (one warp per shell quartet); large
- * blocks (>= 200 components) put a whole CTA on one shell quartet, its warps
- * splitting the primitive quartets, so that classes with few quartets still
- * fill the SMs.  After the primitive loop the block is staged in shared
- * memory and transformed with the X tables; U is updated with FP64 atomics.
+ * the (e0|f0) components in registers.  Small blocks run G primitive
+ * quartets side by side in one warp, each with its own accumulators (one
+ * warp per shell quartet); large blocks (>= 200 components) put a whole CTA
+ * on one shell quartet, its warps splitting the primitive quartets and each
+ * warp building the tables of G2 primitive quartets at once into one set of
+ * accumulators.  After the primitive loop the block is staged in shared
+ * memory and transformed with the X' tables; U is updated with FP64 atomics.
  *
  * Arithmetic.  R = double: everything FP64.  R = float or double-float
- * (df64): the Boys argument T, 1/(p+q) and the prefactor are formed once per
- * primitive quartet in FP64; the Chebyshev evaluation of the Rys roots and
- * weights runs in double-float (its small high-order terms in FP32), so the
- * roots keep FP64-class accuracy (~1e-14) on the FP32 pipes; 2D tables and
+ * (df64, an unevaluated sum of two FP32 numbers, ~48-bit significand): the
+ * Boys argument T, 1/(p+q), the prefactor and the Chebyshev evaluation of
+ * the Rys roots and weights run in double-float (the small high-order
+ * Chebyshev terms in FP32) with no FP64 instruction, so roots and weights
+ * keep ~1e-14 relative accuracy on the FP32 pipes; the 2D tables and the
  * component sums run in R.  The transform to U is FP64 in every case.
  */
 #ifndef VSVB_ERI_IMPL_CUH
@@ -45,11 +51,26 @@
 
 namespace {
 
-/* Cartesian exponents in CCA order, l = 0..2: [l][k][xyz] */
-__constant__ int c_cart[3][6][3] = {
-    {{0, 0, 0}},
-    {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}},
-    {{2, 0, 0}, {1, 1, 0}, {1, 0, 1}, {0, 2, 0}, {0, 1, 1}, {0, 0, 2}}};
+/* Cartesian exponents of function k of the list l0, l0+1, ... (each
+ * angular momentum in CCA order: x-power descending, then y-power) */
+__device__ __forceinline__ void list_exp(int l0, int k, int e[3]) {
+  for (int l = l0;; ++l) {
+    const int n = (l + 1) * (l + 2) / 2;
+    if (k < n) {
+      for (int lx = l; lx >= 0; --lx) {
+        const int m = l - lx + 1;
+        if (k < m) {
+          e[0] = lx;
+          e[1] = l - lx - k;
+          e[2] = k;
+          return;
+        }
+        k -= m;
+      }
+    }
+    k -= n;
+  }
+}
 
 constexpr int RYS_NCHEB_D = 12;
 constexpr double RYS_TMAX_D = 64.0;
@@ -229,12 +250,19 @@ template <int L>
 struct NC {
   static constexpr int v = (L + 1) * (L + 2) / 2;
 };
+/* functions of angular momentum la .. la+lb: the (e0| list of a pair */
+constexpr int ne_c(int la, int lb) {
+  int n = 0;
+  for (int l = la; l <= la + lb; ++l) n += (l + 1) * (l + 2) / 2;
+  return n;
+}
 
-/* x (or y, z) 2D factor for one root: G(i,k) by the Rys recurrences, then
- * horizontal transfer to (ia, ib, kc, kd). */
-template <int LA, int LB, int LC, int LD, typename R>
-__device__ __forceinline__ void rys_2d(R g00, R c00, R d00, R b00, R b10, R b01, R ab, R cd, R *__restrict__ out) {
-  constexpr int LAB = LA + LB, LCD = LC + LD;
+/* x (or y, z) 2D factor for one root: G(i, k), i <= LAB on the bra centre
+ * A, k <= LCD on the ket centre C, by the Rys recurrences.  The horizontal
+ * transfers to the second centres are not done here: they are folded into
+ * the weight tables (X' = X M), so the components contracted are (e0|f0). */
+template <int LAB, int LCD, typename R>
+__device__ __forceinline__ void rys_g(R g00, R c00, R d00, R b00, R b10, R b01, R *__restrict__ out) {
   R G[LAB + 1][LCD + 1];
   G[0][0] = g00;
 #pragma unroll
@@ -249,49 +277,23 @@ __device__ __forceinline__ void rys_2d(R g00, R c00, R d00, R b00, R b10, R b01,
       G[i][k + 1] = v;
     }
   }
-  /* ket transfer: K[i][c][d] = G(i, c+d) reduced to (c,d) */
-  R K[LAB + 1][LC + 1][LD + 1];
 #pragma unroll
-  for (int i = 0; i <= LAB; ++i) {
-    R W[LCD + 1][LD + 1];
+  for (int i = 0; i <= LAB; ++i)
 #pragma unroll
-    for (int c = 0; c <= LCD; ++c) W[c][0] = G[i][c];
-#pragma unroll
-    for (int d = 1; d <= LD; ++d)
-#pragma unroll
-      for (int c = 0; c <= LCD - d; ++c) W[c][d] = W[c + 1][d - 1] + cd * W[c][d - 1];
-#pragma unroll
-    for (int c = 0; c <= LC; ++c)
-#pragma unroll
-      for (int d = 0; d <= LD; ++d) K[i][c][d] = W[c][d];
-  }
-  /* bra transfer */
-#pragma unroll
-  for (int c = 0; c <= LC; ++c)
-#pragma unroll
-    for (int d = 0; d <= LD; ++d) {
-      R V[LAB + 1][LB + 1];
-#pragma unroll
-      for (int a = 0; a <= LAB; ++a) V[a][0] = K[a][c][d];
-#pragma unroll
-      for (int b = 1; b <= LB; ++b)
-#pragma unroll
-        for (int a = 0; a <= LAB - b; ++a) V[a][b] = V[a + 1][b - 1] + ab * V[a][b - 1];
-#pragma unroll
-      for (int a = 0; a <= LA; ++a)
-#pragma unroll
-        for (int b = 0; b <= LB; ++b) out[((a * (LB + 1) + b) * (LC + 1) + c) * (LD + 1) + d] = V[a][b];
-    }
+    for (int k = 0; k <= LCD; ++k) out[i * (LCD + 1) + k] = G[i][k];
 }
 
 constexpr int WARPS = 4;
 
-template <int LA, int LB, int LC, int LD>
+/* RB: bytes of one element of the arithmetic type (2D tables, roots) */
+template <int LA, int LB, int LC, int LD, int RB = 8>
 struct QuartetShape {
-  static constexpr int NA = NC<LA>::v, NB = NC<LB>::v, NCc = NC<LC>::v, ND = NC<LD>::v;
-  static constexpr int NAB = NA * NB, NCD = NCc * ND, NCOMP = NAB * NCD;
-  static constexpr int NR = (LA + LB + LC + LD) / 2 + 1;
-  static constexpr int N2D = (LA + 1) * (LB + 1) * (LC + 1) * (LD + 1);
+  static constexpr int NAB = NC<LA>::v * NC<LB>::v; /* transferred bra functions (Schwarz) */
+  static constexpr int LAB = LA + LB, LCD = LC + LD;
+  static constexpr int NEA = ne_c(LA, LB), NEC = ne_c(LC, LD); /* (e0| and |f0) functions */
+  static constexpr int NCOMP = NEA * NEC;
+  static constexpr int NR = (LAB + LCD) / 2 + 1;
+  static constexpr int N2D = (LAB + 1) * (LCD + 1);
   /* primitive quartets processed side by side per warp iteration: each takes
    * 3*NR lanes for its 2D tables (G2 slots).  Small blocks keep a separate
    * accumulator per slot (NITEM = G * NCOMP items spread over the lanes);
@@ -305,9 +307,9 @@ struct QuartetShape {
   static constexpr int NITEM = G * NCOMP;
   static constexpr int PER_LANE = (NITEM + 31) / 32;
   static constexpr int JCH = 8; /* ket orbital pairs per transform chunk */
-  static constexpr int NMAX = NAB > NCD ? NAB : NCD;
-  static constexpr int SM_2D = G2 * 3 * NR * N2D; /* per warp, doubles */
-  static constexpr int SM_ROOT = 2 * 32 * NR + 32; /* per warp: roots, weights, 1/(p+q) */
+  static constexpr int NMAX = NEA > NEC ? NEA : NEC;
+  static constexpr int SM_2D = (G2 * 3 * NR * N2D * RB + 7) / 8; /* per warp, in doubles */
+  static constexpr int SM_ROOT = ((2 * 32 * NR + 32) * RB + 7) / 8; /* per warp: roots, weights, 1/(p+q) */
   /* staging: E[NCOMP] + max(slot buffer, transform chunk); per warp in warp
    * mode, one per CTA in CTA mode */
   static constexpr int SM_TR = NCOMP + (NITEM > JCH * NMAX ? NITEM : JCH * NMAX);
@@ -323,7 +325,7 @@ struct QuartetShape {
  */
 template <int LA, int LB, int LC, int LD, typename R, int MODE>
 __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int2 *__restrict__ work, int nwork) {
-  using S = QuartetShape<LA, LB, LC, LD>;
+  using S = QuartetShape<LA, LB, LC, LD, sizeof(R)>;
   constexpr bool CTA = S::CTA;
   constexpr bool DFROOT = !std::is_same<R, double>::value;
   extern __shared__ double smem[];
@@ -336,19 +338,14 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   const int tid = CTA ? (int)threadIdx.x : lane;
   const int nthr = CTA ? (int)blockDim.x : 32;
 
+  /* component c = (e, f) of the (e0|f0) block: offsets into the x, y, z 2D tables */
   for (int c = threadIdx.x; c < S::NCOMP; c += blockDim.x) {
-    int a = c / (S::NB * S::NCD), b = (c / S::NCD) % S::NB, cc = (c / S::ND) % S::NCc, d = c % S::ND;
-    int pw[4][3];
-#pragma unroll
-    for (int t = 0; t < 3; ++t) {
-      pw[0][t] = c_cart[LA][a][t];
-      pw[1][t] = c_cart[LB][b][t];
-      pw[2][t] = c_cart[LC][cc][t];
-      pw[3][t] = c_cart[LD][d][t];
-    }
-    const int ix = ((pw[0][0] * (LB + 1) + pw[1][0]) * (LC + 1) + pw[2][0]) * (LD + 1) + pw[3][0];
-    const int iy = ((pw[0][1] * (LB + 1) + pw[1][1]) * (LC + 1) + pw[2][1]) * (LD + 1) + pw[3][1];
-    const int iz = ((pw[0][2] * (LB + 1) + pw[1][2]) * (LC + 1) + pw[2][2]) * (LD + 1) + pw[3][2];
+    int pe[3], pf[3];
+    list_exp(LA, c / S::NEC, pe);
+    list_exp(LC, c % S::NEC, pf);
+    const int ix = pe[0] * (S::LCD + 1) + pf[0];
+    const int iy = pe[1] * (S::LCD + 1) + pf[1];
+    const int iz = pe[2] * (S::LCD + 1) + pf[2];
     idx[c] = ix | (iy << 10) | (iz << 20);
   }
   __syncthreads();
@@ -394,7 +391,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
             const double dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
             const double Tb = p * q * ipq * (dx * dx + dy * dy + dz * dz);
             const double pref = two_pi_25 * pp.Kp * qq.Kp * sqrt(ipq);
-#pragma unroll
+#pragma unroll 1
             for (int rr = 0; rr < S::NR; ++rr) {
               double u, w;
               rys_root(S::NR, rr, Tb, args.rys, args.rc, u, w);
@@ -429,7 +426,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
             } else {
               sc = df_rsqrt(Tb);
             }
-#pragma unroll
+#pragma unroll 1
             for (int rr = 0; rr < S::NR; ++rr) {
               df64 x, w;
               rys_root_df(S::NR, rr, j, Tf < (float)RYS_TMAX_D, t, sc, args.rysdf, args.rc, x, w);
@@ -452,36 +449,33 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
           /* 2D recurrence coefficients in R, from the primitive-pair and
            * pair-geometry data stored in R */
           const PrimT<R> &pr = primR[P.prim0 + ip], &qr = primR[Q.prim0 + iq];
-          const GeomT<R> &gp = geomR[pq.x], &gq = geomR[pq.y];
+          const R Ad = geomR[pq.x].A[dir], Cd = geomR[pq.y].A[dir];
           const R Pd = pr.P[dir], Qd = qr.P[dir];
           const R PQ = Pd - Qd, uq = uR * ipqR;
           const R b00 = R(0.5f) * uq;
           const R b10 = R(0.5f) * pr.inv_p * (R(1) - qr.p * uq);
           const R b01 = R(0.5f) * qr.inv_p * (R(1) - pr.p * uq);
-          const R c00 = (Pd - gp.A[dir]) - qr.p * uq * PQ;
-          const R d00 = (Qd - gq.A[dir]) + pr.p * uq * PQ;
+          const R c00 = (Pd - Ad) - qr.p * uq * PQ;
+          const R d00 = (Qd - Cd) + pr.p * uq * PQ;
           const R g00 = dir == 2 ? wR : R(1);
-          rys_2d<LA, LB, LC, LD, R>(g00, c00, d00, b00, b10, b01, gp.AB[dir], gq.AB[dir],
-                                    h2d + (size_t)((g * 3 + dir) * S::NR + r) * S::N2D);
+          rys_g<S::LAB, S::LCD, R>(g00, c00, d00, b00, b10, b01, h2d + (size_t)((g * 3 + dir) * S::NR + r) * S::N2D);
         }
         __syncwarp();
         const int nact = min(S::G2, nch - sub);
         if constexpr (CTA) {
+          /* one (slot, root) table set at a time, so that the unrolled body
+           * covers only the lane's components (instruction-cache footprint) */
+#pragma unroll 1
+          for (int t = 0; t < nact * S::NR; ++t) {
+            const R *hx = h2d + (size_t)((t / S::NR) * 3 * S::NR + t % S::NR) * S::N2D;
+            const R *hy = hx + S::NR * S::N2D, *hz = hy + S::NR * S::N2D;
 #pragma unroll
-          for (int m = 0; m < S::PER_LANE; ++m) {
-            const int c = lane + 32 * m;
-            if (c < S::NCOMP) {
-              const int id = idx[c];
-              const int ix = id & 1023, iy = (id >> 10) & 1023, iz = id >> 20;
-              R sacc = acc[m];
-              for (int gg = 0; gg < nact; ++gg) {
-                const R *hx = h2d + (size_t)(gg * 3 + 0) * S::NR * S::N2D;
-                const R *hy = hx + S::NR * S::N2D, *hz = hy + S::NR * S::N2D;
-#pragma unroll
-                for (int rr = 0; rr < S::NR; ++rr)
-                  acc3(sacc, hx[rr * S::N2D + ix], hy[rr * S::N2D + iy], hz[rr * S::N2D + iz]);
+            for (int m = 0; m < S::PER_LANE; ++m) {
+              const int c = lane + 32 * m;
+              if (c < S::NCOMP) {
+                const int id = idx[c];
+                acc3(acc[m], hx[id & 1023], hy[(id >> 10) & 1023], hz[id >> 20]);
               }
-              acc[m] = sacc;
             }
           }
         } else
@@ -541,11 +535,23 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
       __syncwarp();
     }
     if (MODE == 1) {
-      /* Schwarz: max over diagonal components (ab|ab), by the first warp */
+      /* Schwarz: max over the diagonal (ab|ab) = M_ab E M_ab^T (P == Q), by
+       * the first warp */
       if (!CTA || warp == 0) {
+        const double *M = args.hrr + P.m0;
         double mx = 0.0;
-        for (int c = lane; c < S::NCOMP; c += 32)
-          if ((c / S::NCD) == (c % S::NCD)) mx = fmax(mx, fabs(E[c]));
+        for (int ab = lane; ab < S::NAB; ab += 32) {
+          const double *m = M + (size_t)ab * S::NEA;
+          double v = 0.0;
+          for (int e = 0; e < S::NEA; ++e) {
+            const double me = m[e];
+            if (me == 0.0) continue;
+            double t = 0.0;
+            for (int f = 0; f < S::NEC; ++f) t = fma(E[e * S::NEC + f], m[f], t);
+            v = fma(me, t, v);
+          }
+          mx = fmax(mx, fabs(v));
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         if (lane == 0) args.qmax_out[pq.x] = sqrt(mx);
@@ -556,8 +562,8 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
     }
 
     double *Y = stage + S::NCOMP;
-    const double *XP = args.xtab + P.x0;
-    const double *XQ = args.xtab + Q.x0;
+    const double *XP = args.xtab + P.xh0;
+    const double *XQ = args.xtab + Q.xh0;
     const int *opP = args.pair_opid + P.op0;
     const int *opQ = args.pair_opid + Q.op0;
     const bool same = pq.x == pq.y;
@@ -569,24 +575,24 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
       for (int j0 = 0; j0 < Q.nop; j0 += S::JCH) {
         const int nj = min(S::JCH, Q.nop - j0);
         /* Y[jl][ab] = sum_cd E[ab][cd] X_Q[jl][cd] */
-        for (int o = tid; o < nj * S::NAB; o += nthr) {
-          const int jl = o / S::NAB, abi = o - jl * S::NAB;
-          const double *xq = XQ + (size_t)(j0 + jl) * S::NCD;
-          const double *e = E + abi * S::NCD;
+        for (int o = tid; o < nj * S::NEA; o += nthr) {
+          const int jl = o / S::NEA, abi = o - jl * S::NEA;
+          const double *xq = XQ + (size_t)(j0 + jl) * S::NEC;
+          const double *e = E + abi * S::NEC;
           double s = 0.0;
 #pragma unroll
-          for (int c = 0; c < S::NCD; ++c) s = fma(e[c], __ldg(xq + c), s);
+          for (int c = 0; c < S::NEC; ++c) s = fma(e[c], __ldg(xq + c), s);
           Y[o] = s;
         }
         sync();
         /* Z[ik][jl] = sum_ab X_P[ik][ab] Y[jl][ab] -> U (one orientation) */
         for (int o = tid; o < P.nop * nj; o += nthr) {
           const int ik = o / nj, jl = o - ik * nj;
-          const double *xp = XP + (size_t)ik * S::NAB;
-          const double *y = Y + jl * S::NAB;
+          const double *xp = XP + (size_t)ik * S::NEA;
+          const double *y = Y + jl * S::NEA;
           double s = 0.0;
 #pragma unroll
-          for (int c = 0; c < S::NAB; ++c) s = fma(__ldg(xp + c), y[c], s);
+          for (int c = 0; c < S::NEA; ++c) s = fma(__ldg(xp + c), y[c], s);
           const int a = __ldg(opP + ik), b = __ldg(opQ + j0 + jl);
           atomicAdd(args.T + (size_t)a * args.np + b, same ? 0.5 * s : s);
         }
@@ -598,57 +604,57 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
        * (Tbar[ik][jl] (+ Tbar[jl][ik] when the pairs differ)):
        * dX_P[ik][ab] += sum_jl W(ik,jl) (E X_Q^T)[ab][jl] and
        * dX_Q[jl][cd] += sum_ik W(ik,jl) (X_P E)[ik][cd] */
-      double *XPb = args.xbar + P.x0;
-      double *XQb = args.xbar + Q.x0;
+      double *XPb = args.xbar + P.xh0;
+      double *XQb = args.xbar + Q.xh0;
       for (int j0 = 0; j0 < Q.nop; j0 += S::JCH) {
         const int nj = min(S::JCH, Q.nop - j0);
-        for (int o = tid; o < nj * S::NAB; o += nthr) {
-          const int jl = o / S::NAB, abi = o - jl * S::NAB;
-          const double *xq = XQ + (size_t)(j0 + jl) * S::NCD;
-          const double *e = E + abi * S::NCD;
+        for (int o = tid; o < nj * S::NEA; o += nthr) {
+          const int jl = o / S::NEA, abi = o - jl * S::NEA;
+          const double *xq = XQ + (size_t)(j0 + jl) * S::NEC;
+          const double *e = E + abi * S::NEC;
           double s = 0.0;
 #pragma unroll
-          for (int c = 0; c < S::NCD; ++c) s = fma(e[c], __ldg(xq + c), s);
+          for (int c = 0; c < S::NEC; ++c) s = fma(e[c], __ldg(xq + c), s);
           Y[o] = s;
         }
         sync();
-        for (int o = tid; o < P.nop * S::NAB; o += nthr) {
-          const int ik = o / S::NAB, abi = o - ik * S::NAB;
+        for (int o = tid; o < P.nop * S::NEA; o += nthr) {
+          const int ik = o / S::NEA, abi = o - ik * S::NEA;
           const int a = __ldg(opP + ik);
           double s = 0.0;
           for (int jl = 0; jl < nj; ++jl) {
             const int b = __ldg(opQ + j0 + jl);
             double wv = args.Tbar[(size_t)a * args.np + b];
             if (!same) wv += args.Tbar[(size_t)b * args.np + a];
-            s = fma(wv, Y[jl * S::NAB + abi], s);
+            s = fma(wv, Y[jl * S::NEA + abi], s);
           }
-          atomicAdd(XPb + (size_t)ik * S::NAB + abi, s);
+          atomicAdd(XPb + (size_t)ik * S::NEA + abi, s);
         }
         sync();
       }
       constexpr int ICH = S::JCH;
       for (int i0 = 0; i0 < P.nop; i0 += ICH) {
         const int ni = min(ICH, P.nop - i0);
-        for (int o = tid; o < ni * S::NCD; o += nthr) {
-          const int ik = o / S::NCD, cdi = o - ik * S::NCD;
-          const double *xp = XP + (size_t)(i0 + ik) * S::NAB;
+        for (int o = tid; o < ni * S::NEC; o += nthr) {
+          const int ik = o / S::NEC, cdi = o - ik * S::NEC;
+          const double *xp = XP + (size_t)(i0 + ik) * S::NEA;
           double s = 0.0;
 #pragma unroll
-          for (int c = 0; c < S::NAB; ++c) s = fma(__ldg(xp + c), E[c * S::NCD + cdi], s);
+          for (int c = 0; c < S::NEA; ++c) s = fma(__ldg(xp + c), E[c * S::NEC + cdi], s);
           Y[o] = s;
         }
         sync();
-        for (int o = tid; o < Q.nop * S::NCD; o += nthr) {
-          const int jl = o / S::NCD, cdi = o - jl * S::NCD;
+        for (int o = tid; o < Q.nop * S::NEC; o += nthr) {
+          const int jl = o / S::NEC, cdi = o - jl * S::NEC;
           const int b = __ldg(opQ + jl);
           double s = 0.0;
           for (int ik = 0; ik < ni; ++ik) {
             const int a = __ldg(opP + i0 + ik);
             double wv = args.Tbar[(size_t)a * args.np + b];
             if (!same) wv += args.Tbar[(size_t)b * args.np + a];
-            s = fma(wv, Y[ik * S::NCD + cdi], s);
+            s = fma(wv, Y[ik * S::NEC + cdi], s);
           }
-          atomicAdd(XQb + (size_t)jl * S::NCD + cdi, s);
+          atomicAdd(XQb + (size_t)jl * S::NEC + cdi, s);
         }
         sync();
       }
@@ -660,7 +666,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
 template <int LA, int LB, int LC, int LD, typename R, int MODE>
 int launch_one(const EriArgs &args, const int2 *work, int nwork, int nsm, cudaStream_t st) {
   if (nwork <= 0) return 0;
-  using S = QuartetShape<LA, LB, LC, LD>;
+  using S = QuartetShape<LA, LB, LC, LD, sizeof(R)>;
   size_t shm = sizeof(double) * ((S::NCOMP + 1) / 2 + 1 + (size_t)WARPS * S::PER_WARP + S::SHARED);
   auto kfn = eri_kernel<LA, LB, LC, LD, R, MODE>;
   static bool attr_done = false;

@@ -64,6 +64,60 @@ struct DBuf {
 };
 
 int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+
+/* Cartesian exponents of component k of angular momentum l in CCA order
+ * (x-power descending, then y-power descending) */
+void cart_exp(int l, int k, int e[3]) {
+  for (int lx = l; lx >= 0; --lx) {
+    const int n = l - lx + 1;
+    if (k < n) {
+      e[0] = lx;
+      e[1] = l - lx - k;
+      e[2] = k;
+      return;
+    }
+    k -= n;
+  }
+  e[0] = e[1] = e[2] = 0;
+}
+int cca_index(const int e[3]) {
+  const int l = e[0] + e[1] + e[2], u = l - e[0];
+  return u * (u + 1) / 2 + e[2];
+}
+
+/* horizontal transfer of a shell pair (la, lb) with AB = A - B as a matrix:
+ * (a b| = sum_e M(ab, e) (e 0|, e over the Cartesian functions of angular
+ * momentum la .. la+lb on centre A.  Per direction
+ * (a, b)_1D = sum_k binom(b, k) AB^(b-k) (a+k, 0)_1D. */
+int pair_ne(int la, int lb) {
+  int n = 0;
+  for (int l = la; l <= la + lb; ++l) n += ncart(l);
+  return n;
+}
+void hrr_matrix(int la, int lb, const double AB[3], std::vector<double> &out) {
+  const int na = ncart(la), nb = ncart(lb), ne = pair_ne(la, lb);
+  int off[8] = {0};
+  for (int l = la + 1; l <= la + lb + 1; ++l) off[l - la] = off[l - la - 1] + ncart(l - 1);
+  static const double binom[3][3] = {{1, 0, 0}, {1, 1, 0}, {1, 2, 1}};
+  const size_t base = out.size();
+  out.resize(base + (size_t)na * nb * ne, 0.0);
+  for (int ia = 0; ia < na; ++ia)
+    for (int ib = 0; ib < nb; ++ib) {
+      int a[3], b[3];
+      cart_exp(la, ia, a);
+      cart_exp(lb, ib, b);
+      for (int kx = 0; kx <= b[0]; ++kx)
+        for (int ky = 0; ky <= b[1]; ++ky)
+          for (int kz = 0; kz <= b[2]; ++kz) {
+            const int k[3] = {kx, ky, kz};
+            double c = 1.0;
+            for (int d = 0; d < 3; ++d) c *= binom[b[d]][k[d]] * std::pow(AB[d], b[d] - k[d]);
+            const int e[3] = {a[0] + kx, a[1] + ky, a[2] + kz};
+            const int col = off[kx + ky + kz] + cca_index(e);
+            out[base + (size_t)(ia * nb + ib) * ne + col] += c;
+          }
+    }
+}
 int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; } /* la >= lb */
 
 double dblfac(int n) {
@@ -113,8 +167,9 @@ struct vsvb_gpu {
   RysConst rc{};
   DBuf<int> pair_opid;
   DBuf<XTerm> xterms;
-  DBuf<long long> xelem0;
-  long long nxelem = 0;
+  DBuf<long long> xelem0, xh_elem0;
+  DBuf<double> hrr, xtabh;
+  long long nxelem = 0, nxh = 0;
   int nxterm = 0;
   DBuf<int> obs_n, obs_ao, term0, term_slot, term_j, term_m, term_f, ndf_orb;
   DBuf<double> coeff_d, ndf_scale, orb_scale, Craw, C, So, Ho, xtab, T, qmax;
@@ -123,7 +178,7 @@ struct vsvb_gpu {
   int ld_scratch = 0;
   DBuf<double> part_e1, part_wf, part_e2, result;
   /* adjoint */
-  DBuf<double> Tbar, Sbar, Hbar, xbar, Cbar, vtot, Gglob, coeff_bar;
+  DBuf<double> Tbar, Sbar, Hbar, xbar, xbarh, Cbar, vtot, Gglob, coeff_bar;
   bool grad_ready = false;
   int last_singular = 0;
 };
@@ -177,6 +232,10 @@ XtabArgs xtab_args(vsvb_gpu *h) {
   x.dtol = h->dtol;
   x.xtab = h->xtab.p;
   x.xbar_scale = 1.0;
+  x.xh_elem0 = h->xh_elem0.p;
+  x.nxh = h->nxh;
+  x.hrr = h->hrr.p;
+  x.xtabh = h->xtabh.p;
   return x;
 }
 
@@ -194,12 +253,13 @@ EriArgs eri_args(vsvb_gpu *h) {
   a.rys = h->rys.p;
   a.rysdf = h->rysdf.p;
   a.pair_opid = h->pair_opid.p;
-  a.xtab = h->xtab.p;
+  a.xtab = h->xtabh.p;
+  a.hrr = h->hrr.p;
   a.T = h->T.p;
   a.np = h->np;
   a.qmax_out = h->qmax.p;
   a.Tbar = h->Tbar.p;
-  a.xbar = h->xbar.p;
+  a.xbar = h->xbarh.p;
   return a;
 }
 
@@ -484,8 +544,9 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   std::vector<PrimPair> prims;
   std::vector<int> opid;
   std::vector<XTerm> xterms;
-  std::vector<long long> xelem0;
-  long long nx = 0;
+  std::vector<long long> xelem0, xh_elem0;
+  std::vector<double> hrr;
+  long long nx = 0, nxh = 0;
   for (int A0 = 0; A0 < h->nsh; ++A0)
     for (int B0 = 0; B0 <= A0; ++B0) {
       int A = A0, B = B0;
@@ -524,6 +585,12 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
       P.op0 = (int)opid.size();
       P.nop = (int)ops.size();
       P.x0 = (int)nx;
+      P.xh0 = (int)nxh;
+      P.m0 = (int)hrr.size();
+      {
+        const double AB[3] = {P.A[0] - P.B[0], P.A[1] - P.B[1], P.A[2] - P.B[2]};
+        hrr_matrix(sh[A].l, sh[B].l, AB, hrr);
+      }
       for (auto &ik : ops) {
         int i = ik.first, k = ik.second;
         opid.push_back(i * (i + 1) / 2 + k);
@@ -539,17 +606,21 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
         t.aoA = sh[A].ao0;
         t.aoB = sh[B].ao0;
         t.same_shell = A == B;
+        t.m0 = P.m0;
         xterms.push_back(t);
         xelem0.push_back(nx);
+        xh_elem0.push_back(nxh);
         nx += ncart(sh[A].l) * ncart(sh[B].l);
+        nxh += pair_ne(sh[A].l, sh[B].l);
       }
       pairs.push_back(P);
     }
-  if (nx > (long long)0x7fffffff) {
+  if (nx > (long long)0x7fffffff || nxh > (long long)0x7fffffff || hrr.size() > (size_t)0x7fffffff) {
     h->err = "weight tables exceed 2^31 elements";
     return VSVB_ERR_UNSUPPORTED;
   }
   h->nxelem = nx;
+  h->nxh = nxh;
   h->nxterm = (int)xterms.size();
   CK(h->pairs.upload(pairs), "upload pairs");
   CK(h->prims.upload(prims), "upload prims");
@@ -597,7 +668,10 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   CK(h->pair_opid.upload(opid), "upload opid");
   CK(h->xterms.upload(xterms), "upload xterms");
   CK(h->xelem0.upload(xelem0), "upload xelem0");
+  CK(h->xh_elem0.upload(xh_elem0.empty() ? std::vector<long long>(1, 0) : xh_elem0), "upload xh_elem0");
+  CK(h->hrr.upload(hrr.empty() ? std::vector<double>(1, 0.0) : hrr), "upload hrr");
   CK(h->xtab.alloc(std::max<long long>(nx, 1)), "alloc xtab");
+  CK(h->xtabh.alloc(std::max<long long>(nxh, 1)), "alloc xtabh");
   CK(h->qmax.alloc(std::max<size_t>(pairs.size(), 1)), "alloc qmax");
   CK(h->T.alloc(std::max<size_t>((size_t)h->np * h->np, 1)), "alloc T");
   /* Rys tables */
@@ -757,6 +831,7 @@ int alloc_grad(vsvb_gpu *h) {
   CK(h->Sbar.alloc((size_t)h->nsp * h->nsp), "alloc Sbar");
   CK(h->Hbar.alloc((size_t)h->nsp * h->nsp), "alloc Hbar");
   CK(h->xbar.alloc(std::max<long long>(h->nxelem, 1)), "alloc xbar");
+  CK(h->xbarh.alloc(std::max<long long>(h->nxh, 1)), "alloc xbarh");
   CK(h->Cbar.alloc((size_t)h->norb_all * h->maxobs), "alloc Cbar");
   CK(h->vtot.alloc((size_t)nq * h->nsplit), "alloc vtot");
   CK(h->Gglob.alloc(std::max<long long>(nq * (na * na + nb * nb), 1)), "alloc G");
@@ -815,7 +890,9 @@ int forward(vsvb_gpu *h, bool fused = false) {
     XtabArgs xa = xtab_args(h);
     xtab_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa);
     CK(cudaGetLastError(), "xtab");
-    h->launches++;
+    xhrr_kernel<<<(unsigned)((h->nxh + 255) / 256), 256, 0, st>>>(xa);
+    CK(cudaGetLastError(), "xhrr");
+    h->launches += 2;
   }
   CK(cudaMemsetAsync(h->sing.p, 0, sizeof(int) * h->sing.n, st), "memset sing");
   DetCtx dc = det_ctx(h);
@@ -826,7 +903,7 @@ int forward(vsvb_gpu *h, bool fused = false) {
     int rc = alloc_grad(h);
     if (rc) return rc;
     CK(cudaMemsetAsync(h->Tbar.p, 0, sizeof(double) * h->Tbar.n, st), "memset Tbar");
-    CK(cudaMemsetAsync(h->xbar.p, 0, sizeof(double) * h->xbar.n, st), "memset xbar");
+    CK(cudaMemsetAsync(h->xbarh.p, 0, sizeof(double) * h->xbarh.n, st), "memset xbarh");
     AsmArgs ad = asm_args(h);
     CK(launch_assemble(2, dim3((unsigned)h->ds.nq, h->nsplit), 128, 0, st, dc, ad), "density walk");
     h->launches++;
@@ -886,7 +963,7 @@ int backward(vsvb_gpu *h, double e_num, double w, bool fused) {
   const int na = h->ds.nalpha, nb = h->ds.nbeta;
   if (!fused) {
     CK(cudaMemsetAsync(h->Tbar.p, 0, sizeof(double) * h->Tbar.n, st), "memset");
-    CK(cudaMemsetAsync(h->xbar.p, 0, sizeof(double) * h->xbar.n, st), "memset");
+    CK(cudaMemsetAsync(h->xbarh.p, 0, sizeof(double) * h->xbarh.n, st), "memset");
   }
   CK(cudaMemsetAsync(h->Sbar.p, 0, sizeof(double) * h->Sbar.n, st), "memset");
   CK(cudaMemsetAsync(h->Hbar.p, 0, sizeof(double) * h->Hbar.n, st), "memset");
@@ -910,8 +987,11 @@ int backward(vsvb_gpu *h, double e_num, double w, bool fused) {
   if (h->nxelem > 0) {
     XtabArgs xa = xtab_args(h);
     if (fused) xa.xbar_scale = 1.0 / w; /* the sweep used the unscaled densities */
+    xhrr_adjoint_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa, h->xbarh.p, h->xbar.p);
+    CK(cudaGetLastError(), "xhrr adjoint");
     xtab_adjoint_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa, h->xbar.p, h->Cbar.p);
     CK(cudaGetLastError(), "xtab adjoint");
+    h->launches++;
   }
   OrbArgs oa = orb_args(h);
   orb_1e_adjoint_kernel<<<h->nsp, 128, 0, st>>>(oa, h->Sbar.p, h->Hbar.p, h->nsp, h->Cbar.p);

@@ -16,6 +16,9 @@
  *   xtab_kernel     per shell pair and orbital pair the weight products
  *                   X(a,b) of int2e (dij/dkl, valence.F90:3372-3396) with its
  *                   per-shell LCAO screen sum(c^2) > dtol (:3296-3348).
+ *   xhrr_kernel     the horizontal transfer of each shell pair folded into
+ *                   its weights: X' = X M (M from the pair geometry), so the
+ *                   ERI kernels contract (e0|f0) integrals.
  *   orb_grad kernels  the adjoints of the above for the weight gradient.
  */
 #include <cuda_runtime.h>
@@ -358,6 +361,52 @@ __global__ void xtab_adjoint_kernel(XtabArgs x, const double *xbar, double *Cbar
     atomicAdd(gk + tm.sAk + ia, g * ci[tm.sBi + ib]);
     atomicAdd(gi + tm.sBi + ib, g * ck[tm.sAk + ia]);
   }
+}
+
+/* number of Cartesian functions (a+k, 0) the transfer of an (la, lb) pair
+ * starts from: l = la .. la+lb */
+__device__ __forceinline__ int ne_of(int la, int lb) { return ncart_upto(la + lb) - (la > 0 ? ncart_upto(la - 1) : 0); }
+
+__device__ __forceinline__ int term_of(const long long *e0, int n, long long t) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (e0[mid] <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+/* X'(op, e) = sum_ab X(op, ab) M(ab, e): the horizontal transfer
+ * (ab| = sum_e M(ab, e) (e0| of the pair, folded into its weights so the ERI
+ * kernels contract (e0|f0) integrals directly.  One thread per X' element. */
+__global__ void xhrr_kernel(XtabArgs x) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= x.nxh) return;
+  const int k = term_of(x.xh_elem0, x.nterm, t);
+  const XTerm &tm = x.terms[k];
+  const int e = (int)(t - x.xh_elem0[k]);
+  const int nab = ncart(tm.la) * ncart(tm.lb), ne = ne_of(tm.la, tm.lb);
+  const double *X = x.xtab + x.elem0[k];
+  const double *M = x.hrr + tm.m0;
+  double s = 0.0;
+  for (int ab = 0; ab < nab; ++ab) s = fma(X[ab], M[ab * ne + e], s);
+  x.xtabh[t] = s;
+}
+
+/* adjoint: dE/dX(op, ab) = sum_e dE/dX'(op, e) M(ab, e); one thread per X element */
+__global__ void xhrr_adjoint_kernel(XtabArgs x, const double *xbarh, double *xbar) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= x.nelem) return;
+  const int k = term_of(x.elem0, x.nterm, t);
+  const XTerm &tm = x.terms[k];
+  const int ab = (int)(t - x.elem0[k]);
+  const int ne = ne_of(tm.la, tm.lb);
+  const double *Xb = xbarh + x.xh_elem0[k];
+  const double *M = x.hrr + tm.m0 + (size_t)ab * ne;
+  double s = 0.0;
+  for (int e = 0; e < ne; ++e) s = fma(Xb[e], M[e], s);
+  xbar[t] = s;
 }
 
 /* adjoint of orb_1e_kernel: Cbar_i(k) += sum_j (Sbar_ij + Sbar_ji) (S C_j)(k)

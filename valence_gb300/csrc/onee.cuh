@@ -37,7 +37,7 @@ struct XTerm {
   int sAi, sBi, sAk, sBk;/* OBS slot of shell A/B in orbital i/k, -1 if absent */
   int aoA, aoB;          /* first global AO of shells A, B */
   int same_shell;
-  int pad;
+  int m0;                /* the pair's transfer matrix in hrr */
 };
 
 struct XtabArgs {
@@ -51,6 +51,11 @@ struct XtabArgs {
   double dtol;
   double *xtab;
   double xbar_scale; /* adjoint: factor applied to dE/dX */
+  /* horizontal transfer folded into the weights: X'(op, e) = sum_ab X(op, ab) M(ab, e) */
+  const long long *xh_elem0; /* first X' element of each term */
+  long long nxh;
+  const double *hrr;
+  double *xtabh;
 };
 
 __global__ void ao_1e_kernel(Ao1eArgs a);
@@ -59,6 +64,8 @@ __global__ void orb_norm_kernel(OrbArgs a);
 __global__ void orb_1e_kernel(OrbArgs a, double *So, double *Ho);
 __global__ void xtab_kernel(XtabArgs x);
 __global__ void xtab_adjoint_kernel(XtabArgs x, const double *xbar, double *Cbar);
+__global__ void xhrr_kernel(XtabArgs x);
+__global__ void xhrr_adjoint_kernel(XtabArgs x, const double *xbarh, double *xbar);
 __global__ void orb_1e_adjoint_kernel(OrbArgs a, const double *Sbar, const double *Hbar, int nsp, double *Cbar);
 __global__ void orb_norm_adjoint_kernel(OrbArgs a, const double *Cbar, double *coeff_bar);
 #endif

@@ -80,6 +80,8 @@ struct ShellPair {
   int prim0, nprim;  /* into prims */
   int op0, nop;      /* into pair_ops / orbital-pair lists */
   int x0;            /* into xtab: nop * n_a * n_b doubles */
+  int xh0;           /* into the transferred table X' = X M: nop * ne doubles */
+  int m0;            /* into hrr: the n_a n_b x ne transfer matrix M */
   double A[3], B[3];
   double qmax;       /* sqrt(max (ab|ab)) */
   double pad;
