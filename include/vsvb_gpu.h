@@ -102,7 +102,9 @@ typedef struct vsvb_energy_result {
   double e1, e2;   /* its parts */
   double wfnorm;   /* valence.F90:1106 */
   double enucrep;  /* tools_module.F90:19-40 */
-  double err_est;  /* mixed path: bound on |E_mixed - E_fp64| from the FP32 quartets; 0 on FP64 */
+  double err_est;  /* mixed paths: estimate of |E_mixed - E_fp64| from the FP32 quartets
+                      (FP32 rounding of the untransferred integral sizes behind them, in units
+                      of the two-electron energy per Schwarz-bound mass); 0 on FP64 */
   long long n_quartets_fp64, n_quartets_fp32; /* AO shell quartets evaluated */
   long long n_tasks;                           /* orbital-quartet tasks (valence.F90:1153-1157) */
   int n_singular_pairs;                        /* determinant pairs on the exact-minor path */

@@ -98,6 +98,24 @@ def test_mixed_precision_error_bound(vg, tmp_path):
     rm = vg.System(p, precision=vg.MIXED).energy()
     assert rm["n_quartets_fp32"] > 0
     assert abs(rm["energy"] - e64) <= 1e-6
+    assert abs(rm["energy"] - e64) <= rm["err_est"]
+
+
+@pytest.mark.parametrize("thr", [1e-6, 1e-4, 1e-3])
+def test_mixed_error_estimate_covers_error(vg, tmp_path, thr):
+    """err_est (FP32 rounding of the untransferred integral sizes behind the
+    FP32 quartets, in units of |e2|/W per Schwarz-bound mass) must cover the
+    measured |E_mixed - E_fp64| at every threshold without overshooting it
+    by more than 10^3."""
+    from valence_gb300 import configs
+    p = configs.ch_chain(str(tmp_path / "chain.inp"))
+    e64 = vg.System(p, precision=vg.FP64).energy()["energy"]
+    for prec in (vg.MIXED, vg.MIXED_DF64):
+        r = vg.System(p, precision=prec, mixed_threshold=thr).energy()
+        assert r["err_est"] > 0.0
+        assert abs(r["energy"] - e64) <= r["err_est"], (prec, thr, r["energy"] - e64, r["err_est"])
+        assert r["err_est"] <= 1e3 * abs(r["energy"] - e64), (prec, thr, r["energy"] - e64, r["err_est"])
+    assert vg.System(p, precision=vg.FP64).energy()["err_est"] == 0.0
 
 
 def test_double_float_path_matches_fp64(vg, tmp_path):

@@ -44,6 +44,19 @@ def test_golden_guess_energy(lib_built, case):
     s.close()
 
 
+@pytest.mark.parametrize("case", _cases(), ids=[f'{c["suite"]}/{c["name"]}' for c in _cases()])
+def test_golden_guess_energy_mixed(lib_built, case):
+    """The mixed path (FP32 below a Schwarz bound of 1e-6, double-float
+    above) against the reference goldens: within 1e-6 Eh, and within its own
+    error estimate of the golden (plus the goldens' 1e-8 tolerance)."""
+    s = lib_built.System(os.path.join(GOLD, case["input"]), precision=lib_built.MIXED_DF64)
+    r = s.energy()
+    d = abs(r["energy"] - case["guess_energy"])
+    assert d < 1e-6, (r["energy"], case["guess_energy"])
+    assert d <= r["err_est"] + 1e-8, (d, r["err_est"], r["n_quartets_fp32"])
+    s.close()
+
+
 def _orbital_checks(sysobj, o, nsp, tol_rel=1e-11):
     S, H = sysobj.orbital_1e()
     T = sysobj.orbital_eri()

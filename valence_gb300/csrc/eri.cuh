@@ -25,7 +25,8 @@ struct EriArgs {
   const double *hrr;       /* per-pair transfer matrices M (n_a n_b x ne) */
   double *T;               /* np x np orbital-pair ERIs (mode 0) */
   int np;
-  double *qmax_out;        /* mode 1 */
+  double *qmax_out;        /* mode 1: sqrt(max_ab |(ab|ab)|) per pair */
+  double *q0max_out;       /* mode 1: sqrt(max_e |(e0|e0)|) per pair */
   const double *Tbar;      /* mode 2: dE/dT */
   double *xbar;            /* mode 2: dE/dX' */
 };

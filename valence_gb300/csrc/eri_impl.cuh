@@ -540,6 +540,12 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
       if (!CTA || warp == 0) {
         const double *M = args.hrr + P.m0;
         double mx = 0.0;
+        /* and sqrt(max_e |(e0|e0)|), the size of the untransferred block */
+        double mx0 = 0.0;
+        for (int e = lane; e < S::NEA; e += 32) mx0 = fmax(mx0, fabs(E[e * S::NEC + e]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx0 = fmax(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
+        if (lane == 0) args.q0max_out[pq.x] = sqrt(mx0);
         for (int ab = lane; ab < S::NAB; ab += 32) {
           const double *m = M + (size_t)ab * S::NEA;
           double v = 0.0;
