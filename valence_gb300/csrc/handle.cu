@@ -826,7 +826,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   long long ntij = (long long)nsp * (nsp + 1) / 2;
   h->ntasks = ntij * (ntij + 1) / 2;
   long long work = std::max<long long>(h->ntasks, (long long)ds.nelec * ds.nelec);
-  long long want = (2LL * h->nsm + nq - 1) / nq;
+  long long want = (16LL * h->nsm + nq - 1) / nq;
   long long maxs = (work + 127) / 128;
   h->nsplit = (int)std::max<long long>(1, std::min(want, maxs));
   size_t nslot = (size_t)nq * h->nsplit;
