@@ -14,10 +14,13 @@ and |dE| of each against FP64 is reported.
   value          device-resident weights (vsvb_gpu_energy_grad_device)
   e2e            public host API (vsvb_gpu_energy_grad): pinned host weights
                  copied in and the energy + gradient copied out every step
-  roofline       dominant ERI class launch: algorithmic FLOPs / its CUDA-event
-                 time against the FP64 or FP32 FMA rate measured on this
-                 device by vsvb_gpu_fma_peak (MEASURED_PEAKS.json carries only
-                 HBM and bf16 figures)
+  roofline       dominant ERI class launch of the headline steps: algorithmic
+                 FLOPs / its CUDA-event time inside the timed steps (events
+                 on the side stream it runs on), against the FP64 or FP32 FMA
+                 rate measured on this device by vsvb_gpu_fma_peak
+                 (MEASURED_PEAKS.json carries only HBM and bf16 figures); for
+                 a double-float launch the roofline is that FP32 instruction
+                 rate x 3 flops / 16 instructions per component update
   cpu_baseline   the CPU oracle (a literal C restatement of the reference,
                  energy only -- the reference has no gradient) on all host
                  cores, one full evaluation
@@ -41,6 +44,17 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "VSVB energy+grad evals/s, mixed vs plain FP64 on 1 GB300 at |ΔE|<=1e-6 Eh"
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the ERI class
+# launches, from the ncu --set full captures summarised in profiles/
+# (keys: workload, 100*kind + 10*bra pair class + ket pair class; kind 2 =
+# double-float, pair classes ss ps pp ds dp dd = 0..5)
+PROFILED_TRAFFIC = {
+    ("ch_chain", 253): 1.230848e6 + 0.0,  # (dd|ds) double-float, forward + adjoint
+    ("ch_chain", 254): 1.250304e6 + 0.0,  # (dd|dp)
+    ("ch_chain", 255): 0.813312e6 + 0.0,  # (dd|dd)
+}
 
 
 def _args():
@@ -176,7 +190,7 @@ def run_ours(a, rank, world):
     for s in (s64, smx, smn):
         s.set_stream(stream.cuda_stream)
 
-    def timed(fn, steps, warmup):
+    def timed(fn, steps, warmup, after_step=None):
         for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
@@ -193,6 +207,8 @@ def run_ours(a, rank, world):
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
             launches += last["n_kernel_launches"]
+            if after_step is not None:
+                after_step()
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -211,10 +227,25 @@ def run_ours(a, rank, world):
             return r.as_dict()
         return f
 
+    # per-class ERI launch times inside the timed steps (CUDA events on the
+    # side stream each class runs on, read back after each step)
+    sweep = {}
+    sweep_wall = []
+
+    def collect():
+        for x in smx.sweep_times():
+            acc = sweep.setdefault(x["cls"], [0.0, 0.0, 0])
+            acc[0] += x["ms"]
+            acc[1] += x["flops"]
+            acc[2] += 1
+        sweep_wall.append(smx.sweep_wall_ms())
+
+    smx.set_sweep_timing(True)
     clk = Clocks(dev)
     clk.start()
-    ms_mx, launches_mx, r_mx = timed(dev_step(smx), a.steps, a.warmup)
+    ms_mx, launches_mx, r_mx = timed(dev_step(smx), a.steps, a.warmup, after_step=collect)
     clocks = clk.stop()
+    smx.set_sweep_timing(False)
     if a.headline_only:
         ms_64, r_64, ms_mn, r_mn, ms_e2e = ms_mx, r_mx, ms_mx, r_mx, ms_mx
     else:
@@ -239,20 +270,43 @@ def run_ours(a, rank, world):
         return
     # roofline of the dominant ERI launch of the headline (mixed) run
     fp64_peak, fp32_peak = api.fma_peak(dev)
-    prof = smx.eri_profile()
-    prof.sort(key=lambda x: -x["ms"])
-    top = prof[0]
-    prec = {0: "fp64", 1: "fp32", 2: "double-float"}[top["cls"] // 100]
-    peak = fp64_peak if prec == "fp64" else fp32_peak
-    achieved = top["flops"] / (top["ms"] * 1e-3)
-    eri_total_ms = sum(x["ms"] for x in prof)
-    roofline = {"bound": ("fp64" if prec == "fp64" else "fp32") + "_pipe",
-                "kernel": f"eri_kernel class {top['cls']:03d} ({prec})",
-                "achieved_unit_note": "algorithmic FP64-equivalent FLOPs of the Rys formulation (eri_flops) per second",
-                "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": None, "share_of_eri_pass": top["ms"] / eri_total_ms,
-                "peak_source": "measured on this device by vsvb_gpu_fma_peak (FMA chain kernel)",
-                "fp64_peak_tflops": fp64_peak / 1e12, "fp32_peak_tflops": fp32_peak / 1e12}
+    # Roofline of the ERI kernel (all class launches of one step's sweep, run
+    # concurrently on the library's side streams), timed in situ.  Per
+    # arithmetic kind the bound rate for the algorithmic FLOPs (eri_flops:
+    # mostly component updates acc += x*y*z, 3 flops) is the measured FP32 or
+    # FP64 instruction rate (FMA peak / 2) times 3 flops per update over the
+    # instructions one update takes: 2 for FP32 and FP64 (MUL + FMA), 16 for
+    # double-float.  T* = sum_kind W_kind / P_kind; frac = T* / T_sweep.
+    rate = {0: fp64_peak / 2 * 3 / 2, 1: fp32_peak / 2 * 3 / 2, 2: fp32_peak / 2 * 3 / 16}
+    n_sw = len(sweep_wall)
+    W = {k: 0.0 for k in rate}
+    for c, (_, fl, cnt) in sweep.items():
+        W[c // 100] += fl / cnt
+    t_star = sum(W[k] / rate[k] for k in rate)
+    t_sweep = statistics.mean(sweep_wall) * 1e-3
+    w_tot = sum(W.values())
+    cls_top, (t_top, f_top, n_top) = max(sweep.items(), key=lambda kv: kv[1][0])
+    kind_name = {0: "fp64", 1: "fp32", 2: "double-float"}
+    pair_l = ["s s", "p s", "p p", "d s", "d p", "d d"]
+    roofline = {"bound": "fp32_pipe",
+                "kernel": "eri_kernel: every class launch of the step's ERI sweep (forward + adjoint), "
+                          "concurrent on 6 streams",
+                "achieved": w_tot / t_sweep / 1e12, "peak": w_tot / t_star / 1e12, "unit": "TFLOP/s",
+                "frac": t_star / t_sweep,
+                "achieved_unit_note": "algorithmic FP64-equivalent FLOPs of the Rys formulation (eri_flops) per "
+                                      "second of sweep wall time",
+                "peak_basis": "T* = sum over kinds of W_kind / P_kind; P = measured FMA instruction rate "
+                              "(vsvb_gpu_fma_peak / 2) x 3 flops per component update / instructions per update "
+                              "(2 FP32 or FP64, 16 double-float)",
+                "flops_per_step": {kind_name[k]: W[k] for k in W}, "sweep_ms": t_sweep * 1e3,
+                "sweeps_timed": n_sw, "share_of_step": t_sweep * 1e3 / (statistics.mean(ms_mx)),
+                "traffic": PROFILED_TRAFFIC.get((a.workload, cls_top)),
+                "traffic_note": "dram read+write bytes per launch of the longest class launch "
+                                "(ncu capture summarised in profiles/)",
+                "longest_launch": {"class": f"({pair_l[(cls_top // 10) % 10]}|{pair_l[cls_top % 10]}) "
+                                            f"{kind_name[cls_top // 100]}",
+                                   "ms_in_situ": t_top / n_top, "flops": f_top / n_top},
+                "fp64_fma_tflops": fp64_peak / 1e12, "fp32_fma_tflops": fp32_peak / 1e12}
     cpu = None
     if world == 1 and not a.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as d:

@@ -94,6 +94,9 @@ typedef struct vsvb_options {
                            * weights taken from the unscreened cofactor densities;
                            * 1: a second sweep recomputes the ERIs against the
                            * exactly screened dE/dT (valence.F90:1189-1190,1286-1287) */
+  double prim_screen;     /* primitive-quartet Schwarz screen: a primitive quartet whose bound
+                           * sqrt(max (e0|e0)_p) sqrt(max (f0|f0)_q) falls below this is skipped
+                           * (default 1e-17; 0 evaluates every primitive quartet) */
 } vsvb_options;
 
 typedef struct vsvb_energy_result {
@@ -164,6 +167,21 @@ int vsvb_gpu_set_stream(vsvb_gpu *h, void *stream);
  * primitive quartet / shell quartet), cls[i] = 100*prec + 10*bra + ket.
  * Returns the number of launches or a negative status. */
 int vsvb_gpu_eri_profile(vsvb_gpu *h, double *ms, double *flops, int *cls, int cap);
+
+/* In-situ timing of the ERI class launches inside ordinary calls: with
+ * vsvb_gpu_set_sweep_timing(h, 1) every ERI sweep records a CUDA event pair
+ * around each class launch on the side stream it runs on (the launches of
+ * one sweep run concurrently).  vsvb_gpu_sweep_times then returns, for the
+ * last sweep, per class launch i (up to cap): ms[i] its duration, flops[i]
+ * its algorithmic FLOP count for the sweep's mode (forward, or forward plus
+ * adjoint on the fused gradient path), cls[i] = 100*kind + 10*bra + ket with
+ * kind 0 FP64, 1 FP32, 2 double-float.  Returns the number of launches (0
+ * when timing is off) or a negative status. */
+int vsvb_gpu_set_sweep_timing(vsvb_gpu *h, int on);
+int vsvb_gpu_sweep_times(vsvb_gpu *h, double *ms, double *flops, int *cls, int cap);
+/* Wall time of the last ERI sweep (fork to join on the handle's stream) in
+ * *ms; 0 when timing is off. */
+int vsvb_gpu_sweep_wall_ms(vsvb_gpu *h, double *ms);
 
 /* Measured FP64 and FP32 FMA throughput of this device in FLOP/s (a dependent
  * FMA chain kernel sized to fill every SM), for roofline denominators. */

@@ -143,3 +143,24 @@ def test_double_float_golden(vg):
         s = vg.System(os.path.join(ROOT, "tests", "golden", g[name]["input"]), precision=vg.MIXED_DF64,
                       mixed_threshold=0.0)
         assert abs(s.energy()["energy"] - g[name]["guess_energy"]) < 1e-8, name
+
+
+def test_sweep_timing_reports_every_class(vg, tmp_path):
+    """In-situ ERI class timing: one entry per class launch of the last
+    sweep, positive durations, and FLOP counts that include the adjoint on
+    the fused gradient path."""
+    from valence_gb300 import configs
+    p = configs.water_vshf(str(tmp_path / "water.inp"))
+    s = vg.System(p)
+    assert s.sweep_times() == []
+    s.set_sweep_timing(True)
+    s.energy()
+    fwd = {x["cls"]: x for x in s.sweep_times()}
+    s.energy_grad()
+    both = {x["cls"]: x for x in s.sweep_times()}
+    assert fwd and set(fwd) == set(both)
+    for c in fwd:
+        assert fwd[c]["ms"] > 0 and both[c]["ms"] > 0
+        assert both[c]["flops"] > fwd[c]["flops"] > 0
+    wall = s.sweep_wall_ms()
+    assert wall >= 0.99 * max(x["ms"] for x in both.values())

@@ -48,7 +48,7 @@ class Desc(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("mixed_threshold", ctypes.c_double), ("ao_screen", ctypes.c_double),
-                ("device", ctypes.c_int), ("grad_mode", ctypes.c_int)]
+                ("device", ctypes.c_int), ("grad_mode", ctypes.c_int), ("prim_screen", ctypes.c_double)]
 
 
 class Result(ctypes.Structure):
@@ -88,6 +88,9 @@ def lib():
         L.vsvb_gpu_batch_energy_grad.argtypes = [P(ctypes.c_void_p), I, P(P(D)), P(Result), P(P(D))]
         L.vsvb_gpu_set_stream.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.vsvb_gpu_eri_profile.argtypes = [ctypes.c_void_p, P(D), P(D), P(I), I]
+        L.vsvb_gpu_set_sweep_timing.argtypes = [ctypes.c_void_p, I]
+        L.vsvb_gpu_sweep_times.argtypes = [ctypes.c_void_p, P(D), P(D), P(I), I]
+        L.vsvb_gpu_sweep_wall_ms.argtypes = [ctypes.c_void_p, P(D)]
         L.vsvb_gpu_fma_peak.argtypes = [I, P(D), P(D)]
         L.vsvb_det_factor.argtypes = [ctypes.c_void_p, I, I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_void_p]
@@ -110,7 +113,7 @@ def read_input(path):
     return d
 
 
-def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, grad_mode=0):
+def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, grad_mode=0, prim_screen=None):
     o = Options()
     lib().vsvb_default_options(ctypes.byref(o))
     o.precision = precision
@@ -118,6 +121,8 @@ def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0
     o.ao_screen = ao_screen
     o.device = device
     o.grad_mode = grad_mode
+    if prim_screen is not None:
+        o.prim_screen = prim_screen
     return o
 
 
@@ -125,7 +130,7 @@ class System:
     """One molecule on the GPU: a parsed input plus a device handle."""
 
     def __init__(self, path, precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, coords_angstrom=None,
-                 grad_mode=0):
+                 grad_mode=0, prim_screen=None):
         self.path = path
         self._desc = read_input(path)
         d = self._desc.contents
@@ -135,7 +140,7 @@ class System:
         self._coords_bohr = np.ctypeslib.as_array(d.coords, shape=(3 * d.natom,))
         if coords_angstrom is not None:
             self._coords_bohr[:] = np.asarray(coords_angstrom, dtype=np.float64).ravel() * 1.889725987722
-        self.opt = make_options(precision, mixed_threshold, ao_screen, device, grad_mode)
+        self.opt = make_options(precision, mixed_threshold, ao_screen, device, grad_mode, prim_screen)
         self._h = ctypes.c_void_p()
         rc = lib().vsvb_gpu_create(self._desc, ctypes.byref(self.opt), ctypes.byref(self._h))
         if rc:
@@ -201,6 +206,27 @@ class System:
         if n < 0:
             raise VSVBError("eri_profile failed")
         return [dict(cls=int(cl[i]), ms=float(ms[i]), flops=float(fl[i])) for i in range(n)]
+
+    def set_sweep_timing(self, on=True):
+        """Record CUDA events around every ERI class launch of later calls."""
+        self._check(lib().vsvb_gpu_set_sweep_timing(self._h, 1 if on else 0), "set_sweep_timing")
+
+    def sweep_times(self, cap=128):
+        """Per class launch of the last ERI sweep: duration (ms, in situ,
+        concurrent with the other classes) and algorithmic FLOPs."""
+        ms = np.zeros(cap)
+        fl = np.zeros(cap)
+        cl = np.zeros(cap, dtype=np.int32)
+        n = lib().vsvb_gpu_sweep_times(self._h, _dptr(ms), _dptr(fl), cl.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), cap)
+        if n < 0:
+            raise VSVBError("sweep_times failed")
+        return [dict(cls=int(cl[i]), ms=float(ms[i]), flops=float(fl[i])) for i in range(n)]
+
+    def sweep_wall_ms(self):
+        """Wall time (ms) of the last ERI sweep, fork to join."""
+        v = ctypes.c_double()
+        self._check(lib().vsvb_gpu_sweep_wall_ms(self._h, ctypes.byref(v)), "sweep_wall_ms")
+        return v.value
 
     def orbital_eri(self):
         n = lib().vsvb_gpu_num_orbitals(self._h)

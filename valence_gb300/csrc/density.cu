@@ -251,9 +251,11 @@ __device__ double block_sum_d(double v, double *red) {
 
 __device__ __forceinline__ int opidx(int i, int k) { return i >= k ? i * (i + 1) / 2 + k : k * (k + 1) / 2 + i; }
 
-/* xm_dtriang / xm_dtriang8: 1-based triangular index -> (i, j), j <= i */
+/* xm_dtriang / xm_dtriang8: 1-based triangular index -> (i, j), j <= i.
+ * An FP32 square root as the first guess (no FP64 on this path), then
+ * exact integer correction. */
 __device__ __forceinline__ void dtriang(long long ij, int &i, int &j) {
-  long long ii = (long long)sqrt((double)(2 * ij));
+  long long ii = (long long)sqrtf((float)(2 * ij));
   while ((ii * ii + ii) / 2 < ij) ++ii;
   while (ii > 1 && ((ii - 1) * (ii - 1) + (ii - 1)) / 2 >= ij) --ii;
   i = (int)ii;
@@ -489,10 +491,10 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
     const int pik = opidx(io, ko), pjl = opidx(jo, lo), pil = opidx(io, lo), pjk = opidx(jo, ko);
     double sik = 0.0, sjl = 0.0, sil = 0.0, sjk = 0.0;
     if (!DENS) {
-      sik = sqrt(fmax(a.T[(size_t)pik * np + pik], 0.0));
-      sjl = sqrt(fmax(a.T[(size_t)pjl * np + pjl], 0.0));
-      sil = sqrt(fmax(a.T[(size_t)pil * np + pil], 0.0));
-      sjk = sqrt(fmax(a.T[(size_t)pjk * np + pjk], 0.0));
+      sik = a.sq[pik];
+      sjl = a.sq[pjl];
+      sil = a.sq[pil];
+      sjk = a.sq[pjk];
     }
     bool es = sik * sjl > itol, xs = sil * sjk > itol;
     double eint = 0.0, xint = 0.0;

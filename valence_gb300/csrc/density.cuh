@@ -19,6 +19,7 @@ struct DetCtx {
 
 struct AsmArgs {
   const double *T;  /* np x np orbital-pair ERIs */
+  const double *sq; /* [np] sqrt(max(T[p][p], 0)) */
   int np;
   double itol;
   long long ntasks;

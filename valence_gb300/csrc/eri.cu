@@ -28,7 +28,7 @@
 
 namespace {
 
-__global__ void symmetrize_kernel(double *T, int np) {
+__global__ void symmetrize_kernel(double *T, int np, double *sq) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long n = (long long)np * (np + 1) / 2;
   if (t >= n) return;
@@ -38,7 +38,10 @@ __global__ void symmetrize_kernel(double *T, int np) {
   long long j = t - i * (i + 1) / 2;
   double *a = T + i * np + j, *b = T + j * np + i;
   double v = *a + *b;
-  if (i == j) v = 2.0 * (*a);
+  if (i == j) {
+    v = 2.0 * (*a);
+    sq[i] = sqrt(fmax(v, 0.0)); /* Schwarz factor of orbital pair i (schwarz_ints, valence.F90:1516) */
+  }
   *a = v;
   *b = v;
 }
@@ -47,11 +50,12 @@ __global__ void symmetrize_kernel(double *T, int np) {
 
 }  // namespace
 
-/* T = U + U^T after the forward pass (the kernels accumulate one orientation) */
-int eri_symmetrize(double *T, int np, cudaStream_t st) {
+/* T = U + U^T after the forward pass (the kernels accumulate one
+ * orientation); sq[p] = sqrt(max(T[p][p], 0)) */
+int eri_symmetrize(double *T, int np, double *sq, cudaStream_t st) {
   long long n = (long long)np * (np + 1) / 2;
   if (n == 0) return 0;
-  symmetrize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(T, np);
+  symmetrize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(T, np, sq);
   return cudaGetLastError() != cudaSuccess;
 }
 
@@ -59,8 +63,9 @@ int eri_symmetrize(double *T, int np, cudaStream_t st) {
  * formulation: per primitive quartet the n_r roots (two 12-term Clenshaw sums
  * each), the 3 n_r 2D recurrence tables G(i, k) and the (e0|f0) component
  * sums (3 flops per component and root); per quartet the two transform
- * GEMVs with the transferred weights X' (ne_P x ne_Q block). */
-double eri_flops(int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ) {
+ * GEMVs with the transferred weights X' (ne_P x ne_Q block), and in modes 2
+ * and 3 the four GEMVs of the adjoint (dX'_P and dX'_Q). */
+double eri_flops(int mode, int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ) {
   static const int la_[6] = {0, 1, 1, 2, 2, 2}, lb_[6] = {0, 0, 1, 0, 1, 2};
   const int la = la_[cp], lb = lb_[cp], lc = la_[cq], ld = lb_[cq];
   auto nc = [](int l) { return (l + 1) * (l + 2) / 2; };
@@ -75,7 +80,10 @@ double eri_flops(int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ) {
   const double twod = 3.0 * nr * 5.0 * (la + lb + 1) * (lc + ld + 1);
   const double comp = 3.0 * nr * (double)nea * nec;
   const double prim = 30.0 + roots + twod + comp;
-  const double tr = 2.0 * nopQ * (double)nea * nec + 2.0 * nopP * (double)nopQ * nea;
+  const double fwd = 2.0 * nopQ * (double)nea * nec + 2.0 * nopP * (double)nopQ * nea;
+  const double adj = 2.0 * nopQ * (double)nea * nec + 2.0 * nopP * (double)nopQ * nea +
+                     2.0 * nopP * (double)nea * nec + 2.0 * nopQ * (double)nopP * nec;
+  const double tr = (mode == 0 ? fwd : 0.0) + (mode == 2 ? adj : 0.0) + (mode == 3 ? fwd + adj : 0.0);
   return (double)nprimP * nprimQ * prim + tr;
 }
 

@@ -27,6 +27,8 @@ struct EriArgs {
   int np;
   double *qmax_out;        /* mode 1: sqrt(max_ab |(ab|ab)|) per pair */
   double *q0max_out;       /* mode 1: sqrt(max_e |(e0|e0)|) per pair */
+  const float *prim_q0;    /* per primitive pair (prims order): sqrt(max_e |(e0|e0)|) */
+  float prim_eps;          /* primitive quartets with q0_p q0_q below this are skipped (0: none) */
   const double *Tbar;      /* mode 2: dE/dT */
   double *xbar;            /* mode 2: dE/dX' */
 };
@@ -41,6 +43,6 @@ int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int2 
 int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
 int eri_dispatch_f32(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
 int eri_dispatch_df64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
-double eri_flops(int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ);
-int eri_symmetrize(double *T, int np, cudaStream_t st);
+double eri_flops(int mode, int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ);
+int eri_symmetrize(double *T, int np, double *sq, cudaStream_t st);
 #endif

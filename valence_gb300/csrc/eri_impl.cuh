@@ -309,7 +309,8 @@ struct QuartetShape {
   static constexpr int JCH = 8; /* ket orbital pairs per transform chunk */
   static constexpr int NMAX = NEA > NEC ? NEA : NEC;
   static constexpr int SM_2D = (G2 * 3 * NR * N2D * RB + 7) / 8; /* per warp, in doubles */
-  static constexpr int SM_ROOT = ((2 * 32 * NR + 32) * RB + 7) / 8; /* per warp: roots, weights, 1/(p+q) */
+  /* per warp: roots, weights, 1/(p+q) of 32 primitive quartets, and their indices */
+  static constexpr int SM_ROOT = ((2 * 32 * NR + 32) * RB + 7) / 8 + 16;
   /* staging: E[NCOMP] + max(slot buffer, transform chunk); per warp in warp
    * mode, one per CTA in CTA mode */
   static constexpr int SM_TR = NCOMP + (NITEM > JCH * NMAX ? NITEM : JCH * NMAX);
@@ -364,7 +365,22 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
     R acc[S::PER_LANE];
 #pragma unroll
     for (int m = 0; m < S::PER_LANE; ++m) acc[m] = R(0);
-    const int npq = P.nprim * Q.nprim;
+    /* primitive screen: pairs' primitives are sorted by their bound q0, so
+     * rows ip whose q0_p q0_q(first) falls below eps end the contraction */
+    const float eps = args.prim_eps;
+    int nrow = P.nprim;
+    if (eps > 0.f) {
+      const float qtop = args.prim_q0[Q.prim0];
+      for (int base = 0; base < P.nprim; base += 32) {
+        const int ip = base + lane;
+        const unsigned fail = __ballot_sync(0xffffffffu, ip < P.nprim && args.prim_q0[P.prim0 + ip] * qtop < eps);
+        if (fail) {
+          nrow = base + __ffs(fail) - 1;
+          break;
+        }
+      }
+    }
+    const int npq = nrow * Q.nprim;
     /* lane roles in the 2D phase: slot g, root r, direction dir */
     const int g = lane / (3 * S::NR), rem = lane - g * (3 * S::NR);
     const int r = rem / 3, dir = rem - 3 * (rem / 3);
@@ -375,13 +391,37 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
     R *rx = reinterpret_cast<R *>(ws + S::SM_2D); /* [32][NR] roots */
     R *rw = rx + 32 * S::NR;                      /* [32][NR] scaled weights */
     R *ripq = rw + 32 * S::NR;                    /* [32] 1/(p+q) */
+    int *plist = reinterpret_cast<int *>(ws + S::SM_2D + S::SM_ROOT - 16); /* [32] kept quartets */
 
-    for (int chunk = cfirst; chunk < npq; chunk += cstep) {
+    /* FP32 sums are taken smallest first: the chunks (and the quartets in a
+     * chunk) in reverse, against the descending order of the bounds */
+    constexpr bool ASC = std::is_same<R, float>::value;
+    const int nchunk = npq > cfirst ? (npq - cfirst + cstep - 1) / cstep : 0;
+    for (int kc = 0; kc < nchunk; ++kc) {
+      const int chunk = cfirst + (ASC ? nchunk - 1 - kc : kc) * cstep;
+      /* compaction: the chunk's primitive quartets that pass the screen */
+      int nch;
+      {
+        const int pqi = chunk + lane;
+        bool keep = pqi < npq;
+        if (keep && eps > 0.f) {
+          const int ip = pqi / Q.nprim, iq = pqi - ip * Q.nprim;
+          keep = args.prim_q0[P.prim0 + ip] * args.prim_q0[Q.prim0 + iq] >= eps;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        nch = __popc(bal);
+        if (keep) {
+          const int pos = __popc(bal & ((1u << lane) - 1u));
+          plist[ASC ? nch - 1 - pos : pos] = pqi;
+        }
+      }
+      __syncwarp();
+      if (nch == 0) continue;
       /* phase R: one primitive quartet per lane -- Boys argument, 1/(p+q),
        * prefactor and the n_r Rys roots/weights */
       {
-        const int pqi = chunk + lane;
-        if (pqi < npq) {
+        if (lane < nch) {
+          const int pqi = plist[lane];
           const int ip = pqi / Q.nprim, iq = pqi - ip * Q.nprim;
           if constexpr (!DFROOT) {
             const PrimPair &pp = args.prims[P.prim0 + ip];
@@ -438,12 +478,11 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         }
       }
       __syncwarp();
-      const int nch = min(32, npq - chunk);
       for (int sub = 0; sub < nch; sub += S::G2) {
         const int li = sub + g; /* local index of this slot's primitive quartet */
         const bool act = lane_a && li < nch;
         if (act) {
-          const int pqi = chunk + li;
+          const int pqi = plist[li];
           const int ip = pqi / Q.nprim, iq = pqi - ip * Q.nprim;
           const R uR = rx[li * S::NR + r], wR = rw[li * S::NR + r], ipqR = ripq[li];
           /* 2D recurrence coefficients in R, from the primitive-pair and

@@ -137,6 +137,11 @@ struct vsvb_gpu {
   static constexpr int NAUX = 6;  /* side streams for concurrent ERI class launches */
   cudaStream_t aux[NAUX] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[NAUX] = {};
+  /* in-situ timing of the class launches of the last sweep (optional) */
+  bool sweep_timing = false;
+  int sweep_mode = -1;
+  std::vector<cudaEvent_t> sweep_ev; /* 2 per class launch */
+  cudaEvent_t sweep_t0 = nullptr, sweep_t1 = nullptr; /* fork and join of the last sweep */
   std::vector<int> class_order;   /* (prec, a, c) packed, by decreasing work */
   int launches = 0;              /* kernels enqueued by the current call */
   /* dims */
@@ -162,6 +167,7 @@ struct vsvb_gpu {
   DBuf<PrimT<double>> prim64;
   DBuf<PrimT<float>> prim32;
   DBuf<PrimT<df64>> primdf;
+  DBuf<float> prim_q0; /* per primitive pair: sqrt(max_e |(e0|e0)|), pairs sorted descending */
   DBuf<GeomT<double>> geom64;
   DBuf<GeomT<float>> geom32;
   DBuf<GeomT<df64>> geomdf;
@@ -173,7 +179,7 @@ struct vsvb_gpu {
   long long nxelem = 0, nxh = 0;
   int nxterm = 0;
   DBuf<int> obs_n, obs_ao, term0, term_slot, term_j, term_m, term_f, ndf_orb;
-  DBuf<double> coeff_d, ndf_scale, orb_scale, Craw, C, So, Ho, xtab, T, qmax, q0max;
+  DBuf<double> coeff_d, ndf_scale, orb_scale, Craw, C, So, Ho, xtab, T, sqT, qmax, q0max;
   DBuf<int> pair_slot, slot_pair, slot_which, sing, status;
   DBuf<double> coeff_sc, det_a, det_b, Ta, Tb, scratch;
   int ld_scratch = 0;
@@ -260,6 +266,8 @@ EriArgs eri_args(vsvb_gpu *h) {
   a.np = h->np;
   a.qmax_out = h->qmax.p;
   a.q0max_out = h->q0max.p;
+  a.prim_q0 = h->prim_q0.p;
+  a.prim_eps = (float)h->opt.prim_screen;
   a.Tbar = h->Tbar.p;
   a.xbar = h->xbarh.p;
   return a;
@@ -285,6 +293,7 @@ DetCtx det_ctx(vsvb_gpu *h) {
 AsmArgs asm_args(vsvb_gpu *h) {
   AsmArgs a{};
   a.T = h->T.p;
+  a.sq = h->sqT.p;
   a.np = h->np;
   a.itol = h->itol;
   a.ntasks = h->ntasks;
@@ -311,6 +320,34 @@ int eri_kind(const vsvb_gpu *h, int list) {
 }
 
 /* ---------------- set-up ---------------- */
+
+/* the primitive-pair table in every kernel arithmetic */
+int upload_prims(vsvb_gpu *h, const std::vector<PrimPair> &prims) {
+  std::vector<PrimT<double>> p64(prims.size());
+  std::vector<PrimT<float>> p32(prims.size());
+  std::vector<PrimT<df64>> pdf(prims.size());
+  for (size_t i = 0; i < prims.size(); ++i) {
+    for (int k = 0; k < 3; ++k) {
+      p64[i].P[k] = prims[i].P[k];
+      p32[i].P[k] = (float)prims[i].P[k];
+      pdf[i].P[k] = df64(prims[i].P[k]);
+    }
+    p64[i].p = prims[i].p;
+    p64[i].inv_p = prims[i].inv_p;
+    p64[i].Kp = prims[i].Kp;
+    p32[i].p = (float)prims[i].p;
+    p32[i].inv_p = (float)prims[i].inv_p;
+    p32[i].Kp = (float)prims[i].Kp;
+    pdf[i].p = df64(prims[i].p);
+    pdf[i].inv_p = df64(prims[i].inv_p);
+    pdf[i].Kp = df64(prims[i].Kp);
+  }
+  CK(h->prims.upload(prims), "upload prims");
+  CK(h->prim64.upload(p64), "upload prim64");
+  CK(h->prim32.upload(p32), "upload prim32");
+  CK(h->primdf.upload(pdf), "upload primdf");
+  return VSVB_OK;
+}
 
 int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   if (d->npair > 0 && d->nspinc < 1) {
@@ -625,28 +662,11 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   h->nxh = nxh;
   h->nxterm = (int)xterms.size();
   CK(h->pairs.upload(pairs), "upload pairs");
-  CK(h->prims.upload(prims), "upload prims");
   {
-    /* the same primitive-pair and pair data in each kernel arithmetic */
-    std::vector<PrimT<double>> p64(prims.size());
-    std::vector<PrimT<float>> p32(prims.size());
-    std::vector<PrimT<df64>> pdf(prims.size());
-    for (size_t i = 0; i < prims.size(); ++i) {
-      for (int k = 0; k < 3; ++k) {
-        p64[i].P[k] = prims[i].P[k];
-        p32[i].P[k] = (float)prims[i].P[k];
-        pdf[i].P[k] = df64(prims[i].P[k]);
-      }
-      p64[i].p = prims[i].p;
-      p64[i].inv_p = prims[i].inv_p;
-      p64[i].Kp = prims[i].Kp;
-      p32[i].p = (float)prims[i].p;
-      p32[i].inv_p = (float)prims[i].inv_p;
-      p32[i].Kp = (float)prims[i].Kp;
-      pdf[i].p = df64(prims[i].p);
-      pdf[i].inv_p = df64(prims[i].inv_p);
-      pdf[i].Kp = df64(prims[i].Kp);
-    }
+    int rc = upload_prims(h, prims);
+    if (rc) return rc;
+  }
+  {
     std::vector<GeomT<double>> g64(pairs.size());
     std::vector<GeomT<float>> g32(pairs.size());
     std::vector<GeomT<df64>> gdf(pairs.size());
@@ -660,9 +680,6 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
         gdf[i].A[k] = df64(A);
         gdf[i].AB[k] = df64(AB);
       }
-    CK(h->prim64.upload(p64), "upload prim64");
-    CK(h->prim32.upload(p32), "upload prim32");
-    CK(h->primdf.upload(pdf), "upload primdf");
     CK(h->geom64.upload(g64), "upload geom64");
     CK(h->geom32.upload(g32), "upload geom32");
     CK(h->geomdf.upload(gdf), "upload geomdf");
@@ -677,6 +694,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   CK(h->qmax.alloc(std::max<size_t>(pairs.size(), 1)), "alloc qmax");
   CK(h->q0max.alloc(std::max<size_t>(pairs.size(), 1)), "alloc q0max");
   CK(h->T.alloc(std::max<size_t>((size_t)h->np * h->np, 1)), "alloc T");
+  CK(h->sqT.alloc(std::max<size_t>((size_t)h->np, 1)), "alloc sqT");
   /* Rys tables */
   CK(h->rys.upload(std::vector<double>(rys_table_data, rys_table_data + sizeof(rys_table_data) / sizeof(double))),
      "upload rys");
@@ -705,6 +723,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     std::vector<int2> diag[6];
     for (size_t p = 0; p < pairs.size(); ++p) diag[pairs[p].cls].push_back(make_int2((int)p, (int)p));
     EriArgs ea = eri_args(h);
+    ea.prim_eps = 0.f;
     DBuf<int2> wd[6];
     for (int c = 0; c < 6; ++c) {
       if (diag[c].empty()) continue;
@@ -723,6 +742,72 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     }
     for (size_t p = 0; p < pairs.size(); ++p) pairs[p].qmax = q[p];
     CK(h->pairs.upload(pairs), "upload pairs");
+  }
+  /* primitive Schwarz bounds: the same diagonal pass over one-primitive
+   * copies of every shell pair gives sqrt(max_e |(e0|e0)|) per primitive
+   * pair; each pair's primitives are then sorted by it, descending, so that
+   * the kernels' primitive screen q0_p q0_q < prim_screen cuts a tail */
+  {
+    std::vector<ShellPair> vp;
+    std::vector<GeomT<double>> vg;
+    std::vector<int2> vdiag[6];
+    for (size_t pi = 0; pi < pairs.size(); ++pi) {
+      GeomT<double> g;
+      for (int k = 0; k < 3; ++k) {
+        g.A[k] = pairs[pi].A[k];
+        g.AB[k] = pairs[pi].A[k] - pairs[pi].B[k];
+      }
+      for (int ip = 0; ip < pairs[pi].nprim; ++ip) {
+        ShellPair v = pairs[pi];
+        v.prim0 = pairs[pi].prim0 + ip;
+        v.nprim = 1;
+        vdiag[v.cls].push_back(make_int2((int)vp.size(), (int)vp.size()));
+        vp.push_back(v);
+        vg.push_back(g);
+      }
+    }
+    DBuf<ShellPair> vp_d;
+    DBuf<GeomT<double>> vg_d;
+    DBuf<double> vq, vq0;
+    DBuf<int2> wd[6];
+    CK(vp_d.upload(vp), "upload prim pairs");
+    CK(vg_d.upload(vg), "upload prim geometry");
+    CK(vq.alloc(std::max<size_t>(vp.size(), 1)), "alloc prim bounds");
+    CK(vq0.alloc(std::max<size_t>(vp.size(), 1)), "alloc prim bounds");
+    EriArgs ea = eri_args(h);
+    ea.pairs = vp_d.p;
+    ea.geom64 = vg_d.p;
+    ea.qmax_out = vq.p;
+    ea.q0max_out = vq0.p;
+    ea.prim_eps = 0.f;
+    for (int c = 0; c < 6; ++c) {
+      if (vdiag[c].empty()) continue;
+      CK(wd[c].upload(vdiag[c]), "upload prim diag");
+      if (eri_launch(1, 0, c, c, ea, wd[c].p, (int)vdiag[c].size(), h->nsm, h->st)) {
+        h->err = "primitive Schwarz kernel launch failed";
+        return VSVB_ERR_CUDA;
+      }
+    }
+    std::vector<double> pq0(vp.size());
+    CK(cudaStreamSynchronize(h->st), "prim schwarz sync");
+    if (!vp.empty()) CK(cudaMemcpy(pq0.data(), vq0.p, sizeof(double) * pq0.size(), cudaMemcpyDeviceToHost), "prim q0");
+    /* vp is in prims order, so pq0[i] belongs to prims[i] */
+    std::vector<float> q0f(prims.size());
+    for (size_t pi = 0; pi < pairs.size(); ++pi) {
+      const int p0 = pairs[pi].prim0, n = pairs[pi].nprim;
+      std::vector<int> ord(n);
+      for (int k = 0; k < n; ++k) ord[k] = k;
+      std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return pq0[p0 + x] > pq0[p0 + y]; });
+      std::vector<PrimPair> seg(n);
+      for (int k = 0; k < n; ++k) {
+        seg[k] = prims[p0 + ord[k]];
+        q0f[p0 + k] = (float)pq0[p0 + ord[k]];
+      }
+      for (int k = 0; k < n; ++k) prims[p0 + k] = seg[k];
+    }
+    int rc = upload_prims(h, prims);
+    if (rc) return rc;
+    CK(h->prim_q0.upload(q0f.empty() ? std::vector<float>(1, 0.f) : q0f), "upload prim q0");
   }
   /* size of the arithmetic behind a pair's transferred integrals: the
    * (e0|e0) bound times the largest row 1-norm of its transfer matrix */
@@ -767,7 +852,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
           if (w.empty()) continue;
           CK(h->work_d[p][a][c].upload(w), "upload work");
           double f = 0.0;
-          for (const int2 &q : w) f += eri_flops(a, c, pairs[q.x].nprim, pairs[q.y].nprim, pairs[q.x].nop, pairs[q.y].nop);
+          for (const int2 &q : w) f += eri_flops(0, a, c, pairs[q.x].nprim, pairs[q.y].nprim, pairs[q.x].nop, pairs[q.y].nop);
           cost.push_back({f, p * 100 + a * 10 + c});
         }
     std::sort(cost.begin(), cost.end(), [](const std::pair<double, int> &x, const std::pair<double, int> &y) {
@@ -871,23 +956,40 @@ int alloc_grad(vsvb_gpu *h);
 int eri_sweep(vsvb_gpu *h, int mode) {
   cudaStream_t st = h->st;
   EriArgs ea = eri_args(h);
+  if (h->sweep_timing && !h->sweep_t0) {
+    CK(cudaEventCreate(&h->sweep_t0), "cudaEventCreate");
+    CK(cudaEventCreate(&h->sweep_t1), "cudaEventCreate");
+  }
+  if (h->sweep_timing) CK(cudaEventRecord(h->sweep_t0, st), "event record");
   CK(cudaEventRecord(h->ev_fork, st), "event record");
   for (int k = 0; k < vsvb_gpu::NAUX; ++k) CK(cudaStreamWaitEvent(h->aux[k], h->ev_fork, 0), "stream wait");
   int i = 0;
+  if (h->sweep_timing && h->sweep_ev.size() < 2 * h->class_order.size()) {
+    for (size_t k = h->sweep_ev.size(); k < 2 * h->class_order.size(); ++k) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e), "cudaEventCreate");
+      h->sweep_ev.push_back(e);
+    }
+  }
   for (int code : h->class_order) {
     const int p = code / 100, a = (code / 10) % 10, c = code % 10;
     const int n = (int)h->work_h[p][a][c].size();
-    if (eri_launch(mode, eri_kind(h, p), a, c, ea, h->work_d[p][a][c].p, n, h->nsm, h->aux[i % vsvb_gpu::NAUX])) {
+    cudaStream_t sa = h->aux[i % vsvb_gpu::NAUX];
+    if (h->sweep_timing) CK(cudaEventRecord(h->sweep_ev[2 * i], sa), "event record");
+    if (eri_launch(mode, eri_kind(h, p), a, c, ea, h->work_d[p][a][c].p, n, h->nsm, sa)) {
       h->err = "ERI kernel launch failed";
       return VSVB_ERR_CUDA;
     }
+    if (h->sweep_timing) CK(cudaEventRecord(h->sweep_ev[2 * i + 1], sa), "event record");
     h->launches++;
     ++i;
   }
+  h->sweep_mode = mode;
   for (int k = 0; k < vsvb_gpu::NAUX; ++k) {
     CK(cudaEventRecord(h->ev_join[k], h->aux[k]), "event record");
     CK(cudaStreamWaitEvent(st, h->ev_join[k], 0), "stream wait");
   }
+  if (h->sweep_timing) CK(cudaEventRecord(h->sweep_t1, st), "event record");
   return VSVB_OK;
 }
 
@@ -937,7 +1039,7 @@ int forward(vsvb_gpu *h, bool fused = false) {
     int rc = eri_sweep(h, fused ? 3 : 0);
     if (rc) return rc;
   }
-  if (eri_symmetrize(h->T.p, h->np, st)) {
+  if (eri_symmetrize(h->T.p, h->np, h->sqT.p, st)) {
     h->err = "symmetrize launch failed";
     return VSVB_ERR_CUDA;
   }
@@ -1047,6 +1149,7 @@ void vsvb_default_options(vsvb_options *o) {
   o->ao_screen = 1e-15;
   o->device = 0;
   o->grad_mode = 0;
+  o->prim_screen = 1e-17;
 }
 
 int vsvb_gpu_create(const vsvb_system_desc *d, const vsvb_options *opt, vsvb_gpu **out) {
@@ -1071,6 +1174,9 @@ void vsvb_gpu_destroy(vsvb_gpu *h) {
     if (h->ev_join[k]) cudaEventDestroy(h->ev_join[k]);
   }
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  for (cudaEvent_t e : h->sweep_ev) cudaEventDestroy(e);
+  if (h->sweep_t0) cudaEventDestroy(h->sweep_t0);
+  if (h->sweep_t1) cudaEventDestroy(h->sweep_t1);
   delete h;
   if (st) cudaStreamDestroy(st);
 }
@@ -1191,13 +1297,56 @@ int vsvb_gpu_eri_profile(vsvb_gpu *h, double *ms, double *flops, int *cls, int c
         cudaEventDestroy(e1);
         double f = 0.0;
         for (const int2 &q : w)
-          f += eri_flops(a, c, pairs[q.x].nprim, pairs[q.y].nprim, pairs[q.x].nop, pairs[q.y].nop);
+          f += eri_flops(0, a, c, pairs[q.x].nprim, pairs[q.y].nprim, pairs[q.x].nop, pairs[q.y].nop);
         ms[k] = t;
         flops[k] = f;
         cls[k] = 100 * eri_kind(h, p) + 10 * a + c;
         ++k;
       }
   return k;
+}
+
+int vsvb_gpu_set_sweep_timing(vsvb_gpu *h, int on) {
+  if (!h) return VSVB_ERR_INPUT;
+  h->sweep_timing = on != 0;
+  return VSVB_OK;
+}
+
+int vsvb_gpu_sweep_times(vsvb_gpu *h, double *ms, double *flops, int *cls, int cap) {
+  if (!h) return -VSVB_ERR_INPUT;
+  if (!h->sweep_timing || h->sweep_mode < 0) return 0;
+  if (cudaSetDevice(h->dev) != cudaSuccess) return -VSVB_ERR_CUDA;
+  std::vector<ShellPair> pairs(h->pairs.n);
+  if (!pairs.empty() &&
+      cudaMemcpy(pairs.data(), h->pairs.p, sizeof(ShellPair) * pairs.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -VSVB_ERR_CUDA;
+  int k = 0;
+  for (size_t i = 0; i < h->class_order.size() && k < cap; ++i, ++k) {
+    const int code = h->class_order[i];
+    const int p = code / 100, a = (code / 10) % 10, c = code % 10;
+    if (cudaEventSynchronize(h->sweep_ev[2 * i + 1]) != cudaSuccess) return -VSVB_ERR_CUDA;
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, h->sweep_ev[2 * i], h->sweep_ev[2 * i + 1]) != cudaSuccess) return -VSVB_ERR_CUDA;
+    double f = 0.0;
+    for (const int2 &q : h->work_h[p][a][c])
+      f += eri_flops(h->sweep_mode, a, c, pairs[q.x].nprim, pairs[q.y].nprim, pairs[q.x].nop, pairs[q.y].nop);
+    ms[k] = t;
+    flops[k] = f;
+    cls[k] = 100 * eri_kind(h, p) + 10 * a + c;
+  }
+  return k;
+}
+
+int vsvb_gpu_sweep_wall_ms(vsvb_gpu *h, double *ms) {
+  if (!h || !ms) return VSVB_ERR_INPUT;
+  *ms = 0.0;
+  if (!h->sweep_timing || h->sweep_mode < 0 || !h->sweep_t1) return VSVB_OK;
+  CK(cudaSetDevice(h->dev), "cudaSetDevice");
+  CK(cudaEventSynchronize(h->sweep_t1), "event sync");
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, h->sweep_t0, h->sweep_t1), "event time");
+  *ms = t;
+  return VSVB_OK;
 }
 
 int vsvb_gpu_debug_orbital_eri(vsvb_gpu *h, double *out, size_t cap) {
