@@ -97,6 +97,9 @@ typedef struct vsvb_options {
   double prim_screen;     /* primitive-quartet Schwarz screen: a primitive quartet whose bound
                            * sqrt(max (e0|e0)_p) sqrt(max (f0|f0)_q) falls below this is skipped
                            * (default 1e-17; 0 evaluates every primitive quartet) */
+  int prim_split;         /* mixed paths: the primitive quartets of the FP64-class shell
+                           * quartets whose bound falls below mixed_threshold also run in
+                           * FP32 (default 1; 0 keeps whole shell quartets in one arithmetic) */
 } vsvb_options;
 
 typedef struct vsvb_energy_result {
@@ -112,6 +115,8 @@ typedef struct vsvb_energy_result {
   long long n_tasks;                           /* orbital-quartet tasks (valence.F90:1153-1157) */
   int n_singular_pairs;                        /* determinant pairs on the exact-minor path */
   int n_kernel_launches;                       /* kernels this call enqueued */
+  double n_prim_quartets;                      /* primitive quartets evaluated (after the screen) */
+  double n_prim_quartets_fp32;                 /* of which in FP32 */
 } vsvb_energy_result;
 
 typedef struct vsvb_gpu vsvb_gpu;
@@ -167,6 +172,11 @@ int vsvb_gpu_set_stream(vsvb_gpu *h, void *stream);
  * primitive quartet / shell quartet), cls[i] = 100*prec + 10*bra + ket.
  * Returns the number of launches or a negative status. */
 int vsvb_gpu_eri_profile(vsvb_gpu *h, double *ms, double *flops, int *cls, int cap);
+/* The same with the launches one after another in mode 0 (forward) or 3
+ * (forward + adjoint; needs a previous vsvb_gpu_energy_grad on the handle,
+ * whose dE/dT it reuses).  cls[i] = 100*k + 10*bra + ket, k = 0 FP64,
+ * 1 FP32, 2 double-float, 3 the FP32 tail of an FP64-class schedule. */
+int vsvb_gpu_eri_profile_mode(vsvb_gpu *h, int mode, double *ms, double *flops, int *cls, int cap);
 
 /* In-situ timing of the ERI class launches inside ordinary calls: with
  * vsvb_gpu_set_sweep_timing(h, 1) every ERI sweep records a CUDA event pair

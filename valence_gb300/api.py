@@ -48,7 +48,8 @@ class Desc(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("mixed_threshold", ctypes.c_double), ("ao_screen", ctypes.c_double),
-                ("device", ctypes.c_int), ("grad_mode", ctypes.c_int), ("prim_screen", ctypes.c_double)]
+                ("device", ctypes.c_int), ("grad_mode", ctypes.c_int), ("prim_screen", ctypes.c_double),
+                ("prim_split", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -56,7 +57,8 @@ class Result(ctypes.Structure):
                 ("e2", ctypes.c_double), ("wfnorm", ctypes.c_double), ("enucrep", ctypes.c_double),
                 ("err_est", ctypes.c_double), ("n_quartets_fp64", ctypes.c_longlong),
                 ("n_quartets_fp32", ctypes.c_longlong), ("n_tasks", ctypes.c_longlong),
-                ("n_singular_pairs", ctypes.c_int), ("n_kernel_launches", ctypes.c_int)]
+                ("n_singular_pairs", ctypes.c_int), ("n_kernel_launches", ctypes.c_int),
+                ("n_prim_quartets", ctypes.c_double), ("n_prim_quartets_fp32", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -88,6 +90,7 @@ def lib():
         L.vsvb_gpu_batch_energy_grad.argtypes = [P(ctypes.c_void_p), I, P(P(D)), P(Result), P(P(D))]
         L.vsvb_gpu_set_stream.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.vsvb_gpu_eri_profile.argtypes = [ctypes.c_void_p, P(D), P(D), P(I), I]
+        L.vsvb_gpu_eri_profile_mode.argtypes = [ctypes.c_void_p, I, P(D), P(D), P(I), I]
         L.vsvb_gpu_set_sweep_timing.argtypes = [ctypes.c_void_p, I]
         L.vsvb_gpu_sweep_times.argtypes = [ctypes.c_void_p, P(D), P(D), P(I), I]
         L.vsvb_gpu_sweep_wall_ms.argtypes = [ctypes.c_void_p, P(D)]
@@ -113,7 +116,8 @@ def read_input(path):
     return d
 
 
-def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, grad_mode=0, prim_screen=None):
+def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, grad_mode=0, prim_screen=None,
+                 prim_split=None):
     o = Options()
     lib().vsvb_default_options(ctypes.byref(o))
     o.precision = precision
@@ -123,6 +127,8 @@ def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0
     o.grad_mode = grad_mode
     if prim_screen is not None:
         o.prim_screen = prim_screen
+    if prim_split is not None:
+        o.prim_split = int(prim_split)
     return o
 
 
@@ -130,7 +136,7 @@ class System:
     """One molecule on the GPU: a parsed input plus a device handle."""
 
     def __init__(self, path, precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, coords_angstrom=None,
-                 grad_mode=0, prim_screen=None):
+                 grad_mode=0, prim_screen=None, prim_split=None):
         self.path = path
         self._desc = read_input(path)
         d = self._desc.contents
@@ -140,7 +146,7 @@ class System:
         self._coords_bohr = np.ctypeslib.as_array(d.coords, shape=(3 * d.natom,))
         if coords_angstrom is not None:
             self._coords_bohr[:] = np.asarray(coords_angstrom, dtype=np.float64).ravel() * 1.889725987722
-        self.opt = make_options(precision, mixed_threshold, ao_screen, device, grad_mode, prim_screen)
+        self.opt = make_options(precision, mixed_threshold, ao_screen, device, grad_mode, prim_screen, prim_split)
         self._h = ctypes.c_void_p()
         rc = lib().vsvb_gpu_create(self._desc, ctypes.byref(self.opt), ctypes.byref(self._h))
         if rc:
@@ -198,11 +204,14 @@ class System:
         the handle's own stream)."""
         self._check(lib().vsvb_gpu_set_stream(self._h, ctypes.c_void_p(stream_ptr or None)), "set_stream")
 
-    def eri_profile(self, cap=128):
+    def eri_profile(self, cap=128, mode=0):
+        """Per ERI launch of one sweep run one after another (mode 0 forward,
+        3 forward + adjoint): ms, algorithmic FLOPs and class code."""
         ms = np.zeros(cap)
         fl = np.zeros(cap)
         cl = np.zeros(cap, dtype=np.int32)
-        n = lib().vsvb_gpu_eri_profile(self._h, _dptr(ms), _dptr(fl), cl.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), cap)
+        n = lib().vsvb_gpu_eri_profile_mode(self._h, mode, _dptr(ms), _dptr(fl),
+                                            cl.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), cap)
         if n < 0:
             raise VSVBError("eri_profile failed")
         return [dict(cls=int(cl[i]), ms=float(ms[i]), flops=float(fl[i])) for i in range(n)]

@@ -24,6 +24,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "eri.cuh"
 
 namespace {
@@ -48,7 +50,19 @@ __global__ void symmetrize_kernel(double *T, int np, double *sq) {
 
 
 
+__global__ void to_float_kernel(const double *in, float *out, size_t n) {
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    out[t] = (float)in[t];
+}
+
 }  // namespace
+
+int eri_to_float(const double *in, float *out, size_t n, cudaStream_t st) {
+  if (n == 0) return 0;
+  const size_t blocks = std::min<size_t>((n + 255) / 256, 152 * 16);
+  to_float_kernel<<<(unsigned)blocks, 256, 0, st>>>(in, out, n);
+  return cudaGetLastError() != cudaSuccess;
+}
 
 /* T = U + U^T after the forward pass (the kernels accumulate one
  * orientation); sq[p] = sqrt(max(T[p][p], 0)) */
@@ -64,8 +78,9 @@ int eri_symmetrize(double *T, int np, double *sq, cudaStream_t st) {
  * each), the 3 n_r 2D recurrence tables G(i, k) and the (e0|f0) component
  * sums (3 flops per component and root); per quartet the two transform
  * GEMVs with the transferred weights X' (ne_P x ne_Q block), and in modes 2
- * and 3 the four GEMVs of the adjoint (dX'_P and dX'_Q). */
-double eri_flops(int mode, int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ) {
+ * and 3 the four GEMVs of the adjoint (dX'_P and dX'_Q).  nprimq: the
+ * primitive quartets evaluated (after the primitive screen). */
+double eri_flops(int mode, int cp, int cq, double nprimq, int nopP, int nopQ) {
   static const int la_[6] = {0, 1, 1, 2, 2, 2}, lb_[6] = {0, 0, 1, 0, 1, 2};
   const int la = la_[cp], lb = lb_[cp], lc = la_[cq], ld = lb_[cq];
   auto nc = [](int l) { return (l + 1) * (l + 2) / 2; };
@@ -84,7 +99,7 @@ double eri_flops(int mode, int cp, int cq, int nprimP, int nprimQ, int nopP, int
   const double adj = 2.0 * nopQ * (double)nea * nec + 2.0 * nopP * (double)nopQ * nea +
                      2.0 * nopP * (double)nea * nec + 2.0 * nopQ * (double)nopP * nec;
   const double tr = (mode == 0 ? fwd : 0.0) + (mode == 2 ? adj : 0.0) + (mode == 3 ? fwd + adj : 0.0);
-  return (double)nprimP * nprimQ * prim + tr;
+  return nprimq * prim + tr;
 }
 
 int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int nsm,

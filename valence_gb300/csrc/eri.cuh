@@ -23,12 +23,14 @@ struct EriArgs {
   const int *pair_opid;    /* orbital-pair index of every pair term */
   const double *xtab;      /* transferred weight tables X' = X M (nop x ne per pair) */
   const double *hrr;       /* per-pair transfer matrices M (n_a n_b x ne) */
+  const float *xtab32;     /* X' in FP32 (the FP32 kernels' transform) */
+  const float *Tbar32;     /* dE/dT in FP32 (the FP32 kernels' adjoint) */
   double *T;               /* np x np orbital-pair ERIs (mode 0) */
   int np;
   double *qmax_out;        /* mode 1: sqrt(max_ab |(ab|ab)|) per pair */
   double *q0max_out;       /* mode 1: sqrt(max_e |(e0|e0)|) per pair */
   const float *prim_q0;    /* per primitive pair (prims order): sqrt(max_e |(e0|e0)|) */
-  float prim_eps;          /* primitive quartets with q0_p q0_q below this are skipped (0: none) */
+  float prim_lo, prim_hi;  /* evaluate the primitive quartets with prim_lo <= q0_p q0_q < prim_hi */
   const double *Tbar;      /* mode 2: dE/dT */
   double *xbar;            /* mode 2: dE/dX' */
 };
@@ -43,6 +45,8 @@ int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int2 
 int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
 int eri_dispatch_f32(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
 int eri_dispatch_df64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
-double eri_flops(int mode, int cp, int cq, int nprimP, int nprimQ, int nopP, int nopQ);
+double eri_flops(int mode, int cp, int cq, double nprimq, int nopP, int nopQ);
 int eri_symmetrize(double *T, int np, double *sq, cudaStream_t st);
+/* out[i] = (float)in[i] */
+int eri_to_float(const double *in, float *out, size_t n, cudaStream_t st);
 #endif

@@ -142,6 +142,12 @@ __device__ __forceinline__ double to_double(double v) { return v; }
 __device__ __forceinline__ double to_double(float v) { return (double)v; }
 __device__ __forceinline__ double to_double(df64 v) { return (double)v.hi + (double)v.lo; }
 
+/* s += a*b and read-only loads in the transform arithmetic (FP64 or FP32) */
+__device__ __forceinline__ void mad(double &s, double a, double b) { s = fma(a, b, s); }
+__device__ __forceinline__ void mad(float &s, float a, float b) { s = fmaf(a, b, s); }
+__device__ __forceinline__ double ldt(const double *p) { return __ldg(p); }
+__device__ __forceinline__ float ldt(const float *p) { return __ldg(p); }
+
 /* ---- Rys roots ------------------------------------------------------------ */
 
 __device__ __forceinline__ double clenshaw12(const double *__restrict__ c, double t) {
@@ -316,6 +322,8 @@ struct QuartetShape {
   static constexpr int SM_TR = NCOMP + (NITEM > JCH * NMAX ? NITEM : JCH * NMAX);
   static constexpr int PER_WARP = CTA ? SM_2D + SM_ROOT : (SM_2D + SM_ROOT > SM_TR ? SM_2D + SM_ROOT : SM_TR);
   static constexpr int SHARED = CTA ? SM_TR : 0;
+  /* CTA mode stages each warp's partial block in that warp's table area */
+  static_assert(!CTA || PER_WARP * 8 >= NCOMP * (RB == 4 ? 4 : 8), "per-warp area too small for the partial block");
 };
 
 /*
@@ -367,7 +375,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
     for (int m = 0; m < S::PER_LANE; ++m) acc[m] = R(0);
     /* primitive screen: pairs' primitives are sorted by their bound q0, so
      * rows ip whose q0_p q0_q(first) falls below eps end the contraction */
-    const float eps = args.prim_eps;
+    const float eps = args.prim_lo, eps_hi = args.prim_hi;
     int nrow = P.nprim;
     if (eps > 0.f) {
       const float qtop = args.prim_q0[Q.prim0];
@@ -404,9 +412,10 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
       {
         const int pqi = chunk + lane;
         bool keep = pqi < npq;
-        if (keep && eps > 0.f) {
+        if (keep && (eps > 0.f || eps_hi < INFINITY)) {
           const int ip = pqi / Q.nprim, iq = pqi - ip * Q.nprim;
-          keep = args.prim_q0[P.prim0 + ip] * args.prim_q0[Q.prim0 + iq] >= eps;
+          const float b = args.prim_q0[P.prim0 + ip] * args.prim_q0[Q.prim0 + iq];
+          keep = b >= eps && b < eps_hi;
         }
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
         nch = __popc(bal);
@@ -540,34 +549,50 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
       }
     }
 
-    /* stage the block: E[c] (double) */
-    double *E = stage;
+    /* stage the block E[c] in the transform arithmetic TT: FP32 for the
+     * FP32 kernels (small quartets, or the small-primitive tail of large
+     * ones); FP64 otherwise -- for the double-float kernels too, whose FP64
+     * transform runs on the otherwise idle FP64 pipe beside the other warps'
+     * FP32 work (a double-float transform measured slower) */
+    using TT = typename std::conditional<std::is_same<R, float>::value, float, double>::type;
+    auto tt = [](R v) -> TT {
+      if constexpr (std::is_same<R, float>::value) return v;
+      else return to_double(v);
+    };
+    TT *E = reinterpret_cast<TT *>(stage);
     if (CTA) {
-      for (int c = tid; c < S::NCOMP; c += nthr) E[c] = 0.0;
-      __syncthreads();
+      /* per-warp partial blocks (in the warps' own, now idle, table
+       * areas), summed in warp order: deterministic */
+      TT *part = reinterpret_cast<TT *>(ws);
 #pragma unroll
       for (int m = 0; m < S::PER_LANE; ++m) {
         const int c = lane + 32 * m;
-        if (c < S::NCOMP) atomicAdd(E + c, to_double(acc[m]));
+        if (c < S::NCOMP) part[c] = tt(acc[m]);
+      }
+      __syncthreads();
+      for (int c = tid; c < S::NCOMP; c += nthr) {
+        TT sum = reinterpret_cast<const TT *>(wbase)[c];
+        for (int w = 1; w < WARPS; ++w) sum += reinterpret_cast<const TT *>(wbase + (size_t)w * S::PER_WARP)[c];
+        E[c] = sum;
       }
       __syncthreads();
     } else if (S::G == 1) {
 #pragma unroll
       for (int m = 0; m < S::PER_LANE; ++m) {
         const int c = lane + 32 * m;
-        if (c < S::NCOMP) E[c] = to_double(acc[m]);
+        if (c < S::NCOMP) E[c] = tt(acc[m]);
       }
       __syncwarp();
     } else {
-      double *E2 = stage + S::NCOMP;
+      TT *E2 = E + S::NCOMP;
 #pragma unroll
       for (int m = 0; m < S::PER_LANE; ++m) {
         const int it = lane + 32 * m;
-        if (it < S::NITEM) E2[it] = to_double(acc[m]);
+        if (it < S::NITEM) E2[it] = tt(acc[m]);
       }
       __syncwarp();
       for (int c = lane; c < S::NCOMP; c += 32) {
-        double sum = 0.0;
+        TT sum = TT(0);
         for (int gg = 0; gg < S::G; ++gg) sum += E2[gg * S::NCOMP + c];
         E[c] = sum;
       }
@@ -581,7 +606,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         double mx = 0.0;
         /* and sqrt(max_e |(e0|e0)|), the size of the untransferred block */
         double mx0 = 0.0;
-        for (int e = lane; e < S::NEA; e += 32) mx0 = fmax(mx0, fabs(E[e * S::NEC + e]));
+        for (int e = lane; e < S::NEA; e += 32) mx0 = fmax(mx0, fabs((double)E[e * S::NEC + e]));
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx0 = fmax(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
         if (lane == 0) args.q0max_out[pq.x] = sqrt(mx0);
@@ -592,7 +617,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
             const double me = m[e];
             if (me == 0.0) continue;
             double t = 0.0;
-            for (int f = 0; f < S::NEC; ++f) t = fma(E[e * S::NEC + f], m[f], t);
+            for (int f = 0; f < S::NEC; ++f) t = fma((double)E[e * S::NEC + f], m[f], t);
             v = fma(me, t, v);
           }
           mx = fmax(mx, fabs(v));
@@ -606,9 +631,18 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
       continue;
     }
 
-    double *Y = stage + S::NCOMP;
-    const double *XP = args.xtab + P.xh0;
-    const double *XQ = args.xtab + Q.xh0;
+    TT *Y = E + S::NCOMP;
+    const TT *xtT;
+    const TT *TbarT;
+    if constexpr (std::is_same<TT, float>::value) {
+      xtT = args.xtab32;
+      TbarT = args.Tbar32;
+    } else {
+      xtT = args.xtab;
+      TbarT = args.Tbar;
+    }
+    const TT *XP = xtT + P.xh0;
+    const TT *XQ = xtT + Q.xh0;
     const int *opP = args.pair_opid + P.op0;
     const int *opQ = args.pair_opid + Q.op0;
     const bool same = pq.x == pq.y;
@@ -622,24 +656,24 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         /* Y[jl][ab] = sum_cd E[ab][cd] X_Q[jl][cd] */
         for (int o = tid; o < nj * S::NEA; o += nthr) {
           const int jl = o / S::NEA, abi = o - jl * S::NEA;
-          const double *xq = XQ + (size_t)(j0 + jl) * S::NEC;
-          const double *e = E + abi * S::NEC;
-          double s = 0.0;
+          const TT *xq = XQ + (size_t)(j0 + jl) * S::NEC;
+          const TT *e = E + abi * S::NEC;
+          TT s = TT(0);
 #pragma unroll
-          for (int c = 0; c < S::NEC; ++c) s = fma(e[c], __ldg(xq + c), s);
+          for (int c = 0; c < S::NEC; ++c) mad(s, e[c], ldt(xq + c));
           Y[o] = s;
         }
         sync();
         /* Z[ik][jl] = sum_ab X_P[ik][ab] Y[jl][ab] -> U (one orientation) */
         for (int o = tid; o < P.nop * nj; o += nthr) {
           const int ik = o / nj, jl = o - ik * nj;
-          const double *xp = XP + (size_t)ik * S::NEA;
-          const double *y = Y + jl * S::NEA;
-          double s = 0.0;
+          const TT *xp = XP + (size_t)ik * S::NEA;
+          const TT *y = Y + jl * S::NEA;
+          TT s = TT(0);
 #pragma unroll
-          for (int c = 0; c < S::NEA; ++c) s = fma(__ldg(xp + c), y[c], s);
+          for (int c = 0; c < S::NEA; ++c) mad(s, ldt(xp + c), y[c]);
           const int a = __ldg(opP + ik), b = __ldg(opQ + j0 + jl);
-          atomicAdd(args.T + (size_t)a * args.np + b, same ? 0.5 * s : s);
+          atomicAdd(args.T + (size_t)a * args.np + b, same ? 0.5 * (double)s : (double)s);
         }
         sync();
       }
@@ -655,25 +689,25 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         const int nj = min(S::JCH, Q.nop - j0);
         for (int o = tid; o < nj * S::NEA; o += nthr) {
           const int jl = o / S::NEA, abi = o - jl * S::NEA;
-          const double *xq = XQ + (size_t)(j0 + jl) * S::NEC;
-          const double *e = E + abi * S::NEC;
-          double s = 0.0;
+          const TT *xq = XQ + (size_t)(j0 + jl) * S::NEC;
+          const TT *e = E + abi * S::NEC;
+          TT s = TT(0);
 #pragma unroll
-          for (int c = 0; c < S::NEC; ++c) s = fma(e[c], __ldg(xq + c), s);
+          for (int c = 0; c < S::NEC; ++c) mad(s, e[c], ldt(xq + c));
           Y[o] = s;
         }
         sync();
         for (int o = tid; o < P.nop * S::NEA; o += nthr) {
           const int ik = o / S::NEA, abi = o - ik * S::NEA;
           const int a = __ldg(opP + ik);
-          double s = 0.0;
+          TT s = TT(0);
           for (int jl = 0; jl < nj; ++jl) {
             const int b = __ldg(opQ + j0 + jl);
-            double wv = args.Tbar[(size_t)a * args.np + b];
-            if (!same) wv += args.Tbar[(size_t)b * args.np + a];
-            s = fma(wv, Y[jl * S::NEA + abi], s);
+            TT wv = ldt(TbarT + (size_t)a * args.np + b);
+            if (!same) wv += ldt(TbarT + (size_t)b * args.np + a);
+            mad(s, wv, Y[jl * S::NEA + abi]);
           }
-          atomicAdd(XPb + (size_t)ik * S::NEA + abi, s);
+          atomicAdd(XPb + (size_t)ik * S::NEA + abi, (double)s);
         }
         sync();
       }
@@ -682,24 +716,24 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         const int ni = min(ICH, P.nop - i0);
         for (int o = tid; o < ni * S::NEC; o += nthr) {
           const int ik = o / S::NEC, cdi = o - ik * S::NEC;
-          const double *xp = XP + (size_t)(i0 + ik) * S::NEA;
-          double s = 0.0;
+          const TT *xp = XP + (size_t)(i0 + ik) * S::NEA;
+          TT s = TT(0);
 #pragma unroll
-          for (int c = 0; c < S::NEA; ++c) s = fma(__ldg(xp + c), E[c * S::NEC + cdi], s);
+          for (int c = 0; c < S::NEA; ++c) mad(s, ldt(xp + c), E[c * S::NEC + cdi]);
           Y[o] = s;
         }
         sync();
         for (int o = tid; o < Q.nop * S::NEC; o += nthr) {
           const int jl = o / S::NEC, cdi = o - jl * S::NEC;
           const int b = __ldg(opQ + jl);
-          double s = 0.0;
+          TT s = TT(0);
           for (int ik = 0; ik < ni; ++ik) {
             const int a = __ldg(opP + i0 + ik);
-            double wv = args.Tbar[(size_t)a * args.np + b];
-            if (!same) wv += args.Tbar[(size_t)b * args.np + a];
-            s = fma(wv, Y[ik * S::NEC + cdi], s);
+            TT wv = ldt(TbarT + (size_t)a * args.np + b);
+            if (!same) wv += ldt(TbarT + (size_t)b * args.np + a);
+            mad(s, wv, Y[ik * S::NEC + cdi]);
           }
-          atomicAdd(XQb + (size_t)jl * S::NEC + cdi, s);
+          atomicAdd(XQb + (size_t)jl * S::NEC + cdi, (double)s);
         }
         sync();
       }

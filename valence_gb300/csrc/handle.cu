@@ -142,7 +142,17 @@ struct vsvb_gpu {
   int sweep_mode = -1;
   std::vector<cudaEvent_t> sweep_ev; /* 2 per class launch */
   cudaEvent_t sweep_t0 = nullptr, sweep_t1 = nullptr; /* fork and join of the last sweep */
-  std::vector<int> class_order;   /* (prec, a, c) packed, by decreasing work */
+  /* one ERI launch of a sweep: a class schedule (list 0: FP64-class shell
+   * quartets, 1: FP32-class), the arithmetic it runs in and the window
+   * [lo, hi) of primitive-quartet bounds it evaluates */
+  struct SweepItem {
+    int list, kind, a, c;
+    float lo, hi;
+    double nprimq;           /* primitive quartets inside the window */
+    double flops_fwd, flops_grad;
+    int code;                /* 100*k + 10*a + c; k = kind, or 3 for the FP32 tail of an FP64-class list */
+  };
+  std::vector<SweepItem> sweep; /* by decreasing work */
   int launches = 0;              /* kernels enqueued by the current call */
   /* dims */
   int natom = 0, nsh = 0, nao = 0, norb_all = 0, nsp = 0, ndf = 0, totlen = 0, maxobs = 0, np = 0;
@@ -155,6 +165,7 @@ struct vsvb_gpu {
   std::vector<int2> work_h[2][6][6];
   DBuf<int2> work_d[2][6][6];
   long long nq_fp64 = 0, nq_fp32 = 0;
+  double nprimq_fp32 = 0.0, nprimq_all = 0.0; /* primitive quartets evaluated in FP32 / in total */
   double err_bound = 0.0; /* sum over FP32 quartets of the Schwarz bound */
   double bound_all = 0.0; /* the same over every evaluated quartet */
   /* device data */
@@ -176,6 +187,7 @@ struct vsvb_gpu {
   DBuf<XTerm> xterms;
   DBuf<long long> xelem0, xh_elem0;
   DBuf<double> hrr, xtabh;
+  DBuf<float> xtabh32, Tbar32;
   long long nxelem = 0, nxh = 0;
   int nxterm = 0;
   DBuf<int> obs_n, obs_ao, term0, term_slot, term_j, term_m, term_f, ndf_orb;
@@ -243,6 +255,7 @@ XtabArgs xtab_args(vsvb_gpu *h) {
   x.nxh = h->nxh;
   x.hrr = h->hrr.p;
   x.xtabh = h->xtabh.p;
+  x.xtabh32 = h->xtabh32.p;
   return x;
 }
 
@@ -262,12 +275,15 @@ EriArgs eri_args(vsvb_gpu *h) {
   a.pair_opid = h->pair_opid.p;
   a.xtab = h->xtabh.p;
   a.hrr = h->hrr.p;
+  a.xtab32 = h->xtabh32.p;
+  a.Tbar32 = h->Tbar32.p;
   a.T = h->T.p;
   a.np = h->np;
   a.qmax_out = h->qmax.p;
   a.q0max_out = h->q0max.p;
   a.prim_q0 = h->prim_q0.p;
-  a.prim_eps = (float)h->opt.prim_screen;
+  a.prim_lo = (float)h->opt.prim_screen;
+  a.prim_hi = INFINITY;
   a.Tbar = h->Tbar.p;
   a.xbar = h->xbarh.p;
   return a;
@@ -691,6 +707,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   CK(h->hrr.upload(hrr.empty() ? std::vector<double>(1, 0.0) : hrr), "upload hrr");
   CK(h->xtab.alloc(std::max<long long>(nx, 1)), "alloc xtab");
   CK(h->xtabh.alloc(std::max<long long>(nxh, 1)), "alloc xtabh");
+  CK(h->xtabh32.alloc(std::max<long long>(nxh, 1)), "alloc xtabh32");
   CK(h->qmax.alloc(std::max<size_t>(pairs.size(), 1)), "alloc qmax");
   CK(h->q0max.alloc(std::max<size_t>(pairs.size(), 1)), "alloc q0max");
   CK(h->T.alloc(std::max<size_t>((size_t)h->np * h->np, 1)), "alloc T");
@@ -719,11 +736,13 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   }
   /* Schwarz bounds (diagonal quartets) */
   std::vector<double> q0;
+  std::vector<float> q0f; /* per primitive pair, sorted descending within each shell pair */
   {
     std::vector<int2> diag[6];
     for (size_t p = 0; p < pairs.size(); ++p) diag[pairs[p].cls].push_back(make_int2((int)p, (int)p));
     EriArgs ea = eri_args(h);
-    ea.prim_eps = 0.f;
+    ea.prim_lo = 0.f;
+    ea.prim_hi = INFINITY;
     DBuf<int2> wd[6];
     for (int c = 0; c < 6; ++c) {
       if (diag[c].empty()) continue;
@@ -779,7 +798,8 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     ea.geom64 = vg_d.p;
     ea.qmax_out = vq.p;
     ea.q0max_out = vq0.p;
-    ea.prim_eps = 0.f;
+    ea.prim_lo = 0.f;
+    ea.prim_hi = INFINITY;
     for (int c = 0; c < 6; ++c) {
       if (vdiag[c].empty()) continue;
       CK(wd[c].upload(vdiag[c]), "upload prim diag");
@@ -792,7 +812,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     CK(cudaStreamSynchronize(h->st), "prim schwarz sync");
     if (!vp.empty()) CK(cudaMemcpy(pq0.data(), vq0.p, sizeof(double) * pq0.size(), cudaMemcpyDeviceToHost), "prim q0");
     /* vp is in prims order, so pq0[i] belongs to prims[i] */
-    std::vector<float> q0f(prims.size());
+    q0f.assign(prims.size(), 0.f);
     for (size_t pi = 0; pi < pairs.size(); ++pi) {
       const int p0 = pairs[pi].prim0, n = pairs[pi].nprim;
       std::vector<int> ord(n);
@@ -825,6 +845,26 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   }
   /* quartet schedule */
   const bool mixed = h->opt.precision == VSVB_MIXED || h->opt.precision == VSVB_MIXED_DF64;
+  const float eps = (float)h->opt.prim_screen, tau = (float)h->opt.mixed_threshold;
+  const bool split = mixed && h->opt.prim_split;
+  /* primitive quartets of (P, Q) with lo <= q0_p q0_q < hi (FP32 products,
+   * as the kernels form them; rows cut where q0_p q0_q(first) < lo), and
+   * the sum of their bounds */
+  auto window = [&](int P, int Q, float lo, float hi, double &sum) -> double {
+    const float *a = q0f.data() + pairs[P].prim0, *b = q0f.data() + pairs[Q].prim0;
+    const int na = pairs[P].nprim, nb = pairs[Q].nprim;
+    double n = 0.0;
+    sum = 0.0;
+    int jlo = nb, jhi = nb;
+    for (int i = 0; i < na; ++i) {
+      if (!(a[i] * b[0] >= lo)) break;
+      while (jlo > 0 && !(a[i] * b[jlo - 1] >= lo)) --jlo;
+      while (jhi > 0 && !(a[i] * b[jhi - 1] >= hi)) --jhi;
+      n += jlo - jhi;
+      for (int j = jhi; j < jlo; ++j) sum += (double)a[i] * b[j];
+    }
+    return n;
+  };
   h->err_bound = 0.0;
   h->bound_all = 0.0;
   for (size_t P = 0; P < pairs.size(); ++P)
@@ -835,30 +875,58 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
       if (pairs[a].cls < pairs[c].cls) std::swap(a, c);
       int prec = (mixed && b < h->opt.mixed_threshold) ? 1 : 0;
       h->bound_all += b;
+      double sb = 0.0;
+      const double nall = window(a, c, eps, INFINITY, sb);
+      h->nprimq_all += nall;
       if (prec) {
         h->nq_fp32++;
+        h->nprimq_fp32 += nall;
         h->err_bound += amp[P] * amp[Q];
       } else {
         h->nq_fp64++;
+        if (split) {
+          /* the FP32 tail: its bound mass in units of the pair bounds, with
+           * the transfer norms of both pairs */
+          const double nt = window(a, c, eps, tau, sb);
+          h->nprimq_fp32 += nt;
+          h->err_bound += sb * (amp[P] / std::max(q0[P], 1e-300)) * (amp[Q] / std::max(q0[Q], 1e-300));
+        }
       }
       h->work_h[prec][pairs[a].cls][pairs[c].cls].push_back(make_int2(a, c));
     }
   {
-    std::vector<std::pair<double, int>> cost;
     for (int p = 0; p < 2; ++p)
       for (int a = 0; a < 6; ++a)
         for (int c = 0; c < 6; ++c) {
           const auto &w = h->work_h[p][a][c];
           if (w.empty()) continue;
           CK(h->work_d[p][a][c].upload(w), "upload work");
-          double f = 0.0;
-          for (const int2 &q : w) f += eri_flops(0, a, c, pairs[q.x].nprim, pairs[q.y].nprim, pairs[q.x].nop, pairs[q.y].nop);
-          cost.push_back({f, p * 100 + a * 10 + c});
+          /* launches over this list: FP32-class lists in FP32; FP64-class
+           * lists in the handle's FP64-class arithmetic, and with the split
+           * their primitive quartets below tau in FP32 */
+          std::vector<vsvb_gpu::SweepItem> items;
+          if (p == 1) {
+            items.push_back({p, ERI_F32, a, c, eps, INFINITY, 0, 0, 0, 100 * ERI_F32 + 10 * a + c});
+          } else if (split) {
+            items.push_back({p, eri_kind(h, 0), a, c, std::max(eps, tau), INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
+            items.push_back({p, ERI_F32, a, c, eps, tau, 0, 0, 0, 300 + 10 * a + c});
+          } else {
+            items.push_back({p, eri_kind(h, 0), a, c, eps, INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
+          }
+          for (auto &it : items) {
+            for (const int2 &q : w) {
+              double sb = 0.0;
+              const double n = window(q.x, q.y, it.lo, it.hi, sb);
+              it.nprimq += n;
+              it.flops_fwd += eri_flops(0, a, c, n, pairs[q.x].nop, pairs[q.y].nop);
+              it.flops_grad += eri_flops(3, a, c, n, pairs[q.x].nop, pairs[q.y].nop);
+            }
+            if (it.nprimq > 0) h->sweep.push_back(it);
+          }
         }
-    std::sort(cost.begin(), cost.end(), [](const std::pair<double, int> &x, const std::pair<double, int> &y) {
-      return x.first > y.first;
+    std::sort(h->sweep.begin(), h->sweep.end(), [](const vsvb_gpu::SweepItem &x, const vsvb_gpu::SweepItem &y) {
+      return x.flops_fwd > y.flops_fwd;
     });
-    for (auto &c : cost) h->class_order.push_back(c.second);
   }
 
   /* determinant pairs */
@@ -937,6 +1005,7 @@ int alloc_grad(vsvb_gpu *h) {
   const long long nq = h->ds.nq;
   const int na = h->ds.nalpha, nb = h->ds.nbeta;
   CK(h->Tbar.alloc(std::max<size_t>((size_t)h->np * h->np, 1)), "alloc Tbar");
+  CK(h->Tbar32.alloc(std::max<size_t>((size_t)h->np * h->np, 1)), "alloc Tbar32");
   CK(h->Sbar.alloc((size_t)h->nsp * h->nsp), "alloc Sbar");
   CK(h->Hbar.alloc((size_t)h->nsp * h->nsp), "alloc Hbar");
   CK(h->xbar.alloc(std::max<long long>(h->nxelem, 1)), "alloc xbar");
@@ -964,19 +1033,20 @@ int eri_sweep(vsvb_gpu *h, int mode) {
   CK(cudaEventRecord(h->ev_fork, st), "event record");
   for (int k = 0; k < vsvb_gpu::NAUX; ++k) CK(cudaStreamWaitEvent(h->aux[k], h->ev_fork, 0), "stream wait");
   int i = 0;
-  if (h->sweep_timing && h->sweep_ev.size() < 2 * h->class_order.size()) {
-    for (size_t k = h->sweep_ev.size(); k < 2 * h->class_order.size(); ++k) {
+  if (h->sweep_timing && h->sweep_ev.size() < 2 * h->sweep.size()) {
+    for (size_t k = h->sweep_ev.size(); k < 2 * h->sweep.size(); ++k) {
       cudaEvent_t e;
       CK(cudaEventCreate(&e), "cudaEventCreate");
       h->sweep_ev.push_back(e);
     }
   }
-  for (int code : h->class_order) {
-    const int p = code / 100, a = (code / 10) % 10, c = code % 10;
-    const int n = (int)h->work_h[p][a][c].size();
+  for (const auto &it : h->sweep) {
+    const int n = (int)h->work_h[it.list][it.a][it.c].size();
     cudaStream_t sa = h->aux[i % vsvb_gpu::NAUX];
+    ea.prim_lo = it.lo;
+    ea.prim_hi = it.hi;
     if (h->sweep_timing) CK(cudaEventRecord(h->sweep_ev[2 * i], sa), "event record");
-    if (eri_launch(mode, eri_kind(h, p), a, c, ea, h->work_d[p][a][c].p, n, h->nsm, sa)) {
+    if (eri_launch(mode, it.kind, it.a, it.c, ea, h->work_d[it.list][it.a][it.c].p, n, h->nsm, sa)) {
       h->err = "ERI kernel launch failed";
       return VSVB_ERR_CUDA;
     }
@@ -1032,7 +1102,11 @@ int forward(vsvb_gpu *h, bool fused = false) {
     CK(cudaMemsetAsync(h->xbarh.p, 0, sizeof(double) * h->xbarh.n, st), "memset xbarh");
     AsmArgs ad = asm_args(h);
     CK(launch_assemble(2, dim3((unsigned)h->ds.nq, h->nsplit), 128, 0, st, dc, ad), "density walk");
-    h->launches++;
+    if (eri_to_float(h->Tbar.p, h->Tbar32.p, h->Tbar.n, st)) {
+      h->err = "Tbar conversion launch failed";
+      return VSVB_ERR_CUDA;
+    }
+    h->launches += 2;
   }
   CK(cudaMemsetAsync(h->T.p, 0, sizeof(double) * h->T.n, st), "memset T");
   {
@@ -1074,6 +1148,8 @@ int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
     out->n_quartets_fp32 = h->nq_fp32;
     out->n_tasks = h->ntasks;
     out->n_kernel_launches = h->launches;
+    out->n_prim_quartets = h->nprimq_all;
+    out->n_prim_quartets_fp32 = h->nprimq_fp32;
     /* error estimate of the FP32 quartets: FP32 rounding (2^-24) of the
      * arithmetic behind their integrals -- per quartet the (e0|e0) bounds
      * times the transfer-matrix norms of both pairs -- converted to energy by
@@ -1150,6 +1226,7 @@ void vsvb_default_options(vsvb_options *o) {
   o->device = 0;
   o->grad_mode = 0;
   o->prim_screen = 1e-17;
+  o->prim_split = 1;
 }
 
 int vsvb_gpu_create(const vsvb_system_desc *d, const vsvb_options *opt, vsvb_gpu **out) {
@@ -1266,44 +1343,50 @@ int vsvb_gpu_set_stream(vsvb_gpu *h, void *stream) {
   return VSVB_OK;
 }
 
-int vsvb_gpu_eri_profile(vsvb_gpu *h, double *ms, double *flops, int *cls, int cap) {
-  if (!h) return -VSVB_ERR_INPUT;
+int vsvb_gpu_eri_profile_mode(vsvb_gpu *h, int mode, double *ms, double *flops, int *cls, int cap) {
+  if (!h || (mode != 0 && mode != 3)) return -VSVB_ERR_INPUT;
+  if (mode == 3 && !h->grad_ready) return -VSVB_ERR_INPUT;
   if (cudaSetDevice(h->dev) != cudaSuccess) return -VSVB_ERR_CUDA;
-  std::vector<double> P(h->pairs.n);
-  std::vector<ShellPair> pairs(h->pairs.n);
-  if (!pairs.empty() &&
-      cudaMemcpy(pairs.data(), h->pairs.p, sizeof(ShellPair) * pairs.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
-    return -VSVB_ERR_CUDA;
   EriArgs ea = eri_args(h);
   if (cudaMemsetAsync(h->T.p, 0, sizeof(double) * h->T.n, h->st) != cudaSuccess) return -VSVB_ERR_CUDA;
-  int k = 0;
-  for (int p = 0; p < 2; ++p)
-    for (int a = 0; a < 6; ++a)
-      for (int c = 0; c <= a; ++c) {
-        const auto &w = h->work_h[p][a][c];
-        if (w.empty()) continue;
-        if (k >= cap) return k;
-        cudaEvent_t e0, e1;
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        cudaEventRecord(e0, h->st);
-        if (eri_launch(0, eri_kind(h, p), a, c, ea, h->work_d[p][a][c].p, (int)w.size(), h->nsm, h->st))
-          return -VSVB_ERR_CUDA;
-        cudaEventRecord(e1, h->st);
-        if (cudaEventSynchronize(e1) != cudaSuccess) return -VSVB_ERR_CUDA;
-        float t = 0.f;
-        cudaEventElapsedTime(&t, e0, e1);
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        double f = 0.0;
-        for (const int2 &q : w)
-          f += eri_flops(0, a, c, pairs[q.x].nprim, pairs[q.y].nprim, pairs[q.x].nop, pairs[q.y].nop);
-        ms[k] = t;
-        flops[k] = f;
-        cls[k] = 100 * eri_kind(h, p) + 10 * a + c;
-        ++k;
-      }
-  return k;
+  if (mode == 3 && cudaMemsetAsync(h->xbarh.p, 0, sizeof(double) * h->xbarh.n, h->st) != cudaSuccess)
+    return -VSVB_ERR_CUDA;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return -VSVB_ERR_CUDA;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return -VSVB_ERR_CUDA;
+  }
+  int k = 0, rc = 0;
+  for (const auto &it : h->sweep) {
+    if (k >= cap) break;
+    ea.prim_lo = it.lo;
+    ea.prim_hi = it.hi;
+    cudaEventRecord(e0, h->st);
+    if (eri_launch(mode, it.kind, it.a, it.c, ea, h->work_d[it.list][it.a][it.c].p,
+                   (int)h->work_h[it.list][it.a][it.c].size(), h->nsm, h->st)) {
+      rc = -VSVB_ERR_CUDA;
+      break;
+    }
+    cudaEventRecord(e1, h->st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = -VSVB_ERR_CUDA;
+      break;
+    }
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    ms[k] = t;
+    flops[k] = mode == 0 ? it.flops_fwd : it.flops_grad;
+    cls[k] = it.code;
+    ++k;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc ? rc : k;
+}
+
+int vsvb_gpu_eri_profile(vsvb_gpu *h, double *ms, double *flops, int *cls, int cap) {
+  return vsvb_gpu_eri_profile_mode(h, 0, ms, flops, cls, cap);
 }
 
 int vsvb_gpu_set_sweep_timing(vsvb_gpu *h, int on) {
@@ -1321,18 +1404,14 @@ int vsvb_gpu_sweep_times(vsvb_gpu *h, double *ms, double *flops, int *cls, int c
       cudaMemcpy(pairs.data(), h->pairs.p, sizeof(ShellPair) * pairs.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
     return -VSVB_ERR_CUDA;
   int k = 0;
-  for (size_t i = 0; i < h->class_order.size() && k < cap; ++i, ++k) {
-    const int code = h->class_order[i];
-    const int p = code / 100, a = (code / 10) % 10, c = code % 10;
+  for (size_t i = 0; i < h->sweep.size() && k < cap; ++i, ++k) {
+    const auto &it = h->sweep[i];
     if (cudaEventSynchronize(h->sweep_ev[2 * i + 1]) != cudaSuccess) return -VSVB_ERR_CUDA;
     float t = 0.f;
     if (cudaEventElapsedTime(&t, h->sweep_ev[2 * i], h->sweep_ev[2 * i + 1]) != cudaSuccess) return -VSVB_ERR_CUDA;
-    double f = 0.0;
-    for (const int2 &q : h->work_h[p][a][c])
-      f += eri_flops(h->sweep_mode, a, c, pairs[q.x].nprim, pairs[q.y].nprim, pairs[q.x].nop, pairs[q.y].nop);
     ms[k] = t;
-    flops[k] = f;
-    cls[k] = 100 * eri_kind(h, p) + 10 * a + c;
+    flops[k] = h->sweep_mode == 0 ? it.flops_fwd : it.flops_grad;
+    cls[k] = it.code;
   }
   return k;
 }

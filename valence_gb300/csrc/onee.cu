@@ -392,6 +392,7 @@ __global__ void xhrr_kernel(XtabArgs x) {
   double s = 0.0;
   for (int ab = 0; ab < nab; ++ab) s = fma(X[ab], M[ab * ne + e], s);
   x.xtabh[t] = s;
+  x.xtabh32[t] = (float)s;
 }
 
 /* adjoint: dE/dX(op, ab) = sum_e dE/dX'(op, e) M(ab, e); one thread per X element */

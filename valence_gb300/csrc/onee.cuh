@@ -56,6 +56,7 @@ struct XtabArgs {
   long long nxh;
   const double *hrr;
   double *xtabh;
+  float *xtabh32; /* the same in FP32 */
 };
 
 __global__ void ao_1e_kernel(Ao1eArgs a);
