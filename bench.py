@@ -50,11 +50,55 @@ METRIC = "VSVB energy+grad evals/s, mixed vs plain FP64 on 1 GB300 at |ΔE|<=1e-
 # launches, from the ncu --set full captures summarised in profiles/
 # (keys: workload, 100*kind + 10*bra pair class + ket pair class; kind 2 =
 # double-float, pair classes ss ps pp ds dp dd = 0..5)
-PROFILED_TRAFFIC = {
-    ("ch_chain", 253): 1.230848e6 + 0.0,  # (dd|ds) double-float, forward + adjoint
-    ("ch_chain", 254): 1.250304e6 + 0.0,  # (dd|dp)
-    ("ch_chain", 255): 0.813312e6 + 0.0,  # (dd|dd)
+PROFILED_TRAFFIC = {  # profiles/eri_df64_ch_chain.md
+    ("ch_chain", 253): 1.233664e6 + 0.0,  # (dd|ds) double-float, forward + adjoint
+    ("ch_chain", 254): 1.255168e6 + 0.0,  # (dd|dp)
+    ("ch_chain", 255): 0.816384e6 + 0.0,  # (dd|dd)
 }
+
+
+def eri_roofline(sweep, sweep_wall, fp64_peak, fp32_peak, step_ms, workload):
+    """Roofline of the ERI kernel: all class launches of one step's sweep, run
+    concurrently on the library's side streams, timed in situ.
+
+    sweep: {class code: [summed ms, summed FLOPs, launches]} over the timed
+    steps; sweep_wall: fork-to-join ms per step.  Class code = 100*kind +
+    10*bra + ket; kinds 0 FP64, 1 FP32, 2 double-float, 3 the FP32 tail
+    (small primitive quartets) of an FP64-class schedule.  Per kind the bound
+    rate for the algorithmic FLOPs (eri_flops: mostly component updates
+    acc += x*y*z, 3 flops) is the measured FMA instruction rate (FMA peak / 2)
+    times 3 flops per update over the instructions one update takes: 2 for
+    FP32 and FP64 (MUL + FMA), 16 for double-float.
+    T* = sum_kind W_kind / P_kind; frac = T* / T_sweep."""
+    rate = {0: fp64_peak / 2 * 3 / 2, 1: fp32_peak / 2 * 3 / 2, 2: fp32_peak / 2 * 3 / 16, 3: fp32_peak / 2 * 3 / 2}
+    kind_name = {0: "fp64", 1: "fp32", 2: "double-float", 3: "fp32 tail"}
+    pair_l = ["s s", "p s", "p p", "d s", "d p", "d d"]
+    W = {k: 0.0 for k in rate}
+    for c, (_, fl, cnt) in sweep.items():
+        W[c // 100] += fl / cnt
+    t_star = sum(W[k] / rate[k] for k in rate)
+    t_sweep = sum(sweep_wall) / len(sweep_wall) * 1e-3
+    w_tot = sum(W.values())
+    cls_top, (t_top, f_top, n_top) = max(sweep.items(), key=lambda kv: kv[1][0])
+    return {"bound": "fp32_pipe",
+            "kernel": "eri_kernel: every class launch of the step's ERI sweep (forward + adjoint), "
+                      "concurrent on 6 streams",
+            "achieved": w_tot / t_sweep / 1e12, "peak": w_tot / t_star / 1e12, "unit": "TFLOP/s",
+            "frac": t_star / t_sweep,
+            "achieved_unit_note": "algorithmic FP64-equivalent FLOPs of the Rys formulation (eri_flops) per "
+                                  "second of sweep wall time",
+            "peak_basis": "T* = sum over kinds of W_kind / P_kind; P = measured FMA instruction rate "
+                          "(vsvb_gpu_fma_peak / 2) x 3 flops per component update / instructions per update "
+                          "(2 FP32 or FP64, 16 double-float)",
+            "flops_per_step": {kind_name[k]: W[k] for k in W}, "sweep_ms": t_sweep * 1e3,
+            "sweeps_timed": len(sweep_wall), "share_of_step": t_sweep * 1e3 / step_ms,
+            "traffic": PROFILED_TRAFFIC.get((workload, cls_top)),
+            "traffic_note": "dram read+write bytes per launch of the longest class launch "
+                            "(ncu capture summarised in profiles/)",
+            "longest_launch": {"class": f"({pair_l[(cls_top // 10) % 10]}|{pair_l[cls_top % 10]}) "
+                                        f"{kind_name[cls_top // 100]}",
+                               "ms_in_situ": t_top / n_top, "flops": f_top / n_top},
+            "fp64_fma_tflops": fp64_peak / 1e12, "fp32_fma_tflops": fp32_peak / 1e12}
 
 
 def _args():
@@ -270,43 +314,7 @@ def run_ours(a, rank, world):
         return
     # roofline of the dominant ERI launch of the headline (mixed) run
     fp64_peak, fp32_peak = api.fma_peak(dev)
-    # Roofline of the ERI kernel (all class launches of one step's sweep, run
-    # concurrently on the library's side streams), timed in situ.  Per
-    # arithmetic kind the bound rate for the algorithmic FLOPs (eri_flops:
-    # mostly component updates acc += x*y*z, 3 flops) is the measured FP32 or
-    # FP64 instruction rate (FMA peak / 2) times 3 flops per update over the
-    # instructions one update takes: 2 for FP32 and FP64 (MUL + FMA), 16 for
-    # double-float.  T* = sum_kind W_kind / P_kind; frac = T* / T_sweep.
-    rate = {0: fp64_peak / 2 * 3 / 2, 1: fp32_peak / 2 * 3 / 2, 2: fp32_peak / 2 * 3 / 16}
-    n_sw = len(sweep_wall)
-    W = {k: 0.0 for k in rate}
-    for c, (_, fl, cnt) in sweep.items():
-        W[c // 100] += fl / cnt
-    t_star = sum(W[k] / rate[k] for k in rate)
-    t_sweep = statistics.mean(sweep_wall) * 1e-3
-    w_tot = sum(W.values())
-    cls_top, (t_top, f_top, n_top) = max(sweep.items(), key=lambda kv: kv[1][0])
-    kind_name = {0: "fp64", 1: "fp32", 2: "double-float"}
-    pair_l = ["s s", "p s", "p p", "d s", "d p", "d d"]
-    roofline = {"bound": "fp32_pipe",
-                "kernel": "eri_kernel: every class launch of the step's ERI sweep (forward + adjoint), "
-                          "concurrent on 6 streams",
-                "achieved": w_tot / t_sweep / 1e12, "peak": w_tot / t_star / 1e12, "unit": "TFLOP/s",
-                "frac": t_star / t_sweep,
-                "achieved_unit_note": "algorithmic FP64-equivalent FLOPs of the Rys formulation (eri_flops) per "
-                                      "second of sweep wall time",
-                "peak_basis": "T* = sum over kinds of W_kind / P_kind; P = measured FMA instruction rate "
-                              "(vsvb_gpu_fma_peak / 2) x 3 flops per component update / instructions per update "
-                              "(2 FP32 or FP64, 16 double-float)",
-                "flops_per_step": {kind_name[k]: W[k] for k in W}, "sweep_ms": t_sweep * 1e3,
-                "sweeps_timed": n_sw, "share_of_step": t_sweep * 1e3 / (statistics.mean(ms_mx)),
-                "traffic": PROFILED_TRAFFIC.get((a.workload, cls_top)),
-                "traffic_note": "dram read+write bytes per launch of the longest class launch "
-                                "(ncu capture summarised in profiles/)",
-                "longest_launch": {"class": f"({pair_l[(cls_top // 10) % 10]}|{pair_l[cls_top % 10]}) "
-                                            f"{kind_name[cls_top // 100]}",
-                                   "ms_in_situ": t_top / n_top, "flops": f_top / n_top},
-                "fp64_fma_tflops": fp64_peak / 1e12, "fp32_fma_tflops": fp32_peak / 1e12}
+    roofline = eri_roofline(sweep, sweep_wall, fp64_peak, fp32_peak, statistics.mean(ms_mx), a.workload)
     cpu = None
     if world == 1 and not a.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as d:
