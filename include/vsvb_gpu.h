@@ -100,6 +100,8 @@ typedef struct vsvb_options {
   int prim_split;         /* mixed paths: the primitive quartets of the FP64-class shell
                            * quartets whose bound falls below mixed_threshold also run in
                            * FP32 (default 1; 0 keeps whole shell quartets in one arithmetic) */
+  int cuda_graph;         /* energy + gradient calls replay one captured CUDA graph of the
+                           * whole evaluation from the second call on (default 1) */
 } vsvb_options;
 
 typedef struct vsvb_energy_result {
@@ -159,6 +161,25 @@ int vsvb_gpu_energy_grad_device(vsvb_gpu *h, const double *coeff_dev, vsvb_energ
  * are host arrays of handle i's totlen (grads may be NULL for energy only). */
 int vsvb_gpu_batch_energy_grad(vsvb_gpu *const *handles, int n, const double *const *weights,
                                vsvb_energy_result *results, double *const *grads);
+
+/* Batched energy + gradient of many molecules as ONE CUDA graph launch.
+ * vsvb_batch_create takes handles on one device (gradient-capable: no
+ * derived basis functions), runs one warm-up evaluation on each, and keeps
+ * them borrowed for the batch's life.  vsvb_batch_energy_grad copies
+ * weights_dev[i] (device, handle i's totlen) in, evaluates every molecule
+ * -- each on its own stream branch of the graph, so their kernels run
+ * concurrently -- and writes dE/dweights to grads_dev[i] (device) and the
+ * energies to results[i] (host, may be NULL).  The graph is captured on the
+ * first call and replayed while the pointer arrays stay the same; changed
+ * pointers trigger a new capture.  stream: a cudaStream_t to launch on, or
+ * NULL for the batch's own.  Returns after the results are on the host. */
+typedef struct vsvb_batch vsvb_batch;
+int vsvb_batch_create(vsvb_gpu *const *handles, int n, vsvb_batch **batch);
+int vsvb_batch_energy_grad(vsvb_batch *batch, const double *const *weights_dev, double *const *grads_dev,
+                           vsvb_energy_result *results, void *stream);
+int vsvb_batch_launches(const vsvb_batch *batch); /* kernels per graph launch */
+const char *vsvb_batch_last_error(const vsvb_batch *batch);
+void vsvb_batch_destroy(vsvb_batch *batch);
 
 /* Run the handle's work on a caller-owned stream (a cudaStream_t passed as
  * void*; NULL restores the handle's own stream).  Lets a host time calls with

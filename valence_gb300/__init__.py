@@ -5,8 +5,8 @@ package is the thin Python host mirroring the reference's API
 (valence_api.F90: initialize / calculate_energy / finalize) plus a
 torch.autograd.Function for the weight gradient.
 """
-from .api import (VSVBError, System, Options, FP64, MIXED, MIXED_DF64, valence_api_initialize,
+from .api import (VSVBError, System, Batch, Options, FP64, MIXED, MIXED_DF64, valence_api_initialize,
                   valence_api_calculate_energy, valence_api_finalize, VSVBEnergy, library_path)
 
-__all__ = ["VSVBError", "System", "Options", "FP64", "MIXED", "MIXED_DF64", "valence_api_initialize",
+__all__ = ["VSVBError", "System", "Batch", "Options", "FP64", "MIXED", "MIXED_DF64", "valence_api_initialize",
            "valence_api_calculate_energy", "valence_api_finalize", "VSVBEnergy", "library_path"]

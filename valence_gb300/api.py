@@ -49,7 +49,7 @@ class Desc(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("mixed_threshold", ctypes.c_double), ("ao_screen", ctypes.c_double),
                 ("device", ctypes.c_int), ("grad_mode", ctypes.c_int), ("prim_screen", ctypes.c_double),
-                ("prim_split", ctypes.c_int)]
+                ("prim_split", ctypes.c_int), ("cuda_graph", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -98,6 +98,13 @@ def lib():
         L.vsvb_det_factor.argtypes = [ctypes.c_void_p, I, I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_void_p]
         L.vsvb_det_factor_noalloc.argtypes = L.vsvb_det_factor.argtypes
+        L.vsvb_batch_create.argtypes = [P(ctypes.c_void_p), I, P(ctypes.c_void_p)]
+        L.vsvb_batch_energy_grad.argtypes = [ctypes.c_void_p, P(ctypes.c_void_p), P(ctypes.c_void_p), P(Result),
+                                             ctypes.c_void_p]
+        L.vsvb_batch_launches.argtypes = [ctypes.c_void_p]
+        L.vsvb_batch_last_error.argtypes = [ctypes.c_void_p]
+        L.vsvb_batch_last_error.restype = ctypes.c_char_p
+        L.vsvb_batch_destroy.argtypes = [ctypes.c_void_p]
         _LIB = L
     return _LIB
 
@@ -117,7 +124,7 @@ def read_input(path):
 
 
 def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, grad_mode=0, prim_screen=None,
-                 prim_split=None):
+                 prim_split=None, cuda_graph=None):
     o = Options()
     lib().vsvb_default_options(ctypes.byref(o))
     o.precision = precision
@@ -129,6 +136,8 @@ def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0
         o.prim_screen = prim_screen
     if prim_split is not None:
         o.prim_split = int(prim_split)
+    if cuda_graph is not None:
+        o.cuda_graph = int(cuda_graph)
     return o
 
 
@@ -136,7 +145,7 @@ class System:
     """One molecule on the GPU: a parsed input plus a device handle."""
 
     def __init__(self, path, precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, coords_angstrom=None,
-                 grad_mode=0, prim_screen=None, prim_split=None):
+                 grad_mode=0, prim_screen=None, prim_split=None, cuda_graph=None):
         self.path = path
         self._desc = read_input(path)
         d = self._desc.contents
@@ -146,7 +155,8 @@ class System:
         self._coords_bohr = np.ctypeslib.as_array(d.coords, shape=(3 * d.natom,))
         if coords_angstrom is not None:
             self._coords_bohr[:] = np.asarray(coords_angstrom, dtype=np.float64).ravel() * 1.889725987722
-        self.opt = make_options(precision, mixed_threshold, ao_screen, device, grad_mode, prim_screen, prim_split)
+        self.opt = make_options(precision, mixed_threshold, ao_screen, device, grad_mode, prim_screen, prim_split,
+                                cuda_graph)
         self._h = ctypes.c_void_p()
         rc = lib().vsvb_gpu_create(self._desc, ctypes.byref(self.opt), ctypes.byref(self._h))
         if rc:
@@ -359,3 +369,46 @@ try:
             return gout * g, None
 except ImportError:  # pragma: no cover
     VSVBEnergy = None
+
+
+class Batch:
+    """Energy + gradient of many molecules as one CUDA graph launch
+    (vsvb_batch_*).  systems: System objects on one device; they must stay
+    alive while the batch is used."""
+
+    def __init__(self, systems):
+        self.systems = list(systems)
+        arr = (ctypes.c_void_p * len(self.systems))(*[s._h for s in self.systems])
+        self._b = ctypes.c_void_p()
+        rc = lib().vsvb_batch_create(arr, len(self.systems), ctypes.byref(self._b))
+        if rc:
+            msg = lib().vsvb_batch_last_error(self._b).decode() if self._b else ""
+            self.close()
+            raise VSVBError(f"vsvb_batch_create failed ({rc}): {msg}")
+
+    def energy_grad_device(self, weight_ptrs, grad_ptrs, stream=None):
+        """weight_ptrs / grad_ptrs: device addresses (one per molecule).
+        Returns the list of result dicts."""
+        n = len(self.systems)
+        w = (ctypes.c_void_p * n)(*weight_ptrs)
+        g = (ctypes.c_void_p * n)(*grad_ptrs)
+        res = (Result * n)()
+        rc = lib().vsvb_batch_energy_grad(self._b, w, g, res, ctypes.c_void_p(stream) if stream else None)
+        if rc:
+            raise VSVBError(f"vsvb_batch_energy_grad failed ({rc}): {lib().vsvb_batch_last_error(self._b).decode()}")
+        return [r.as_dict() for r in res]
+
+    @property
+    def launches(self):
+        return lib().vsvb_batch_launches(self._b)
+
+    def close(self):
+        if getattr(self, "_b", None):
+            lib().vsvb_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -158,4 +158,12 @@ def random_molecule(path, seed, nat_range=(2, 12), zs=(1, 3, 6, 7, 8, 9), min_se
     return path
 
 
+def batch_molecules(dirpath, n=256, seed0=1000):
+    """n independent random molecules (2-12 atoms, Z in {1,3,6,7,8,9}, 4-80
+    functions, 0-2 coupled pairs, DOCC for the rest, one unpaired orbital when
+    the electron count is odd), seeds seed0, seed0+1, ...  Returns the paths."""
+    import os
+    return [random_molecule(os.path.join(dirpath, f"mol{seed0 + i:05d}.inp"), seed0 + i) for i in range(n)]
+
+
 WORKLOADS = {"water_vshf": water_vshf, "ch_chain": ch_chain, "lif_cluster": lif_cluster}

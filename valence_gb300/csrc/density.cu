@@ -453,6 +453,12 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
     }
   }
   double e1 = 0.0, wf = 0.0, e2 = 0.0, vtot = 0.0;
+  double inv_w = a.inv_w, dw_coef = a.dw_coef;
+  if (GRAD && a.res) {
+    const double W = a.res[4];
+    inv_w = 1.0 / W;
+    dw_coef = -a.res[1] / (W * W * (double)nelec);
+  }
   const long long stride = (long long)nsplit * blockDim.x;
   /* one-electron part (valence.F90:1072-1101) */
   for (long long t = (long long)split * blockDim.x + threadIdx.x; !DENS && t < (long long)nelec * nelec; t += stride) {
@@ -468,11 +474,11 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
     e1 += h * c.v;
     wf += s * c.v;
     if (GRAD) {
-      const double coef = h * a.inv_w + a.dw_coef * s;
+      const double coef = h * inv_w + dw_coef * s;
       vtot += coef * c.v;
       accum_G(d, q, qi, c, coef, Ga, Gb, lda, ldb);
-      atomicAdd(a.Hbar + si * nsp + sj, c.v * a.inv_w);
-      atomicAdd(a.Sbar + si * nsp + sj, c.v * a.dw_coef);
+      atomicAdd(a.Hbar + si * nsp + sj, c.v * inv_w);
+      atomicAdd(a.Sbar + si * nsp + sj, c.v * dw_coef);
     }
   }
   /* two-electron tasks (valence.F90:1153-1433) */
@@ -568,8 +574,8 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
               } else if (xs && cx_c.ok) {
                 cvx = xint;
               }
-              cve *= fac * a.inv_w;
-              cvx *= fac * a.inv_w;
+              cve *= fac * inv_w;
+              cvx *= fac * inv_w;
               if (ce_c.ok && cve != 0.0) {
                 vtot += cve * ce_c.v;
                 accum_G(d, q, qi, ce_c, cve, Ga, Gb, lda, ldb);
@@ -593,7 +599,7 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
       }
     }
     if (GRAD && !a.skip_tbar) {
-      const double ge = fac * a.inv_w * dsum_e, gx = -fac * a.inv_w * dsum_x;
+      const double ge = fac * inv_w * dsum_e, gx = -fac * inv_w * dsum_x;
       if (diag) {
         if (es || xs) atomicAdd(a.Tbar + (size_t)pik * np + pik, (es ? ge : 0.0) + (xs ? gx : 0.0));
       } else {

@@ -27,6 +27,7 @@ struct AsmArgs {
   int *status;
   /* adjoint pass */
   double inv_w, dw_coef;  /* 1/W and -E_num/(W^2 nelec) */
+  const double *res;      /* when set: read e_num = res[1], W = res[4] on the device instead */
   double *Tbar, *Sbar, *Hbar;
   double *vtot;            /* [nq * nsplit] */
   double *Gglob;           /* [nq][na*na + nb*nb] */

@@ -137,6 +137,11 @@ struct vsvb_gpu {
   static constexpr int NAUX = 6;  /* side streams for concurrent ERI class launches */
   cudaStream_t aux[NAUX] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[NAUX] = {};
+  /* CUDA graph of one energy + gradient evaluation (forward + adjoint),
+   * captured on the second call and replayed after that */
+  bool warm = false;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_launches = 0;
   /* in-situ timing of the class launches of the last sweep (optional) */
   bool sweep_timing = false;
   int sweep_mode = -1;
@@ -1126,17 +1131,9 @@ int forward(vsvb_gpu *h, bool fused = false) {
   return VSVB_OK;
 }
 
-int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
-  double r[5];
-  int status = 0;
-  CK(cudaMemcpyAsync(r, h->result.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, h->st), "copy result");
-  CK(cudaMemcpyAsync(&status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->st), "copy status");
-  CK(cudaStreamSynchronize(h->st), "sync");
-  if (status & 1) {
-    h->err = "an orbital has non-positive self-overlap";
-    return VSVB_ERR_NOT_NORMALISABLE;
-  }
-  if (out) {
+/* the result record of handle h from the device result r[0..4] */
+void fill_result(const vsvb_gpu *h, const double *r, vsvb_energy_result *out) {
+  {
     std::memset(out, 0, sizeof(*out));
     out->energy = r[0];
     out->e_num = r[1];
@@ -1160,10 +1157,26 @@ int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
     if (h->nq_fp32 > 0 && h->bound_all > 0.0 && r[4] != 0.0)
       out->err_est = std::ldexp(std::fabs(r[3] / r[4]) * (h->err_bound / h->bound_all), -30);
   }
+}
+
+int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
+  double r[5];
+  int status = 0;
+  CK(cudaMemcpyAsync(r, h->result.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, h->st), "copy result");
+  CK(cudaMemcpyAsync(&status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->st), "copy status");
+  CK(cudaStreamSynchronize(h->st), "sync");
+  if (status & 1) {
+    h->err = "an orbital has non-positive self-overlap";
+    return VSVB_ERR_NOT_NORMALISABLE;
+  }
+  if (out) fill_result(h, r, out);
   return VSVB_OK;
 }
 
-int backward(vsvb_gpu *h, double e_num, double w, bool fused) {
+/* adjoint pass; reads e_num and W from the forward pass's device result, so
+ * forward + backward enqueue without a host round trip (and can be captured
+ * into a CUDA graph) */
+int backward(vsvb_gpu *h, bool fused) {
   if (h->ndf > 0) {
     h->err = "gradient through derived basis functions is not implemented";
     return VSVB_ERR_UNSUPPORTED;
@@ -1184,8 +1197,7 @@ int backward(vsvb_gpu *h, double e_num, double w, bool fused) {
   DetCtx dc = det_ctx(h);
   AsmArgs aa = asm_args(h);
   aa.status = h->status.p;
-  aa.inv_w = 1.0 / w;
-  aa.dw_coef = -e_num / (w * w * (double)h->ds.nelec);
+  aa.res = h->result.p;
   aa.skip_tbar = fused ? 1 : 0;
   size_t gsh = aa.g_in_smem ? sizeof(double) * (size_t)(na * na + nb * nb) : 0;
   CK(launch_assemble(1, dim3((unsigned)h->ds.nq, h->nsplit), 128, gsh, st, dc, aa), "assemble grad");
@@ -1197,7 +1209,7 @@ int backward(vsvb_gpu *h, double e_num, double w, bool fused) {
   }
   if (h->nxelem > 0) {
     XtabArgs xa = xtab_args(h);
-    if (fused) xa.xbar_scale = 1.0 / w; /* the sweep used the unscaled densities */
+    if (fused) xa.wres = h->result.p; /* the sweep used the unscaled densities: scale by 1/W */
     xhrr_adjoint_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa, h->xbarh.p, h->xbar.p);
     CK(cudaGetLastError(), "xhrr adjoint");
     xtab_adjoint_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa, h->xbar.p, h->Cbar.p);
@@ -1227,6 +1239,7 @@ void vsvb_default_options(vsvb_options *o) {
   o->grad_mode = 0;
   o->prim_screen = 1e-17;
   o->prim_split = 1;
+  o->cuda_graph = 1;
 }
 
 int vsvb_gpu_create(const vsvb_system_desc *d, const vsvb_options *opt, vsvb_gpu **out) {
@@ -1251,6 +1264,7 @@ void vsvb_gpu_destroy(vsvb_gpu *h) {
     if (h->ev_join[k]) cudaEventDestroy(h->ev_join[k]);
   }
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
   for (cudaEvent_t e : h->sweep_ev) cudaEventDestroy(e);
   if (h->sweep_t0) cudaEventDestroy(h->sweep_t0);
   if (h->sweep_t1) cudaEventDestroy(h->sweep_t1);
@@ -1282,28 +1296,65 @@ int vsvb_gpu_energy(vsvb_gpu *h, const double *coeff, vsvb_energy_result *out) {
   return finish_result(h, out);
 }
 
+/* forward + adjoint on h->st: eagerly, or as a replay of the captured CUDA
+ * graph of the same sequence.  The first call runs eagerly (it allocates the
+ * adjoint buffers and sets kernel attributes); the second captures and
+ * replays.  A failed capture falls back to eager launches for good. */
+static int enqueue_eval(vsvb_gpu *h, bool fused) {
+  const bool graph = h->opt.cuda_graph && !h->sweep_timing && h->warm;
+  if (graph && !h->gexec) {
+    if (cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      int rc = forward(h, fused);
+      const int nl = h->launches;
+      if (!rc) rc = backward(h, fused);
+      h->graph_launches = nl + h->launches;
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(h->st, &g);
+      if (rc == 0 && e == cudaSuccess && g && cudaGraphInstantiate(&h->gexec, g, 0) == cudaSuccess) {
+        cudaGraphDestroy(g);
+      } else {
+        if (g) cudaGraphDestroy(g);
+        h->gexec = nullptr;
+        h->opt.cuda_graph = 0;
+        (void)cudaGetLastError();
+        if (rc) return rc;
+      }
+    } else {
+      (void)cudaGetLastError();
+      h->opt.cuda_graph = 0;
+    }
+  }
+  if (graph && h->gexec) {
+    CK(cudaGraphLaunch(h->gexec, h->st), "graph launch");
+    h->launches = h->graph_launches;
+    return VSVB_OK;
+  }
+  int rc = forward(h, fused);
+  if (rc) return rc;
+  const int nl = h->launches;
+  rc = backward(h, fused);
+  h->launches += nl;
+  if (rc) return rc;
+  h->warm = true;
+  return VSVB_OK;
+}
+
 static int energy_grad_common(vsvb_gpu *h, vsvb_energy_result *out, double *grad, bool grad_on_device) {
   const bool fused = h->opt.grad_mode == 0;
   if (h->ndf > 0) {
     h->err = "gradient through derived basis functions is not implemented";
     return VSVB_ERR_UNSUPPORTED;
   }
-  int rc = forward(h, fused);
+  int rc = enqueue_eval(h, fused);
   if (rc) return rc;
-  int nl = h->launches;
-  vsvb_energy_result r;
-  rc = finish_result(h, &r);
-  if (rc) return rc;
-  rc = backward(h, r.e_num, r.wfnorm, fused);
-  h->launches += nl;
-  if (rc) return rc;
-  int status = 0;
-  r.n_kernel_launches = h->launches;
-  CK(cudaMemcpyAsync(&status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->st), "status");
   CK(cudaMemcpyAsync(grad, h->coeff_bar.p, sizeof(double) * h->totlen,
                      grad_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->st),
      "copy grad");
-  CK(cudaStreamSynchronize(h->st), "sync");
+  vsvb_energy_result r;
+  rc = finish_result(h, &r); /* copies the result and status, one stream sync */
+  if (rc) return rc;
+  int status = 0;
+  CK(cudaMemcpy(&status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost), "status");
   if (status & 2) {
     h->err = "gradient through a singular determinant pair is not implemented";
     return VSVB_ERR_SINGULAR;
@@ -1335,6 +1386,183 @@ int vsvb_gpu_batch_energy_grad(vsvb_gpu *const *hs, int n, const double *const *
     if (rc) return rc;
   }
   return VSVB_OK;
+}
+
+}  // extern "C"
+
+/* ---------------- batched evaluation as one CUDA graph ---------------- */
+
+struct vsvb_batch {
+  std::vector<vsvb_gpu *> hs;
+  int dev = 0;
+  std::string err;
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<const double *> w; /* pointers the graph was captured with */
+  std::vector<double *> g;
+  DBuf<double> res; /* [n][5] */
+  DBuf<int> stat;   /* [n] */
+  int launches = 0;
+};
+
+namespace {
+
+int batch_fail(vsvb_batch *b, cudaError_t e, const char *what) {
+  b->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return VSVB_ERR_CUDA;
+}
+#define BCK(call, what)                                \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return batch_fail(b, e_, what); \
+  } while (0)
+
+/* capture every handle's evaluation (copy weights in, forward + adjoint,
+ * copy gradient and result out) as one graph, each handle on its own stream
+ * forked from and joined into the batch stream */
+int batch_capture(vsvb_batch *b, const double *const *w, double *const *g) {
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  const int n = (int)b->hs.size();
+  BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal), "begin capture");
+  BCK(cudaEventRecord(b->fork, b->st), "event record");
+  int rc = VSVB_OK, launches = 0;
+  for (int i = 0; i < n && !rc; ++i) {
+    vsvb_gpu *h = b->hs[i];
+    cudaStream_t saved = h->st;
+    h->st = h->own_st;
+    const bool fused = h->opt.grad_mode == 0;
+    if (cudaStreamWaitEvent(h->st, b->fork, 0) != cudaSuccess ||
+        cudaMemcpyAsync(h->coeff_d.p, w[i], sizeof(double) * h->totlen, cudaMemcpyDeviceToDevice, h->st) != cudaSuccess)
+      rc = VSVB_ERR_CUDA;
+    if (!rc) rc = forward(h, fused);
+    const int nl = h->launches;
+    if (!rc) rc = backward(h, fused);
+    launches += nl + h->launches;
+    if (!rc && (cudaMemcpyAsync(g[i], h->coeff_bar.p, sizeof(double) * h->totlen, cudaMemcpyDeviceToDevice,
+                                h->st) != cudaSuccess ||
+                cudaMemcpyAsync(b->res.p + 5 * i, h->result.p, sizeof(double) * 5, cudaMemcpyDeviceToDevice,
+                                h->st) != cudaSuccess ||
+                cudaMemcpyAsync(b->stat.p + i, h->status.p, sizeof(int), cudaMemcpyDeviceToDevice, h->st) != cudaSuccess ||
+                cudaEventRecord(b->join[i], h->st) != cudaSuccess ||
+                cudaStreamWaitEvent(b->st, b->join[i], 0) != cudaSuccess))
+      rc = VSVB_ERR_CUDA;
+    if (rc && h->err.size()) b->err = "molecule " + std::to_string(i) + ": " + h->err;
+    h->st = saved;
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(b->st, &graph);
+  if (rc || e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    (void)cudaGetLastError();
+    if (b->err.empty()) b->err = "batch capture failed";
+    return rc ? rc : VSVB_ERR_CUDA;
+  }
+  const cudaError_t ei = cudaGraphInstantiate(&b->exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) {
+    b->exec = nullptr;
+    return batch_fail(b, ei, "graph instantiate");
+  }
+  b->w.assign(w, w + n);
+  b->g.assign(g, g + n);
+  b->launches = launches;
+  return VSVB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vsvb_batch_create(vsvb_gpu *const *handles, int n, vsvb_batch **out) {
+  if (!handles || n < 1 || !out) return VSVB_ERR_INPUT;
+  *out = nullptr;
+  auto *b = new vsvb_batch();
+  b->dev = handles[0]->dev;
+  for (int i = 0; i < n; ++i) {
+    vsvb_gpu *h = handles[i];
+    if (!h || h->dev != b->dev || h->ndf > 0) {
+      delete b;
+      return VSVB_ERR_INPUT;
+    }
+    b->hs.push_back(h);
+  }
+  *out = b;
+  BCK(cudaSetDevice(b->dev), "cudaSetDevice");
+  BCK(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking), "cudaStreamCreate");
+  BCK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "cudaEventCreate");
+  b->join.assign(n, nullptr);
+  for (int i = 0; i < n; ++i) BCK(cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming), "cudaEventCreate");
+  BCK(b->res.alloc((size_t)5 * n), "alloc results");
+  BCK(b->stat.alloc((size_t)n), "alloc status");
+  /* one eager evaluation per handle: allocates its adjoint buffers and sets
+   * kernel attributes, neither of which may happen inside a capture */
+  std::vector<double> grad;
+  for (vsvb_gpu *h : b->hs) {
+    if (h->warm) continue;
+    grad.assign(h->totlen, 0.0);
+    int rc = vsvb_gpu_energy_grad(h, nullptr, nullptr, grad.data());
+    if (rc) {
+      b->err = "warm-up: " + h->err;
+      return rc;
+    }
+  }
+  return VSVB_OK;
+}
+
+int vsvb_batch_energy_grad(vsvb_batch *b, const double *const *weights_dev, double *const *grads_dev,
+                           vsvb_energy_result *results, void *stream) {
+  if (!b || !weights_dev || !grads_dev) return VSVB_ERR_INPUT;
+  const int n = (int)b->hs.size();
+  BCK(cudaSetDevice(b->dev), "cudaSetDevice");
+  bool same = b->exec && (int)b->w.size() == n;
+  for (int i = 0; same && i < n; ++i) same = b->w[i] == weights_dev[i] && b->g[i] == grads_dev[i];
+  if (!same) {
+    int rc = batch_capture(b, weights_dev, grads_dev);
+    if (rc) return rc;
+  }
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->st;
+  BCK(cudaGraphLaunch(b->exec, st), "graph launch");
+  std::vector<double> r((size_t)5 * n);
+  std::vector<int> stat(n);
+  BCK(cudaMemcpyAsync(r.data(), b->res.p, sizeof(double) * r.size(), cudaMemcpyDeviceToHost, st), "copy results");
+  BCK(cudaMemcpyAsync(stat.data(), b->stat.p, sizeof(int) * n, cudaMemcpyDeviceToHost, st), "copy status");
+  BCK(cudaStreamSynchronize(st), "sync");
+  for (int i = 0; i < n; ++i) {
+    if (stat[i] & 1) {
+      b->err = "molecule " + std::to_string(i) + ": an orbital has non-positive self-overlap";
+      return VSVB_ERR_NOT_NORMALISABLE;
+    }
+    if (stat[i] & 2) {
+      b->err = "molecule " + std::to_string(i) + ": gradient through a singular determinant pair";
+      return VSVB_ERR_SINGULAR;
+    }
+    if (results) {
+      fill_result(b->hs[i], r.data() + 5 * i, &results[i]);
+      results[i].n_kernel_launches = b->launches;
+    }
+  }
+  return VSVB_OK;
+}
+
+int vsvb_batch_launches(const vsvb_batch *b) { return b ? b->launches : -1; }
+
+const char *vsvb_batch_last_error(const vsvb_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+void vsvb_batch_destroy(vsvb_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->dev);
+  if (b->st) cudaStreamSynchronize(b->st);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (cudaEvent_t e : b->join)
+    if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
 }
 
 int vsvb_gpu_set_stream(vsvb_gpu *h, void *stream) {

@@ -349,7 +349,8 @@ __global__ void xtab_adjoint_kernel(XtabArgs x, const double *xbar, double *Cbar
   int na = ncart(tm.la), nb = ncart(tm.lb);
   int ia = e / nb, ib = e - ia * nb;
   const double *ci = x.C + (size_t)tm.oi * x.maxobs, *ck = x.C + (size_t)tm.ok * x.maxobs;
-  double g = xbar[t] * x.xbar_scale * x.angn[tm.aoA + ia] * x.angn[tm.aoB + ib];
+  const double scale = x.wres ? x.xbar_scale / x.wres[4] : x.xbar_scale;
+  double g = xbar[t] * scale * x.angn[tm.aoA + ia] * x.angn[tm.aoB + ib];
   if (g == 0.0) return;
   auto kept = [&](const double *c, int s0, int n) -> bool { return s0 >= 0 && shell_kept(c, s0, n, x.dtol); };
   double *gi = Cbar + (size_t)tm.oi * x.maxobs, *gk = Cbar + (size_t)tm.ok * x.maxobs;

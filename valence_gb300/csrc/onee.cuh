@@ -51,6 +51,7 @@ struct XtabArgs {
   double dtol;
   double *xtab;
   double xbar_scale; /* adjoint: factor applied to dE/dX */
+  const double *wres; /* when set: the factor is xbar_scale / wres[4] (W read on the device) */
   /* horizontal transfer folded into the weights: X'(op, e) = sum_ab X(op, ab) M(ab, e) */
   const long long *xh_elem0; /* first X' element of each term */
   long long nxh;
