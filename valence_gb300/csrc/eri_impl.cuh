@@ -267,7 +267,7 @@ constexpr int ne_c(int la, int lb) {
  * A, k <= LCD on the ket centre C, by the Rys recurrences.  The horizontal
  * transfers to the second centres are not done here: they are folded into
  * the weight tables (X' = X M), so the components contracted are (e0|f0). */
-template <int LAB, int LCD, typename R>
+template <int LAB, int LCD, typename R, int STRIDE>
 __device__ __forceinline__ void rys_g(R g00, R c00, R d00, R b00, R b10, R b01, R *__restrict__ out) {
   R G[LAB + 1][LCD + 1];
   G[0][0] = g00;
@@ -286,7 +286,40 @@ __device__ __forceinline__ void rys_g(R g00, R c00, R d00, R b00, R b10, R b01, 
 #pragma unroll
   for (int i = 0; i <= LAB; ++i)
 #pragma unroll
-    for (int k = 0; k <= LCD; ++k) out[i * (LCD + 1) + k] = G[i][k];
+    for (int k = 0; k <= LCD; ++k) out[(i * (LCD + 1) + k) * STRIDE] = G[i][k];
+}
+
+/* vector load of V consecutive table entries (V * sizeof(R) bytes, aligned) */
+template <int V>
+__device__ __forceinline__ void ldv(const float *p, float (&o)[V]) {
+  if constexpr (V == 4) {
+    const float4 f = *reinterpret_cast<const float4 *>(p);
+    o[0] = f.x; o[1] = f.y; o[2] = f.z; o[3] = f.w;
+  } else if constexpr (V == 2) {
+    const float2 f = *reinterpret_cast<const float2 *>(p);
+    o[0] = f.x; o[1] = f.y;
+  } else {
+    o[0] = *p;
+  }
+}
+template <int V>
+__device__ __forceinline__ void ldv(const double *p, double (&o)[V]) {
+  if constexpr (V == 2) {
+    const double2 f = *reinterpret_cast<const double2 *>(p);
+    o[0] = f.x; o[1] = f.y;
+  } else {
+    o[0] = *p;
+  }
+}
+template <int V>
+__device__ __forceinline__ void ldv(const df64 *p, df64 (&o)[V]) {
+  if constexpr (V == 2) {
+    const float4 f = *reinterpret_cast<const float4 *>(p);
+    o[0] = df64(f.x, f.y);
+    o[1] = df64(f.z, f.w);
+  } else {
+    o[0] = *p;
+  }
 }
 
 constexpr int WARPS = 4;
@@ -314,13 +347,21 @@ struct QuartetShape {
   static constexpr int PER_LANE = (NITEM + 31) / 32;
   static constexpr int JCH = 8; /* ket orbital pairs per transform chunk */
   static constexpr int NMAX = NEA > NEC ? NEA : NEC;
-  static constexpr int SM_2D = (G2 * 3 * NR * N2D * RB + 7) / 8; /* per warp, in doubles */
+  /* 2D tables are stored root-innermost, [slot][dir][entry][root], each
+   * entry padded to NRP roots so that VEC roots load as one 8/16-byte
+   * vector: NGF full vector groups and REM roots loaded one by one */
+  static constexpr int VEC = RB == 4 ? (NR >= 4 ? 4 : (NR >= 2 ? 2 : 1)) : (NR >= 2 ? 2 : 1);
+  static constexpr int NRP = (NR + VEC - 1) / VEC * VEC;
+  static constexpr int NGF = NR / VEC, REM = NR % VEC;
+  static constexpr int SM_2D = (G2 * 3 * N2D * NRP * RB + 15) / 16 * 2; /* per warp, in doubles (16-byte multiple) */
   /* per warp: roots, weights, 1/(p+q) of 32 primitive quartets, and their indices */
-  static constexpr int SM_ROOT = ((2 * 32 * NR + 32) * RB + 7) / 8 + 16;
+  static constexpr int SM_ROOT = (((2 * 32 * NR + 32) * RB + 7) / 8 + 16 + 1) / 2 * 2;
+  static constexpr int IDXD = (((NCOMP + 1) / 2 + 1) + 1) / 2 * 2; /* component index table, doubles */
   /* staging: E[NCOMP] + max(slot buffer, transform chunk); per warp in warp
    * mode, one per CTA in CTA mode */
   static constexpr int SM_TR = NCOMP + (NITEM > JCH * NMAX ? NITEM : JCH * NMAX);
-  static constexpr int PER_WARP = CTA ? SM_2D + SM_ROOT : (SM_2D + SM_ROOT > SM_TR ? SM_2D + SM_ROOT : SM_TR);
+  static constexpr int PER_WARP0 = CTA ? SM_2D + SM_ROOT : (SM_2D + SM_ROOT > SM_TR ? SM_2D + SM_ROOT : SM_TR);
+  static constexpr int PER_WARP = (PER_WARP0 + 1) / 2 * 2;
   static constexpr int SHARED = CTA ? SM_TR : 0;
   /* CTA mode stages each warp's partial block in that warp's table area */
   static_assert(!CTA || PER_WARP * 8 >= NCOMP * (RB == 4 ? 4 : 8), "per-warp area too small for the partial block");
@@ -339,7 +380,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   constexpr bool DFROOT = !std::is_same<R, double>::value;
   extern __shared__ double smem[];
   int *idx = reinterpret_cast<int *>(smem);
-  double *wbase = smem + (S::NCOMP + 1) / 2 + 1;
+  double *wbase = smem + S::IDXD;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double *ws = wbase + (size_t)warp * S::PER_WARP;
   /* staging area: per warp (warp mode) or shared by the CTA */
@@ -506,23 +547,46 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
           const R c00 = (Pd - Ad) - qr.p * uq * PQ;
           const R d00 = (Qd - Cd) + pr.p * uq * PQ;
           const R g00 = dir == 2 ? wR : R(1);
-          rys_g<S::LAB, S::LCD, R>(g00, c00, d00, b00, b10, b01, h2d + (size_t)((g * 3 + dir) * S::NR + r) * S::N2D);
+          rys_g<S::LAB, S::LCD, R, S::NRP>(g00, c00, d00, b00, b10, b01,
+                                           h2d + (size_t)(g * 3 + dir) * S::N2D * S::NRP + r);
         }
         __syncwarp();
         const int nact = min(S::G2, nch - sub);
+        constexpr int DS = S::N2D * S::NRP; /* one direction's table */
         if constexpr (CTA) {
-          /* one (slot, root) table set at a time, so that the unrolled body
-           * covers only the lane's components (instruction-cache footprint) */
+          /* one (slot, root group) at a time, so that the unrolled body covers
+           * only the lane's components (instruction-cache footprint) */
 #pragma unroll 1
-          for (int t = 0; t < nact * S::NR; ++t) {
-            const R *hx = h2d + (size_t)((t / S::NR) * 3 * S::NR + t % S::NR) * S::N2D;
-            const R *hy = hx + S::NR * S::N2D, *hz = hy + S::NR * S::N2D;
+          for (int t = 0; t < nact * S::NGF; ++t) {
+            const int gg = t / S::NGF, rg = t - gg * S::NGF;
+            const R *hx = h2d + (size_t)gg * 3 * DS + rg * S::VEC;
 #pragma unroll
             for (int m = 0; m < S::PER_LANE; ++m) {
               const int c = lane + 32 * m;
               if (c < S::NCOMP) {
                 const int id = idx[c];
-                acc3(acc[m], hx[id & 1023], hy[(id >> 10) & 1023], hz[id >> 20]);
+                R x[S::VEC], y[S::VEC], z[S::VEC];
+                ldv<S::VEC>(hx + (id & 1023) * S::NRP, x);
+                ldv<S::VEC>(hx + DS + ((id >> 10) & 1023) * S::NRP, y);
+                ldv<S::VEC>(hx + 2 * DS + (id >> 20) * S::NRP, z);
+#pragma unroll
+                for (int v = 0; v < S::VEC; ++v) acc3(acc[m], x[v], y[v], z[v]);
+              }
+            }
+          }
+          if constexpr (S::REM > 0) {
+#pragma unroll 1
+            for (int t = 0; t < nact * S::REM; ++t) {
+              const int gg = t / S::REM, rr = S::NGF * S::VEC + (t - gg * S::REM);
+              const R *hx = h2d + (size_t)gg * 3 * DS + rr;
+#pragma unroll
+              for (int m = 0; m < S::PER_LANE; ++m) {
+                const int c = lane + 32 * m;
+                if (c < S::NCOMP) {
+                  const int id = idx[c];
+                  acc3(acc[m], hx[(id & 1023) * S::NRP], hx[DS + ((id >> 10) & 1023) * S::NRP],
+                       hx[2 * DS + (id >> 20) * S::NRP]);
+                }
               }
             }
           }
@@ -534,13 +598,21 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
             const int gg = it / S::NCOMP, c = it - gg * S::NCOMP;
             if (gg < nact) {
               const int id = idx[c];
-              const int ix = id & 1023, iy = (id >> 10) & 1023, iz = id >> 20;
-              const R *hx = h2d + (size_t)(gg * 3 + 0) * S::NR * S::N2D;
-              const R *hy = hx + S::NR * S::N2D, *hz = hy + S::NR * S::N2D;
+              const R *hx = h2d + (size_t)gg * 3 * DS + (id & 1023) * S::NRP;
+              const R *hy = h2d + (size_t)gg * 3 * DS + DS + ((id >> 10) & 1023) * S::NRP;
+              const R *hz = h2d + (size_t)gg * 3 * DS + 2 * DS + (id >> 20) * S::NRP;
               R sacc = acc[m];
 #pragma unroll
-              for (int rr = 0; rr < S::NR; ++rr)
-                acc3(sacc, hx[rr * S::N2D + ix], hy[rr * S::N2D + iy], hz[rr * S::N2D + iz]);
+              for (int rg = 0; rg < S::NGF; ++rg) {
+                R x[S::VEC], y[S::VEC], z[S::VEC];
+                ldv<S::VEC>(hx + rg * S::VEC, x);
+                ldv<S::VEC>(hy + rg * S::VEC, y);
+                ldv<S::VEC>(hz + rg * S::VEC, z);
+#pragma unroll
+                for (int v = 0; v < S::VEC; ++v) acc3(sacc, x[v], y[v], z[v]);
+              }
+#pragma unroll
+              for (int rr = S::NGF * S::VEC; rr < S::NR; ++rr) acc3(sacc, hx[rr], hy[rr], hz[rr]);
               acc[m] = sacc;
             }
           }
@@ -746,7 +818,7 @@ template <int LA, int LB, int LC, int LD, typename R, int MODE>
 int launch_one(const EriArgs &args, const int2 *work, int nwork, int nsm, cudaStream_t st) {
   if (nwork <= 0) return 0;
   using S = QuartetShape<LA, LB, LC, LD, sizeof(R)>;
-  size_t shm = sizeof(double) * ((S::NCOMP + 1) / 2 + 1 + (size_t)WARPS * S::PER_WARP + S::SHARED);
+  size_t shm = sizeof(double) * (S::IDXD + (size_t)WARPS * S::PER_WARP + S::SHARED);
   auto kfn = eri_kernel<LA, LB, LC, LD, R, MODE>;
   static bool attr_done = false;
   if (!attr_done) {
