@@ -102,6 +102,8 @@ typedef struct vsvb_options {
                            * FP32 (default 1; 0 keeps whole shell quartets in one arithmetic) */
   int cuda_graph;         /* energy + gradient calls replay one captured CUDA graph of the
                            * whole evaluation from the second call on (default 1) */
+  int autotune;           /* pick the ERI grid caps and assembly task splits by timing them on
+                           * this device at create (default 0: fixed heuristics) */
 } vsvb_options;
 
 typedef struct vsvb_energy_result {
@@ -210,6 +212,12 @@ int vsvb_gpu_eri_profile_mode(vsvb_gpu *h, int mode, double *ms, double *flops, 
  * when timing is off) or a negative status. */
 int vsvb_gpu_set_sweep_timing(vsvb_gpu *h, int on);
 int vsvb_gpu_sweep_times(vsvb_gpu *h, double *ms, double *flops, int *cls, int cap);
+/* The launch geometry in use (after the autotuner, if enabled): the
+ * assembly task splits per determinant pair, and per ERI launch of the
+ * sweep (up to cap) its class code and grid cap in blocks per SM.  Returns
+ * the number of ERI launches written. */
+int vsvb_gpu_launch_config(const vsvb_gpu *h, int *nsplit, int *codes, int *blocks_per_sm, int cap);
+
 /* Wall time of the last ERI sweep (fork to join on the handle's stream) in
  * *ms; 0 when timing is off. */
 int vsvb_gpu_sweep_wall_ms(vsvb_gpu *h, double *ms);

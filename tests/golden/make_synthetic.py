@@ -1,0 +1,40 @@
+"""Regenerate tests/golden/synthetic.json: CPU-oracle energies of the seeded
+synthetic workloads (valence_gb300.configs), used as fixtures by the GPU
+parity tests.  Run from the repository root:
+
+    python tests/golden/make_synthetic.py
+"""
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from valence_gb300 import configs  # noqa: E402
+
+CASES = {"ch_chain": dict(fn=configs.ch_chain, seed=2), "lif_cluster_small": dict(fn=configs.lif_cluster_small, seed=3)}
+
+
+def main():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    exe = os.path.join(ROOT, "oracle", "_build", "vsvb_oracle")
+    nthreads = os.cpu_count() or 1
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        for name, c in CASES.items():
+            path = c["fn"](os.path.join(d, name + ".inp"), seed=c["seed"])
+            txt = subprocess.run([exe, path, str(nthreads)], capture_output=True, text=True, check=True).stdout
+            e = float([ln for ln in txt.splitlines() if "guess energy" in ln][0].split()[2])
+            f = [ln for ln in txt.splitlines() if ln.strip().startswith("e1")][0].split()
+            out[name] = {"seed": c["seed"], "energy": e, "wfnorm": float(f[5]), "e1": float(f[1]), "e2": float(f[3]),
+                         "source": f"oracle/_build/vsvb_oracle on valence_gb300.configs.{c['fn'].__name__}"
+                                   f"(seed={c['seed']}), {nthreads} threads"}
+    with open(os.path.join(ROOT, "tests", "golden", "synthetic.json"), "w") as fh:
+        json.dump(out, fh, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -76,3 +76,16 @@ def test_batch_matches_individual(vg, tmp_path, precision):
     r0, g0 = systems[0].energy_grad(ws[0].cpu().numpy())
     assert abs(res[0]["energy"] - r0["energy"]) < 1e-9 * max(1.0, abs(r0["energy"]))
     b.close()
+
+
+def test_autotune_changes_geometry_not_results(vg, tmp_path):
+    from valence_gb300 import configs
+    p = configs.ch_chain(str(tmp_path / "chain.inp"))
+    r0, g0 = vg.System(p, precision=vg.MIXED_DF64).energy_grad()
+    s = vg.System(p, precision=vg.MIXED_DF64, autotune=1)
+    cfg = s.launch_config()
+    assert cfg["nsplit"] >= 1 and cfg["eri"]
+    assert all(b in (2, 4, 8, 16) for _, b in cfg["eri"])
+    r1, g1 = s.energy_grad()
+    assert abs(r1["energy"] - r0["energy"]) < 1e-9
+    assert np.max(np.abs(g1 - g0)) < 1e-9

@@ -110,6 +110,26 @@ def test_synthetic_chain_matches_fixture(lib_built):
     assert abs(r["wfnorm"] - fx["wfnorm"]) < 1e-10 * max(1.0, abs(fx["wfnorm"]))
 
 
+@pytest.mark.parametrize("precision", ["FP64", "MIXED", "MIXED_DF64"])
+def test_synthetic_cluster_matches_fixture(lib_built, tmp_path, precision):
+    """The Li/F cluster workload's geometry and basis family at 2x2x2 (72
+    functions, 12 DOCC, wfnorm 0.16) against the oracle fixture: FP64 within
+    1e-8 relative, the mixed paths within 1e-6 Eh and their own estimate."""
+    import json
+    from valence_gb300 import configs
+    fx = json.load(open(os.path.join(GOLD, "synthetic.json")))["lif_cluster_small"]
+    p = configs.lif_cluster_small(str(tmp_path / "lif.inp"), seed=fx["seed"])
+    s = lib_built.System(p, precision=getattr(lib_built, precision))
+    r = s.energy()
+    d = abs(r["energy"] - fx["energy"])
+    if precision == "FP64":
+        assert d < 1e-8 * max(1.0, abs(fx["energy"]))
+        assert abs(r["wfnorm"] - fx["wfnorm"]) < 1e-10
+    else:
+        assert d < 1e-6, d
+        assert d <= r["err_est"] + 1e-8 * abs(fx["energy"]), (d, r["err_est"])
+
+
 def test_energy_is_repeatable(lib_built):
     s = lib_built.System(os.path.join(GOLD, "cases", "examples", "h2o"))
     a = s.energy()["energy"]

@@ -49,7 +49,7 @@ class Desc(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("mixed_threshold", ctypes.c_double), ("ao_screen", ctypes.c_double),
                 ("device", ctypes.c_int), ("grad_mode", ctypes.c_int), ("prim_screen", ctypes.c_double),
-                ("prim_split", ctypes.c_int), ("cuda_graph", ctypes.c_int)]
+                ("prim_split", ctypes.c_int), ("cuda_graph", ctypes.c_int), ("autotune", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -94,6 +94,7 @@ def lib():
         L.vsvb_gpu_set_sweep_timing.argtypes = [ctypes.c_void_p, I]
         L.vsvb_gpu_sweep_times.argtypes = [ctypes.c_void_p, P(D), P(D), P(I), I]
         L.vsvb_gpu_sweep_wall_ms.argtypes = [ctypes.c_void_p, P(D)]
+        L.vsvb_gpu_launch_config.argtypes = [ctypes.c_void_p, P(I), P(I), P(I), I]
         L.vsvb_gpu_fma_peak.argtypes = [I, P(D), P(D)]
         L.vsvb_det_factor.argtypes = [ctypes.c_void_p, I, I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_void_p]
@@ -124,7 +125,7 @@ def read_input(path):
 
 
 def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, grad_mode=0, prim_screen=None,
-                 prim_split=None, cuda_graph=None):
+                 prim_split=None, cuda_graph=None, autotune=None):
     o = Options()
     lib().vsvb_default_options(ctypes.byref(o))
     o.precision = precision
@@ -138,6 +139,8 @@ def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0
         o.prim_split = int(prim_split)
     if cuda_graph is not None:
         o.cuda_graph = int(cuda_graph)
+    if autotune is not None:
+        o.autotune = int(autotune)
     return o
 
 
@@ -145,7 +148,7 @@ class System:
     """One molecule on the GPU: a parsed input plus a device handle."""
 
     def __init__(self, path, precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, coords_angstrom=None,
-                 grad_mode=0, prim_screen=None, prim_split=None, cuda_graph=None):
+                 grad_mode=0, prim_screen=None, prim_split=None, cuda_graph=None, autotune=None):
         self.path = path
         self._desc = read_input(path)
         d = self._desc.contents
@@ -156,7 +159,7 @@ class System:
         if coords_angstrom is not None:
             self._coords_bohr[:] = np.asarray(coords_angstrom, dtype=np.float64).ravel() * 1.889725987722
         self.opt = make_options(precision, mixed_threshold, ao_screen, device, grad_mode, prim_screen, prim_split,
-                                cuda_graph)
+                                cuda_graph, autotune)
         self._h = ctypes.c_void_p()
         rc = lib().vsvb_gpu_create(self._desc, ctypes.byref(self.opt), ctypes.byref(self._h))
         if rc:
@@ -240,6 +243,16 @@ class System:
         if n < 0:
             raise VSVBError("sweep_times failed")
         return [dict(cls=int(cl[i]), ms=float(ms[i]), flops=float(fl[i])) for i in range(n)]
+
+    def launch_config(self, cap=256):
+        """Launch geometry in use: {"nsplit": task splits, "eri": [(class code, blocks per SM)]}."""
+        ns = ctypes.c_int()
+        codes = (ctypes.c_int * cap)()
+        bps = (ctypes.c_int * cap)()
+        k = lib().vsvb_gpu_launch_config(self._h, ctypes.byref(ns), codes, bps, cap)
+        if k < 0:
+            raise VSVBError("launch_config failed")
+        return {"nsplit": ns.value, "eri": [(codes[i], bps[i]) for i in range(k)]}
 
     def sweep_wall_ms(self):
         """Wall time (ms) of the last ERI sweep, fork to join."""

@@ -166,4 +166,11 @@ def batch_molecules(dirpath, n=256, seed0=1000):
     return [random_molecule(os.path.join(dirpath, f"mol{seed0 + i:05d}.inp"), seed0 + i) for i in range(n)]
 
 
-WORKLOADS = {"water_vshf": water_vshf, "ch_chain": ch_chain, "lif_cluster": lif_cluster}
+def lif_cluster_small(path, seed=3):
+    """The cluster workload's geometry and basis family at 2x2x2 (8 atoms, 72
+    functions, 12 DOCC): a size the CPU oracle evaluates in seconds."""
+    return lif_cluster(path, seed=seed, n=2, ndocc=12)
+
+
+WORKLOADS = {"water_vshf": water_vshf, "ch_chain": ch_chain, "lif_cluster": lif_cluster,
+             "lif_cluster_small": lif_cluster_small}

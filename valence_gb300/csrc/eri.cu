@@ -102,11 +102,11 @@ double eri_flops(int mode, int cp, int cq, double nprimq, int nopP, int nopQ) {
   return nprimq * prim + tr;
 }
 
-int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int nsm,
+int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int max_blocks,
                cudaStream_t st) {
   /* the Schwarz pass and the separate adjoint sweep (grad_mode 1) always run
    * in FP64; the FP32 / double-float kinds instantiate modes 0 and 3 only */
-  if (mode == 1 || mode == 2 || kind == ERI_F64) return eri_dispatch_f64(mode, cp, cq, a, work, nwork, nsm, st);
-  if (kind == ERI_F32) return eri_dispatch_f32(mode, cp, cq, a, work, nwork, nsm, st);
-  return eri_dispatch_df64(mode, cp, cq, a, work, nwork, nsm, st);
+  if (mode == 1 || mode == 2 || kind == ERI_F64) return eri_dispatch_f64(mode, cp, cq, a, work, nwork, max_blocks, st);
+  if (kind == ERI_F32) return eri_dispatch_f32(mode, cp, cq, a, work, nwork, max_blocks, st);
+  return eri_dispatch_df64(mode, cp, cq, a, work, nwork, max_blocks, st);
 }

@@ -39,12 +39,14 @@ struct EriArgs {
 enum { ERI_F64 = 0, ERI_F32 = 1, ERI_DF64 = 2 };
 
 /* cp >= cq are pair classes 0..5; mode 0 forward, 1 Schwarz (F64 only),
- * 2 adjoint, 3 forward + adjoint. */
-int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int nsm,
+ * 2 adjoint, 3 forward + adjoint.  max_blocks caps the grid (the blocks then
+ * stride over the work list). */
+int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int max_blocks,
                cudaStream_t st);
-int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
-int eri_dispatch_f32(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
-int eri_dispatch_df64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st);
+int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int max_blocks, cudaStream_t st);
+int eri_dispatch_f32(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int max_blocks, cudaStream_t st);
+int eri_dispatch_df64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int max_blocks,
+                      cudaStream_t st);
 double eri_flops(int mode, int cp, int cq, double nprimq, int nopP, int nopQ);
 int eri_symmetrize(double *T, int np, double *sq, cudaStream_t st);
 /* out[i] = (float)in[i] */

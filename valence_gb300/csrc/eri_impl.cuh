@@ -815,7 +815,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
 }
 
 template <int LA, int LB, int LC, int LD, typename R, int MODE>
-int launch_one(const EriArgs &args, const int2 *work, int nwork, int nsm, cudaStream_t st) {
+int launch_one(const EriArgs &args, const int2 *work, int nwork, int max_blocks, cudaStream_t st) {
   if (nwork <= 0) return 0;
   using S = QuartetShape<LA, LB, LC, LD, sizeof(R)>;
   size_t shm = sizeof(double) * (S::IDXD + (size_t)WARPS * S::PER_WARP + S::SHARED);
@@ -827,8 +827,7 @@ int launch_one(const EriArgs &args, const int2 *work, int nwork, int nsm, cudaSt
   }
   const int per_block = S::CTA ? 1 : WARPS;
   int blocks = (nwork + per_block - 1) / per_block;
-  int cap = nsm * 16;
-  if (blocks > cap) blocks = cap;
+  if (blocks > max_blocks) blocks = max_blocks; /* grid-stride beyond this */
   kfn<<<blocks, WARPS * 32, shm, st>>>(args, work, nwork);
   return cudaGetLastError() != cudaSuccess;
 }
@@ -844,14 +843,14 @@ template <> struct ClsL<4> { static constexpr int a = 2, b = 1; };
 template <> struct ClsL<5> { static constexpr int a = 2, b = 2; };
 
 template <int CP, int CQ, typename R, int MODE>
-int launch_cls(const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st) {
-  return launch_one<ClsL<CP>::a, ClsL<CP>::b, ClsL<CQ>::a, ClsL<CQ>::b, R, MODE>(a, w, n, nsm, st);
+int launch_cls(const EriArgs &a, const int2 *w, int n, int max_blocks, cudaStream_t st) {
+  return launch_one<ClsL<CP>::a, ClsL<CP>::b, ClsL<CQ>::a, ClsL<CQ>::b, R, MODE>(a, w, n, max_blocks, st);
 }
 
 template <typename R, int MODE>
-int dispatch(int cp, int cq, const EriArgs &a, const int2 *w, int n, int nsm, cudaStream_t st) {
+int dispatch(int cp, int cq, const EriArgs &a, const int2 *w, int n, int max_blocks, cudaStream_t st) {
 #define CASE(X, Y) \
-  if (cp == X && cq == Y) return launch_cls<X, Y, R, MODE>(a, w, n, nsm, st);
+  if (cp == X && cq == Y) return launch_cls<X, Y, R, MODE>(a, w, n, max_blocks, st);
   CASE(0, 0) CASE(1, 0) CASE(1, 1) CASE(2, 0) CASE(2, 1) CASE(2, 2)
   CASE(3, 0) CASE(3, 1) CASE(3, 2) CASE(3, 3) CASE(4, 0) CASE(4, 1) CASE(4, 2) CASE(4, 3) CASE(4, 4)
   CASE(5, 0) CASE(5, 1) CASE(5, 2) CASE(5, 3) CASE(5, 4) CASE(5, 5)

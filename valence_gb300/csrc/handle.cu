@@ -156,6 +156,7 @@ struct vsvb_gpu {
     double nprimq;           /* primitive quartets inside the window */
     double flops_fwd, flops_grad;
     int code;                /* 100*k + 10*a + c; k = kind, or 3 for the FP32 tail of an FP64-class list */
+    int bps = 16;            /* grid cap: blocks per SM (autotuned) */
   };
   std::vector<SweepItem> sweep; /* by decreasing work */
   int launches = 0;              /* kernels enqueued by the current call */
@@ -164,7 +165,7 @@ struct vsvb_gpu {
   DetSetup ds{};
   double enuc = 0.0, dtol = 0.0, itol = 0.0;
   long long ntasks = 0;
-  int nsplit = 1;
+  int nsplit = 1, nsplit_max = 1; /* task splits per determinant pair (assembly grids) */
   std::vector<double> coeff0;
   /* schedules: [prec][cp][cq] */
   std::vector<int2> work_h[2][6][6];
@@ -752,7 +753,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     for (int c = 0; c < 6; ++c) {
       if (diag[c].empty()) continue;
       CK(wd[c].upload(diag[c]), "upload diag");
-      if (eri_launch(1, 0, c, c, ea, wd[c].p, (int)diag[c].size(), h->nsm, h->st)) {
+      if (eri_launch(1, 0, c, c, ea, wd[c].p, (int)diag[c].size(), h->nsm * 16, h->st)) {
         h->err = "Schwarz kernel launch failed";
         return VSVB_ERR_CUDA;
       }
@@ -808,7 +809,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     for (int c = 0; c < 6; ++c) {
       if (vdiag[c].empty()) continue;
       CK(wd[c].upload(vdiag[c]), "upload prim diag");
-      if (eri_launch(1, 0, c, c, ea, wd[c].p, (int)vdiag[c].size(), h->nsm, h->st)) {
+      if (eri_launch(1, 0, c, c, ea, wd[c].p, (int)vdiag[c].size(), h->nsm * 16, h->st)) {
         h->err = "primitive Schwarz kernel launch failed";
         return VSVB_ERR_CUDA;
       }
@@ -987,7 +988,8 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   long long want = (16LL * h->nsm + nq - 1) / nq;
   long long maxs = (work + 127) / 128;
   h->nsplit = (int)std::max<long long>(1, std::min(want, maxs));
-  size_t nslot = (size_t)nq * h->nsplit;
+  h->nsplit_max = (int)std::max<long long>(1, std::min(4 * want, maxs)); /* autotuner range */
+  size_t nslot = (size_t)nq * h->nsplit_max;
   CK(h->part_e1.alloc(nslot), "alloc parts");
   CK(h->part_wf.alloc(nslot), "alloc parts");
   CK(h->part_e2.alloc(nslot), "alloc parts");
@@ -1016,7 +1018,7 @@ int alloc_grad(vsvb_gpu *h) {
   CK(h->xbar.alloc(std::max<long long>(h->nxelem, 1)), "alloc xbar");
   CK(h->xbarh.alloc(std::max<long long>(h->nxh, 1)), "alloc xbarh");
   CK(h->Cbar.alloc((size_t)h->norb_all * h->maxobs), "alloc Cbar");
-  CK(h->vtot.alloc((size_t)nq * h->nsplit), "alloc vtot");
+  CK(h->vtot.alloc((size_t)nq * h->nsplit_max), "alloc vtot");
   CK(h->Gglob.alloc(std::max<long long>(nq * (na * na + nb * nb), 1)), "alloc G");
   CK(h->coeff_bar.alloc(h->totlen), "alloc coeff_bar");
   h->grad_ready = true;
@@ -1051,7 +1053,7 @@ int eri_sweep(vsvb_gpu *h, int mode) {
     ea.prim_lo = it.lo;
     ea.prim_hi = it.hi;
     if (h->sweep_timing) CK(cudaEventRecord(h->sweep_ev[2 * i], sa), "event record");
-    if (eri_launch(mode, it.kind, it.a, it.c, ea, h->work_d[it.list][it.a][it.c].p, n, h->nsm, sa)) {
+    if (eri_launch(mode, it.kind, it.a, it.c, ea, h->work_d[it.list][it.a][it.c].p, n, h->nsm * it.bps, sa)) {
       h->err = "ERI kernel launch failed";
       return VSVB_ERR_CUDA;
     }
@@ -1173,6 +1175,94 @@ int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
   return VSVB_OK;
 }
 
+/* Autotuner: launch geometry picked by timing on this device, once per
+ * handle (vsvb_options.autotune).
+ *  - per ERI launch of the sweep: the grid cap, 2/4/8/16 blocks per SM
+ *    (beyond it the blocks stride over the quartet list);
+ *  - the task splits per determinant pair of the assembly grids, from half
+ *    to four times the default.
+ * Each candidate runs 3 times on the handle's own data (min taken); the
+ * choice changes launch shapes only, never the arithmetic. */
+int autotune(vsvb_gpu *h) {
+  if (h->sweep.empty() && h->ntasks == 0) return VSVB_OK;
+  int rc = forward(h); /* weight tables, T and determinant pairs for the timed launches */
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->st), "autotune sync");
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0), "cudaEventCreate");
+  CK(cudaEventCreate(&e1), "cudaEventCreate");
+  auto time_it = [&](auto &&launch) -> float {
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+      cudaEventRecord(e0, h->st);
+      if (launch()) return -1.f;
+      cudaEventRecord(e1, h->st);
+      if (cudaEventSynchronize(e1) != cudaSuccess) return -1.f;
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      best = std::min(best, t);
+    }
+    return best;
+  };
+  /* ERI grid caps (forward launches into a scratch copy of U) */
+  EriArgs ea = eri_args(h);
+  int fail = 0;
+  for (auto &it : h->sweep) {
+    const int n = (int)h->work_h[it.list][it.a][it.c].size();
+    ea.prim_lo = it.lo;
+    ea.prim_hi = it.hi;
+    float best = 1e30f;
+    int pick = it.bps;
+    for (int bps : {2, 4, 8, 16}) {
+      const float t = time_it([&]() {
+        return eri_launch(0, it.kind, it.a, it.c, ea, h->work_d[it.list][it.a][it.c].p, n, h->nsm * bps, h->st);
+      });
+      if (t < 0.f) {
+        fail = 1;
+        break;
+      }
+      if (t < best * 0.97f) {
+        best = t;
+        pick = bps;
+      }
+    }
+    if (fail) break;
+    it.bps = pick;
+  }
+  /* assembly task splits */
+  if (!fail) {
+    DetCtx dc = det_ctx(h);
+    AsmArgs aa = asm_args(h);
+    const int base = h->nsplit;
+    float best = 1e30f;
+    int pick = base;
+    for (int ns : {base / 2, base, 2 * base, 4 * base}) {
+      if (ns < 1 || ns > h->nsplit_max) continue;
+      const float t = time_it([&]() {
+        return (int)(launch_assemble(0, dim3((unsigned)h->ds.nq, ns), 128, 0, h->st, dc, aa) != cudaSuccess);
+      });
+      if (t < 0.f) {
+        fail = 1;
+        break;
+      }
+      if (t < best * 0.97f) {
+        best = t;
+        pick = ns;
+      }
+    }
+    h->nsplit = pick;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (fail) {
+    h->err = "autotune launch failed";
+    return VSVB_ERR_CUDA;
+  }
+  CK(cudaMemsetAsync(h->T.p, 0, sizeof(double) * h->T.n, h->st), "memset T");
+  CK(cudaStreamSynchronize(h->st), "autotune sync");
+  return VSVB_OK;
+}
+
 /* adjoint pass; reads e_num and W from the forward pass's device result, so
  * forward + backward enqueue without a host round trip (and can be captured
  * into a CUDA graph) */
@@ -1240,6 +1330,7 @@ void vsvb_default_options(vsvb_options *o) {
   o->prim_screen = 1e-17;
   o->prim_split = 1;
   o->cuda_graph = 1;
+  o->autotune = 0;
 }
 
 int vsvb_gpu_create(const vsvb_system_desc *d, const vsvb_options *opt, vsvb_gpu **out) {
@@ -1250,6 +1341,7 @@ int vsvb_gpu_create(const vsvb_system_desc *d, const vsvb_options *opt, vsvb_gpu
   if (opt) h->opt = *opt;
   h->dev = h->opt.device;
   int rc = build(h, d);
+  if (!rc && h->opt.autotune) rc = autotune(h);
   *out = h;
   return rc;
 }
@@ -1592,7 +1684,7 @@ int vsvb_gpu_eri_profile_mode(vsvb_gpu *h, int mode, double *ms, double *flops, 
     ea.prim_hi = it.hi;
     cudaEventRecord(e0, h->st);
     if (eri_launch(mode, it.kind, it.a, it.c, ea, h->work_d[it.list][it.a][it.c].p,
-                   (int)h->work_h[it.list][it.a][it.c].size(), h->nsm, h->st)) {
+                   (int)h->work_h[it.list][it.a][it.c].size(), h->nsm * it.bps, h->st)) {
       rc = -VSVB_ERR_CUDA;
       break;
     }
@@ -1640,6 +1732,19 @@ int vsvb_gpu_sweep_times(vsvb_gpu *h, double *ms, double *flops, int *cls, int c
     ms[k] = t;
     flops[k] = h->sweep_mode == 0 ? it.flops_fwd : it.flops_grad;
     cls[k] = it.code;
+  }
+  return k;
+}
+
+int vsvb_gpu_launch_config(const vsvb_gpu *h, int *nsplit, int *codes, int *blocks_per_sm, int cap) {
+  if (!h) return -VSVB_ERR_INPUT;
+  if (nsplit) *nsplit = h->nsplit;
+  int k = 0;
+  for (const auto &it : h->sweep) {
+    if (k >= cap) break;
+    if (codes) codes[k] = it.code;
+    if (blocks_per_sm) blocks_per_sm[k] = it.bps;
+    ++k;
   }
   return k;
 }
