@@ -31,13 +31,15 @@
  * accumulators.  After the primitive loop the block is staged in shared
  * memory and transformed with the X' tables; U is updated with FP64 atomics.
  *
- * Arithmetic.  R = double: everything FP64.  R = float or double-float
- * (df64, an unevaluated sum of two FP32 numbers, ~48-bit significand): the
- * Boys argument T, 1/(p+q), the prefactor and the Chebyshev evaluation of
- * the Rys roots and weights run in double-float (the small high-order
- * Chebyshev terms in FP32) with no FP64 instruction, so roots and weights
- * keep ~1e-14 relative accuracy on the FP32 pipes; the 2D tables and the
- * component sums run in R.  The transform to U is FP64 in every case.
+ * Arithmetic.  R = double: everything FP64.  R = double-float (df64, an
+ * unevaluated sum of two FP32 numbers, ~48-bit significand): the Boys
+ * argument T, 1/(p+q), the prefactor and the Chebyshev evaluation of the Rys
+ * roots and weights run in double-float (the small high-order Chebyshev
+ * terms in FP32) with no FP64 instruction, so roots and weights keep ~1e-14
+ * relative accuracy on the FP32 pipes; tables and component sums in df64;
+ * the transform in FP64.  R = float (quartets, or primitive quartets, whose
+ * Schwarz bound is below the mixed threshold): everything in FP32, including
+ * the roots and the transform, with FP64 atomics into U.
  */
 #ifndef VSVB_ERI_IMPL_CUH
 #define VSVB_ERI_IMPL_CUH
@@ -216,6 +218,20 @@ __device__ __forceinline__ void rys_root_df(int n, int r, int j, bool in_table, 
     x = df64(rc.axf[n - 1][r].x, rc.axf[n - 1][r].y) * s * s;
     w = df64(rc.awf[n - 1][r].x, rc.awf[n - 1][r].y) * s;
   }
+}
+
+/* FP32 Chebyshev sum and root for the FP32 kernels (their integrals carry
+ * FP32 rounding anyway): the hi parts of the same tables */
+__device__ __forceinline__ float clenshaw12_f(const float2 *__restrict__ c, float t) {
+  float b1 = 0.f, b2 = 0.f;
+  const float t2 = 2.f * t;
+#pragma unroll
+  for (int k = RYS_NCHEB_D - 1; k > 0; --k) {
+    const float b0 = fmaf(t2, b1, c[k].x - b2);
+    b2 = b1;
+    b1 = b0;
+  }
+  return fmaf(t, b1, c[0].x - b2);
 }
 
 __device__ __forceinline__ const PrimT<df64> *args_primdf(const EriArgs &a) {
@@ -489,6 +505,33 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
               rw[lane * S::NR + rr] = R(w * pref);
             }
             ripq[lane] = R(ipq);
+          } else if constexpr (std::is_same<R, float>::value) {
+            /* FP32 kernels: roots, weights and prefactor in FP32 */
+            const PrimT<float> &pp = primR[P.prim0 + ip];
+            const PrimT<float> &qq = primR[Q.prim0 + iq];
+            const float ipq = 1.f / (pp.p + qq.p);
+            const float dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
+            const float Tb = pp.p * qq.p * ipq * (dx * dx + dy * dy + dz * dz);
+            const float pref = 34.98683665f /* 2 pi^(5/2) */ * pp.Kp * qq.Kp * sqrtf(ipq);
+            if (Tb < (float)RYS_TMAX_D) {
+              const int j = max(0, min((int)(Tb * (float)(1.0 / RYS_H_D)), (int)(RYS_TMAX_D / RYS_H_D) - 1));
+              const float t = (Tb - (float)(j * RYS_H_D)) * (float)(2.0 / RYS_H_D) - 1.f;
+              const float sc = rsqrtf(1.f + Tb);
+              const float2 *c = args.rysdf + args.rc.off[S::NR - 1] + (size_t)j * (2 * S::NR) * RYS_NCHEB_D;
+#pragma unroll 1
+              for (int rr = 0; rr < S::NR; ++rr) {
+                rx[lane * S::NR + rr] = clenshaw12_f(c + rr * RYS_NCHEB_D, t) * sc * sc;
+                rw[lane * S::NR + rr] = clenshaw12_f(c + (S::NR + rr) * RYS_NCHEB_D, t) * sc * pref;
+              }
+            } else {
+              const float sc = rsqrtf(Tb);
+#pragma unroll 1
+              for (int rr = 0; rr < S::NR; ++rr) {
+                rx[lane * S::NR + rr] = args.rc.axf[S::NR - 1][rr].x * sc * sc;
+                rw[lane * S::NR + rr] = args.rc.awf[S::NR - 1][rr].x * sc * pref;
+              }
+            }
+            ripq[lane] = ipq;
           } else {
             /* double-float throughout: no FP64 instruction on this path */
             const PrimT<df64> &pp = args_primdf(args)[P.prim0 + ip];

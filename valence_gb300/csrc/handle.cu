@@ -1153,11 +1153,11 @@ void fill_result(const vsvb_gpu *h, const double *r, vsvb_energy_result *out) {
      * arithmetic behind their integrals -- per quartet the (e0|e0) bounds
      * times the transfer-matrix norms of both pairs -- converted to energy by
      * the two-electron energy per unit of Schwarz-bound mass,
-     * |e2/W| / sum_PQ b_PQ, with a factor 2^-6 for the looseness of these
+     * |e2/W| / sum_PQ b_PQ, with a factor 2^-5 for the looseness of these
      * product bounds (on the C/H chain at thresholds 1e-6 .. all-FP32 the
-     * measured error stays 8-70x below the estimate) */
+     * measured error stays 5-90x below the estimate) */
     if (h->nq_fp32 > 0 && h->bound_all > 0.0 && r[4] != 0.0)
-      out->err_est = std::ldexp(std::fabs(r[3] / r[4]) * (h->err_bound / h->bound_all), -30);
+      out->err_est = std::ldexp(std::fabs(r[3] / r[4]) * (h->err_bound / h->bound_all), -29);
   }
 }
 
