@@ -78,6 +78,9 @@ struct QInfo {
   int isc, jsc;
   unsigned bb, kb;
   double w;
+  /* after the determinant pairs are factorised (load_dets) */
+  double da, db; /* det of the alpha / beta block */
+  int sing;      /* exact-minor flags per spin block */
 };
 
 __device__ __forceinline__ QInfo decode_q(const DetCtx &d, long long q) {
@@ -90,7 +93,15 @@ __device__ __forceinline__ QInfo decode_q(const DetCtx &d, long long q) {
   r.isc = (int)(sp / d.ds.nsc);
   r.jsc = (int)(sp % d.ds.nsc);
   r.w = d.coeff_sc[r.isc] * d.coeff_sc[r.jsc];
+  r.da = r.db = 0.0;
+  r.sing = 0;
   return r;
+}
+
+__device__ __forceinline__ void load_dets(const DetCtx &d, long long q, QInfo &qi) {
+  qi.da = d.det_a[q];
+  qi.db = d.det_b[q];
+  qi.sing = d.sing[q];
 }
 
 /* exact determinant of spin block sp of pair q with up to two strikes, by LU
@@ -148,18 +159,22 @@ struct Cof {
   double Ja, Jb;  /* reduced factors */
 };
 
-/* cofactor of determinant pair q for up to two (bra slot, ket slot) strikes */
-__device__ Cof cofactor(const DetCtx &d, long long q, const QInfo &qi, int nst, const int *sb, const int *sk,
-                        int *status) {
+/* spin and block position of a spin-orbital slot in the bra / ket determinant */
+struct Loc {
+  int spin, pos;
+};
+
+/* cofactor of determinant pair q for up to two strikes (bra slot -> ket
+ * slot), given their locations */
+__device__ Cof cofactor_loc(const DetCtx &d, long long q, const QInfo &qi, int nst, const Loc *lb, const Loc *lk,
+                            int *status) {
   Cof c;
   c.ok = false;
   c.v = 0.0;
   c.na_s = c.nb_s = 0;
   c.Ja = c.Jb = 1.0;
   for (int t = 0; t < nst; ++t) {
-    int s1, p1, s2, p2;
-    slot_loc(d, qi.isc, qi.bb, sb[t], s1, p1);
-    slot_loc(d, qi.jsc, qi.kb, sk[t], s2, p2);
+    const int s1 = lb[t].spin, p1 = lb[t].pos, s2 = lk[t].spin, p2 = lk[t].pos;
     if (s1 != s2) return c;
     if (s1 == 0) {
       c.ra[c.na_s] = p1;
@@ -173,7 +188,7 @@ __device__ Cof cofactor(const DetCtx &d, long long q, const QInfo &qi, int nst, 
   }
   c.ok = true;
   const int na = d.ds.nalpha, nb = d.ds.nbeta;
-  const int sing = d.sing[q];
+  const int sing = qi.sing;
   double fa, fb;
   if ((sing & 1) && c.na_s > 0) {
     fa = struck_det_exact(d, qi, 0, c.na_s, c.ra, c.ca);
@@ -184,7 +199,7 @@ __device__ Cof cofactor(const DetCtx &d, long long q, const QInfo &qi, int nst, 
     if (c.na_s == 1) c.Ja = Ta[c.ca[0] * na + c.ra[0]];
     else if (c.na_s == 2)
       c.Ja = Ta[c.ca[0] * na + c.ra[0]] * Ta[c.ca[1] * na + c.ra[1]] - Ta[c.ca[0] * na + c.ra[1]] * Ta[c.ca[1] * na + c.ra[0]];
-    fa = d.det_a[q] * c.Ja;
+    fa = qi.da * c.Ja;
   }
   if ((sing & 2) && c.nb_s > 0) {
     fb = struck_det_exact(d, qi, 1, c.nb_s, c.rb, c.cb);
@@ -195,10 +210,32 @@ __device__ Cof cofactor(const DetCtx &d, long long q, const QInfo &qi, int nst, 
     if (c.nb_s == 1) c.Jb = Tb[c.cb[0] * nb + c.rb[0]];
     else if (c.nb_s == 2)
       c.Jb = Tb[c.cb[0] * nb + c.rb[0]] * Tb[c.cb[1] * nb + c.rb[1]] - Tb[c.cb[0] * nb + c.rb[1]] * Tb[c.cb[1] * nb + c.rb[0]];
-    fb = d.det_b[q] * c.Jb;
+    fb = qi.db * c.Jb;
   }
   c.v = qi.w * fa * fb;
   return c;
+}
+
+__device__ __forceinline__ Loc loc_bra(const DetCtx &d, const QInfo &qi, int s) {
+  Loc l;
+  slot_loc(d, qi.isc, qi.bb, s, l.spin, l.pos);
+  return l;
+}
+__device__ __forceinline__ Loc loc_ket(const DetCtx &d, const QInfo &qi, int s) {
+  Loc l;
+  slot_loc(d, qi.jsc, qi.kb, s, l.spin, l.pos);
+  return l;
+}
+
+/* cofactor of determinant pair q for up to two (bra slot, ket slot) strikes */
+__device__ __forceinline__ Cof cofactor(const DetCtx &d, long long q, const QInfo &qi, int nst, const int *sb,
+                                        const int *sk, int *status) {
+  Loc lb[2], lk[2];
+  for (int t = 0; t < nst; ++t) {
+    lb[t] = loc_bra(d, qi, sb[t]);
+    lk[t] = loc_ket(d, qi, sk[t]);
+  }
+  return cofactor_loc(d, q, qi, nst, lb, lk, status);
 }
 
 /* dJ/dT accumulation for one cofactor with coefficient coef on v */
@@ -206,7 +243,7 @@ __device__ void accum_G(const DetCtx &d, long long q, const QInfo &qi, const Cof
                         int lda, int ldb) {
   if (!c.ok || coef == 0.0) return;
   const int na = d.ds.nalpha, nb = d.ds.nbeta;
-  const double dd = qi.w * d.det_a[q] * d.det_b[q];
+  const double dd = qi.w * qi.da * qi.db;
   if (c.na_s > 0) {
     const double *Ta = d.Ta + (size_t)q * na * na;
     const double f = coef * dd * c.Jb;
@@ -436,16 +473,21 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
   extern __shared__ double gsh[];
   const long long q = blockIdx.x;
   const int split = blockIdx.y, nsplit = gridDim.y;
-  const QInfo qi = decode_q(d, q);
+  QInfo qi = decode_q(d, q);
+  load_dets(d, q, qi);
   const int nelec = d.ds.nelec, nnd = d.ds.nnd, nsp = d.ds.nsp;
   const int na = d.ds.nalpha, nb = d.ds.nbeta;
   double *Ga = nullptr, *Gb = nullptr;
   int lda = na, ldb = nb;
   if (GRAD) {
     if (a.g_in_smem) {
-      Ga = gsh;
-      Gb = gsh + na * na;
-      for (int t = threadIdx.x; t < na * na + nb * nb; t += blockDim.x) gsh[t] = 0.0;
+      /* g_in_smem = number of copies: one per warp (less atomic contention)
+       * or one per block */
+      const int ng = na * na + nb * nb;
+      const int copy = a.g_in_smem > 1 ? (int)(threadIdx.x >> 5) % a.g_in_smem : 0;
+      Ga = gsh + (size_t)copy * ng;
+      Gb = Ga + na * na;
+      for (int t = threadIdx.x; t < ng * a.g_in_smem; t += blockDim.x) gsh[t] = 0.0;
       __syncthreads();
     } else {
       Ga = a.Gglob + (size_t)q * (na * na + nb * nb);
@@ -528,14 +570,18 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
     for (int is = 0; is < iso; ++is) {
       /* 0-based slot; 1-based formula 2*io - nnd + is - 2 with 1-based io */
       const int i = id ? 2 * (io + 1) - nnd + (is + 1) - 2 - 1 : io;
+      const Loc Li = loc_bra(d, qi, i);
       for (int js = 0; js < jso; ++js) {
         const int j = jd ? 2 * (jo + 1) - nnd + (js + 1) - 2 - 1 : jo;
         if (!(j < i)) continue;
+        const Loc Lb[2] = {Li, loc_bra(d, qi, j)};
         for (int ks = 0; ks < kso; ++ks) {
           const int k = kd ? 2 * (ko + 1) - nnd + (ks + 1) - 2 - 1 : ko;
+          const Loc Lk = loc_ket(d, qi, k);
           for (int ls = 0; ls < lso; ++ls) {
             const int l = ld ? 2 * (lo + 1) - nnd + (ls + 1) - 2 - 1 : lo;
             if (!(l < k)) continue;
+            const Loc Ll = loc_ket(d, qi, l);
             /* 1-based parity for the DOCC spin integration */
             const bool ik0 = id && kd && ((i + 1) & 1) != ((k + 1) & 1);
             const bool jl0 = jd && ld && ((j + 1) & 1) != ((l + 1) & 1);
@@ -547,12 +593,12 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
             ce_c.ok = false;
             cx_c.ok = false;
             if (es) {
-              int sb[2] = {i, j}, sk[2] = {k, l};
-              ce_c = cofactor(d, q, qi, 2, sb, sk, a.status);
+              const Loc lk[2] = {Lk, Ll};
+              ce_c = cofactor_loc(d, q, qi, 2, Lb, lk, a.status);
             }
             if (xs) {
-              int sb[2] = {i, j}, sk[2] = {l, k};
-              cx_c = cofactor(d, q, qi, 2, sb, sk, a.status);
+              const Loc lk[2] = {Ll, Lk};
+              cx_c = cofactor_loc(d, q, qi, 2, Lb, lk, a.status);
             }
             double dd = 0.0, xd = 0.0;
             if (es && ce_c.ok) dd = ce_c.v;
@@ -617,9 +663,13 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
     if (threadIdx.x == 0) a.vtot[slot] = vtot;
     if (a.g_in_smem) {
       __syncthreads();
-      double *Gq = a.Gglob + (size_t)q * (na * na + nb * nb);
-      for (int t = threadIdx.x; t < na * na + nb * nb; t += blockDim.x)
-        if (gsh[t] != 0.0) atomicAdd(Gq + t, gsh[t]);
+      const int ng = na * na + nb * nb;
+      double *Gq = a.Gglob + (size_t)q * ng;
+      for (int t = threadIdx.x; t < ng; t += blockDim.x) {
+        double v = 0.0;
+        for (int c = 0; c < a.g_in_smem; ++c) v += gsh[(size_t)c * ng + t];
+        if (v != 0.0) atomicAdd(Gq + t, v);
+      }
     }
   } else if (!DENS && threadIdx.x == 0) {
     a.part_e1[slot] = e1;

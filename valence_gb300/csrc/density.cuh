@@ -31,7 +31,7 @@ struct AsmArgs {
   double *Tbar, *Sbar, *Hbar;
   double *vtot;            /* [nq * nsplit] */
   double *Gglob;           /* [nq][na*na + nb*nb] */
-  int g_in_smem;
+  int g_in_smem;            /* copies of G per block in shared memory (0: G in global memory) */
   int skip_tbar; /* adjoint walk without dE/dT (single-sweep mode) */
 };
 

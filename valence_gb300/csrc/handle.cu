@@ -329,7 +329,12 @@ AsmArgs asm_args(vsvb_gpu *h) {
   a.vtot = h->vtot.p;
   a.Gglob = h->Gglob.p;
   int na = h->ds.nalpha, nb = h->ds.nbeta;
-  a.g_in_smem = (size_t)(na * na + nb * nb) * sizeof(double) <= 40 * 1024;
+  {
+    /* dJ/dT accumulators: one copy per warp of the 128-thread block when
+     * they fit, else one per block, else global memory */
+    const size_t gbytes = (size_t)(na * na + nb * nb) * sizeof(double);
+    a.g_in_smem = 4 * gbytes <= 40 * 1024 ? 4 : (gbytes <= 40 * 1024 ? 1 : 0);
+  }
   return a;
 }
 
@@ -1289,7 +1294,7 @@ int backward(vsvb_gpu *h, bool fused) {
   aa.status = h->status.p;
   aa.res = h->result.p;
   aa.skip_tbar = fused ? 1 : 0;
-  size_t gsh = aa.g_in_smem ? sizeof(double) * (size_t)(na * na + nb * nb) : 0;
+  size_t gsh = sizeof(double) * (size_t)(na * na + nb * nb) * aa.g_in_smem;
   CK(launch_assemble(1, dim3((unsigned)h->ds.nq, h->nsplit), 128, gsh, st, dc, aa), "assemble grad");
   detpair_adjoint_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, aa, h->nsplit);
   CK(cudaGetLastError(), "detpair adjoint");
