@@ -157,7 +157,12 @@ struct vsvb_gpu {
     double flops_fwd, flops_grad;
     int code;                /* 100*k + 10*a + c; k = kind, or 3 for the FP32 tail of an FP64-class list */
     int bps = 16;            /* grid cap: blocks per SM (autotuned) */
+    int wl = -1;             /* its own quartet list: item_wh / item_wd */
   };
+  /* per launch: the quartets with work in its window, most primitive
+   * quartets first */
+  std::vector<std::vector<int2>> item_wh;
+  std::vector<DBuf<int2>> item_wd;
   std::vector<SweepItem> sweep; /* by decreasing work */
   int launches = 0;              /* kernels enqueued by the current call */
   /* dims */
@@ -169,7 +174,6 @@ struct vsvb_gpu {
   std::vector<double> coeff0;
   /* schedules: [prec][cp][cq] */
   std::vector<int2> work_h[2][6][6];
-  DBuf<int2> work_d[2][6][6];
   long long nq_fp64 = 0, nq_fp32 = 0;
   double nprimq_fp32 = 0.0, nprimq_all = 0.0; /* primitive quartets evaluated in FP32 / in total */
   double err_bound = 0.0; /* sum over FP32 quartets of the Schwarz bound */
@@ -906,12 +910,12 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
       h->work_h[prec][pairs[a].cls][pairs[c].cls].push_back(make_int2(a, c));
     }
   {
+    std::vector<std::vector<int2>> iwl;
     for (int p = 0; p < 2; ++p)
       for (int a = 0; a < 6; ++a)
         for (int c = 0; c < 6; ++c) {
           const auto &w = h->work_h[p][a][c];
           if (w.empty()) continue;
-          CK(h->work_d[p][a][c].upload(w), "upload work");
           /* launches over this list: FP32-class lists in FP32; FP64-class
            * lists in the handle's FP64-class arithmetic, and with the split
            * their primitive quartets below tau in FP32 */
@@ -925,19 +929,32 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
             items.push_back({p, eri_kind(h, 0), a, c, eps, INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
           }
           for (auto &it : items) {
+            std::vector<std::pair<double, int2>> kept;
             for (const int2 &q : w) {
               double sb = 0.0;
               const double n = window(q.x, q.y, it.lo, it.hi, sb);
+              if (n <= 0.0) continue;
+              kept.push_back({n, q});
               it.nprimq += n;
               it.flops_fwd += eri_flops(0, a, c, n, pairs[q.x].nop, pairs[q.y].nop);
               it.flops_grad += eri_flops(3, a, c, n, pairs[q.x].nop, pairs[q.y].nop);
             }
-            if (it.nprimq > 0) h->sweep.push_back(it);
+            if (kept.empty()) continue;
+            std::stable_sort(kept.begin(), kept.end(), [](const std::pair<double, int2> &x,
+                                                          const std::pair<double, int2> &y) { return x.first > y.first; });
+            std::vector<int2> lst(kept.size());
+            for (size_t k = 0; k < kept.size(); ++k) lst[k] = kept[k].second;
+            it.wl = (int)iwl.size();
+            iwl.push_back(std::move(lst));
+            h->sweep.push_back(it);
           }
         }
     std::sort(h->sweep.begin(), h->sweep.end(), [](const vsvb_gpu::SweepItem &x, const vsvb_gpu::SweepItem &y) {
       return x.flops_fwd > y.flops_fwd;
     });
+    h->item_wh = std::move(iwl);
+    h->item_wd = std::vector<DBuf<int2>>(h->item_wh.size());
+    for (size_t k = 0; k < h->item_wh.size(); ++k) CK(h->item_wd[k].upload(h->item_wh[k]), "upload item work");
   }
 
   /* determinant pairs */
@@ -1053,12 +1070,12 @@ int eri_sweep(vsvb_gpu *h, int mode) {
     }
   }
   for (const auto &it : h->sweep) {
-    const int n = (int)h->work_h[it.list][it.a][it.c].size();
+    const int n = (int)h->item_wh[it.wl].size();
     cudaStream_t sa = h->aux[i % vsvb_gpu::NAUX];
     ea.prim_lo = it.lo;
     ea.prim_hi = it.hi;
     if (h->sweep_timing) CK(cudaEventRecord(h->sweep_ev[2 * i], sa), "event record");
-    if (eri_launch(mode, it.kind, it.a, it.c, ea, h->work_d[it.list][it.a][it.c].p, n, h->nsm * it.bps, sa)) {
+    if (eri_launch(mode, it.kind, it.a, it.c, ea, h->item_wd[it.wl].p, n, h->nsm * it.bps, sa)) {
       h->err = "ERI kernel launch failed";
       return VSVB_ERR_CUDA;
     }
@@ -1213,14 +1230,14 @@ int autotune(vsvb_gpu *h) {
   EriArgs ea = eri_args(h);
   int fail = 0;
   for (auto &it : h->sweep) {
-    const int n = (int)h->work_h[it.list][it.a][it.c].size();
+    const int n = (int)h->item_wh[it.wl].size();
     ea.prim_lo = it.lo;
     ea.prim_hi = it.hi;
     float best = 1e30f;
     int pick = it.bps;
     for (int bps : {2, 4, 8, 16}) {
       const float t = time_it([&]() {
-        return eri_launch(0, it.kind, it.a, it.c, ea, h->work_d[it.list][it.a][it.c].p, n, h->nsm * bps, h->st);
+        return eri_launch(0, it.kind, it.a, it.c, ea, h->item_wd[it.wl].p, n, h->nsm * bps, h->st);
       });
       if (t < 0.f) {
         fail = 1;
@@ -1688,8 +1705,8 @@ int vsvb_gpu_eri_profile_mode(vsvb_gpu *h, int mode, double *ms, double *flops, 
     ea.prim_lo = it.lo;
     ea.prim_hi = it.hi;
     cudaEventRecord(e0, h->st);
-    if (eri_launch(mode, it.kind, it.a, it.c, ea, h->work_d[it.list][it.a][it.c].p,
-                   (int)h->work_h[it.list][it.a][it.c].size(), h->nsm * it.bps, h->st)) {
+    if (eri_launch(mode, it.kind, it.a, it.c, ea, h->item_wd[it.wl].p, (int)h->item_wh[it.wl].size(),
+                   h->nsm * it.bps, h->st)) {
       rc = -VSVB_ERR_CUDA;
       break;
     }
