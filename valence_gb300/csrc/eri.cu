@@ -102,7 +102,7 @@ double eri_flops(int mode, int cp, int cq, double nprimq, int nopP, int nopQ) {
   return nprimq * prim + tr;
 }
 
-int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int max_blocks,
+int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int4 *work, int nwork, int max_blocks,
                cudaStream_t st) {
   /* the Schwarz pass and the separate adjoint sweep (grad_mode 1) always run
    * in FP64; the FP32 / double-float kinds instantiate modes 0 and 3 only */

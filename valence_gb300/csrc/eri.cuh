@@ -39,13 +39,15 @@ struct EriArgs {
 enum { ERI_F64 = 0, ERI_F32 = 1, ERI_DF64 = 2 };
 
 /* cp >= cq are pair classes 0..5; mode 0 forward, 1 Schwarz (F64 only),
- * 2 adjoint, 3 forward + adjoint.  max_blocks caps the grid (the blocks then
- * stride over the work list). */
-int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int2 *work, int nwork, int max_blocks,
+ * 2 adjoint, 3 forward + adjoint.  Work items (P, Q, r0, r1): shell pairs P
+ * (class cp) and Q, and the rows r0 <= ip < r1 of P's primitive pairs to
+ * evaluate (a large quartet is split into row ranges).  max_blocks caps the
+ * grid (the blocks then stride over the work list). */
+int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int4 *work, int nwork, int max_blocks,
                cudaStream_t st);
-int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int max_blocks, cudaStream_t st);
-int eri_dispatch_f32(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int max_blocks, cudaStream_t st);
-int eri_dispatch_df64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int max_blocks,
+int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st);
+int eri_dispatch_f32(int mode, int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st);
+int eri_dispatch_df64(int mode, int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks,
                       cudaStream_t st);
 double eri_flops(int mode, int cp, int cq, double nprimq, int nopP, int nopQ);
 int eri_symmetrize(double *T, int np, double *sq, cudaStream_t st);

@@ -4,7 +4,7 @@
  */
 #include "eri_impl.cuh"
 
-int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int2 *w, int n, int max_blocks, cudaStream_t st) {
+int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st) {
   if (mode == 0) return dispatch<double, 0>(cp, cq, a, w, n, max_blocks, st);
   if (mode == 1) return dispatch<double, 1>(cp, cq, a, w, n, max_blocks, st);
   if (mode == 2) return dispatch<double, 2>(cp, cq, a, w, n, max_blocks, st);

@@ -390,7 +390,7 @@ struct QuartetShape {
  * MODE 3: forward and adjoint from one evaluation of each quartet.
  */
 template <int LA, int LB, int LC, int LD, typename R, int MODE>
-__global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int2 *__restrict__ work, int nwork) {
+__global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int4 *__restrict__ work, int nwork) {
   using S = QuartetShape<LA, LB, LC, LD, sizeof(R)>;
   constexpr bool CTA = S::CTA;
   constexpr bool DFROOT = !std::is_same<R, double>::value;
@@ -424,7 +424,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   const int item0 = CTA ? (int)blockIdx.x : (int)blockIdx.x * WARPS + warp;
   const int istep = CTA ? (int)gridDim.x : (int)gridDim.x * WARPS;
   for (int item = item0; item < nwork; item += istep) {
-    const int2 pq = work[item];
+    const int4 pq = work[item];
     const ShellPair &P = args.pairs[pq.x];
     const ShellPair &Q = args.pairs[pq.y];
     R acc[S::PER_LANE];
@@ -445,7 +445,9 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         }
       }
     }
-    const int npq = nrow * Q.nprim;
+    /* this item's rows of P's primitive pairs */
+    const int r1 = min(pq.w, nrow), pq_begin = pq.z * Q.nprim;
+    const int npq = r1 > pq.z ? (r1 - pq.z) * Q.nprim : 0;
     /* lane roles in the 2D phase: slot g, root r, direction dir */
     const int g = lane / (3 * S::NR), rem = lane - g * (3 * S::NR);
     const int r = rem / 3, dir = rem - 3 * (rem / 3);
@@ -467,8 +469,8 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
       /* compaction: the chunk's primitive quartets that pass the screen */
       int nch;
       {
-        const int pqi = chunk + lane;
-        bool keep = pqi < npq;
+        const int pqi = pq_begin + chunk + lane;
+        bool keep = chunk + lane < npq;
         if (keep && (eps > 0.f || eps_hi < INFINITY)) {
           const int ip = pqi / Q.nprim, iq = pqi - ip * Q.nprim;
           const float b = args.prim_q0[P.prim0 + ip] * args.prim_q0[Q.prim0 + iq];
@@ -858,7 +860,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
 }
 
 template <int LA, int LB, int LC, int LD, typename R, int MODE>
-int launch_one(const EriArgs &args, const int2 *work, int nwork, int max_blocks, cudaStream_t st) {
+int launch_one(const EriArgs &args, const int4 *work, int nwork, int max_blocks, cudaStream_t st) {
   if (nwork <= 0) return 0;
   using S = QuartetShape<LA, LB, LC, LD, sizeof(R)>;
   size_t shm = sizeof(double) * (S::IDXD + (size_t)WARPS * S::PER_WARP + S::SHARED);
@@ -886,12 +888,12 @@ template <> struct ClsL<4> { static constexpr int a = 2, b = 1; };
 template <> struct ClsL<5> { static constexpr int a = 2, b = 2; };
 
 template <int CP, int CQ, typename R, int MODE>
-int launch_cls(const EriArgs &a, const int2 *w, int n, int max_blocks, cudaStream_t st) {
+int launch_cls(const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st) {
   return launch_one<ClsL<CP>::a, ClsL<CP>::b, ClsL<CQ>::a, ClsL<CQ>::b, R, MODE>(a, w, n, max_blocks, st);
 }
 
 template <typename R, int MODE>
-int dispatch(int cp, int cq, const EriArgs &a, const int2 *w, int n, int max_blocks, cudaStream_t st) {
+int dispatch(int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st) {
 #define CASE(X, Y) \
   if (cp == X && cq == Y) return launch_cls<X, Y, R, MODE>(a, w, n, max_blocks, st);
   CASE(0, 0) CASE(1, 0) CASE(1, 1) CASE(2, 0) CASE(2, 1) CASE(2, 2)

@@ -161,8 +161,8 @@ struct vsvb_gpu {
   };
   /* per launch: the quartets with work in its window, most primitive
    * quartets first */
-  std::vector<std::vector<int2>> item_wh;
-  std::vector<DBuf<int2>> item_wd;
+  std::vector<std::vector<int4>> item_wh; /* (P, Q, first row, end row of P's primitives) */
+  std::vector<DBuf<int4>> item_wd;
   std::vector<SweepItem> sweep; /* by decreasing work */
   int launches = 0;              /* kernels enqueued by the current call */
   /* dims */
@@ -753,12 +753,12 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   std::vector<double> q0;
   std::vector<float> q0f; /* per primitive pair, sorted descending within each shell pair */
   {
-    std::vector<int2> diag[6];
-    for (size_t p = 0; p < pairs.size(); ++p) diag[pairs[p].cls].push_back(make_int2((int)p, (int)p));
+    std::vector<int4> diag[6];
+    for (size_t p = 0; p < pairs.size(); ++p) diag[pairs[p].cls].push_back(make_int4((int)p, (int)p, 0, 1 << 30));
     EriArgs ea = eri_args(h);
     ea.prim_lo = 0.f;
     ea.prim_hi = INFINITY;
-    DBuf<int2> wd[6];
+    DBuf<int4> wd[6];
     for (int c = 0; c < 6; ++c) {
       if (diag[c].empty()) continue;
       CK(wd[c].upload(diag[c]), "upload diag");
@@ -784,7 +784,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   {
     std::vector<ShellPair> vp;
     std::vector<GeomT<double>> vg;
-    std::vector<int2> vdiag[6];
+    std::vector<int4> vdiag[6];
     for (size_t pi = 0; pi < pairs.size(); ++pi) {
       GeomT<double> g;
       for (int k = 0; k < 3; ++k) {
@@ -795,7 +795,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
         ShellPair v = pairs[pi];
         v.prim0 = pairs[pi].prim0 + ip;
         v.nprim = 1;
-        vdiag[v.cls].push_back(make_int2((int)vp.size(), (int)vp.size()));
+        vdiag[v.cls].push_back(make_int4((int)vp.size(), (int)vp.size(), 0, 1 << 30));
         vp.push_back(v);
         vg.push_back(g);
       }
@@ -803,7 +803,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     DBuf<ShellPair> vp_d;
     DBuf<GeomT<double>> vg_d;
     DBuf<double> vq, vq0;
-    DBuf<int2> wd[6];
+    DBuf<int4> wd[6];
     CK(vp_d.upload(vp), "upload prim pairs");
     CK(vg_d.upload(vg), "upload prim geometry");
     CK(vq.alloc(std::max<size_t>(vp.size(), 1)), "alloc prim bounds");
@@ -880,6 +880,19 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     }
     return n;
   };
+  /* the same per row of P's primitive pairs (rows[i] for i < na) */
+  auto window_rows = [&](int P, int Q, float lo, float hi, std::vector<int> &rows) {
+    const float *a = q0f.data() + pairs[P].prim0, *b = q0f.data() + pairs[Q].prim0;
+    const int na = pairs[P].nprim, nb = pairs[Q].nprim;
+    rows.assign(na, 0);
+    int jlo = nb, jhi = nb;
+    for (int i = 0; i < na; ++i) {
+      if (!(a[i] * b[0] >= lo)) break;
+      while (jlo > 0 && !(a[i] * b[jlo - 1] >= lo)) --jlo;
+      while (jhi > 0 && !(a[i] * b[jhi - 1] >= hi)) --jhi;
+      rows[i] = jlo - jhi;
+    }
+  };
   h->err_bound = 0.0;
   h->bound_all = 0.0;
   for (size_t P = 0; P < pairs.size(); ++P)
@@ -910,7 +923,12 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
       h->work_h[prec][pairs[a].cls][pairs[c].cls].push_back(make_int2(a, c));
     }
   {
-    std::vector<std::vector<int2>> iwl;
+    std::vector<std::vector<int4>> iwl;
+    /* a quartet with more than this many primitive quartets in a launch's
+     * window is split into row ranges of P's primitives, so that the largest
+     * quartets do not leave a tail of lone CTAs at the end of the launch */
+    constexpr int SPLIT_PRIMQ = 512;
+    std::vector<int> rows;
     for (int p = 0; p < 2; ++p)
       for (int a = 0; a < 6; ++a)
         for (int c = 0; c < 6; ++c) {
@@ -929,20 +947,35 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
             items.push_back({p, eri_kind(h, 0), a, c, eps, INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
           }
           for (auto &it : items) {
-            std::vector<std::pair<double, int2>> kept;
+            std::vector<std::pair<double, int4>> kept;
             for (const int2 &q : w) {
-              double sb = 0.0;
-              const double n = window(q.x, q.y, it.lo, it.hi, sb);
+              window_rows(q.x, q.y, it.lo, it.hi, rows);
+              double n = 0.0;
+              for (int r : rows) n += r;
               if (n <= 0.0) continue;
-              kept.push_back({n, q});
+              const int parts = (int)std::ceil(n / SPLIT_PRIMQ);
+              const double target = n / parts;
+              int r0 = 0;
+              double acc = 0.0;
+              for (int r = 0; r < (int)rows.size(); ++r) {
+                acc += rows[r];
+                const bool last = r + 1 == (int)rows.size();
+                if (acc > 0.0 && (acc >= target || last)) {
+                  kept.push_back({acc, make_int4(q.x, q.y, r0, last ? 1 << 30 : r + 1)});
+                  it.flops_fwd += eri_flops(0, a, c, acc, pairs[q.x].nop, pairs[q.y].nop);
+                  it.flops_grad += eri_flops(3, a, c, acc, pairs[q.x].nop, pairs[q.y].nop);
+                  r0 = r + 1;
+                  acc = 0.0;
+                } else if (acc == 0.0) {
+                  r0 = r + 1;
+                }
+              }
               it.nprimq += n;
-              it.flops_fwd += eri_flops(0, a, c, n, pairs[q.x].nop, pairs[q.y].nop);
-              it.flops_grad += eri_flops(3, a, c, n, pairs[q.x].nop, pairs[q.y].nop);
             }
             if (kept.empty()) continue;
-            std::stable_sort(kept.begin(), kept.end(), [](const std::pair<double, int2> &x,
-                                                          const std::pair<double, int2> &y) { return x.first > y.first; });
-            std::vector<int2> lst(kept.size());
+            std::stable_sort(kept.begin(), kept.end(), [](const std::pair<double, int4> &x,
+                                                          const std::pair<double, int4> &y) { return x.first > y.first; });
+            std::vector<int4> lst(kept.size());
             for (size_t k = 0; k < kept.size(); ++k) lst[k] = kept[k].second;
             it.wl = (int)iwl.size();
             iwl.push_back(std::move(lst));
@@ -953,7 +986,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
       return x.flops_fwd > y.flops_fwd;
     });
     h->item_wh = std::move(iwl);
-    h->item_wd = std::vector<DBuf<int2>>(h->item_wh.size());
+    h->item_wd = std::vector<DBuf<int4>>(h->item_wh.size());
     for (size_t k = 0; k < h->item_wh.size(); ++k) CK(h->item_wd[k].upload(h->item_wh[k]), "upload item work");
   }
 
