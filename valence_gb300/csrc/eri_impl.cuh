@@ -283,20 +283,49 @@ constexpr int ne_c(int la, int lb) {
  * A, k <= LCD on the ket centre C, by the Rys recurrences.  The horizontal
  * transfers to the second centres are not done here: they are folded into
  * the weight tables (X' = X M), so the components contracted are (e0|f0). */
+/* a*b + c in R: FMA for float/double; for df64 the product's error terms
+ * come from FMAs and are added with c under one TwoSum and one final
+ * renormalisation (15 FP32 operations against 18 for a product then a sum) */
+__device__ __forceinline__ float mad_r(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double mad_r(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ df64 mad_r(df64 a, df64 b, df64 c) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float s = p + c.hi;
+  const float v = s - p;
+  const float t = ((p - (s - v)) + (c.hi - v)) + (e + c.lo);
+  return df_quick(s, t);
+}
+
 template <int LAB, int LCD, typename R, int STRIDE>
 __device__ __forceinline__ void rys_g(R g00, R c00, R d00, R b00, R b10, R b01, R *__restrict__ out) {
+  /* integer multiples of the coefficients, formed once */
+  R ib10[LAB > 1 ? LAB : 1], ib00[LAB + 1], kb01[LCD > 1 ? LCD : 1];
+#pragma unroll
+  for (int i = 1; i < LAB; ++i) ib10[i] = R(i) * b10;
+#pragma unroll
+  for (int i = 1; i <= LAB; ++i) ib00[i] = R(i) * b00;
+#pragma unroll
+  for (int k = 1; k < LCD; ++k) kb01[k] = R(k) * b01;
   R G[LAB + 1][LCD + 1];
   G[0][0] = g00;
 #pragma unroll
-  for (int i = 0; i < LAB; ++i) G[i + 1][0] = c00 * G[i][0] + (i > 0 ? R(i) * b10 * G[i > 0 ? i - 1 : 0][0] : R(0));
+  for (int i = 0; i < LAB; ++i)
+    G[i + 1][0] = i > 0 ? mad_r(c00, G[i][0], ib10[i > 0 ? i : 0] * G[i > 0 ? i - 1 : 0][0]) : c00 * G[0][0];
 #pragma unroll
   for (int k = 0; k < LCD; ++k) {
 #pragma unroll
     for (int i = 0; i <= LAB; ++i) {
-      R v = d00 * G[i][k];
-      if (k > 0) v += R(k) * b01 * G[i][k > 0 ? k - 1 : 0];
-      if (i > 0) v += R(i) * b00 * G[i > 0 ? i - 1 : 0][k];
-      G[i][k + 1] = v;
+      R t;
+      if (k > 0 && i > 0)
+        t = mad_r(kb01[k > 0 ? k : 0], G[i][k > 0 ? k - 1 : 0], ib00[i] * G[i > 0 ? i - 1 : 0][k]);
+      else if (k > 0)
+        t = kb01[k > 0 ? k : 0] * G[i][k > 0 ? k - 1 : 0];
+      else if (i > 0)
+        t = ib00[i] * G[i > 0 ? i - 1 : 0][k];
+      G[i][k + 1] = (k > 0 || i > 0) ? mad_r(d00, G[i][k], t) : d00 * G[i][k];
     }
   }
 #pragma unroll
