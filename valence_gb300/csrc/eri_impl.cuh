@@ -25,7 +25,7 @@
  * of the n_r roots in shared memory, then lanes accumulate their share of
  * the (e0|f0) components in registers.  Small blocks run G primitive
  * quartets side by side in one warp, each with its own accumulators (one
- * warp per shell quartet); large blocks (>= 200 components) put a whole CTA
+ * warp per shell quartet); blocks of >= 80 components put a whole CTA
  * on one shell quartet, its warps splitting the primitive quartets and each
  * warp building the tables of G2 primitive quartets at once into one set of
  * accumulators.  After the primitive loop the block is staged in shared
@@ -385,7 +385,7 @@ struct QuartetShape {
    * the slots, so that the registers stay bounded, and put the CTA's warps on
    * one shell quartet */
   static constexpr int G0 = 32 / (3 * NR) < 1 ? 1 : 32 / (3 * NR);
-  static constexpr bool CTA = NCOMP >= 200;
+  static constexpr bool CTA = NCOMP >= 80;
   static constexpr int G = CTA ? 1 : G0;
   static constexpr int G2 = G0;
   static constexpr int NITEM = G * NCOMP;
