@@ -481,8 +481,10 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
     const int g = lane / (3 * S::NR), rem = lane - g * (3 * S::NR);
     const int r = rem / 3, dir = rem - 3 * (rem / 3);
     const bool lane_a = g < S::G2;
-    /* this warp's chunks of 32 primitive quartets */
-    const int cfirst = CTA ? warp * 32 : 0;
+    /* rounds of 32 candidate primitive quartets per warp; in CTA mode a
+     * round covers 32*WARPS consecutive candidates interleaved over the warps
+     * (stride WARPS), so that the survivors -- concentrated at low indices by
+     * the sorted primitives -- spread evenly over the warps */
     const int cstep = CTA ? WARPS * 32 : 32;
     R *rx = reinterpret_cast<R *>(ws + S::SM_2D); /* [32][NR] roots */
     R *rw = rx + 32 * S::NR;                      /* [32][NR] scaled weights */
@@ -492,14 +494,15 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
     /* FP32 sums are taken smallest first: the chunks (and the quartets in a
      * chunk) in reverse, against the descending order of the bounds */
     constexpr bool ASC = std::is_same<R, float>::value;
-    const int nchunk = npq > cfirst ? (npq - cfirst + cstep - 1) / cstep : 0;
+    const int nchunk = (npq + cstep - 1) / cstep;
     for (int kc = 0; kc < nchunk; ++kc) {
-      const int chunk = cfirst + (ASC ? nchunk - 1 - kc : kc) * cstep;
+      const int round = ASC ? nchunk - 1 - kc : kc;
+      const int cand = CTA ? round * cstep + lane * WARPS + warp : round * cstep + lane;
       /* compaction: the chunk's primitive quartets that pass the screen */
       int nch;
       {
-        const int pqi = pq_begin + chunk + lane;
-        bool keep = chunk + lane < npq;
+        const int pqi = pq_begin + cand;
+        bool keep = cand < npq;
         if (keep && (eps > 0.f || eps_hi < INFINITY)) {
           const int ip = pqi / Q.nprim, iq = pqi - ip * Q.nprim;
           const float b = args.prim_q0[P.prim0 + ip] * args.prim_q0[Q.prim0 + iq];
