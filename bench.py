@@ -51,9 +51,9 @@ METRIC = "VSVB energy+grad evals/s, mixed vs plain FP64 on 1 GB300 at |ΔE|<=1e-
 # (keys: workload, 100*kind + 10*bra pair class + ket pair class; kind 2 =
 # double-float, pair classes ss ps pp ds dp dd = 0..5)
 PROFILED_TRAFFIC = {  # profiles/eri_df64_ch_chain.md
-    ("ch_chain", 253): 1.232128e6 + 0.0,  # (dd|ds) double-float, forward + adjoint
-    ("ch_chain", 254): 1.264128e6 + 0.0,  # (dd|dp)
-    ("ch_chain", 255): 0.840448e6 + 0.0,  # (dd|dd)
+    ("ch_chain", 253): 1.254656e6 + 0.0,  # (dd|ds) double-float, forward + adjoint
+    ("ch_chain", 254): 1.284096e6 + 0.0,  # (dd|dp)
+    ("ch_chain", 255): 0.847104e6 + 0.0,  # (dd|dd)
 }
 
 
