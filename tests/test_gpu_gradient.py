@@ -88,7 +88,9 @@ def test_torch_autograd_function(vg, tmp_path):
     e.backward()
     r, g = s.energy_grad()
     assert abs(e.item() - r["energy"]) < 1e-12
-    assert np.allclose(w.grad.numpy(), g, rtol=0, atol=1e-12)
+    # the two calls differ only in the order of floating-point atomics
+    d = np.abs(w.grad.numpy() - g).max()
+    assert d < 1e-11 * max(1.0, np.abs(g).max()), d
 
 
 def test_mixed_precision_error_bound(vg, tmp_path):

@@ -464,10 +464,15 @@ __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
  * MODE 1: adjoint walk: dE/dS_orb, dE/dh_orb, per-pair dJ/dT; dE/dT as well
  *         unless a.skip_tbar.
  * MODE 2: unscreened density walk: Tbar += fac*dd at (ik,jl) and -fac*xd at
- *         (il,jk), unscaled by 1/W, for the single-sweep adjoint. */
+ *         (il,jk), unscaled by 1/W, for the single-sweep adjoint.
+ * MODE 4: MODE 0 and MODE 1 (without dE/dT) in one walk, for the fused
+ *         energy + gradient: the adjoint quantities are accumulated without
+ *         1/W and E_num/W^2 -- those come later from the reduced energy
+ *         (grad_scale_kernel) -- so the walk need not wait for it. */
 template <int MODE>
 __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
-  constexpr bool GRAD = MODE == 1;
+  constexpr bool UNSC = MODE == 4;
+  constexpr bool GRAD = MODE == 1 || UNSC;
   constexpr bool DENS = MODE == 2;
   __shared__ double red[8];
   extern __shared__ double gsh[];
@@ -494,9 +499,9 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
       Gb = Ga + na * na;
     }
   }
-  double e1 = 0.0, wf = 0.0, e2 = 0.0, vtot = 0.0;
-  double inv_w = a.inv_w, dw_coef = a.dw_coef;
-  if (GRAD && a.res) {
+  double e1 = 0.0, wf = 0.0, e2 = 0.0, vtot = 0.0, vtot_s = 0.0;
+  double inv_w = UNSC ? 1.0 : a.inv_w, dw_coef = UNSC ? 0.0 : a.dw_coef;
+  if (MODE == 1 && a.res) {
     const double W = a.res[4];
     inv_w = 1.0 / W;
     dw_coef = -a.res[1] / (W * W * (double)nelec);
@@ -515,7 +520,16 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
     const double h = d.Ho[si * nsp + sj], s = d.So[si * nsp + sj];
     e1 += h * c.v;
     wf += s * c.v;
-    if (GRAD) {
+    if (UNSC) {
+      /* dE/dh part (scaled by 1/W later) and dE/dS part (scaled by
+       * -E_num/(W^2 nelec) later) kept apart */
+      vtot += h * c.v;
+      vtot_s += s * c.v;
+      accum_G(d, q, qi, c, h, Ga, Gb, lda, ldb);
+      double *Gsa = a.Gs + (size_t)q * (na * na + nb * nb);
+      accum_G(d, q, qi, c, s, Gsa, Gsa + na * na, na, nb);
+      atomicAdd(a.D1 + si * nsp + sj, c.v);
+    } else if (GRAD) {
       const double coef = h * inv_w + dw_coef * s;
       vtot += coef * c.v;
       accum_G(d, q, qi, c, coef, Ga, Gb, lda, ldb);
@@ -658,6 +672,15 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
   wf = block_sum_d(wf, red);
   e2 = block_sum_d(e2, red);
   const size_t slot = (size_t)q * nsplit + split;
+  if (UNSC) {
+    vtot_s = block_sum_d(vtot_s, red);
+    if (threadIdx.x == 0) {
+      a.vtot_s[slot] = vtot_s;
+      a.part_e1[slot] = e1;
+      a.part_wf[slot] = wf;
+      a.part_e2[slot] = e2;
+    }
+  }
   if (GRAD) {
     vtot = block_sum_d(vtot, red);
     if (threadIdx.x == 0) a.vtot[slot] = vtot;
@@ -735,11 +758,38 @@ __global__ void detpair_adjoint_kernel(DetCtx d, AsmArgs a, int nsplit) {
   }
 }
 
+/* after the MODE 4 walk and the energy reduction: dJ/dT, vtot, dE/dh and
+ * dE/dS with 1/W and -E_num/(W^2 nelec) applied (one block per determinant
+ * pair; block 0 also writes Hbar and Sbar over the orbital pairs) */
+__global__ void grad_scale_kernel(DetCtx d, AsmArgs a, int nsplit) {
+  const long long q = blockIdx.x;
+  const double W = a.res[4];
+  const double inv_w = 1.0 / W, dw = -a.res[1] / (W * W * (double)d.ds.nelec);
+  const int ng = d.ds.nalpha * d.ds.nalpha + d.ds.nbeta * d.ds.nbeta;
+  double *G = a.Gglob + (size_t)q * ng;
+  const double *Gs = a.Gs + (size_t)q * ng;
+  for (int t = threadIdx.x; t < ng; t += blockDim.x) G[t] = inv_w * G[t] + dw * Gs[t];
+  for (int s = threadIdx.x; s < nsplit; s += blockDim.x) {
+    const size_t slot = (size_t)q * nsplit + s;
+    a.vtot[slot] = inv_w * a.vtot[slot] + dw * a.vtot_s[slot];
+  }
+  if (q == 0) {
+    const int n2 = d.ds.nsp * d.ds.nsp;
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+      a.Hbar[t] = inv_w * a.D1[t];
+      a.Sbar[t] = dw * a.D1[t];
+    }
+  }
+}
+
 cudaError_t launch_assemble(int mode, dim3 grid, int threads, size_t smem, cudaStream_t st, const DetCtx &d,
                             const AsmArgs &a) {
   if (mode == 1) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(assemble_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     assemble_kernel<1><<<grid, threads, smem, st>>>(d, a);
+  } else if (mode == 4) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(assemble_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    assemble_kernel<4><<<grid, threads, smem, st>>>(d, a);
   } else if (mode == 2) {
     assemble_kernel<2><<<grid, threads, 0, st>>>(d, a);
   } else {

@@ -33,6 +33,10 @@ struct AsmArgs {
   double *Gglob;           /* [nq][na*na + nb*nb] */
   int g_in_smem;            /* copies of G per block in shared memory (0: G in global memory) */
   int skip_tbar; /* adjoint walk without dE/dT (single-sweep mode) */
+  /* MODE 4 (unscaled adjoint walk): the dE/dS parts kept apart */
+  double *Gs;     /* [nq][na*na + nb*nb] */
+  double *vtot_s; /* [nq * nsplit] */
+  double *D1;     /* [nsp*nsp] first-order cofactor densities */
 };
 
 __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch);
@@ -40,4 +44,5 @@ cudaError_t launch_assemble(int mode, dim3 grid, int threads, size_t smem, cudaS
                             const AsmArgs &a);
 __global__ void energy_reduce_kernel(AsmArgs a, long long nslot, int nelec, double enuc, double *out);
 __global__ void detpair_adjoint_kernel(DetCtx d, AsmArgs a, int nsplit);
+__global__ void grad_scale_kernel(DetCtx d, AsmArgs a, int nsplit);
 #endif

@@ -208,6 +208,7 @@ struct vsvb_gpu {
   DBuf<double> part_e1, part_wf, part_e2, result;
   /* adjoint */
   DBuf<double> Tbar, Sbar, Hbar, xbar, xbarh, Cbar, vtot, Gglob, coeff_bar;
+  DBuf<double> Gs, vtot_s, D1; /* dE/dS parts of the fused (unscaled) adjoint walk */
   bool grad_ready = false;
   int last_singular = 0;
 };
@@ -332,6 +333,9 @@ AsmArgs asm_args(vsvb_gpu *h) {
   a.Hbar = h->Hbar.p;
   a.vtot = h->vtot.p;
   a.Gglob = h->Gglob.p;
+  a.Gs = h->Gs.p;
+  a.vtot_s = h->vtot_s.p;
+  a.D1 = h->D1.p;
   int na = h->ds.nalpha, nb = h->ds.nbeta;
   {
     /* dJ/dT accumulators: one copy per warp of the 128-thread block when
@@ -1075,6 +1079,9 @@ int alloc_grad(vsvb_gpu *h) {
   CK(h->Cbar.alloc((size_t)h->norb_all * h->maxobs), "alloc Cbar");
   CK(h->vtot.alloc((size_t)nq * h->nsplit_max), "alloc vtot");
   CK(h->Gglob.alloc(std::max<long long>(nq * (na * na + nb * nb), 1)), "alloc G");
+  CK(h->Gs.alloc(std::max<long long>(nq * (na * na + nb * nb), 1)), "alloc Gs");
+  CK(h->vtot_s.alloc((size_t)nq * h->nsplit_max), "alloc vtot_s");
+  CK(h->D1.alloc((size_t)h->nsp * h->nsp), "alloc D1");
   CK(h->coeff_bar.alloc(h->totlen), "alloc coeff_bar");
   h->grad_ready = true;
   return VSVB_OK;
@@ -1181,7 +1188,19 @@ int forward(vsvb_gpu *h, bool fused = false) {
   }
   h->launches++;
   AsmArgs aa = asm_args(h);
-  CK(launch_assemble(0, dim3((unsigned)h->ds.nq, h->nsplit), 128, 0, st, dc, aa), "assemble");
+  if (fused) {
+    /* one walk for the energy sums and the (unscaled) adjoint quantities */
+    const int na = h->ds.nalpha, nb = h->ds.nbeta;
+    CK(cudaMemsetAsync(h->Gglob.p, 0, sizeof(double) * h->Gglob.n, st), "memset G");
+    CK(cudaMemsetAsync(h->Gs.p, 0, sizeof(double) * h->Gs.n, st), "memset Gs");
+    CK(cudaMemsetAsync(h->D1.p, 0, sizeof(double) * h->D1.n, st), "memset D1");
+    aa.status = h->status.p;
+    aa.skip_tbar = 1;
+    const size_t gsh = sizeof(double) * (size_t)(na * na + nb * nb) * aa.g_in_smem;
+    CK(launch_assemble(4, dim3((unsigned)h->ds.nq, h->nsplit), 128, gsh, st, dc, aa), "energy + adjoint walk");
+  } else {
+    CK(launch_assemble(0, dim3((unsigned)h->ds.nq, h->nsplit), 128, 0, st, dc, aa), "assemble");
+  }
   energy_reduce_kernel<<<1, 256, 0, st>>>(aa, h->ds.nq * h->nsplit, h->ds.nelec, h->enuc, h->result.p);
   CK(cudaGetLastError(), "reduce");
   h->launches += 2;
@@ -1334,18 +1353,24 @@ int backward(vsvb_gpu *h, bool fused) {
     CK(cudaMemsetAsync(h->Tbar.p, 0, sizeof(double) * h->Tbar.n, st), "memset");
     CK(cudaMemsetAsync(h->xbarh.p, 0, sizeof(double) * h->xbarh.n, st), "memset");
   }
-  CK(cudaMemsetAsync(h->Sbar.p, 0, sizeof(double) * h->Sbar.n, st), "memset");
-  CK(cudaMemsetAsync(h->Hbar.p, 0, sizeof(double) * h->Hbar.n, st), "memset");
   CK(cudaMemsetAsync(h->Cbar.p, 0, sizeof(double) * h->Cbar.n, st), "memset");
-  CK(cudaMemsetAsync(h->Gglob.p, 0, sizeof(double) * h->Gglob.n, st), "memset");
   CK(cudaMemsetAsync(h->coeff_bar.p, 0, sizeof(double) * h->coeff_bar.n, st), "memset");
   DetCtx dc = det_ctx(h);
   AsmArgs aa = asm_args(h);
   aa.status = h->status.p;
   aa.res = h->result.p;
-  aa.skip_tbar = fused ? 1 : 0;
-  size_t gsh = sizeof(double) * (size_t)(na * na + nb * nb) * aa.g_in_smem;
-  CK(launch_assemble(1, dim3((unsigned)h->ds.nq, h->nsplit), 128, gsh, st, dc, aa), "assemble grad");
+  if (fused) {
+    /* the forward walk accumulated the adjoint quantities unscaled */
+    grad_scale_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, aa, h->nsplit);
+    CK(cudaGetLastError(), "grad scale");
+  } else {
+    CK(cudaMemsetAsync(h->Sbar.p, 0, sizeof(double) * h->Sbar.n, st), "memset");
+    CK(cudaMemsetAsync(h->Hbar.p, 0, sizeof(double) * h->Hbar.n, st), "memset");
+    CK(cudaMemsetAsync(h->Gglob.p, 0, sizeof(double) * h->Gglob.n, st), "memset");
+    aa.skip_tbar = 0;
+    size_t gsh = sizeof(double) * (size_t)(na * na + nb * nb) * aa.g_in_smem;
+    CK(launch_assemble(1, dim3((unsigned)h->ds.nq, h->nsplit), 128, gsh, st, dc, aa), "assemble grad");
+  }
   detpair_adjoint_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, aa, h->nsplit);
   CK(cudaGetLastError(), "detpair adjoint");
   if (!fused) {
