@@ -445,6 +445,18 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   }
   __syncthreads();
 
+  /* FP32 CTA kernels keep their components' packed table offsets in
+   * registers (they have the room; the shared-memory load in front of the
+   * three dependent table loads otherwise dominates their stalls) */
+  constexpr bool HOIST = CTA && std::is_same<R, float>::value;
+  int idr[HOIST ? S::PER_LANE : 1];
+  if constexpr (HOIST) {
+#pragma unroll
+    for (int m = 0; m < S::PER_LANE; ++m) {
+      const int c = lane + 32 * m;
+      idr[m] = c < S::NCOMP ? idx[c] : 0;
+    }
+  }
   R *h2d = reinterpret_cast<R *>(ws);
   const double two_pi_25 = 34.98683665524972; /* 2 pi^(5/2) */
   const PrimT<R> *__restrict__ primR = static_cast<const PrimT<R> *>(prec_data<R>::prim(args));
@@ -641,7 +653,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
             for (int m = 0; m < S::PER_LANE; ++m) {
               const int c = lane + 32 * m;
               if (c < S::NCOMP) {
-                const int id = idx[c];
+                const int id = HOIST ? idr[HOIST ? m : 0] : idx[c];
                 R x[S::VEC], y[S::VEC], z[S::VEC];
                 ldv<S::VEC>(hx + (id & 1023) * S::NRP, x);
                 ldv<S::VEC>(hx + DS + ((id >> 10) & 1023) * S::NRP, y);
