@@ -133,6 +133,19 @@ void vsvb_default_options(vsvb_options *opt);
 int vsvb_read_input(const char *path, vsvb_system_desc **desc, char *err, int errlen);
 void vsvb_free_desc(vsvb_system_desc *desc);
 
+/* The reference's 'orbitals' output (xm_output, xm_module.F90:464-577): per
+ * orbital -- spin-coupled, unpaired, doubly occupied, then after a blank
+ * line the derived basis functions -- format(5x,i2,5x,10i4) with the atom
+ * list and length and format(4(i4,1x,f13.8)) with the (basis index, weight)
+ * pairs, then the total energy (and, with done, the convergence line).
+ * coeff: weights to write (NULL: desc->coeff).  vsvb_format_orbitals writes
+ * the text to buf (cap bytes including the terminating zero; NULL buf: only
+ * *len); vsvb_write_orbitals writes it to a file. */
+int vsvb_format_orbitals(const vsvb_system_desc *desc, const double *coeff, double energy, double etol, int done,
+                         char *buf, long cap, long *len);
+int vsvb_write_orbitals(const char *path, const vsvb_system_desc *desc, const double *coeff, double energy,
+                        double etol, int done);
+
 /* Build a handle: normalises primitives (norm_prim, valence.F90:2264-2305),
  * builds the shell-pair tables, AO one-electron matrices, Schwarz bounds and
  * quartet schedules on the GPU.  Replaces the set-up half of

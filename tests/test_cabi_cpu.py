@@ -147,3 +147,70 @@ def test_bench_reference_arm_two_gloo_ranks():
     j = lines[0]
     assert j["impl"] == "reference" and j["n_gpus"] == 2 and j["value"] > 0
     assert j["cpu_baseline"]["kind"] == "port"
+
+
+def test_orbitals_writer_reproduces_reference_sections(lib):
+    """vsvb_format_orbitals (xm_output's format(5x,i2,5x,10i4) and
+    format(4(i4,1x,f13.8))) against the orbital sections of the golden
+    inputs that xm_output wrote: every line, byte for byte, in order."""
+    from valence_gb300 import api
+    matched = 0
+    for c in oracle_py.goldens()["cases"]:
+        path = os.path.join(oracle_py.GOLDEN, c["input"])
+        d = api.read_input(path)
+        txt = api.format_orbitals(d)
+        lib.vsvb_free_desc(d)
+        lines = [ln for ln in txt.split("\n total energy")[0].split("\n") if ln.strip()]
+        src = open(path).read().split("\n")
+        if lines[0] not in src or lines[1] not in src:
+            continue  # a hand-written or older-layout orbital section
+        pos = 0
+        for ln in lines:
+            assert ln in src[pos:], (c["name"], ln)
+            pos = src.index(ln, pos) + 1
+        matched += 1
+    assert matched >= 35
+
+
+def test_orbitals_writer_energy_trailer(lib):
+    """format(/,1x,'total energy in atomic units ',f32.16) and
+    format(1x,'converged to ',e10.2,' kCal/mol') as the reference wrote them
+    at the end of testing/be-sv."""
+    from valence_gb300 import api
+    path = os.path.join(oracle_py.GOLDEN, "cases", "testing", "be-sv")
+    d = api.read_input(path)
+    txt = api.format_orbitals(d, energy=-14.5763526671381989, etol=1e-6, done=True)
+    lib.vsvb_free_desc(d)
+    lines = txt.split("\n")
+    src = open(path).read().split("\n")
+    k = lines.index(" total energy in atomic units             -14.5763526671381989")
+    assert lines[k - 1] == "" and lines[k + 1] == " converged to   0.10E-05 kCal/mol"
+    j = src.index(lines[k])
+    assert src[j - 1:j + 2] == lines[k - 1:k + 2]
+    d = api.read_input(path)
+    txt = api.format_orbitals(d, energy=-1.0, etol=1e-4, done=False)
+    lib.vsvb_free_desc(d)
+    assert "converged" not in txt
+
+
+def test_orbitals_writer_round_trip(lib, tmp_path):
+    """Weights written with f13.8 read back within rounding."""
+    import numpy as np
+    from valence_gb300 import api
+    path = os.path.join(oracle_py.GOLDEN, "cases", "testing", "h2o-vdz")
+    d = api.read_input(path)
+    dd = d.contents
+    w = np.random.default_rng(5).uniform(-1, 1, dd.totlen)
+    out = tmp_path / "orbitals"
+    assert lib.vsvb_write_orbitals(str(out).encode(), d, w.ctypes.data_as(api.ctypes.POINTER(api.ctypes.c_double)),
+                                   -76.0, 0.0, 0) == 0
+    vals = []
+    for ln in open(out).read().split("\n"):
+        if "total energy" in ln or not ln.strip():
+            continue
+        if ln.startswith("     ") and ln[5:7].strip() and ln[7:12] == "     ":
+            continue  # an atom-list record
+        for k in range(0, len(ln), 18):
+            vals.append(float(ln[k + 5:k + 18]))
+    lib.vsvb_free_desc(d)
+    assert np.max(np.abs(np.array(vals) - w)) <= 5.1e-9

@@ -99,6 +99,9 @@ def lib():
         L.vsvb_det_factor.argtypes = [ctypes.c_void_p, I, I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_void_p]
         L.vsvb_det_factor_noalloc.argtypes = L.vsvb_det_factor.argtypes
+        L.vsvb_format_orbitals.argtypes = [P(Desc), P(D), D, D, I, ctypes.c_char_p, ctypes.c_long,
+                                           P(ctypes.c_long)]
+        L.vsvb_write_orbitals.argtypes = [ctypes.c_char_p, P(Desc), P(D), D, D, I]
         L.vsvb_batch_create.argtypes = [P(ctypes.c_void_p), I, P(ctypes.c_void_p)]
         L.vsvb_batch_energy_grad.argtypes = [ctypes.c_void_p, P(ctypes.c_void_p), P(ctypes.c_void_p), P(Result),
                                              ctypes.c_void_p]
@@ -108,6 +111,23 @@ def lib():
         L.vsvb_batch_destroy.argtypes = [ctypes.c_void_p]
         _LIB = L
     return _LIB
+
+
+def format_orbitals(desc, coeff=None, energy=0.0, etol=0.0, done=False):
+    """The reference's 'orbitals' file text (xm_output) for a parsed input
+    description (read_input) and optional new weights."""
+    c = None if coeff is None else np.ascontiguousarray(coeff, dtype=np.float64)
+    n = ctypes.c_long()
+    rc = lib().vsvb_format_orbitals(desc, None if c is None else _dptr(c), energy, etol, int(done), None, 0,
+                                    ctypes.byref(n))
+    if rc:
+        raise VSVBError(f"format_orbitals failed ({rc})")
+    buf = ctypes.create_string_buffer(n.value + 1)
+    rc = lib().vsvb_format_orbitals(desc, None if c is None else _dptr(c), energy, etol, int(done), buf,
+                                    n.value + 1, ctypes.byref(n))
+    if rc:
+        raise VSVBError(f"format_orbitals failed ({rc})")
+    return buf.value.decode()
 
 
 def _dptr(a):

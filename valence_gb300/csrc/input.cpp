@@ -293,3 +293,117 @@ extern "C" void vsvb_free_desc(vsvb_system_desc *d) {
   /* d is the first member of Owned */
   delete reinterpret_cast<Owned *>(d);
 }
+
+/* ---- the orbitals file (xm_output, xm_module.F90:464-577) ---------------- */
+
+namespace {
+
+/* Fortran Iw: right-justified, '*' fill when it does not fit */
+void fort_i(std::string &o, long v, int w) {
+  char b[64];
+  const int n = std::snprintf(b, sizeof b, "%ld", v);
+  if (n > w) o.append(w, '*');
+  else o.append(w - n, ' ').append(b);
+}
+
+/* Fortran Fw.d */
+void fort_f(std::string &o, double v, int w, int d) {
+  char b[128];
+  const int n = std::snprintf(b, sizeof b, "%*.*f", w, d, v);
+  if (n > w) o.append(w, '*');
+  else o.append(b);
+}
+
+/* Fortran Ew.d: [-]0.ddE+ee right-justified */
+void fort_e(std::string &o, double v, int w, int d) {
+  char b[128];
+  if (v == 0.0) {
+    std::snprintf(b, sizeof b, "0.%0*dE+00", d, 0);
+  } else {
+    int e = (int)std::floor(std::log10(std::fabs(v))) + 1;
+    double m = std::fabs(v) / std::pow(10.0, e);
+    /* rounding may carry the mantissa to 1.0 */
+    const double scale = std::pow(10.0, d);
+    double mr = std::round(m * scale) / scale;
+    if (mr >= 1.0) {
+      mr /= 10.0;
+      ++e;
+    }
+    std::snprintf(b, sizeof b, "%s0.%0*ldE%c%02d", v < 0 ? "-" : "", d, (long)std::llround(mr * scale),
+                  e < 0 ? '-' : '+', e < 0 ? -e : e);
+  }
+  const int n = (int)std::strlen(b);
+  if (n > w) o.append(w, '*');
+  else o.append(w - n, ' ').append(b);
+}
+
+/* one orbital: format(5x,1i2,5x,10i4) for the atom list and length, then
+ * format(4(1i4,1x,1f13.8)) for its (xpset, coeff) pairs; both with Fortran
+ * format reversion (a new record per exhausted format) */
+void orbital_block(std::string &o, const vsvb_system_desc *d, const double *coeff, int i) {
+  const int natl = d->orbas_atnum[i];
+  std::vector<long> items;
+  items.push_back(natl);
+  for (int j = 0; j < natl; ++j) items.push_back(d->orbas_atset[(size_t)i * d->mxctr + j]);
+  const int b = d->map_orbs[i] - 1, e = d->map_orbs[i + 1] - 1;
+  items.push_back(e - b);
+  size_t k = 0;
+  while (k < items.size()) {
+    o.append(5, ' ');
+    fort_i(o, items[k++], 2);
+    o.append(5, ' ');
+    for (int f = 0; f < 10 && k < items.size(); ++f) fort_i(o, items[k++], 4);
+    o.push_back('\n');
+  }
+  for (int j = b; j < e;) {
+    for (int f = 0; f < 4 && j < e; ++f, ++j) {
+      fort_i(o, d->xpset[j], 4);
+      o.push_back(' ');
+      fort_f(o, coeff[j], 13, 8);
+    }
+    o.push_back('\n');
+  }
+}
+
+}  // namespace
+
+extern "C" int vsvb_format_orbitals(const vsvb_system_desc *d, const double *coeff, double energy, double etol,
+                                    int done, char *buf, long cap, long *len) {
+  if (!d || (!buf && cap > 0)) return VSVB_ERR_INPUT;
+  const double *c = coeff ? coeff : d->coeff;
+  const int norbs = 2 * d->npair + d->nunpd + d->ndocc;
+  std::string o;
+  /* spin-coupled, unpaired and doubly occupied orbitals, then the NDF */
+  for (int i = 0; i < norbs; ++i) orbital_block(o, d, c, i);
+  o.push_back('\n');
+  for (int i = norbs; i < norbs + d->ndf; ++i) orbital_block(o, d, c, i);
+  o.append("\n total energy in atomic units ");
+  fort_f(o, energy, 32, 16);
+  o.push_back('\n');
+  if (done) {
+    o.append(" converged to ");
+    fort_e(o, etol, 10, 2);
+    o.append(" kCal/mol\n");
+  }
+  o.push_back('\n');
+  if (len) *len = (long)o.size();
+  if (!buf) return VSVB_OK;
+  if ((long)o.size() + 1 > cap) return VSVB_ERR_TOO_LARGE;
+  std::memcpy(buf, o.c_str(), o.size() + 1);
+  return VSVB_OK;
+}
+
+extern "C" int vsvb_write_orbitals(const char *path, const vsvb_system_desc *d, const double *coeff, double energy,
+                                   double etol, int done) {
+  if (!path) return VSVB_ERR_INPUT;
+  long n = 0;
+  int rc = vsvb_format_orbitals(d, coeff, energy, etol, done, nullptr, 0, &n);
+  if (rc) return rc;
+  std::vector<char> b((size_t)n + 1);
+  rc = vsvb_format_orbitals(d, coeff, energy, etol, done, b.data(), n + 1, &n);
+  if (rc) return rc;
+  FILE *f = std::fopen(path, "w");
+  if (!f) return VSVB_ERR_INPUT;
+  const bool ok = std::fwrite(b.data(), 1, (size_t)n, f) == (size_t)n;
+  return std::fclose(f) == 0 && ok ? VSVB_OK : VSVB_ERR_INPUT;
+}
