@@ -945,31 +945,20 @@ int vo_guess_energy_sampled(vo_input *in, vo_result *res, int nthreads, long lon
   return rc;
 }
 
-int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
-  memset(res, 0, sizeof(*res));
+/* calculate_vsvb_energy / guess_energy set-up shared by every entry point
+ * (valence.F90:70-182, 309-336): the state, the weights normalised in place
+ * by normal() (NDFs first, then the orbitals, :144-145, 2157-2182) and the
+ * nuclear repulsion (tools_module.F90:19-40) */
+static vo_state *prepare(vo_input *in, double *enuc) {
   if (g_last_state) {
     state_free(g_last_state);
     g_last_state = NULL;
   }
   memcpy(in->coeff, in->coeff_raw, sizeof(double) * in->totlen);
   vo_state *st = state_new(in);
-  /* nuclear repulsion (tools_module.F90:19-40) */
-  double nre = 0.0;
-  for (int i = 2; i <= in->natom; ++i)
-    for (int j = 1; j <= i - 1; ++j) {
-      double zij = in->nuc_charge[in->atom_t[i - 1] - 1] * in->nuc_charge[in->atom_t[j - 1] - 1];
-      if (fabs(zij) > 1e-12) {
-        double rsq = 0.0;
-        for (int d = 0; d < 3; ++d) {
-          double x = in->coords[3 * (i - 1) + d] - in->coords[3 * (j - 1) + d];
-          rsq += x * x;
-        }
-        if (rsq > 1e-5) nre += zij * pow(rsq, -0.5);
-      }
-    }
-  res->enucrep = nre;
+  double nre = vo_nuclear_repulsion(in);
+  *enuc = nre;
   vo_ctx *c0 = ctx_new(st);
-  /* normal(): NDFs first, then the orbitals (valence.F90:144-145, 2157-2182) */
   int nfirst = 2 * in->npair + in->nunpd + in->ndocc + 1;
   for (int i = nfirst; i <= in->norbs; ++i) {
     ovint(c0, i, i);
@@ -981,65 +970,111 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
     double s = pow(c0->sint, -0.5);
     for (int j = in->map_orbs[i - 1]; j <= in->map_orbs[i] - 1; ++j) in->coeff[j - 1] *= s;
   }
-  /* guess_energy bra/ket (valence.F90:324-336) */
+  ctx_free(c0);
+  return st;
+}
+
+/* the bra/ket electron lists of guess_energy / spin_opt (valence.F90:324-336,
+ * 866-879) */
+static void guess_lists(vo_state *st) {
   int nnd = st->nnd;
   for (int i = 1; i <= nnd; ++i) {
     st->bra[i] = i;
     st->ket[i] = i;
   }
-  {
-    int i = nnd + 1;
-    for (int idocc = nnd + 1; idocc <= nnd + in->ndocc; ++idocc) {
-      st->bra[i] = idocc;
-      st->ket[i] = idocc;
-      st->bra[i + 1] = idocc;
-      st->ket[i + 1] = idocc;
-      i += 2;
-    }
+  int i = nnd + 1;
+  for (int idocc = nnd + 1; idocc <= nnd + st->in->ndocc; ++idocc) {
+    st->bra[i] = idocc;
+    st->ket[i] = idocc;
+    st->bra[i + 1] = idocc;
+    st->ket[i + 1] = idocc;
+    i += 2;
   }
+}
+
+static int nthreads_of(int nthreads) {
+  int nth = 1;
+#ifdef _OPENMP
+  nth = nthreads > 0 ? nthreads : omp_get_max_threads();
+#endif
+  (void)nthreads;
+  return nth;
+}
+
+/* wfndet (valence.F90:1440-1480) */
+static void wfndet(vo_state *st, vo_ctx *c0) {
   int nelec = st->nelec;
-  /* wfndet (valence.F90:1440-1480) */
   for (int i = 1; i <= nelec; ++i)
     for (int j = 1; j <= i; ++j) {
       ovint(c0, st->bra[i], st->ket[j]);
       A2(st->wdet, nelec, i, j) = c0->sint;
       A2(st->wdet, nelec, j, i) = c0->sint;
     }
-  /* schwarz_ints (valence.F90:1489-1523); the pairs are independent, so
-   * they are spread over threads like the reference spreads them over ranks
-   * (:1509-1520) */
-  int nsp = st->nsp;
-  int nth = 1;
-#ifdef _OPENMP
-  nth = nthreads > 0 ? nthreads : omp_get_max_threads();
-#endif
-  {
-    long long npairs = ((long long)nsp * nsp + nsp) / 2;
+}
+
+/* schwarz_ints (valence.F90:1489-1523); the pairs are independent, so they
+ * are spread over threads like the reference spreads them over ranks
+ * (:1509-1520) */
+static void schwarz_ints(vo_state *st, int nspat, int nsd, int nth) {
+  long long npairs = ((long long)nspat * nspat + nspat) / 2;
 #pragma omp parallel num_threads(nth)
-    {
-      vo_ctx *cx = ctx_new(st);
-#pragma omp for schedule(dynamic, 1)
-      for (long long t = 0; t < npairs; ++t) {
-        int i, j;
-        long long ii = (long long)sqrt((double)(2 * (t + 1)));
-        while ((ii * ii + ii) / 2 < t + 1) ii++;
-        i = (int)ii;
-        j = (int)(t + 1 - (ii * ii - ii) / 2);
-        int ie = i > nnd ? 2 * i - nnd : i;
-        int je = j > nnd ? 2 * j - nnd : j;
-        int2e(cx, st->bra[ie], st->ket[je], st->bra[ie], st->ket[je]);
-        st->schwarz[indx(i, j)] = sqrt(cx->gint);
-      }
-      ctx_free(cx);
-    }
-  }
-  /* vsvb_energy (valence.F90:1010-1434), iorb=0, spinav=.false.,
-   * ijkl symmetry enabled */
-  state_setup_docc_un(st, c0);
-  double energy = 0.0, wfnorm = 0.0;
   {
-    /* one-electron loop (valence.F90:1072-1101), spread over threads with
-     * per-thread partial sums added in thread order */
+    vo_ctx *cx = ctx_new(st);
+#pragma omp for schedule(dynamic, 1)
+    for (long long t = 0; t < npairs; ++t) {
+      int i, j;
+      long long ii = (long long)sqrt((double)(2 * (t + 1)));
+      while ((ii * ii + ii) / 2 < t + 1) ii++;
+      i = (int)ii;
+      j = (int)(t + 1 - (ii * ii - ii) / 2);
+      int ie = i > nsd ? 2 * i - nsd : i;
+      int je = j > nsd ? 2 * j - nsd : j;
+      int2e(cx, st->bra[ie], st->ket[je], st->bra[ie], st->ket[je]);
+      st->schwarz[indx(i, j)] = sqrt(cx->gint);
+    }
+    ctx_free(cx);
+  }
+}
+
+/* density(spinopt = .true.) (valence.F90:1549-1569): per coupling pair
+ * isc >= jsc, into ham/ovl (nsc x nsc, column-major) */
+static void density_spin(vo_ctx *cx, int nord, double a, double b, double *ham, double *ovl, int cd, int cx_) {
+  vo_input *in = cx->st->in;
+  int nsc = in->nspinc, dima = in->npair + in->ndocc + in->nunpd, dimb = in->npair + in->ndocc;
+  for (int isc = 1; isc <= nsc; ++isc)
+    for (int jsc = 1; jsc <= isc; ++jsc) {
+      double d = 0.0, x = 0.0;
+      dbra(cx, nord, in->npair, in->npair, dima, dimb, &d, &x, isc, jsc, cd, cx_);
+      if (nord == 1) {
+        A2(ham, nsc, isc, jsc) += d * a;
+        A2(ovl, nsc, isc, jsc) += d * b;
+      } else {
+        A2(ham, nsc, isc, jsc) += d * a - x * b;
+      }
+    }
+}
+
+/* vsvb_energy (valence.F90:1010-1434) for the current bra/ket, wdet and
+ * schwarz: nsd = num_non_docc, nspat = num_spatial_orbs, sym =
+ * ijkl_symmetry_is_enabled, jorb = the subject spatial orbital of the
+ * nonsub test (:1200-1207; 0 = none).  With sham/sovl the spinopt sums of
+ * density() are accumulated instead (nsc x nsc). */
+static void vsvb_energy_core(vo_state *st, int nsd, int nspat, int sym, int jorb, int nth, double *e1_out,
+                             double *e2_out, double *wfnorm_out, long long *ndens_out, double *sham, double *sovl) {
+  vo_input *in = st->in;
+  int nelec = st->nelec, nsc = in->nspinc > 0 ? in->nspinc : 1;
+  size_t nsc2 = (size_t)nsc * nsc;
+  {
+    /* set_up_unpaired_docc (:2444-2517) */
+    vo_ctx *c0 = ctx_new(st);
+    state_setup_docc_un(st, c0);
+    ctx_free(c0);
+  }
+  double energy = 0.0, wfnorm = 0.0;
+  double *th = sham ? (double *)calloc(2 * nsc2 * nth, sizeof(double)) : NULL;
+  {
+    /* one-electron loop (:1072-1101), spread over threads with per-thread
+     * partial sums added in thread order */
     double *pe = (double *)calloc(nth, sizeof(double)), *pw = (double *)calloc(nth, sizeof(double));
 #pragma omp parallel num_threads(nth)
     {
@@ -1052,12 +1087,16 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
 #pragma omp for schedule(dynamic, 1)
       for (int t = 0; t < nelec * nelec; ++t) {
         int i = t / nelec + 1, j = t % nelec + 1;
-        int i_docc = i > nnd, j_docc = j > nnd;
+        int i_docc = i > nsd, j_docc = j > nsd;
         if (i_docc && j_docc && (i % 2) != (j % 2)) continue;
         ovint(cx, st->bra[i], st->ket[j]);
         int1e(cx, st->bra[i], st->ket[j]);
         cx->dme_b[1] = i;
         cx->dme_k[1] = j;
+        if (sham) {
+          density_spin(cx, 1, cx->hint, cx->sint, th + 2 * nsc2 * tid, th + 2 * nsc2 * tid + nsc2, 1, 0);
+          continue;
+        }
         double d1 = 0.0, dummy = 0.0;
         density(cx, 1, &d1, &dummy, 1, 0);
         lw += cx->sint * d1;
@@ -1075,10 +1114,8 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
     free(pw);
   }
   wfnorm /= (double)nelec;
-  res->e1 = energy;
-  long long ntij = ((long long)nsp * nsp + nsp) / 2;
-  long long ntasks = (ntij * ntij + ntij) / 2;
-  res->ntasks = ntasks;
+  long long ntij = ((long long)nspat * nspat + nspat) / 2;
+  long long ntasks = sym ? (ntij * ntij + ntij) / 2 : ntij * ntij;
   double itol = in->itol;
   double *part = (double *)calloc(nth, sizeof(double));
   long long *pcount = (long long *)calloc(nth, sizeof(long long));
@@ -1094,22 +1131,28 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
     for (long long task = 0; task < ntasks; ++task) {
       if (g_task_stride > 1 && task % g_task_stride) continue;
       int ijorb, klorb, io, jo, ko, lo;
-      xm_dtriang(1 + task, &ijorb, &klorb);
+      if (sym) {
+        xm_dtriang(1 + task, &ijorb, &klorb);
+      } else {
+        klorb = (int)(1 + task / ntij);
+        ijorb = (int)(1 + task % ntij);
+      }
       xm_dtriang(ijorb, &io, &jo);
       xm_dtriang(klorb, &ko, &lo);
-      if ((io == jo && io <= nnd) || (ko == lo && ko <= nnd)) continue;
+      if ((io == jo && io <= nsd) || (ko == lo && ko <= nsd)) continue;
       int erep_sig = st->schwarz[indx(io, ko)] * st->schwarz[indx(jo, lo)] > itol;
       int x_sig = st->schwarz[indx(io, lo)] * st->schwarz[indx(jo, ko)] > itol;
       double xint = 0.0, eint = 0.0;
       if (erep_sig || x_sig) {
-        if (io == jo && ko == lo) {
+        int nonsub = io != jorb && jo != jorb && ko != jorb && lo != jorb;
+        if (nonsub && io == jo && ko == lo) {
           eint = st->schwarz[indx(io, ko)] * st->schwarz[indx(io, ko)];
           xint = eint;
         } else {
-          int ie = io > nnd ? 2 * io - nnd - 1 : io;
-          int je = jo > nnd ? 2 * jo - nnd - 1 : jo;
-          int ke = ko > nnd ? 2 * ko - nnd - 1 : ko;
-          int le = lo > nnd ? 2 * lo - nnd - 1 : lo;
+          int ie = io > nsd ? 2 * io - nsd - 1 : io;
+          int je = jo > nsd ? 2 * jo - nsd - 1 : jo;
+          int ke = ko > nsd ? 2 * ko - nsd - 1 : ko;
+          int le = lo > nsd ? 2 * lo - nsd - 1 : lo;
           if (erep_sig) {
             int2e(cx, st->bra[ie], st->ket[ke], st->bra[je], st->ket[le]);
             eint = cx->gint;
@@ -1128,17 +1171,17 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
       x_sig = fabs(xint) > itol;
       double esum_t = 0.0, xsum_t = 0.0;
       if (erep_sig || x_sig) {
-        int id = io > nnd, jd = jo > nnd, kd = ko > nnd, ld = lo > nnd;
+        int id = io > nsd, jd = jo > nsd, kd = ko > nsd, ld = lo > nsd;
         int iso = id ? 2 : 1, jso = jd ? 2 : 1, kso = kd ? 2 : 1, lso = ld ? 2 : 1;
         for (int is = 1; is <= iso; ++is) {
-          int i = id ? 2 * io - nnd + is - 2 : io;
+          int i = id ? 2 * io - nsd + is - 2 : io;
           for (int js = 1; js <= jso; ++js) {
-            int j = jd ? 2 * jo - nnd + js - 2 : jo;
+            int j = jd ? 2 * jo - nsd + js - 2 : jo;
             if (!(j < i)) continue;
             for (int ks = 1; ks <= kso; ++ks) {
-              int k = kd ? 2 * ko - nnd + ks - 2 : ko;
+              int k = kd ? 2 * ko - nsd + ks - 2 : ko;
               for (int ls = 1; ls <= lso; ++ls) {
-                int l = ld ? 2 * lo - nnd + ls - 2 : lo;
+                int l = ld ? 2 * lo - nsd + ls - 2 : lo;
                 if (!(l < k)) continue;
                 int ik0 = id && kd && (i % 2) != (k % 2);
                 int jl0 = jd && ld && (j % 2) != (l % 2);
@@ -1151,9 +1194,13 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
                   cx->dme_k[1] = k;
                   cx->dme_b[2] = j;
                   cx->dme_k[2] = l;
+                  cx->ndens2++;
+                  if (sham) {
+                    density_spin(cx, 2, eint, xint, th + 2 * nsc2 * tid, NULL, erep_sig, x_sig);
+                    continue;
+                  }
                   double dd = 0.0, xd = 0.0;
                   density(cx, 2, &dd, &xd, erep_sig, x_sig);
-                  cx->ndens2++;
                   if (erep_sig) esum_t += dd * eint;
                   if (x_sig) xsum_t += xd * xint;
                 }
@@ -1162,7 +1209,7 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
           }
         }
       }
-      if (!(ko == io && lo == jo)) {
+      if (sym && !(ko == io && lo == jo)) {
         esum_t *= 2.0;
         xsum_t *= 2.0;
       }
@@ -1173,20 +1220,250 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
     ctx_free(cx);
   }
   double e2 = 0.0;
+  long long nd = 0;
   for (int t = 0; t < nth; ++t) {
     e2 += part[t];
-    res->ndens2 += pcount[t];
+    nd += pcount[t];
   }
   free(part);
   free(pcount);
-  energy += e2;
+  if (sham) {
+    for (size_t k = 0; k < nsc2; ++k) {
+      sham[k] = 0.0;
+      sovl[k] = 0.0;
+    }
+    for (int t = 0; t < nth; ++t)
+      for (size_t k = 0; k < nsc2; ++k) {
+        sham[k] += th[2 * nsc2 * t + k];
+        sovl[k] += th[2 * nsc2 * t + nsc2 + k];
+      }
+    free(th);
+  }
+  *e1_out = energy;
+  *e2_out = e2;
+  *wfnorm_out = wfnorm;
+  if (ndens_out) *ndens_out = nd;
+}
+
+int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
+  memset(res, 0, sizeof(*res));
+  double nre = 0.0;
+  vo_state *st = prepare(in, &nre);
+  res->enucrep = nre;
+  guess_lists(st);
+  int nth = nthreads_of(nthreads);
+  vo_ctx *c0 = ctx_new(st);
+  wfndet(st, c0);
+  ctx_free(c0);
+  schwarz_ints(st, st->nsp, st->nnd, nth);
+  long long ntij = ((long long)st->nsp * st->nsp + st->nsp) / 2;
+  res->ntasks = (ntij * ntij + ntij) / 2;
+  /* vsvb_energy with iorb = 0, spinav = .false., ijkl symmetry enabled */
+  double e1 = 0.0, e2 = 0.0, wfnorm = 0.0;
+  vsvb_energy_core(st, st->nnd, st->nsp, 1, 0, nth, &e1, &e2, &wfnorm, &res->ndens2, NULL, NULL);
+  res->e1 = e1;
   res->e2 = e2;
   res->wfnorm = wfnorm;
   /* guess_energy tail (valence.F90:342-344) */
-  res->energy = energy / wfnorm + nre;
-  ctx_free(c0);
+  res->energy = (e1 + e2) / wfnorm + nre;
   g_last_state = st;
   return 0;
+}
+
+/* first_order_opt's dummy orbitals (valence.F90:609-672): orbital
+ * norbs + ib carries weight 1 on the ib-th expansion entry of iorb.  The
+ * reference gives each its own one-shell atom at the same centre; here it
+ * keeps iorb's atom set with every other weight zero, which the per-shell
+ * LCAO screen sum(c^2) > dtol of ovint/int1e/int2e reduces to the same
+ * single shell.  Entries that name a derived basis function are served by
+ * that function's own orbital (norbs + idf, :684-686) and leave an empty
+ * gap here, as in the reference. */
+typedef struct {
+  int *orbas_atnum, *orbas_atset, *map_orbs, *xpset;
+  double *coeff;
+} vo_orbital_arrays;
+
+static void add_dummies(vo_input *in, int iorb, vo_orbital_arrays *saved) {
+  int norbs = in->norbs, mx = in->mxctr, b0 = in->map_orbs[iorb - 1], nb = in->map_orbs[iorb] - b0;
+  int tot = in->map_orbs[norbs] - 1;
+  saved->orbas_atnum = in->orbas_atnum;
+  saved->orbas_atset = in->orbas_atset;
+  saved->map_orbs = in->map_orbs;
+  saved->xpset = in->xpset;
+  saved->coeff = in->coeff;
+  int *atn = (int *)calloc(norbs + nb + 1, sizeof(int));
+  int *ats = (int *)calloc((size_t)mx * (norbs + nb + 1), sizeof(int));
+  int *mo = (int *)calloc(norbs + nb + 2, sizeof(int));
+  int *xp = (int *)calloc(tot + nb + 1, sizeof(int));
+  double *co = (double *)calloc(tot + nb + 1, sizeof(double));
+  memcpy(atn, in->orbas_atnum, sizeof(int) * norbs);
+  memcpy(ats, in->orbas_atset, sizeof(int) * (size_t)mx * norbs);
+  memcpy(mo, in->map_orbs, sizeof(int) * (norbs + 1));
+  memcpy(xp, in->xpset, sizeof(int) * tot);
+  memcpy(co, in->coeff, sizeof(double) * tot);
+  for (int ib = 1; ib <= nb; ++ib) {
+    int o = norbs + ib, e = b0 + ib - 1;
+    atn[o - 1] = in->orbas_atnum[iorb - 1];
+    for (int k = 0; k < mx; ++k) ats[k + mx * (o - 1)] = in->orbas_atset[k + mx * (iorb - 1)];
+    if (in->xpset[e - 1] >= 1) {
+      xp[mo[o - 1] - 1] = in->xpset[e - 1];
+      co[mo[o - 1] - 1] = 1.0;
+      mo[o] = mo[o - 1] + 1;
+    } else {
+      mo[o] = mo[o - 1];
+    }
+  }
+  in->orbas_atnum = atn;
+  in->orbas_atset = ats;
+  in->map_orbs = mo;
+  in->xpset = xp;
+  in->coeff = co;
+}
+
+static void drop_dummies(vo_input *in, vo_orbital_arrays *saved) {
+  free(in->orbas_atnum);
+  free(in->orbas_atset);
+  free(in->map_orbs);
+  free(in->xpset);
+  free(in->coeff);
+  in->orbas_atnum = saved->orbas_atnum;
+  in->orbas_atset = saved->orbas_atset;
+  in->map_orbs = saved->map_orbs;
+  in->xpset = saved->xpset;
+  in->coeff = saved->coeff;
+}
+
+/* the H/S loops of first_order_opt for one substituted electron slot eorb
+ * (valence.F90:679-703 and, spin averaged, :714-747) */
+static void hs_loop(vo_state *st, int iorb, int eorb, int nsd, int nspat, int jorb, int nth, int nb, double *ham,
+                    double *ovl, int accumulate) {
+  vo_input *in = st->in;
+  int norbs = in->norbs, nelec = st->nelec, b0 = in->map_orbs[iorb - 1];
+  vo_ctx *c0 = ctx_new(st);
+  for (int ib = 1; ib <= nb; ++ib) {
+    int idf = in->xpset[b0 + ib - 2];
+    st->bra[eorb] = idf < 1 ? norbs + idf : norbs + ib;
+    for (int k = 1; k <= nelec; ++k) {
+      ovint(c0, st->bra[eorb], st->ket[k]);
+      A2(st->wdet, nelec, eorb, k) = c0->sint;
+    }
+    for (int jb = 1; jb <= ib; ++jb) {
+      int jdf = in->xpset[b0 + jb - 2];
+      st->ket[eorb] = jdf < 1 ? norbs + jdf : norbs + jb;
+      for (int k = 1; k <= nelec; ++k) {
+        ovint(c0, st->bra[k], st->ket[eorb]);
+        A2(st->wdet, nelec, k, eorb) = c0->sint;
+      }
+      double e1 = 0.0, e2 = 0.0, w = 0.0;
+      vsvb_energy_core(st, nsd, nspat, 0, jorb, nth, &e1, &e2, &w, NULL, NULL, NULL);
+      if (accumulate) {
+        A2(ham, nb, ib, jb) += e1 + e2;
+        A2(ovl, nb, ib, jb) += w;
+      } else {
+        A2(ham, nb, ib, jb) = e1 + e2;
+        A2(ovl, nb, ib, jb) = w;
+      }
+    }
+  }
+  ctx_free(c0);
+}
+
+int vo_first_order_hs(vo_input *in, int iorb, double *ham, double *ovl, int nthreads) {
+  int nnd = 2 * in->npair + in->nunpd, nsp = nnd + in->ndocc;
+  if (iorb < 1 || iorb > nsp) return 1;
+  double nre = 0.0;
+  vo_state *st = prepare(in, &nre);
+  int nth = nthreads_of(nthreads);
+  int nsd = nnd, nspat = nsp, eorb;
+  /* the wave function's electron lists (valence.F90:555-603) */
+  if (iorb <= nnd) {
+    eorb = iorb;
+    guess_lists(st);
+  } else {
+    for (int i = 1; i <= nnd; ++i) {
+      st->bra[i] = i;
+      st->ket[i] = i;
+    }
+    st->bra[nnd + 1] = st->ket[nnd + 1] = iorb;
+    st->bra[nnd + 2] = st->ket[nnd + 2] = iorb;
+    int i = nnd + 3;
+    for (int idocc = nnd + 1; idocc <= nnd + in->ndocc; ++idocc)
+      if (idocc != iorb) {
+        st->bra[i] = st->ket[i] = idocc;
+        st->bra[i + 1] = st->ket[i + 1] = idocc;
+        i += 2;
+      }
+    eorb = nnd + 1;
+    nsd = nnd + 2;
+    nspat = nsp + 1;
+  }
+  int nb = in->map_orbs[iorb] - in->map_orbs[iorb - 1];
+  vo_orbital_arrays saved;
+  add_dummies(in, iorb, &saved);
+  vo_ctx *c0 = ctx_new(st);
+  wfndet(st, c0);
+  ctx_free(c0);
+  schwarz_ints(st, nspat, nsd, nth);
+  /* the subject orbital of vsvb_energy's nonsub test (:1200-1205) */
+  int jorb = iorb > nnd ? nnd + 1 : iorb;
+  hs_loop(st, iorb, eorb, nsd, nspat, jorb, nth, nb, ham, ovl, 0);
+  if (in->nunpd > 0 && iorb > nnd) {
+    /* spin average (:708-749): restore the alpha slot, substitute the beta */
+    st->bra[eorb] = st->ket[eorb] = iorb;
+    c0 = ctx_new(st);
+    wfndet(st, c0);
+    ctx_free(c0);
+    hs_loop(st, iorb, nnd + 2, nsd, nspat, nnd + 2, nth, nb, ham, ovl, 1);
+  }
+  for (int i = 1; i <= nb; ++i)
+    for (int j = 1; j < i; ++j) {
+      A2(ham, nb, j, i) = A2(ham, nb, i, j);
+      A2(ovl, nb, j, i) = A2(ovl, nb, i, j);
+    }
+  drop_dummies(in, &saved);
+  state_free(st);
+  return 0;
+}
+
+int vo_spin_hs(vo_input *in, double *ham, double *ovl, int nthreads) {
+  if (in->nspinc < 1) return 1;
+  double nre = 0.0;
+  vo_state *st = prepare(in, &nre);
+  int nth = nthreads_of(nthreads), nsc = in->nspinc;
+  guess_lists(st);
+  vo_ctx *c0 = ctx_new(st);
+  wfndet(st, c0);
+  ctx_free(c0);
+  schwarz_ints(st, st->nsp, st->nnd, nth);
+  double e1, e2, w;
+  vsvb_energy_core(st, st->nnd, st->nsp, 0, 0, nth, &e1, &e2, &w, NULL, ham, ovl);
+  /* valence.F90:887-897 */
+  for (int i = 1; i <= nsc; ++i)
+    for (int j = 1; j <= i; ++j) A2(ovl, nsc, i, j) /= (double)st->nelec;
+  for (int i = 1; i <= nsc; ++i)
+    for (int j = 1; j <= i; ++j) {
+      A2(ham, nsc, j, i) = A2(ham, nsc, i, j);
+      A2(ovl, nsc, j, i) = A2(ovl, nsc, i, j);
+    }
+  state_free(st);
+  return 0;
+}
+
+double vo_nuclear_repulsion(vo_input *in) {
+  double nre = 0.0;
+  for (int i = 2; i <= in->natom; ++i)
+    for (int j = 1; j <= i - 1; ++j) {
+      double zij = in->nuc_charge[in->atom_t[i - 1] - 1] * in->nuc_charge[in->atom_t[j - 1] - 1];
+      if (fabs(zij) > 1e-12) {
+        double rsq = 0.0;
+        for (int d = 0; d < 3; ++d) {
+          double x = in->coords[3 * (i - 1) + d] - in->coords[3 * (j - 1) + d];
+          rsq += x * x;
+        }
+        if (rsq > 1e-5) nre += zij * pow(rsq, -0.5);
+      }
+    }
+  return nre;
 }
 
 /* helpers for tests: orbital integrals with the normalised weights left by

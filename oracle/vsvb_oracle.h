@@ -95,6 +95,18 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads);
  * timing on a bounded sample; the energy is then not the full energy). */
 int vo_guess_energy_sampled(vo_input *in, vo_result *res, int nthreads, long long stride);
 
+/* first_order_opt's Hamiltonian and overlap matrices (valence.F90:527-758)
+ * for orbital iorb (1-based) of the wave function with the weights as set
+ * (coeff_raw, normalised first as the reference's coeff is): nb x nb,
+ * column-major, nb = map_orbs(iorb+1) - map_orbs(iorb), ham(ib,jb) the
+ * energy numerator and ovl(ib,jb) the wave-function norm with the bra's
+ * slot of iorb holding entry ib and the ket's entry jb, spin averaged for a
+ * doubly occupied orbital when there are unpaired electrons; symmetrised. */
+int vo_first_order_hs(vo_input *in, int iorb, double *ham, double *ovl, int nthreads);
+/* spin_opt's (valence.F90:850-897): nspinc x nspinc over the couplings. */
+int vo_spin_hs(vo_input *in, double *ham, double *ovl, int nthreads);
+double vo_nuclear_repulsion(vo_input *in);
+
 /* Orbital-level integrals after vo_guess_energy's normalisation:
  * (io ko | jo lo) over the screened LCAO weights (1-based orbitals). */
 double vo_int2e(vo_input *in, int io, int ko, int jo, int lo);

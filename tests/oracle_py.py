@@ -92,3 +92,147 @@ def boys(mmax, t):
 def goldens():
     with open(os.path.join(GOLDEN, "reference_goldens.json")) as f:
         return json.load(f)
+
+
+class VoInput(ctypes.Structure):
+    """Layout of struct vo_input (oracle/vsvb_oracle.h)."""
+    _fields_ = [(n, ctypes.c_int) for n in ("natom", "natom_t", "npair", "nunpd", "ndocc", "totlen", "xpmax",
+                                            "nspinc", "num_sh", "num_pr", "nang", "ndf", "nset", "nxorb", "mxctr",
+                                            "ntol_c", "ntol_d", "ntol_i", "ntol_e_min", "ntol_e_max", "max_iter")] + [
+        ("ptbnmax", ctypes.c_double), ("feather", ctypes.c_double), ("orbset", ctypes.POINTER(ctypes.c_int)),
+        ("atom_t", ctypes.POINTER(ctypes.c_int)), ("coords", ctypes.POINTER(ctypes.c_double)),
+        ("nuc_charge", ctypes.POINTER(ctypes.c_double)), ("map_atom2shell", ctypes.POINTER(ctypes.c_int)),
+        ("num_shell_atom", ctypes.POINTER(ctypes.c_int)), ("map_shell2prim", ctypes.POINTER(ctypes.c_int)),
+        ("ang_mom", ctypes.POINTER(ctypes.c_int)), ("exponent", ctypes.POINTER(ctypes.c_double)),
+        ("uncoef", ctypes.POINTER(ctypes.c_double)), ("con_coeff", ctypes.POINTER(ctypes.c_double)),
+        ("pair_sc", ctypes.POINTER(ctypes.c_int)), ("coeff_sc", ctypes.POINTER(ctypes.c_double)),
+        ("xorb", ctypes.POINTER(ctypes.c_int)), ("root", ctypes.POINTER(ctypes.c_int)), ("norbs", ctypes.c_int),
+        ("orbas_atnum", ctypes.POINTER(ctypes.c_int)), ("orbas_atset", ctypes.POINTER(ctypes.c_int)),
+        ("map_orbs", ctypes.POINTER(ctypes.c_int)), ("xpset", ctypes.POINTER(ctypes.c_int)),
+        ("coeff", ctypes.POINTER(ctypes.c_double)), ("coeff_raw", ctypes.POINTER(ctypes.c_double)),
+        ("dtol", ctypes.c_double), ("itol", ctypes.c_double)]
+
+
+TOKCAL = 627.509469  # valence.F90:2756
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class OptOracle(Oracle):
+    """The reference's orbital / spin-coupling optimisation (minimize_energy,
+    valence.F90:2744-2885; first_order_opt :527-844; spin_opt :850-936) on
+    the oracle's literal H/S builds.  EISPACK rsg (a generalised symmetric
+    eigensolver, rsg.F) is scipy.linalg.eigh here: ascending eigenvalues,
+    eigenvectors normalised to w^T S w = 1."""
+
+    def __init__(self, path):
+        super().__init__(path)
+        L = lib()
+        L.vo_first_order_hs.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        L.vo_spin_hs.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                 ctypes.c_int]
+        L.vo_nuclear_repulsion.argtypes = [ctypes.c_void_p]
+        L.vo_nuclear_repulsion.restype = ctypes.c_double
+        self.inp = ctypes.cast(self.h, ctypes.POINTER(VoInput)).contents
+
+    def coeff_raw(self):
+        return np.ctypeslib.as_array(self.inp.coeff_raw, shape=(self.inp.totlen,)).copy()
+
+    def coeff_sc(self):
+        return np.ctypeslib.as_array(self.inp.coeff_sc, shape=(max(self.inp.nspinc, 1),)).copy()
+
+    def set_coeff_sc(self, c):
+        for k, v in enumerate(c):
+            self.inp.coeff_sc[k] = float(v)
+
+    def norbas(self, iorb):
+        return self.inp.map_orbs[iorb] - self.inp.map_orbs[iorb - 1]
+
+    def first_order_hs(self, iorb, nthreads=0):
+        n = self.norbas(iorb)
+        ham, ovl = np.zeros((n, n)), np.zeros((n, n))
+        hf, of = np.asfortranarray(ham), np.asfortranarray(ovl)
+        if lib().vo_first_order_hs(self.h, iorb, _dp(hf), _dp(of), nthreads):
+            raise ValueError("bad orbital")
+        return hf, of
+
+    def spin_hs(self, nthreads=0):
+        n = self.inp.nspinc
+        hf, of = np.zeros((n, n), order="F"), np.zeros((n, n), order="F")
+        if lib().vo_spin_hs(self.h, _dp(hf), _dp(of), nthreads):
+            raise ValueError("no spin couplings")
+        return hf, of
+
+    def enucrep(self):
+        return lib().vo_nuclear_repulsion(self.h)
+
+    def _root_of(self, iorb):
+        r = 0
+        for k in range(self.inp.nxorb):
+            if self.inp.xorb[k] == iorb:
+                r = self.inp.root[k]
+        return r
+
+    def first_order_opt(self, iorb, nthreads=0):
+        """valence.F90:527-844: H/S, rsg, the selected root into iorb."""
+        import scipy.linalg
+        ham, ovl = self.first_order_hs(iorb, nthreads)
+        eig, w = scipy.linalg.eigh(ham, ovl)
+        r = self._root_of(iorb)
+        c = self.coeff_raw()
+        b0 = self.inp.map_orbs[iorb - 1] - 1
+        c[b0:b0 + len(eig)] = w[:, r]
+        self.set_coeff(c)
+        return eig[r] + self.enucrep()
+
+    def spin_opt(self, nthreads=0):
+        """valence.F90:850-936: lowest root into coeff_sc (not normalised)."""
+        import scipy.linalg
+        ham, ovl = self.spin_hs(nthreads)
+        eig, w = scipy.linalg.eigh(ham, ovl)
+        self.set_coeff_sc(w[:, 0])
+        return eig[0] + self.enucrep()
+
+    def minimize_energy(self, nthreads=0):
+        """minimize_energy (valence.F90:2744-2885) after guess_energy; the
+        first-order method only (dem_gs inputs raise).  Returns the final
+        energy and the number of iterations."""
+        inp = self.inp
+        if inp.ptbnmax > 0.0 and inp.nxorb == 0:
+            raise NotImplementedError("direct energy minimisation (demgs_opt)")
+        energy = self.guess_energy(nthreads).energy
+        num_iter = 0
+        eprv_sc = eprv_orb = 0.0
+        sets = [(inp.orbset[2 * s], inp.orbset[2 * s + 1]) for s in range(inp.nset)]
+        for ntol in range(inp.ntol_e_min, inp.ntol_e_max + 1):
+            etol = 10.0 ** (-ntol)
+            finished = False
+            while not finished:
+                eprv_sc = energy
+                orbconv = False
+                while not orbconv and num_iter < inp.max_iter:
+                    eprv_orb = energy
+                    for lo, hi in sets:
+                        setcnv = False
+                        while not setcnv and num_iter < inp.max_iter:
+                            eprv_set = energy
+                            num_iter += 1
+                            for iorb in range(lo, hi + 1):
+                                energy = self.first_order_opt(iorb, nthreads)
+                            setcnv = abs(energy - eprv_set) * TOKCAL < etol
+                    orbconv = abs(energy - eprv_orb) * TOKCAL < etol
+                    if len(sets) == 1:
+                        orbconv = True
+                        eprv_orb = energy
+                if inp.nspinc > 1:
+                    num_iter += 1
+                    energy = self.spin_opt(nthreads)
+                    finished = abs(energy - eprv_sc) * TOKCAL < etol
+                else:
+                    finished = True
+                if num_iter >= inp.max_iter:
+                    finished = True
+        return energy, num_iter
