@@ -83,6 +83,12 @@ typedef struct vsvb_system_desc {
   const int *map_orbs;            /* [norbs+1], 1-based */
   const int *xpset;               /* [totlen] */
   const double *coeff;            /* [totlen] raw orbital weights */
+  /* optimisation control (line B and the excited-state record; read by
+   * vsvb_read_input, used by vsvb_opt_minimize only) */
+  int ntol_e_min, ntol_e_max, max_iter, nset;
+  double ptbnmax, feather;        /* direct minimisation: first perturbation, its reduction factor */
+  const int *orbset;              /* [2*nset], orbset(1:2, iset): first and last orbital of each set */
+  const int *xorb, *root;         /* [nxorb]: orbital xorb(i) takes eigenvector root(i) (0 = lowest) */
 } vsvb_system_desc;
 
 typedef struct vsvb_options {
@@ -262,6 +268,55 @@ int vsvb_det_factor(const double *a_dev, int n, int nmat, double *det_dev, doubl
  * vsvb_det_factor. */
 int vsvb_det_factor_noalloc(const double *a_dev, int n, int nmat, double *det_dev, double *inv_dev, int *sing_dev,
                             void *stream);
+
+/*
+ * Wave-function optimisation (the reference's minimize_energy with
+ * first_order_opt, spin_opt and demgs_opt, valence.F90:350-936, 2744-2885).
+ * An optimiser owns a copy of the description, a handle for energies and,
+ * created on first use, one handle per orbital (two for a DOCC orbital when
+ * there are unpaired electrons) for first_order_opt's matrices.
+ */
+typedef struct vsvb_opt vsvb_opt;
+
+typedef struct vsvb_opt_result {
+  double energy;         /* final energy (the last eigenvalue + enucrep, as the reference reports it) */
+  double guess_energy;   /* energy of the normalised input weights */
+  double etol;           /* the last tolerance of the feathering loop, kcal/mol */
+  double seconds;        /* wall time of the call */
+  int iterations;        /* num_iter of minimize_energy */
+  int converged;         /* the reference's 'calculation converged' test */
+  long long n_energy_evals, n_hs_builds;
+} vsvb_opt_result;
+
+int vsvb_opt_create(const vsvb_system_desc *desc, const vsvb_options *opt, vsvb_opt **out);
+void vsvb_opt_destroy(vsvb_opt *o);
+const char *vsvb_opt_last_error(const vsvb_opt *o);
+
+/* first_order_opt's Hamiltonian and overlap (valence.F90:609-758) of orbital
+ * iorb (1-based) for raw weights coeff (totlen) and, when nspinc > 0, the
+ * spin-coupling weights coeff_sc (NULL: keep the current ones): nb x nb
+ * column-major, nb = map_orbs(iorb+1) - map_orbs(iorb), element (ib, jb) the
+ * energy numerator / wave-function norm with the bra's slot of iorb holding
+ * entry ib and the ket's entry jb; symmetric. */
+int vsvb_opt_first_order_hs(vsvb_opt *o, const double *coeff, const double *coeff_sc, int iorb, double *ham,
+                            double *ovl);
+/* spin_opt's matrices (valence.F90:866-897), nspinc x nspinc. */
+int vsvb_opt_spin_hs(vsvb_opt *o, const double *coeff, double *ham, double *ovl);
+
+/* minimize_energy (valence.F90:2744-2885) from raw weights coeff (totlen,
+ * updated in place to the optimised, normalised weights) and coeff_sc
+ * (nspinc, updated; may be NULL without spin couplings), with the
+ * description's max_iter, ntol_e_min..ntol_e_max, orbital sets, excited-state
+ * roots and ptbnmax/feather (direct minimisation when ptbnmax > 0 and there
+ * are no excited-state roots). */
+int vsvb_opt_minimize(vsvb_opt *o, double *coeff, double *coeff_sc, vsvb_opt_result *res);
+
+/* EISPACK rsg (rsg.F) on the GPU: ham w = e ovl w for symmetric ham and
+ * positive-definite ovl (n x n, column-major, leading dimension ld);
+ * eigenvalues ascending into eig, eigenvectors (w^T ovl w = 1) into the
+ * columns of w (leading dimension ldw).  VSVB_ERR_SINGULAR when ovl is not
+ * positive definite (rsg's ierr = 7n+1).  n <= 1024. */
+int vsvb_rsg(int n, const double *ham, const double *ovl, int ld, double *eig, double *w, int ldw);
 
 /* Sizes of a handle (for bindings). */
 int vsvb_gpu_totlen(const vsvb_gpu *h);

@@ -43,7 +43,10 @@ class Desc(ctypes.Structure):
         ("con_coeff", ctypes.POINTER(ctypes.c_double)), ("pair_sc", ctypes.POINTER(ctypes.c_int)),
         ("coeff_sc", ctypes.POINTER(ctypes.c_double)), ("orbas_atnum", ctypes.POINTER(ctypes.c_int)),
         ("orbas_atset", ctypes.POINTER(ctypes.c_int)), ("map_orbs", ctypes.POINTER(ctypes.c_int)),
-        ("xpset", ctypes.POINTER(ctypes.c_int)), ("coeff", ctypes.POINTER(ctypes.c_double))]
+        ("xpset", ctypes.POINTER(ctypes.c_int)), ("coeff", ctypes.POINTER(ctypes.c_double)),
+        ("ntol_e_min", ctypes.c_int), ("ntol_e_max", ctypes.c_int), ("max_iter", ctypes.c_int), ("nset", ctypes.c_int),
+        ("ptbnmax", ctypes.c_double), ("feather", ctypes.c_double), ("orbset", ctypes.POINTER(ctypes.c_int)),
+        ("xorb", ctypes.POINTER(ctypes.c_int)), ("root", ctypes.POINTER(ctypes.c_int))]
 
 
 class Options(ctypes.Structure):
@@ -59,6 +62,15 @@ class Result(ctypes.Structure):
                 ("n_quartets_fp32", ctypes.c_longlong), ("n_tasks", ctypes.c_longlong),
                 ("n_singular_pairs", ctypes.c_int), ("n_kernel_launches", ctypes.c_int),
                 ("n_prim_quartets", ctypes.c_double), ("n_prim_quartets_fp32", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class OptResult(ctypes.Structure):
+    _fields_ = [("energy", ctypes.c_double), ("guess_energy", ctypes.c_double), ("etol", ctypes.c_double),
+                ("seconds", ctypes.c_double), ("iterations", ctypes.c_int), ("converged", ctypes.c_int),
+                ("n_energy_evals", ctypes.c_longlong), ("n_hs_builds", ctypes.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -109,6 +121,14 @@ def lib():
         L.vsvb_batch_last_error.argtypes = [ctypes.c_void_p]
         L.vsvb_batch_last_error.restype = ctypes.c_char_p
         L.vsvb_batch_destroy.argtypes = [ctypes.c_void_p]
+        L.vsvb_opt_create.argtypes = [P(Desc), P(Options), P(ctypes.c_void_p)]
+        L.vsvb_opt_destroy.argtypes = [ctypes.c_void_p]
+        L.vsvb_opt_last_error.argtypes = [ctypes.c_void_p]
+        L.vsvb_opt_last_error.restype = ctypes.c_char_p
+        L.vsvb_opt_first_order_hs.argtypes = [ctypes.c_void_p, P(D), P(D), I, P(D), P(D)]
+        L.vsvb_opt_spin_hs.argtypes = [ctypes.c_void_p, P(D), P(D), P(D)]
+        L.vsvb_opt_minimize.argtypes = [ctypes.c_void_p, P(D), P(D), P(OptResult)]
+        L.vsvb_rsg.argtypes = [I, P(D), P(D), I, P(D), P(D), I]
         _LIB = L
     return _LIB
 
@@ -445,3 +465,81 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def rsg(ham, ovl):
+    """EISPACK rsg on the GPU (vsvb_rsg): eigenvalues ascending and
+    eigenvectors (columns, w^T ovl w = 1) of ham w = e ovl w."""
+    h = np.asfortranarray(ham, dtype=np.float64)
+    s = np.asfortranarray(ovl, dtype=np.float64)
+    n = h.shape[0]
+    eig, w = np.zeros(n), np.zeros((n, n), order="F")
+    rc = lib().vsvb_rsg(n, _dptr(h), _dptr(s), n, _dptr(eig), _dptr(w), n)
+    if rc:
+        raise VSVBError(f"vsvb_rsg failed ({rc})")
+    return eig, w
+
+
+class Optimizer:
+    """The reference's wave-function optimisation (minimize_energy with
+    first_order_opt / spin_opt / demgs_opt, valence.F90:350-936, 2744-2885)
+    on the GPU path (vsvb_opt_*)."""
+
+    def __init__(self, path, precision=FP64, device=0, **kw):
+        self.path = path
+        self._desc = read_input(path)
+        d = self._desc.contents
+        self.totlen, self.nspinc = d.totlen, d.nspinc
+        self.map_orbs = np.ctypeslib.as_array(d.map_orbs, shape=(2 * d.npair + d.nunpd + d.ndocc + d.ndf + 1,)).copy()
+        self.coeff0 = np.ctypeslib.as_array(d.coeff, shape=(d.totlen,)).copy()
+        self.coeff_sc0 = np.ctypeslib.as_array(d.coeff_sc, shape=(max(d.nspinc, 1),)).copy()
+        self.opt = make_options(precision, kw.get("mixed_threshold", 1e-6), kw.get("ao_screen", 1e-15), device,
+                                0, kw.get("prim_screen"), kw.get("prim_split"), None, None)
+        self._o = ctypes.c_void_p()
+        rc = lib().vsvb_opt_create(self._desc, ctypes.byref(self.opt), ctypes.byref(self._o))
+        if rc:
+            msg = lib().vsvb_opt_last_error(self._o).decode() if self._o else ""
+            self.close()
+            raise VSVBError(f"vsvb_opt_create failed ({rc}): {msg}")
+
+    def close(self):
+        if getattr(self, "_o", None):
+            lib().vsvb_opt_destroy(self._o)
+            self._o = None
+        if getattr(self, "_desc", None):
+            lib().vsvb_free_desc(self._desc)
+            self._desc = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc:
+            raise VSVBError(f"{what} failed ({rc}): {lib().vsvb_opt_last_error(self._o).decode()}")
+
+    def first_order_hs(self, iorb, coeff=None, coeff_sc=None):
+        c = np.ascontiguousarray(self.coeff0 if coeff is None else coeff, dtype=np.float64)
+        csc = None if coeff_sc is None else np.ascontiguousarray(coeff_sc, dtype=np.float64)
+        n = int(self.map_orbs[iorb] - self.map_orbs[iorb - 1])
+        h, s = np.zeros((n, n), order="F"), np.zeros((n, n), order="F")
+        self._check(lib().vsvb_opt_first_order_hs(self._o, _dptr(c), None if csc is None else _dptr(csc), iorb,
+                                                  _dptr(h), _dptr(s)), "first_order_hs")
+        return h, s
+
+    def spin_hs(self, coeff=None):
+        c = np.ascontiguousarray(self.coeff0 if coeff is None else coeff, dtype=np.float64)
+        n = self.nspinc
+        h, s = np.zeros((n, n), order="F"), np.zeros((n, n), order="F")
+        self._check(lib().vsvb_opt_spin_hs(self._o, _dptr(c), _dptr(h), _dptr(s)), "spin_hs")
+        return h, s
+
+    def minimize(self, coeff=None, coeff_sc=None):
+        """Returns (result dict, optimised weights, spin-coupling weights)."""
+        c = np.array(self.coeff0 if coeff is None else coeff, dtype=np.float64)
+        csc = np.array(self.coeff_sc0 if coeff_sc is None else coeff_sc, dtype=np.float64)
+        r = OptResult()
+        self._check(lib().vsvb_opt_minimize(self._o, _dptr(c), _dptr(csc), ctypes.byref(r)), "minimize")
+        return r.as_dict(), c, csc

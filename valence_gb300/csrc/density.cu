@@ -37,7 +37,9 @@
 
 namespace {
 
-__device__ __forceinline__ int spat(const DetCtx &d, int s) { return s < d.ds.nnd ? s : d.ds.nnd + (s - d.ds.nnd) / 2; }
+/* spin-orbital slot -> spatial orbital (the electron lists of vsvb_energy's
+ * callers: bra(i) = i below num_non_docc, then two slots per DOCC orbital) */
+__device__ __forceinline__ int spat(const DetCtx &d, int s) { return s < d.ds.nsd ? s : d.ds.nsd + (s - d.ds.nsd) / 2; }
 
 __device__ __forceinline__ void slot_loc(const DetCtx &d, int sc, unsigned bits, int s, int &spin, int &pos) {
   const int np = d.ds.npair;
@@ -480,7 +482,9 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
   const int split = blockIdx.y, nsplit = gridDim.y;
   QInfo qi = decode_q(d, q);
   load_dets(d, q, qi);
-  const int nelec = d.ds.nelec, nnd = d.ds.nnd, nsp = d.ds.nsp;
+  /* nnd: num_non_docc of the task loop (spatial level); the spin structure
+   * of the slots (slot_loc) keeps ds.nnd */
+  const int nelec = d.ds.nelec, nnd = d.ds.nsd, nsp = d.ds.nsp;
   const int na = d.ds.nalpha, nb = d.ds.nbeta;
   double *Ga = nullptr, *Gb = nullptr;
   int lda = na, ldb = nb;
@@ -779,6 +783,51 @@ __global__ void grad_scale_kernel(DetCtx d, AsmArgs a, int nsplit) {
       a.Hbar[t] = inv_w * a.D1[t];
       a.Sbar[t] = dw * a.D1[t];
     }
+  }
+}
+
+/* the MODE 4 accumulators combined for the derivative of alpha * E_num +
+ * beta * W * nelec instead of E = E_num / W: (1, 0) gives dE_num, (0,
+ * 1/nelec) dW -- the two first_order_opt matrices come from these (one
+ * block per determinant pair; block 0 also writes Hbar and Sbar) */
+__global__ void hs_scale_kernel(DetCtx d, AsmArgs a, int nsplit, double alpha, double beta) {
+  const long long q = blockIdx.x;
+  const int ng = d.ds.nalpha * d.ds.nalpha + d.ds.nbeta * d.ds.nbeta;
+  double *G = a.Gglob + (size_t)q * ng;
+  const double *Gs = a.Gs + (size_t)q * ng;
+  for (int t = threadIdx.x; t < ng; t += blockDim.x) G[t] = alpha * G[t] + beta * Gs[t];
+  for (int s = threadIdx.x; s < nsplit; s += blockDim.x) {
+    const size_t slot = (size_t)q * nsplit + s;
+    a.vtot[slot] = alpha * a.vtot[slot] + beta * a.vtot_s[slot];
+  }
+  if (q == 0) {
+    const int n2 = d.ds.nsp * d.ds.nsp;
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+      a.Hbar[t] = alpha * a.D1[t];
+      a.Sbar[t] = beta * a.D1[t];
+    }
+  }
+}
+
+/* spin_opt's matrices (valence.F90:850-897) from the partial sums of one
+ * walk with every coupling weight 1: block (isc, jsc) sums the energy
+ * numerator and the norm of its determinant pairs in a fixed order.  One
+ * block per (isc, jsc). */
+__global__ void spin_block_kernel(DetCtx d, AsmArgs a, int nsplit, double *BH, double *BS) {
+  __shared__ double red[8];
+  const int blk = blockIdx.x; /* isc * nsc + jsc */
+  const long long per = 1LL << (2 * d.ds.npair);
+  const long long s0 = (long long)blk * per * nsplit, n = per * nsplit;
+  double h = 0.0, w = 0.0;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    h += a.part_e1[s0 + t] + a.part_e2[s0 + t];
+    w += a.part_wf[s0 + t];
+  }
+  h = block_sum_d(h, red);
+  w = block_sum_d(w, red);
+  if (threadIdx.x == 0) {
+    BH[blk] = h;
+    BS[blk] = w / (double)d.ds.nelec;
   }
 }
 

@@ -45,4 +45,6 @@ cudaError_t launch_assemble(int mode, dim3 grid, int threads, size_t smem, cudaS
 __global__ void energy_reduce_kernel(AsmArgs a, long long nslot, int nelec, double enuc, double *out);
 __global__ void detpair_adjoint_kernel(DetCtx d, AsmArgs a, int nsplit);
 __global__ void grad_scale_kernel(DetCtx d, AsmArgs a, int nsplit);
+__global__ void hs_scale_kernel(DetCtx d, AsmArgs a, int nsplit, double alpha, double beta);
+__global__ void spin_block_kernel(DetCtx d, AsmArgs a, int nsplit, double *BH, double *BS);
 #endif

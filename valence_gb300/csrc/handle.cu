@@ -33,6 +33,7 @@
 #include "../../include/vsvb_gpu.h"
 #include "density.cuh"
 #include "eri.cuh"
+#include "handle_internal.h"
 #include "onee.cuh"
 #include "vsvb_internal.h"
 
@@ -211,6 +212,13 @@ struct vsvb_gpu {
   DBuf<double> Gs, vtot_s, D1; /* dE/dS parts of the fused (unscaled) adjoint walk */
   bool grad_ready = false;
   int last_singular = 0;
+  /* first_order_opt configuration (vsvb_opt): hs_split 1 / 2 when the
+   * description carries one orbital more than its counts, the alpha / beta
+   * slot of the first DOCC pair holding it; hs_sub its spatial index, taken
+   * as given (not normalised); -1 on ordinary handles */
+  int hs_split = 0, hs_sub = -1;
+  DBuf<int> hs_flag;
+  std::vector<double> csc_h; /* the spin-coupling weights in use */
 };
 
 namespace {
@@ -247,6 +255,7 @@ OrbArgs orb_args(vsvb_gpu *h) {
   a.Craw = h->Craw.p;
   a.C = h->C.p;
   a.status = h->status.p;
+  a.fixed_orb = h->hs_sub;
   return a;
 }
 
@@ -267,6 +276,10 @@ XtabArgs xtab_args(vsvb_gpu *h) {
   x.hrr = h->hrr.p;
   x.xtabh = h->xtabh.p;
   x.xtabh32 = h->xtabh32.p;
+  /* first_order_opt's substituted orbital: its matrices are the bilinear
+   * forms over every shell of the orbital, as the reference's one-shell dummy
+   * orbitals give them, so no shell of it is screened out */
+  x.keep_orb = h->hs_sub;
   return x;
 }
 
@@ -410,11 +423,11 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   }
   CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
 
-  const int norbs = 2 * d->npair + d->nunpd + d->ndocc + d->ndf;
+  const int norbs = 2 * d->npair + d->nunpd + d->ndocc + d->ndf + (h->hs_split ? 1 : 0);
   h->natom = d->natom;
   h->ndf = d->ndf;
   h->norb_all = norbs;
-  h->nsp = 2 * d->npair + d->nunpd + d->ndocc;
+  h->nsp = 2 * d->npair + d->nunpd + d->ndocc + (h->hs_split ? 1 : 0);
   h->totlen = d->totlen;
   h->dtol = std::pow(10.0, -(double)d->ntol_d);
   h->itol = std::pow(10.0, -(double)d->ntol_i);
@@ -1003,6 +1016,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   ds.nalpha = d->npair + d->nunpd + d->ndocc;
   ds.nbeta = d->npair + d->ndocc;
   ds.nnd = 2 * d->npair + d->nunpd;
+  ds.nsd = ds.nnd + (h->hs_split ? 2 : 0);
   ds.nsp = nsp;
   ds.nsc = d->nspinc > 0 ? d->nspinc : 1;
   ds.nq = (long long)ds.nsc * ds.nsc << (2 * d->npair);
@@ -1032,6 +1046,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   CK(h->slot_pair.upload(spair.empty() ? std::vector<int>(1, 0) : spair), "upload sc");
   CK(h->slot_which.upload(swhich.empty() ? std::vector<int>(1, 0) : swhich), "upload sc");
   CK(h->coeff_sc.upload(csc), "upload coeff_sc");
+  h->csc_h = csc;
   const long long nq = ds.nq;
   const int na = ds.nalpha, nb = ds.nbeta;
   CK(h->det_a.alloc(nq), "alloc det");
@@ -1859,3 +1874,118 @@ int vsvb_gpu_debug_orbital_1e(vsvb_gpu *h, double *s, double *hc, size_t cap) {
 }
 
 }  /* extern "C" */
+
+/* ---- first_order_opt / spin_opt support (handle_internal.h) ---- */
+
+int vsvb_gpu_create_sub(const vsvb_system_desc *d, const vsvb_options *opt, int split, int sub, vsvb_gpu **out) {
+  if (!d || !out) return VSVB_ERR_INPUT;
+  *out = nullptr;
+  auto *h = new vsvb_gpu();
+  vsvb_default_options(&h->opt);
+  if (opt) h->opt = *opt;
+  h->opt.autotune = 0;
+  h->opt.cuda_graph = 0;
+  h->dev = h->opt.device;
+  h->hs_split = split;
+  h->hs_sub = sub;
+  int rc = build(h, d);
+  *out = h;
+  return rc;
+}
+
+int gpu_hs_columns(vsvb_gpu *h, const double *w_dev, const int *src_dev, int j0, int nb, double *H_dev, double *S_dev) {
+  if (!h || h->hs_sub < 0) return VSVB_ERR_INPUT;
+  CK(cudaSetDevice(h->dev), "cudaSetDevice");
+  cudaStream_t st = h->st;
+  if (!h->hs_flag.p) CK(h->hs_flag.alloc(1), "alloc flag");
+  CK(cudaMemsetAsync(h->hs_flag.p, 0, sizeof(int), st), "memset flag");
+  const unsigned nq = (unsigned)h->ds.nq;
+  for (int nu = 0; nu < nb; ++nu) {
+    hs_weights_kernel<<<(h->totlen + 255) / 256, 256, 0, st>>>(h->coeff_d.p, w_dev, src_dev, h->totlen, j0, nu);
+    CK(cudaGetLastError(), "hs weights");
+    int rc = forward(h, true);
+    if (rc) return rc;
+    DetCtx dc = det_ctx(h);
+    AsmArgs aa = asm_args(h);
+    OrbArgs oa = orb_args(h);
+    /* pass 0: d(E_num)/dw, pass 1: d(W)/dw, from the same forward walk */
+    for (int pass = 0; pass < 2; ++pass) {
+      CK(cudaMemsetAsync(h->Cbar.p, 0, sizeof(double) * h->Cbar.n, st), "memset Cbar");
+      const double alpha = pass == 0 ? 1.0 : 0.0, beta = pass == 0 ? 0.0 : 1.0 / (double)h->ds.nelec;
+      hs_scale_kernel<<<nq, 128, 0, st>>>(dc, aa, h->nsplit, alpha, beta);
+      CK(cudaGetLastError(), "hs scale");
+      detpair_adjoint_kernel<<<nq, 128, 0, st>>>(dc, aa, h->nsplit);
+      CK(cudaGetLastError(), "detpair adjoint");
+      if (pass == 0 && h->nxelem > 0) {
+        XtabArgs xa = xtab_args(h); /* unscaled densities in the sweep: factor 1 */
+        xhrr_adjoint_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa, h->xbarh.p, h->xbar.p);
+        CK(cudaGetLastError(), "xhrr adjoint");
+        xtab_adjoint_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa, h->xbar.p, h->Cbar.p);
+        CK(cudaGetLastError(), "xtab adjoint");
+      }
+      orb_1e_adjoint_kernel<<<h->nsp, 128, 0, st>>>(oa, h->Sbar.p, h->Hbar.p, h->nsp, h->Cbar.p);
+      CK(cudaGetLastError(), "orb_1e adjoint");
+      entry_adjoint_kernel<<<1, 32, 0, st>>>(oa, h->hs_sub, j0, nb, h->Cbar.p,
+                                             (pass == 0 ? H_dev : S_dev) + (size_t)nu * nb, 0.5, h->hs_flag.p);
+      CK(cudaGetLastError(), "entry adjoint");
+    }
+  }
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, h->hs_flag.p, sizeof(int), cudaMemcpyDeviceToHost, st), "copy flag");
+  CK(cudaStreamSynchronize(st), "sync");
+  if (flag & 1) {
+    h->err = "an orbital has non-positive self-overlap";
+    return VSVB_ERR_NOT_NORMALISABLE;
+  }
+  if (flag & 2) {
+    h->err = "first_order_opt matrices through a singular determinant pair are not implemented";
+    return VSVB_ERR_SINGULAR;
+  }
+  return VSVB_OK;
+}
+
+int gpu_set_spin_coeffs(vsvb_gpu *h, const double *csc) {
+  if (!h || !csc) return VSVB_ERR_INPUT;
+  CK(cudaSetDevice(h->dev), "cudaSetDevice");
+  h->csc_h.assign(csc, csc + h->ds.nsc);
+  CK(cudaMemcpyAsync(h->coeff_sc.p, h->csc_h.data(), sizeof(double) * h->ds.nsc, cudaMemcpyHostToDevice, h->st),
+     "copy coeff_sc");
+  CK(cudaStreamSynchronize(h->st), "sync");
+  return VSVB_OK;
+}
+
+int gpu_spin_blocks(vsvb_gpu *h, const double *w_dev, double *BH_dev, double *BS_dev) {
+  if (!h) return VSVB_ERR_INPUT;
+  CK(cudaSetDevice(h->dev), "cudaSetDevice");
+  cudaStream_t st = h->st;
+  const std::vector<double> keep = h->csc_h, ones(h->ds.nsc, 1.0);
+  CK(cudaMemcpyAsync(h->coeff_sc.p, ones.data(), sizeof(double) * h->ds.nsc, cudaMemcpyHostToDevice, st), "copy");
+  CK(cudaMemcpyAsync(h->coeff_d.p, w_dev, sizeof(double) * h->totlen, cudaMemcpyDeviceToDevice, st), "copy coeff");
+  int rc = forward(h, false);
+  if (rc) return rc;
+  AsmArgs aa = asm_args(h);
+  spin_block_kernel<<<h->ds.nsc * h->ds.nsc, 256, 0, st>>>(det_ctx(h), aa, h->nsplit, BH_dev, BS_dev);
+  CK(cudaGetLastError(), "spin blocks");
+  CK(cudaMemcpyAsync(h->coeff_sc.p, keep.data(), sizeof(double) * h->ds.nsc, cudaMemcpyHostToDevice, st), "copy");
+  return finish_result(h, nullptr);
+}
+
+cudaStream_t gpu_stream(vsvb_gpu *h) { return h ? h->st : nullptr; }
+int gpu_nsc(const vsvb_gpu *h) { return h ? h->ds.nsc : 0; }
+
+int gpu_orbital_scales(vsvb_gpu *h, const double *w, double *ndf_scale, double *orb_scale) {
+  if (!h || !w) return VSVB_ERR_INPUT;
+  CK(cudaSetDevice(h->dev), "cudaSetDevice");
+  cudaStream_t st = h->st;
+  CK(cudaMemcpyAsync(h->coeff_d.p, w, sizeof(double) * h->totlen, cudaMemcpyHostToDevice, st), "copy coeff");
+  CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), st), "memset status");
+  OrbArgs oa = orb_args(h);
+  const size_t osh = sizeof(double) * std::max(h->maxobs, 1);
+  if (h->ndf > 0) ndf_norm_kernel<<<h->ndf, 128, osh, st>>>(oa);
+  orb_norm_kernel<<<h->nsp, 128, osh, st>>>(oa);
+  CK(cudaGetLastError(), "orb_norm");
+  if (ndf_scale && h->ndf > 0)
+    CK(cudaMemcpyAsync(ndf_scale, h->ndf_scale.p, sizeof(double) * h->ndf, cudaMemcpyDeviceToHost, st), "copy");
+  if (orb_scale) CK(cudaMemcpyAsync(orb_scale, h->orb_scale.p, sizeof(double) * h->nsp, cudaMemcpyDeviceToHost, st), "copy");
+  return finish_result(h, nullptr);
+}

@@ -22,7 +22,7 @@ namespace {
 struct Owned {
   vsvb_system_desc d;
   std::vector<int> atom_t, map_atom2shell, num_shell_atom, map_shell2prim, ang_mom, pair_sc, orbas_atnum,
-      orbas_atset, map_orbs, xpset;
+      orbas_atset, map_orbs, xpset, orbset, xorb, root;
   std::vector<double> coords, nuc_charge, exponent, con_coeff, coeff_sc, coeff;
 };
 
@@ -130,12 +130,14 @@ extern "C" int vsvb_read_input(const char *path, vsvb_system_desc **out, char *e
   (void)ntol_c;
   d.ntol_d = r.i();
   d.ntol_i = r.i();
-  r.i();
-  r.i();
-  r.i();
-  r.f();
-  r.f();
-  for (int k = 0; k < 2 * nset; ++k) r.i();
+  d.ntol_e_min = r.i();
+  d.ntol_e_max = r.i();
+  d.max_iter = r.i();
+  d.ptbnmax = r.f();
+  d.feather = r.f();
+  d.nset = nset;
+  o->orbset.assign(2 * (size_t)nset + 1, 0);
+  for (int k = 0; k < 2 * nset; ++k) o->orbset[k] = r.i();
   r.end();
   o->atom_t.resize(d.natom);
   o->coords.resize(3 * (size_t)d.natom);
@@ -222,9 +224,14 @@ extern "C" int vsvb_read_input(const char *path, vsvb_system_desc **out, char *e
     }
     r.end();
   }
+  o->xorb.assign((size_t)d.nxorb + 1, 0);
+  o->root.assign((size_t)d.nxorb + 1, 0);
   if (d.nxorb > 0) {
     r.begin();
-    for (int k = 0; k < 2 * d.nxorb; ++k) r.i();
+    for (int k = 0; k < d.nxorb; ++k) {
+      o->xorb[k] = r.i();
+      o->root[k] = r.i();
+    }
     r.end();
   }
   o->orbas_atnum.assign(norbs, 0);
@@ -284,6 +291,9 @@ extern "C" int vsvb_read_input(const char *path, vsvb_system_desc **out, char *e
   d.map_orbs = o->map_orbs.data();
   d.xpset = o->xpset.data();
   d.coeff = o->coeff.data();
+  d.orbset = o->orbset.data();
+  d.xorb = o->xorb.data();
+  d.root = o->root.data();
   *out = &o->d;
   return VSVB_OK;
 }

@@ -264,6 +264,7 @@ __global__ void orb_norm_kernel(OrbArgs a) {
   __syncthreads();
   double s = obs_quad(v, ao, n, a.S, a.nao, red);
   double sc = s > 0.0 ? rsqrt(s) : 0.0;
+  if (o == a.fixed_orb) sc = 1.0; /* first_order_opt's dummy orbitals keep weight 1 */
   if (threadIdx.x == 0) {
     a.orb_scale[o] = sc;
     if (!(s > 0.0)) atomicOr(a.status, 1);
@@ -320,15 +321,17 @@ __global__ void xtab_kernel(XtabArgs x) {
   int na = ncart(tm.la), nb = ncart(tm.lb);
   int ia = e / nb, ib = e - ia * nb;
   const double *ci = x.C + (size_t)tm.oi * x.maxobs, *ck = x.C + (size_t)tm.ok * x.maxobs;
-  auto val = [&](const double *c, int s0, int n, int comp) -> double {
+  /* the orbital keep_orb is never screened (a negative tolerance keeps every shell) */
+  const double dti = tm.oi == x.keep_orb ? -1.0 : x.dtol, dtk = tm.ok == x.keep_orb ? -1.0 : x.dtol;
+  auto val = [&](const double *c, int s0, int n, int comp, double dt) -> double {
     if (s0 < 0) return 0.0;
-    if (!shell_kept(c, s0, n, x.dtol)) return 0.0;
+    if (!shell_kept(c, s0, n, dt)) return 0.0;
     return c[s0 + comp];
   };
-  double ciA = val(ci, tm.sAi, na, ia), ckB = val(ck, tm.sBk, nb, ib);
+  double ciA = val(ci, tm.sAi, na, ia, dti), ckB = val(ck, tm.sBk, nb, ib, dtk);
   double v = ciA * ckB;
   if (!tm.same_shell) {
-    double ckA = val(ck, tm.sAk, na, ia), ciB = val(ci, tm.sBi, nb, ib);
+    double ckA = val(ck, tm.sAk, na, ia, dtk), ciB = val(ci, tm.sBi, nb, ib, dti);
     v += ckA * ciB;
   }
   x.xtab[t] = v * x.angn[tm.aoA + ia] * x.angn[tm.aoB + ib];
@@ -352,13 +355,14 @@ __global__ void xtab_adjoint_kernel(XtabArgs x, const double *xbar, double *Cbar
   const double scale = x.wres ? x.xbar_scale / x.wres[4] : x.xbar_scale;
   double g = xbar[t] * scale * x.angn[tm.aoA + ia] * x.angn[tm.aoB + ib];
   if (g == 0.0) return;
-  auto kept = [&](const double *c, int s0, int n) -> bool { return s0 >= 0 && shell_kept(c, s0, n, x.dtol); };
+  const double dti = tm.oi == x.keep_orb ? -1.0 : x.dtol, dtk = tm.ok == x.keep_orb ? -1.0 : x.dtol;
+  auto kept = [&](const double *c, int s0, int n, double dt) -> bool { return s0 >= 0 && shell_kept(c, s0, n, dt); };
   double *gi = Cbar + (size_t)tm.oi * x.maxobs, *gk = Cbar + (size_t)tm.ok * x.maxobs;
-  if (kept(ci, tm.sAi, na) && kept(ck, tm.sBk, nb)) {
+  if (kept(ci, tm.sAi, na, dti) && kept(ck, tm.sBk, nb, dtk)) {
     atomicAdd(gi + tm.sAi + ia, g * ck[tm.sBk + ib]);
     atomicAdd(gk + tm.sBk + ib, g * ci[tm.sAi + ia]);
   }
-  if (!tm.same_shell && kept(ck, tm.sAk, na) && kept(ci, tm.sBi, nb)) {
+  if (!tm.same_shell && kept(ck, tm.sAk, na, dtk) && kept(ci, tm.sBi, nb, dti)) {
     atomicAdd(gk + tm.sAk + ia, g * ci[tm.sBi + ib]);
     atomicAdd(gi + tm.sBi + ib, g * ck[tm.sAk + ia]);
   }
@@ -462,4 +466,31 @@ __global__ void orb_norm_adjoint_kernel(OrbArgs a, const double *Cbar, double *c
   __syncthreads();
   if (threadIdx.x == 0)
     for (int t = a.term0[o]; t < a.term0[o + 1]; ++t) coeff_bar[a.term_j[t]] += g[a.term_slot[t]];
+}
+
+/* dE/d(weights) of orbital o before normal(): the weight scatter's adjoint
+ * over the orbital's terms (an entry through a derived basis function picks
+ * up that function's normalised expansion), scaled, into out[0..nent) for
+ * the entries j0..j0+nent of the weight array.  One thread, fixed order.
+ * flag (optional) collects the evaluation's status bits. */
+__global__ void entry_adjoint_kernel(OrbArgs a, int o, int j0, int nent, const double *Cbar, double *out, double scale,
+                                     int *flag) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (flag) *flag |= *a.status; /* the evaluation's status bits, kept over the columns */
+  for (int e = 0; e < nent; ++e) out[e] = 0.0;
+  const double *cb = Cbar + (size_t)o * a.maxobs;
+  for (int t = a.term0[o]; t < a.term0[o + 1]; ++t) {
+    double f = 1.0;
+    if (a.term_m[t] >= 0) f = a.coeff[a.term_m[t]] * a.ndf_scale[a.term_f[t]];
+    out[a.term_j[t] - j0] += scale * f * cb[a.term_slot[t]];
+  }
+}
+
+/* the weight array of a first_order_opt evaluation: entry t takes w[src[t]]
+ * from the caller's weights, or (src[t] < 0: the substituted orbital's
+ * entries j0, j0+1, ...) 1 at entry j0 + nu and 0 elsewhere */
+__global__ void hs_weights_kernel(double *coeff, const double *w, const int *src, int n, int j0, int nu) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  coeff[t] = src[t] >= 0 ? w[src[t]] : (t - j0 == nu ? 1.0 : 0.0);
 }

@@ -29,6 +29,7 @@ struct OrbArgs {
   double *ndf_scale, *orb_scale;
   double *Craw, *C;           /* [norb_all * maxobs] */
   int *status;
+  int fixed_orb;              /* orbital taken as given, not normalised (-1: none) */
 };
 
 struct XTerm {
@@ -58,6 +59,7 @@ struct XtabArgs {
   const double *hrr;
   double *xtabh;
   float *xtabh32; /* the same in FP32 */
+  int keep_orb;   /* an orbital exempt from the per-shell LCAO screen (-1: none) */
 };
 
 __global__ void ao_1e_kernel(Ao1eArgs a);
@@ -70,4 +72,7 @@ __global__ void xhrr_kernel(XtabArgs x);
 __global__ void xhrr_adjoint_kernel(XtabArgs x, const double *xbarh, double *xbar);
 __global__ void orb_1e_adjoint_kernel(OrbArgs a, const double *Sbar, const double *Hbar, int nsp, double *Cbar);
 __global__ void orb_norm_adjoint_kernel(OrbArgs a, const double *Cbar, double *coeff_bar);
+__global__ void entry_adjoint_kernel(OrbArgs a, int o, int j0, int nent, const double *Cbar, double *out, double scale,
+                                     int *flag);
+__global__ void hs_weights_kernel(double *coeff, const double *w, const int *src, int n, int j0, int nu);
 #endif

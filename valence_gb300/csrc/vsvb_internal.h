@@ -97,6 +97,10 @@ struct PairOp {
 
 struct DetSetup {
   int nelec, nalpha, nbeta, npair, nunpd, ndocc, nnd, nsp;
+  /* non-DOCC spatial orbitals of the task loop (num_non_docc of vsvb_energy):
+   * nnd, or nnd + 2 when a DOCC orbital's alpha and beta slots hold
+   * different orbitals (first_order_opt, valence.F90:578-603) */
+  int nsd;
   int nsc;          /* number of spin couplings used (>=1) */
   long long nq;     /* determinant pairs */
 };
