@@ -112,6 +112,7 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
                     help="time only the headline mixed arm (used for per-kernel launch lists)")
+    ap.add_argument("--no-optimizer", action="store_true", help="skip the optimiser-path figures")
     ap.add_argument("--batch", type=int, default=256,
                     help="molecules in the batched (one CUDA graph) measurement; 0 skips it")
     return ap.parse_args()
@@ -346,9 +347,62 @@ def run_ours(a, rank, world):
         for k in ("fp64", "mixed_native_fp64", "mixed_over_fp64", "abs_dE_mixed_vs_fp64", "energy_fp64", "e2e"):
             out[k] = None
         out["note"] = "headline mixed arm only (per-kernel launch-list run)"
-    elif a.batch > 0:
-        out["batch"] = run_batch(a, timed, world)
+    else:
+        if a.batch > 0:
+            out["batch"] = run_batch(a, timed, world)
+        if not a.no_optimizer:
+            out["optimizer"] = run_optimizer(a, dev)
     print(json.dumps(out))
+
+
+def run_optimizer(a, dev):
+    """The optimiser path (vsvb_opt_*: first_order_opt's H/S as adjoint
+    columns, rsg, minimize_energy) on the reference's own optimisation test
+    input c2-pt-vshf-p2 (a committed fixture; its optimised energy is pinned
+    at 1e-6 Eh by testing/testing.py) with the CPU oracle's literal H/S build
+    of the same orbital -- nb(nb+1)/2 transition energies, valence.F90:679-703
+    -- timed beside it, and the H/S build of one DOCC orbital of the headline
+    workload in FP64 and double-float."""
+    import numpy as np
+
+    from valence_gb300 import api
+    from tests import oracle_py
+    case = [c for c in oracle_py.goldens()["cases"] if c["converged"] and c["name"] == "c2-pt-vshf-p2"][0]
+    path = os.path.join(oracle_py.GOLDEN, case["input"])
+    opt = api.Optimizer(path, device=dev)
+    iorb = 3
+    opt.first_order_hs(iorb)
+    t = time.perf_counter()
+    h, s = opt.first_order_hs(iorb)
+    t_hs = time.perf_counter() - t
+    t = time.perf_counter()
+    res, _, _ = opt.minimize()
+    t_min = time.perf_counter() - t
+    opt.close()
+    cores = os.cpu_count() or 1
+    o = oracle_py.OptOracle(path)
+    t = time.perf_counter()
+    h_ref, s_ref = o.first_order_hs(iorb, cores)
+    t_cpu = time.perf_counter() - t
+    out = {"input": "c2-pt-vshf-p2 (reference test input; C2, 2 unpaired + 5 DOCC, 76 weights)",
+           "hs_orbital": iorb, "hs_order": int(h.shape[0]),
+           "hs_gpu_ms": 1e3 * t_hs, "hs_cpu_oracle_s": t_cpu, "hs_cpu_cores": cores,
+           "hs_speedup": t_cpu / t_hs, "hs_max_rel_diff": float(np.max(np.abs(h - h_ref)) / np.max(np.abs(h_ref))),
+           "minimize_s": t_min, "minimize_energy": res["energy"], "golden_energy": case["total_energy"],
+           "minimize_abs_dE": abs(res["energy"] - case["total_energy"]), "iterations": res["iterations"],
+           "hs_builds": res["n_hs_builds"]}
+    with tempfile.TemporaryDirectory() as d:
+        wpath = _workload(a.workload, d)
+        for name, prec in (("fp64", api.FP64), ("double_float", api.MIXED_DF64)):
+            opt = api.Optimizer(wpath, precision=prec, device=dev)
+            iorb = opt.desc_counts()["nnd"] + 1  # the first DOCC orbital
+            opt.first_order_hs(iorb)
+            t = time.perf_counter()
+            opt.first_order_hs(iorb)
+            out[f"{a.workload}_hs_{name}_ms"] = 1e3 * (time.perf_counter() - t)
+            out[f"{a.workload}_hs_order"] = int(opt.map_orbs[iorb] - opt.map_orbs[iorb - 1])
+            opt.close()
+    return out
 
 
 def run_batch(a, timed, world):

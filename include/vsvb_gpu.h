@@ -184,8 +184,8 @@ int vsvb_gpu_batch_energy_grad(vsvb_gpu *const *handles, int n, const double *co
                                vsvb_energy_result *results, double *const *grads);
 
 /* Batched energy + gradient of many molecules as ONE CUDA graph launch.
- * vsvb_batch_create takes handles on one device (gradient-capable: no
- * derived basis functions), runs one warm-up evaluation on each, and keeps
+ * vsvb_batch_create takes handles on one device, runs one warm-up
+ * evaluation on each, and keeps
  * them borrowed for the batch's life.  vsvb_batch_energy_grad copies
  * weights_dev[i] (device, handle i's totlen) in, evaluates every molecule
  * -- each on its own stream branch of the graph, so their kernels run

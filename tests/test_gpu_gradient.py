@@ -167,3 +167,40 @@ def test_sweep_timing_reports_every_class(vg, tmp_path):
         assert both[c]["flops"] > fwd[c]["flops"] > 0
     wall = s.sweep_wall_ms()
     assert wall >= 0.99 * max(x["ms"] for x in both.values())
+
+
+@pytest.mark.parametrize("name", ["be+ndf", "h+ndf", "cu+", "c2-pt-vshf-p2"])
+def test_gradient_through_derived_basis_functions(vg, name):
+    """Inputs whose orbitals expand over derived basis functions (NDFs,
+    ndf2obs, valence.F90:2191-2247): the gradient with respect to every
+    weight, the NDFs' own expansion weights included, against central
+    differences of the GPU energy, in both adjoint modes."""
+    oracle = built_oracle()
+    p = os.path.join(oracle.GOLDEN, "cases", "testing", name)
+    s0 = vg.System(p, grad_mode=0)
+    s1 = vg.System(p, grad_mode=1)
+    c0 = s0.coeff0.copy() * (1.0 + 0.02 * np.random.default_rng(4).standard_normal(s0.totlen))
+    r0, g0 = s0.energy_grad(c0)
+    r1, g1 = s1.energy_grad(c0)
+    assert np.max(np.abs(g0 - g1)) < 1e-8 * max(1.0, np.abs(g1).max())
+    js = range(len(c0)) if len(c0) <= 40 else np.random.default_rng(5).choice(len(c0), 40, replace=False)
+    for j in js:
+        cp, cm = c0.copy(), c0.copy()
+        cp[j] += H
+        cm[j] -= H
+        fd = (s0.energy(cp)["energy"] - s0.energy(cm)["energy"]) / (2 * H)
+        assert abs(g0[j] - fd) < 1e-6, (j, g0[j], fd)
+
+
+def test_gradient_through_a_singular_pair_is_a_status(vg):
+    """n2.sc4val-b.p2 has exactly singular determinant pairs (symmetry-equal
+    coupled orbitals); its gradient is refused with VSVB_ERR_SINGULAR, the
+    energy still evaluates, and the handle stays usable."""
+    oracle = built_oracle()
+    p = os.path.join(oracle.GOLDEN, "cases", "testing", "n2.sc4val-b.p2")
+    s = vg.System(p)
+    with pytest.raises(vg.VSVBError, match=r"\(4\)"):
+        s.energy_grad()
+    r = s.energy()
+    assert r["n_singular_pairs"] > 0
+    assert np.isfinite(r["energy"])

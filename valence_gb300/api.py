@@ -490,6 +490,7 @@ class Optimizer:
         self._desc = read_input(path)
         d = self._desc.contents
         self.totlen, self.nspinc = d.totlen, d.nspinc
+        self.npair, self.nunpd, self.ndocc, self.ndf = d.npair, d.nunpd, d.ndocc, d.ndf
         self.map_orbs = np.ctypeslib.as_array(d.map_orbs, shape=(2 * d.npair + d.nunpd + d.ndocc + d.ndf + 1,)).copy()
         self.coeff0 = np.ctypeslib.as_array(d.coeff, shape=(d.totlen,)).copy()
         self.coeff_sc0 = np.ctypeslib.as_array(d.coeff_sc, shape=(max(d.nspinc, 1),)).copy()
@@ -519,6 +520,10 @@ class Optimizer:
     def _check(self, rc, what):
         if rc:
             raise VSVBError(f"{what} failed ({rc}): {lib().vsvb_opt_last_error(self._o).decode()}")
+
+    def desc_counts(self):
+        return {"npair": self.npair, "nunpd": self.nunpd, "ndocc": self.ndocc, "ndf": self.ndf,
+                "nnd": 2 * self.npair + self.nunpd}
 
     def first_order_hs(self, iorb, coeff=None, coeff_sc=None):
         c = np.ascontiguousarray(self.coeff0 if coeff is None else coeff, dtype=np.float64)

@@ -459,6 +459,7 @@ __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
     }
     __syncthreads();
   }
+  if (threadIdx.x == 0 && d.nsing && d.sing[q]) atomicAdd(d.nsing, 1);
 }
 
 /* ---- energy (and adjoint) assembly: grid (nq, nsplit) ---- */

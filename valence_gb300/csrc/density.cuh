@@ -15,6 +15,7 @@ struct DetCtx {
   double *det_a, *det_b;  /* [nq] */
   double *Ta, *Tb;        /* [nq][n*n] inverses (zero on the exact-minor path) */
   int *sing;              /* [nq] bit0 alpha, bit1 beta on the exact-minor path */
+  int *nsing;             /* count of determinant pairs with a bit set (optional) */
 };
 
 struct AsmArgs {

@@ -203,13 +203,14 @@ struct vsvb_gpu {
   int nxterm = 0;
   DBuf<int> obs_n, obs_ao, term0, term_slot, term_j, term_m, term_f, ndf_orb;
   DBuf<double> coeff_d, ndf_scale, orb_scale, Craw, C, So, Ho, xtab, T, sqT, qmax, q0max;
-  DBuf<int> pair_slot, slot_pair, slot_which, sing, status;
+  DBuf<int> pair_slot, slot_pair, slot_which, sing, status, nsing;
   DBuf<double> coeff_sc, det_a, det_b, Ta, Tb, scratch;
   int ld_scratch = 0;
   DBuf<double> part_e1, part_wf, part_e2, result;
   /* adjoint */
   DBuf<double> Tbar, Sbar, Hbar, xbar, xbarh, Cbar, vtot, Gglob, coeff_bar;
   DBuf<double> Gs, vtot_s, D1; /* dE/dS parts of the fused (unscaled) adjoint walk */
+  DBuf<double> ndf_bar;        /* dE/d(scale) of each derived basis function */
   bool grad_ready = false;
   int last_singular = 0;
   /* first_order_opt configuration (vsvb_opt): hs_split 1 / 2 when the
@@ -327,6 +328,7 @@ DetCtx det_ctx(vsvb_gpu *h) {
   d.Ta = h->Ta.p;
   d.Tb = h->Tb.p;
   d.sing = h->sing.p;
+  d.nsing = h->nsing.p;
   return d;
 }
 
@@ -1054,6 +1056,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   CK(h->Ta.alloc(std::max<long long>(nq * na * na, 1)), "alloc Ta");
   CK(h->Tb.alloc(std::max<long long>(nq * nb * nb, 1)), "alloc Tb");
   CK(h->sing.alloc(nq), "alloc sing");
+  CK(h->nsing.alloc(1), "alloc nsing");
   h->ld_scratch = 2 * std::max(na, nb) * std::max(std::max(na, nb), 1);
   CK(h->scratch.alloc(std::max<long long>(nq * h->ld_scratch, 1)), "alloc scratch");
   long long ntij = (long long)nsp * (nsp + 1) / 2;
@@ -1098,6 +1101,7 @@ int alloc_grad(vsvb_gpu *h) {
   CK(h->vtot_s.alloc((size_t)nq * h->nsplit_max), "alloc vtot_s");
   CK(h->D1.alloc((size_t)h->nsp * h->nsp), "alloc D1");
   CK(h->coeff_bar.alloc(h->totlen), "alloc coeff_bar");
+  CK(h->ndf_bar.alloc(std::max(h->ndf, 1)), "alloc ndf_bar");
   h->grad_ready = true;
   return VSVB_OK;
 }
@@ -1175,6 +1179,7 @@ int forward(vsvb_gpu *h, bool fused = false) {
     h->launches += 2;
   }
   CK(cudaMemsetAsync(h->sing.p, 0, sizeof(int) * h->sing.n, st), "memset sing");
+  CK(cudaMemsetAsync(h->nsing.p, 0, sizeof(int), st), "memset nsing");
   DetCtx dc = det_ctx(h);
   detpair_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, h->scratch.p, h->ld_scratch);
   CK(cudaGetLastError(), "detpair");
@@ -1252,15 +1257,19 @@ void fill_result(const vsvb_gpu *h, const double *r, vsvb_energy_result *out) {
 
 int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
   double r[5];
-  int status = 0;
+  int status = 0, nsing = 0;
   CK(cudaMemcpyAsync(r, h->result.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, h->st), "copy result");
   CK(cudaMemcpyAsync(&status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->st), "copy status");
+  CK(cudaMemcpyAsync(&nsing, h->nsing.p, sizeof(int), cudaMemcpyDeviceToHost, h->st), "copy nsing");
   CK(cudaStreamSynchronize(h->st), "sync");
   if (status & 1) {
     h->err = "an orbital has non-positive self-overlap";
     return VSVB_ERR_NOT_NORMALISABLE;
   }
-  if (out) fill_result(h, r, out);
+  if (out) {
+    fill_result(h, r, out);
+    out->n_singular_pairs = nsing;
+  }
   return VSVB_OK;
 }
 
@@ -1356,10 +1365,6 @@ int autotune(vsvb_gpu *h) {
  * forward + backward enqueue without a host round trip (and can be captured
  * into a CUDA graph) */
 int backward(vsvb_gpu *h, bool fused) {
-  if (h->ndf > 0) {
-    h->err = "gradient through derived basis functions is not implemented";
-    return VSVB_ERR_UNSUPPORTED;
-  }
   int rc = alloc_grad(h);
   if (rc) return rc;
   cudaStream_t st = h->st;
@@ -1404,9 +1409,16 @@ int backward(vsvb_gpu *h, bool fused) {
   OrbArgs oa = orb_args(h);
   orb_1e_adjoint_kernel<<<h->nsp, 128, 0, st>>>(oa, h->Sbar.p, h->Hbar.p, h->nsp, h->Cbar.p);
   CK(cudaGetLastError(), "orb_1e adjoint");
+  if (h->ndf > 0) CK(cudaMemsetAsync(h->ndf_bar.p, 0, sizeof(double) * h->ndf, st), "memset ndf_bar");
   orb_norm_adjoint_kernel<<<h->nsp, 128, sizeof(double) * std::max(h->maxobs, 1), st>>>(oa, h->Cbar.p,
-                                                                                     h->coeff_bar.p);
+                                                                                     h->coeff_bar.p, h->ndf_bar.p);
   CK(cudaGetLastError(), "orb_norm adjoint");
+  if (h->ndf > 0) {
+    ndf_norm_adjoint_kernel<<<h->ndf, 128, 2 * sizeof(double) * std::max(h->maxobs, 1), st>>>(oa, h->ndf_bar.p,
+                                                                                            h->coeff_bar.p);
+    CK(cudaGetLastError(), "ndf_norm adjoint");
+    h->launches++;
+  }
   h->launches += 5;
   return VSVB_OK;
 }
@@ -1528,10 +1540,6 @@ static int enqueue_eval(vsvb_gpu *h, bool fused) {
 
 static int energy_grad_common(vsvb_gpu *h, vsvb_energy_result *out, double *grad, bool grad_on_device) {
   const bool fused = h->opt.grad_mode == 0;
-  if (h->ndf > 0) {
-    h->err = "gradient through derived basis functions is not implemented";
-    return VSVB_ERR_UNSUPPORTED;
-  }
   int rc = enqueue_eval(h, fused);
   if (rc) return rc;
   CK(cudaMemcpyAsync(grad, h->coeff_bar.p, sizeof(double) * h->totlen,
@@ -1672,7 +1680,7 @@ int vsvb_batch_create(vsvb_gpu *const *handles, int n, vsvb_batch **out) {
   b->dev = handles[0]->dev;
   for (int i = 0; i < n; ++i) {
     vsvb_gpu *h = handles[i];
-    if (!h || h->dev != b->dev || h->ndf > 0) {
+    if (!h || h->dev != b->dev) {
       delete b;
       return VSVB_ERR_INPUT;
     }

@@ -442,11 +442,14 @@ __global__ void orb_1e_adjoint_kernel(OrbArgs a, const double *Sbar, const doubl
   }
 }
 
-/* adjoint of orb_norm_kernel for orbitals without NDF terms:
+/* adjoint of orb_norm_kernel:
  * C = s Craw, s = (Craw^T S Craw)^(-1/2)
- * => Craw_bar = s Cbar - s^3 (Cbar . Craw) S Craw; then coeff_bar over the
- * orbital's weight terms.  One block per orbital. */
-__global__ void orb_norm_adjoint_kernel(OrbArgs a, const double *Cbar, double *coeff_bar) {
+ * => Craw_bar = s Cbar - s^3 (Cbar . Craw) S Craw; then over the orbital's
+ * weight terms: coeff_bar of its own weight, and for a term through a
+ * derived basis function f (Craw[slot] += c_j c_m s_f) also the NDF's weight
+ * c_m and the adjoint of its scale s_f (ndf_bar, finished by
+ * ndf_norm_adjoint_kernel).  One block per orbital. */
+__global__ void orb_norm_adjoint_kernel(OrbArgs a, const double *Cbar, double *coeff_bar, double *ndf_bar) {
   __shared__ double red[8];
   extern __shared__ double sh[];
   int o = blockIdx.x;
@@ -465,7 +468,44 @@ __global__ void orb_norm_adjoint_kernel(OrbArgs a, const double *Cbar, double *c
   }
   __syncthreads();
   if (threadIdx.x == 0)
-    for (int t = a.term0[o]; t < a.term0[o + 1]; ++t) coeff_bar[a.term_j[t]] += g[a.term_slot[t]];
+    for (int t = a.term0[o]; t < a.term0[o + 1]; ++t) {
+      const double gk = g[a.term_slot[t]];
+      if (a.term_m[t] < 0) {
+        coeff_bar[a.term_j[t]] += gk;
+      } else {
+        const int m = a.term_m[t], f = a.term_f[t];
+        const double cj = a.coeff[a.term_j[t]], cm = a.coeff[m], sf = a.ndf_scale[f];
+        coeff_bar[a.term_j[t]] += gk * cm * sf;
+        atomicAdd(coeff_bar + m, gk * cj * sf);
+        atomicAdd(ndf_bar + f, gk * cj * cm);
+      }
+    }
+}
+
+/* adjoint of ndf_norm_kernel: s_f = (u^T S u)^(-1/2) over the NDF's raw
+ * vector u, so dE/dc_m += ndf_bar[f] * (-s_f^3) (S u)[slot of m].  One block
+ * per NDF, after orb_norm_adjoint_kernel. */
+__global__ void ndf_norm_adjoint_kernel(OrbArgs a, const double *ndf_bar, double *coeff_bar) {
+  extern __shared__ double u[];
+  const int f = blockIdx.x, o = a.ndf_orb[f];
+  const int n = a.obs_n[o];
+  const int *ao = a.obs_ao + (size_t)o * a.maxobs;
+  double *su = u + a.maxobs;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) u[k] = 0.0;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int t = a.term0[o]; t < a.term0[o + 1]; ++t) u[a.term_slot[t]] += a.coeff[a.term_j[t]];
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    double v = 0.0;
+    for (int l = 0; l < n; ++l) v += a.S[(size_t)ao[k] * a.nao + ao[l]] * u[l];
+    su[k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double sf = a.ndf_scale[f], w = -ndf_bar[f] * sf * sf * sf;
+    for (int t = a.term0[o]; t < a.term0[o + 1]; ++t) coeff_bar[a.term_j[t]] += w * su[a.term_slot[t]];
+  }
 }
 
 /* dE/d(weights) of orbital o before normal(): the weight scatter's adjoint

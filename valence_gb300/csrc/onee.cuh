@@ -71,7 +71,8 @@ __global__ void xtab_adjoint_kernel(XtabArgs x, const double *xbar, double *Cbar
 __global__ void xhrr_kernel(XtabArgs x);
 __global__ void xhrr_adjoint_kernel(XtabArgs x, const double *xbarh, double *xbar);
 __global__ void orb_1e_adjoint_kernel(OrbArgs a, const double *Sbar, const double *Hbar, int nsp, double *Cbar);
-__global__ void orb_norm_adjoint_kernel(OrbArgs a, const double *Cbar, double *coeff_bar);
+__global__ void orb_norm_adjoint_kernel(OrbArgs a, const double *Cbar, double *coeff_bar, double *ndf_bar);
+__global__ void ndf_norm_adjoint_kernel(OrbArgs a, const double *ndf_bar, double *coeff_bar);
 __global__ void entry_adjoint_kernel(OrbArgs a, int o, int j0, int nent, const double *Cbar, double *out, double scale,
                                      int *flag);
 __global__ void hs_weights_kernel(double *coeff, const double *w, const int *src, int n, int j0, int nu);
