@@ -130,3 +130,28 @@ def test_minimize_reproduces_optimised_goldens(env, case):
     assert abs(res["energy"] - case["total_energy"]) < tol, (res, case["total_energy"])
     assert res["converged"] == 1
     opt.close()
+
+
+def test_optimised_orbitals_file_round_trip(env, tmp_path):
+    """minimize_energy, then the 'orbitals' file (xm_output) of the result
+    written with the optimised weights and read back as an input: its guess
+    energy is the optimised energy."""
+    api, oracle_py = env
+    path = _path(oracle_py, "examples", "li_opt")
+    opt = api.Optimizer(path)
+    res, c, csc = opt.minimize()
+    d = api.read_input(path)
+    txt = api.format_orbitals(d, c, res["energy"], res["etol"], res["converged"])
+    api.lib().vsvb_free_desc(d)
+    src = open(path).read().split("\n")
+    # the input's orbital section is replaced by the new one (the header,
+    # geometry, basis and coupling records stay)
+    first = [ln for ln in txt.split("\n") if ln.strip()][0]
+    k = [i for i, ln in enumerate(src) if ln.split() == first.split()][0]
+    out = tmp_path / "li_opt.next"
+    out.write_text("\n".join(src[:k]) + "\n" + txt)
+    s = api.System(str(out))
+    e = s.energy()["energy"]
+    s.close()
+    opt.close()
+    assert abs(e - res["energy"]) < 1e-7, (e, res["energy"])

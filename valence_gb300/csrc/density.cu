@@ -82,6 +82,7 @@ struct QInfo {
   double w;
   /* after the determinant pairs are factorised (load_dets) */
   double da, db; /* det of the alpha / beta block */
+  double wdd;    /* w * da * db */
   int sing;      /* exact-minor flags per spin block */
 };
 
@@ -95,7 +96,7 @@ __device__ __forceinline__ QInfo decode_q(const DetCtx &d, long long q) {
   r.isc = (int)(sp / d.ds.nsc);
   r.jsc = (int)(sp % d.ds.nsc);
   r.w = d.coeff_sc[r.isc] * d.coeff_sc[r.jsc];
-  r.da = r.db = 0.0;
+  r.da = r.db = r.wdd = 0.0;
   r.sing = 0;
   return r;
 }
@@ -103,6 +104,7 @@ __device__ __forceinline__ QInfo decode_q(const DetCtx &d, long long q) {
 __device__ __forceinline__ void load_dets(const DetCtx &d, long long q, QInfo &qi) {
   qi.da = d.det_a[q];
   qi.db = d.det_b[q];
+  qi.wdd = qi.w * qi.da * qi.db;
   qi.sing = d.sing[q];
 }
 
@@ -214,7 +216,8 @@ __device__ Cof cofactor_loc(const DetCtx &d, long long q, const QInfo &qi, int n
       c.Jb = Tb[c.cb[0] * nb + c.rb[0]] * Tb[c.cb[1] * nb + c.rb[1]] - Tb[c.cb[0] * nb + c.rb[1]] * Tb[c.cb[1] * nb + c.rb[0]];
     fb = qi.db * c.Jb;
   }
-  c.v = qi.w * fa * fb;
+  /* on the inverse path fa * fb = da * db * Ja * Jb */
+  c.v = (sing & 3) ? qi.w * fa * fb : qi.wdd * (c.Ja * c.Jb);
   return c;
 }
 
@@ -245,7 +248,7 @@ __device__ void accum_G(const DetCtx &d, long long q, const QInfo &qi, const Cof
                         int lda, int ldb) {
   if (!c.ok || coef == 0.0) return;
   const int na = d.ds.nalpha, nb = d.ds.nbeta;
-  const double dd = qi.w * qi.da * qi.db;
+  const double dd = qi.wdd;
   if (c.na_s > 0) {
     const double *Ta = d.Ta + (size_t)q * na * na;
     const double f = coef * dd * c.Jb;
@@ -583,6 +586,7 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
       if (!(es || xs)) continue;
     }
     const double fac = (ko == io && lo == jo) ? 1.0 : 2.0;
+    const double fw = fac * inv_w;
     const bool id = io >= nnd, jd = jo >= nnd, kd = ko >= nnd, ld = lo >= nnd;
     const int iso = id ? 2 : 1, jso = jd ? 2 : 1, kso = kd ? 2 : 1, lso = ld ? 2 : 1;
     double esum = 0.0, xsum = 0.0, dsum_e = 0.0, dsum_x = 0.0;
@@ -622,14 +626,10 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
             double dd = 0.0, xd = 0.0;
             if (es && ce_c.ok) dd = ce_c.v;
             if (xs && cx_c.ok) xd = (es && ce_c.ok) ? ce_c.v : -cx_c.v;
-            if (es) {
-              esum += dd * eint;
-              dsum_e += dd;
-            }
-            if (xs) {
-              xsum += xd * xint;
-              dsum_x += xd;
-            }
+            /* the task's integrals are common to its spin terms: the sums
+             * take the densities, the integrals multiply once below */
+            if (es) dsum_e += dd;
+            if (xs) dsum_x += xd;
             if (GRAD) {
               /* coefficients of the two cofactors in fac*(dd*eint - xd*xint)/W */
               double cve = 0.0, cvx = 0.0;
@@ -639,8 +639,8 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
               } else if (xs && cx_c.ok) {
                 cvx = xint;
               }
-              cve *= fac * inv_w;
-              cvx *= fac * inv_w;
+              cve *= fw;
+              cvx *= fw;
               if (ce_c.ok && cve != 0.0) {
                 vtot += cve * ce_c.v;
                 accum_G(d, q, qi, ce_c, cve, Ga, Gb, lda, ldb);
@@ -654,6 +654,8 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
         }
       }
     }
+    esum = dsum_e * eint;
+    xsum = dsum_x * xint;
     e2 += fac * (esum - xsum);
     if (DENS) {
       if (diag) {
