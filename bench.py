@@ -348,6 +348,7 @@ def run_ours(a, rank, world):
             out[k] = None
         out["note"] = "headline mixed arm only (per-kernel launch-list run)"
     else:
+        out["water"] = run_water(a, timed, dev)
         if a.batch > 0:
             out["batch"] = run_batch(a, timed, world)
         if not a.no_optimizer:
@@ -405,6 +406,34 @@ def run_optimizer(a, dev):
     return out
 
 
+def run_water(a, timed, dev):
+    """The reference's CPU-runnable configuration (H2O, 13 functions, 5
+    DOCC; a parity case): energy + gradient per second in FP64 and on the
+    mixed path, device-resident weights, with the oracle's energy beside it."""
+    import torch
+
+    import valence_gb300 as vg
+    from valence_gb300 import configs
+    out = {"workload": "water_vshf (H2O, 13 functions, 5 DOCC)"}
+    with tempfile.TemporaryDirectory() as d:
+        p = configs.water_vshf(os.path.join(d, "water.inp"))
+        for name, prec in (("fp64", vg.FP64), ("mixed_df64", vg.MIXED_DF64)):
+            s = vg.System(p, precision=prec, device=dev)
+            s.set_stream(torch.cuda.current_stream().cuda_stream)
+            w = torch.tensor(s.coeff0, dtype=torch.float64, device="cuda")
+            g = torch.zeros(s.totlen, dtype=torch.float64, device="cuda")
+            ms, _, r = timed(lambda: s.energy_grad_device(w.data_ptr(), g.data_ptr()), max(a.steps, 10), a.warmup)
+            out[name] = {"value": 1e3 / statistics.mean(ms), "unit": "evals/s", "ms_per_step": statistics.mean(ms),
+                         "energy": r["energy"]}
+            s.close()
+        if not a.no_cpu_baseline:
+            dt, e = _oracle_energy_time(p, os.cpu_count() or 1)
+            out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "evals/s", "cores": os.cpu_count() or 1,
+                                   "kind": "port", "sample": "one full energy evaluation by the CPU oracle",
+                                   "dE_vs_gpu_fp64": abs(e - out["fp64"]["energy"])}
+    return out
+
+
 def run_batch(a, timed, world):
     """Batched energy + gradient: a.batch independent random molecules (2-12
     atoms, Z in {1,3,6,7,8,9}, 4-80 functions, 0-2 coupled pairs; seeds from
@@ -425,7 +454,14 @@ def run_batch(a, timed, world):
             except vg.VSVBError:
                 skipped += 1
                 continue
-            systems.append(s)
+            systems.append((s, p))
+        # CPU baseline: the oracle on every 16th molecule, all host cores
+        cpu_s, sample = 0.0, systems[::16]
+        if not a.no_cpu_baseline:
+            for _, p in sample:
+                dt, _ = _oracle_energy_time(p, os.cpu_count() or 1)
+                cpu_s += dt
+    systems = [s for s, _ in systems]
     ws = [torch.tensor(s.coeff0, dtype=torch.float64, device="cuda") for s in systems]
     gs = [torch.zeros(s.totlen, dtype=torch.float64, device="cuda") for s in systems]
     b = vg.Batch(systems)
@@ -442,6 +478,11 @@ def run_batch(a, timed, world):
            "value": world * len(systems) / (t * 1e-3), "unit": "molecule energy+grad evals/s",
            "ms_per_step": t, "kernels_per_graph_launch": b.launches, "skipped_draws": skipped,
            "weights_total": int(sum(nf))}
+    if cpu_s > 0:
+        out["cpu_baseline"] = {"value": len(sample) / cpu_s, "unit": "molecule energy evals/s",
+                               "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": f"the CPU oracle's full energy of every 16th molecule ({len(sample)} of "
+                                         f"{len(systems)}), one at a time on all host cores; energy only"}
     b.close()
     for s in systems:
         s.close()

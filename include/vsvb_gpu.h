@@ -207,6 +207,12 @@ void vsvb_batch_destroy(vsvb_batch *batch);
  * CUDA events on the stream the kernels are launched on. */
 int vsvb_gpu_set_stream(vsvb_gpu *h, void *stream);
 
+/* Spin-coupling weights coeff_sc (nspinc doubles, host) for the following
+ * evaluations, in place of the description's: the reference's spin_opt
+ * (valence.F90:927-930) changes them between energy calls.  A captured CUDA
+ * graph stays valid (the weights live in device memory). */
+int vsvb_gpu_set_spin_coeffs(vsvb_gpu *h, const double *coeff_sc);
+
 /* Diagnostics for roofline reporting: run the forward ERI pass once with a
  * CUDA event pair around every class launch.  Per launch i (up to cap):
  * ms[i] its duration, flops[i] its algorithmic FLOP count (Rys roots, 2D

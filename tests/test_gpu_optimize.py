@@ -155,3 +155,21 @@ def test_optimised_orbitals_file_round_trip(env, tmp_path):
     s.close()
     opt.close()
     assert abs(e - res["energy"]) < 1e-7, (e, res["energy"])
+
+
+def test_spin_coupling_weights_per_evaluation(env):
+    """vsvb_gpu_set_spin_coeffs: the energy with new coupling weights equals
+    the oracle's with the same weights, also through a replayed graph."""
+    api, oracle_py = env
+    path = _path(oracle_py, "testing", "be-sc")
+    s = api.System(path)
+    o = oracle_py.OptOracle(path)
+    for csc in ([0.3, -1.2], [1.0, 0.0], [0.7, 0.7]):
+        s.set_spin_coeffs(csc)
+        o.set_coeff_sc(csc)
+        e_ref = o.guess_energy(0).energy
+        assert abs(s.energy()["energy"] - e_ref) < 1e-9, (csc, s.energy()["energy"], e_ref)
+        for _ in range(3):
+            r, g = s.energy_grad()
+        assert abs(r["energy"] - e_ref) < 1e-9
+    s.close()

@@ -101,6 +101,7 @@ def lib():
         L.vsvb_gpu_debug_orbital_1e.argtypes = [ctypes.c_void_p, P(D), P(D), ctypes.c_size_t]
         L.vsvb_gpu_batch_energy_grad.argtypes = [P(ctypes.c_void_p), I, P(P(D)), P(Result), P(P(D))]
         L.vsvb_gpu_set_stream.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.vsvb_gpu_set_spin_coeffs.argtypes = [ctypes.c_void_p, P(D)]
         L.vsvb_gpu_eri_profile.argtypes = [ctypes.c_void_p, P(D), P(D), P(I), I]
         L.vsvb_gpu_eri_profile_mode.argtypes = [ctypes.c_void_p, I, P(D), P(D), P(I), I]
         L.vsvb_gpu_set_sweep_timing.argtypes = [ctypes.c_void_p, I]
@@ -238,6 +239,11 @@ class System:
         self._check(lib().vsvb_gpu_energy_grad(self._h, None if c is None else _dptr(c), ctypes.byref(r), _dptr(g)),
                     "energy_grad")
         return r.as_dict(), g
+
+    def set_spin_coeffs(self, coeff_sc):
+        """Spin-coupling weights (nspinc) for the following evaluations."""
+        c = np.ascontiguousarray(coeff_sc, dtype=np.float64)
+        self._check(lib().vsvb_gpu_set_spin_coeffs(self._h, _dptr(c)), "set_spin_coeffs")
 
     def energy_device(self, coeff_ptr):
         """Energy with the weights already in device memory (a raw pointer)."""

@@ -1766,6 +1766,8 @@ int vsvb_gpu_set_stream(vsvb_gpu *h, void *stream) {
   return VSVB_OK;
 }
 
+int vsvb_gpu_set_spin_coeffs(vsvb_gpu *h, const double *coeff_sc) { return gpu_set_spin_coeffs(h, coeff_sc); }
+
 int vsvb_gpu_eri_profile_mode(vsvb_gpu *h, int mode, double *ms, double *flops, int *cls, int cap) {
   if (!h || (mode != 0 && mode != 3)) return -VSVB_ERR_INPUT;
   if (mode == 3 && !h->grad_ready) return -VSVB_ERR_INPUT;
