@@ -47,6 +47,7 @@
 
 #include <cstdint>
 #include <type_traits>
+#include <utility>
 
 #include "eri.cuh"
 #include "vsvb_internal.h"
@@ -72,6 +73,31 @@ __device__ __forceinline__ void list_exp(int l0, int k, int e[3]) {
     }
     k -= n;
   }
+}
+
+/* list_exp at compile time: exponent d (0: x, 1: y, 2: z) of function k */
+__host__ __device__ constexpr int cexp(int l0, int k, int d) {
+  for (int l = l0;; ++l) {
+    const int n = (l + 1) * (l + 2) / 2;
+    if (k < n) {
+      for (int lx = l; lx >= 0; --lx) {
+        const int m = l - lx + 1;
+        if (k < m) return d == 0 ? lx : (d == 1 ? l - lx - k : k);
+        k -= m;
+      }
+    }
+    k -= n;
+  }
+}
+
+/* f(integral_constant<int, 0>), ..., f(integral_constant<int, N-1>) */
+template <typename F, int... I>
+__device__ __forceinline__ void static_for_impl(F &&f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, typename F>
+__device__ __forceinline__ void static_for(F &&f) {
+  static_for_impl(f, std::make_integer_sequence<int, N>{});
 }
 
 constexpr int RYS_NCHEB_D = 12;
@@ -408,6 +434,17 @@ struct QuartetShape {
   static constexpr int PER_WARP0 = CTA ? SM_2D + SM_ROOT : (SM_2D + SM_ROOT > SM_TR ? SM_2D + SM_ROOT : SM_TR);
   static constexpr int PER_WARP = (PER_WARP0 + 1) / 2 * 2;
   static constexpr int SHARED = CTA ? SM_TR : 0;
+  /* FP32 CTA kernels, line mode: a lane owns one function of the larger
+   * side (e for ROWM, else f) and accumulates the whole line of components
+   * it spans, with that function's 2D table entries in registers -- three
+   * shared-memory vectors per table row instead of three per component,
+   * which is what bounds the component loop in FP32.  SL slots side by side
+   * when a line takes at most half a warp. */
+  static constexpr bool ROWM = NEA >= NEC;
+  static constexpr int NL = ROWM ? NEA : NEC, NK = ROWM ? NEC : NEA;
+  static constexpr int KD = ROWM ? LCD + 1 : LAB + 1; /* table rows a lane loads per direction */
+  static constexpr int SL0 = 32 / NL > G2 ? G2 : 32 / NL;
+  static constexpr int SL = SL0 < 1 ? 1 : SL0;
   /* CTA mode stages each warp's partial block in that warp's table area */
   static_assert(!CTA || PER_WARP * 8 >= NCOMP * (RB == 4 ? 4 : 8), "per-warp area too small for the partial block");
 };
@@ -448,8 +485,13 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   /* FP32 CTA kernels keep their components' packed table offsets in
    * registers (they have the room; the shared-memory load in front of the
    * three dependent table loads otherwise dominates their stalls) */
-  constexpr bool HOIST = CTA && std::is_same<R, float>::value;
+  constexpr bool LINE = CTA && std::is_same<R, float>::value;
+  constexpr bool HOIST = CTA && std::is_same<R, float>::value && !LINE;
   int idr[HOIST ? S::PER_LANE : 1];
+  /* line mode: the lane's own function (e for ROWM, else f) and its slot */
+  const int lslot = LINE ? lane / S::NL : 0, lfun = LINE ? lane - lslot * S::NL : 0;
+  int lexp[3] = {0, 0, 0};
+  if constexpr (LINE) list_exp(S::ROWM ? LA : LC, lfun, lexp);
   if constexpr (HOIST) {
 #pragma unroll
     for (int m = 0; m < S::PER_LANE; ++m) {
@@ -468,9 +510,10 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
     const int4 pq = work[item];
     const ShellPair &P = args.pairs[pq.x];
     const ShellPair &Q = args.pairs[pq.y];
-    R acc[S::PER_LANE];
+    constexpr int NACC = LINE ? S::NK : S::PER_LANE;
+    R acc[NACC];
 #pragma unroll
-    for (int m = 0; m < S::PER_LANE; ++m) acc[m] = R(0);
+    for (int m = 0; m < NACC; ++m) acc[m] = R(0);
     /* primitive screen: pairs' primitives are sorted by their bound q0, so
      * rows ip whose q0_p q0_q(first) falls below eps end the contraction */
     const float eps = args.prim_lo, eps_hi = args.prim_hi;
@@ -642,7 +685,56 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         __syncwarp();
         const int nact = min(S::G2, nch - sub);
         constexpr int DS = S::N2D * S::NRP; /* one direction's table */
-        if constexpr (CTA) {
+        if constexpr (LINE) {
+          /* lane (slot lslot, function lfun): the table rows of its function
+           * (one per exponent of the other side), then its line of NK
+           * components, exponents known at compile time */
+          constexpr int LD1 = S::LCD + 1;
+          const int sx = S::ROWM ? lexp[0] * LD1 : lexp[0], sy = S::ROWM ? lexp[1] * LD1 : lexp[1],
+                    sz = S::ROWM ? lexp[2] * LD1 : lexp[2];
+          constexpr int KS = S::ROWM ? 1 : LD1; /* table stride between the loaded rows */
+#pragma unroll 1
+          for (int gs = 0; gs < nact; gs += S::SL) {
+            const int gg = gs + lslot;
+            if (lslot < S::SL && gg < nact) {
+              const R *hx = h2d + (size_t)gg * 3 * DS;
+#pragma unroll 1
+              for (int rg = 0; rg < S::NGF; ++rg) {
+                R X[S::KD][S::VEC], Yv[S::KD][S::VEC], Z[S::KD][S::VEC];
+#pragma unroll
+                for (int kk = 0; kk < S::KD; ++kk) {
+                  ldv<S::VEC>(hx + (sx + kk * KS) * S::NRP + rg * S::VEC, X[kk]);
+                  ldv<S::VEC>(hx + DS + (sy + kk * KS) * S::NRP + rg * S::VEC, Yv[kk]);
+                  ldv<S::VEC>(hx + 2 * DS + (sz + kk * KS) * S::NRP + rg * S::VEC, Z[kk]);
+                }
+                static_for<S::NK>([&](auto kc) {
+                  constexpr int k = decltype(kc)::value;
+                  constexpr int l0 = S::ROWM ? LC : LA;
+                  constexpr int kx = cexp(l0, k, 0), ky = cexp(l0, k, 1), kz = cexp(l0, k, 2);
+#pragma unroll
+                  for (int v = 0; v < S::VEC; ++v) acc3(acc[k], X[kx][v], Yv[ky][v], Z[kz][v]);
+                });
+              }
+              if constexpr (S::REM > 0) {
+#pragma unroll 1
+                for (int rr = S::NGF * S::VEC; rr < S::NR; ++rr) {
+                  R X1[S::KD], Y1[S::KD], Z1[S::KD];
+#pragma unroll
+                  for (int kk = 0; kk < S::KD; ++kk) {
+                    X1[kk] = hx[(sx + kk * KS) * S::NRP + rr];
+                    Y1[kk] = hx[DS + (sy + kk * KS) * S::NRP + rr];
+                    Z1[kk] = hx[2 * DS + (sz + kk * KS) * S::NRP + rr];
+                  }
+                  static_for<S::NK>([&](auto kc) {
+                    constexpr int k = decltype(kc)::value;
+                    constexpr int l0 = S::ROWM ? LC : LA;
+                    acc3(acc[k], X1[cexp(l0, k, 0)], Y1[cexp(l0, k, 1)], Z1[cexp(l0, k, 2)]);
+                  });
+                }
+              }
+            }
+          }
+        } else if constexpr (CTA) {
           /* one (slot, root group) at a time, so that the unrolled body covers
            * only the lane's components (instruction-cache footprint) */
 #pragma unroll 1
@@ -725,10 +817,24 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
       /* per-warp partial blocks (in the warps' own, now idle, table
        * areas), summed in warp order: deterministic */
       TT *part = reinterpret_cast<TT *>(ws);
+      if constexpr (LINE) {
+        /* the slots' partial lines to slot 0, then one line per lane */
 #pragma unroll
-      for (int m = 0; m < S::PER_LANE; ++m) {
-        const int c = lane + 32 * m;
-        if (c < S::NCOMP) part[c] = tt(acc[m]);
+        for (int k = 0; k < S::NK; ++k) {
+          R v = acc[k];
+#pragma unroll
+          for (int s2 = 1; s2 < S::SL; ++s2) v += __shfl_down_sync(0xffffffffu, acc[k], s2 * S::NL);
+          acc[k] = v;
+        }
+        if (lslot == 0)
+#pragma unroll
+          for (int k = 0; k < S::NK; ++k) part[S::ROWM ? lfun * S::NEC + k : k * S::NEC + lfun] = tt(acc[k]);
+      } else {
+#pragma unroll
+        for (int m = 0; m < S::PER_LANE; ++m) {
+          const int c = lane + 32 * m;
+          if (c < S::NCOMP) part[c] = tt(acc[m]);
+        }
       }
       __syncthreads();
       for (int c = tid; c < S::NCOMP; c += nthr) {
