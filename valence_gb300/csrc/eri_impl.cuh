@@ -90,6 +90,13 @@ __host__ __device__ constexpr int cexp(int l0, int k, int d) {
   }
 }
 
+/* warp shuffle down in each arithmetic type */
+__device__ __forceinline__ float shfl_down_r(float v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
+__device__ __forceinline__ double shfl_down_r(double v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
+__device__ __forceinline__ df64 shfl_down_r(df64 v, int d) {
+  return df64(__shfl_down_sync(0xffffffffu, v.hi, d), __shfl_down_sync(0xffffffffu, v.lo, d));
+}
+
 /* f(integral_constant<int, 0>), ..., f(integral_constant<int, N-1>) */
 template <typename F, int... I>
 __device__ __forceinline__ void static_for_impl(F &&f, std::integer_sequence<int, I...>) {
@@ -434,12 +441,12 @@ struct QuartetShape {
   static constexpr int PER_WARP0 = CTA ? SM_2D + SM_ROOT : (SM_2D + SM_ROOT > SM_TR ? SM_2D + SM_ROOT : SM_TR);
   static constexpr int PER_WARP = (PER_WARP0 + 1) / 2 * 2;
   static constexpr int SHARED = CTA ? SM_TR : 0;
-  /* FP32 CTA kernels, line mode: a lane owns one function of the larger
-   * side (e for ROWM, else f) and accumulates the whole line of components
-   * it spans, with that function's 2D table entries in registers -- three
-   * shared-memory vectors per table row instead of three per component,
-   * which is what bounds the component loop in FP32.  SL slots side by side
-   * when a line takes at most half a warp. */
+  /* FP32 and double-float kernels, line mode: a lane owns one function of
+   * the larger side (e for ROWM, else f) and accumulates the whole line of
+   * components it spans, with that function's 2D table entries in registers
+   * -- three shared-memory vectors per table row instead of three per
+   * component, which is what bounds the component loop in FP32.  SL slots
+   * side by side when a line takes at most half a warp. */
   static constexpr bool ROWM = NEA >= NEC;
   static constexpr int NL = ROWM ? NEA : NEC, NK = ROWM ? NEC : NEA;
   static constexpr int KD = ROWM ? LCD + 1 : LAB + 1; /* table rows a lane loads per direction */
@@ -485,7 +492,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   /* FP32 CTA kernels keep their components' packed table offsets in
    * registers (they have the room; the shared-memory load in front of the
    * three dependent table loads otherwise dominates their stalls) */
-  constexpr bool LINE = CTA && std::is_same<R, float>::value;
+  constexpr bool LINE = !std::is_same<R, double>::value;
   constexpr bool HOIST = CTA && std::is_same<R, float>::value && !LINE;
   int idr[HOIST ? S::PER_LANE : 1];
   /* line mode: the lane's own function (e for ROWM, else f) and its slot */
@@ -823,7 +830,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         for (int k = 0; k < S::NK; ++k) {
           R v = acc[k];
 #pragma unroll
-          for (int s2 = 1; s2 < S::SL; ++s2) v += __shfl_down_sync(0xffffffffu, acc[k], s2 * S::NL);
+          for (int s2 = 1; s2 < S::SL; ++s2) v += shfl_down_r(acc[k], s2 * S::NL);
           acc[k] = v;
         }
         if (lslot == 0)
@@ -843,6 +850,19 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         E[c] = sum;
       }
       __syncthreads();
+    } else if constexpr (LINE) {
+      /* warp mode: the slots' partial lines summed by shuffles, one line per lane */
+#pragma unroll
+      for (int k = 0; k < S::NK; ++k) {
+        R v = acc[k];
+#pragma unroll
+        for (int s2 = 1; s2 < S::SL; ++s2) v += shfl_down_r(acc[k], s2 * S::NL);
+        acc[k] = v;
+      }
+      if (lslot == 0)
+#pragma unroll
+        for (int k = 0; k < S::NK; ++k) E[S::ROWM ? lfun * S::NEC + k : k * S::NEC + lfun] = tt(acc[k]);
+      __syncwarp();
     } else if (S::G == 1) {
 #pragma unroll
       for (int m = 0; m < S::PER_LANE; ++m) {
