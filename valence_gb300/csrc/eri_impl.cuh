@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   /* FP32 CTA kernels keep their components' packed table offsets in
    * registers (they have the room; the shared-memory load in front of the
    * three dependent table loads otherwise dominates their stalls) */
-  constexpr bool LINE = !std::is_same<R, double>::value;
+  constexpr bool LINE = true;
   constexpr bool HOIST = CTA && std::is_same<R, float>::value && !LINE;
   int idr[HOIST ? S::PER_LANE : 1];
   /* line mode: the lane's own function (e for ROWM, else f) and its slot */
