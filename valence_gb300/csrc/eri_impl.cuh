@@ -90,6 +90,15 @@ __host__ __device__ constexpr int cexp(int l0, int k, int d) {
   }
 }
 
+/* the inverse: index of exponents (x, y, z) in the list l0, l0+1, ... */
+__host__ __device__ constexpr int kindex(int l0, int x, int y, int z) {
+  int k = 0;
+  const int l = x + y + z;
+  for (int m = l0; m < l; ++m) k += (m + 1) * (m + 2) / 2;
+  for (int lx = l; lx > x; --lx) k += l - lx + 1;
+  return k + z;
+}
+
 /* warp shuffle down in each arithmetic type */
 __device__ __forceinline__ float shfl_down_r(float v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
 __device__ __forceinline__ double shfl_down_r(double v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
@@ -167,6 +176,39 @@ __device__ __forceinline__ void acc3(df64 &acc, df64 x, df64 y, df64 z) {
   float f = fmaf(p, z.hi, -q);
   f = fmaf(p, z.lo, f);
   f = fmaf(e, z.hi, f);
+  const float s = acc.hi + q;
+  const float v = s - acc.hi;
+  const float err = (acc.hi - (s - v)) + (q - v);
+  acc.lo += err + f;
+  acc.hi = s;
+}
+/* the same with the x*y product shared by several z: mul_xy once, then
+ * acc_xyz per component (the arithmetic of acc3, split in two) */
+template <typename R>
+struct XYProd {
+  R v;
+};
+template <>
+struct XYProd<df64> {
+  float p, e; /* unnormalised product hi + error */
+};
+__device__ __forceinline__ XYProd<double> mul_xy(double x, double y) { return {x * y}; }
+__device__ __forceinline__ XYProd<float> mul_xy(float x, float y) { return {x * y}; }
+__device__ __forceinline__ XYProd<df64> mul_xy(df64 x, df64 y) {
+  XYProd<df64> r;
+  r.p = x.hi * y.hi;
+  float e = fmaf(x.hi, y.hi, -r.p);
+  e = fmaf(x.hi, y.lo, e);
+  r.e = fmaf(x.lo, y.hi, e);
+  return r;
+}
+__device__ __forceinline__ void acc_xyz(double &acc, const XYProd<double> &xy, double z) { acc = fma(xy.v, z, acc); }
+__device__ __forceinline__ void acc_xyz(float &acc, const XYProd<float> &xy, float z) { acc = fmaf(xy.v, z, acc); }
+__device__ __forceinline__ void acc_xyz(df64 &acc, const XYProd<df64> &xy, df64 z) {
+  const float q = xy.p * z.hi;
+  float f = fmaf(xy.p, z.hi, -q);
+  f = fmaf(xy.p, z.lo, f);
+  f = fmaf(xy.e, z.hi, f);
   const float s = acc.hi + q;
   const float v = s - acc.hi;
   const float err = (acc.hi - (s - v)) + (q - v);
@@ -714,12 +756,25 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
                   ldv<S::VEC>(hx + DS + (sy + kk * KS) * S::NRP + rg * S::VEC, Yv[kk]);
                   ldv<S::VEC>(hx + 2 * DS + (sz + kk * KS) * S::NRP + rg * S::VEC, Z[kk]);
                 }
-                static_for<S::NK>([&](auto kc) {
-                  constexpr int k = decltype(kc)::value;
-                  constexpr int l0 = S::ROWM ? LC : LA;
-                  constexpr int kx = cexp(l0, k, 0), ky = cexp(l0, k, 1), kz = cexp(l0, k, 2);
+                /* the line's components by (x, y) exponent pair: the x*y
+                 * product once, then one z per angular momentum */
+                constexpr int l0 = S::ROWM ? LC : LA, l1 = S::ROWM ? S::LCD : S::LAB;
+                static_for<l1 + 1>([&](auto kxc) {
+                  constexpr int kx = decltype(kxc)::value;
+                  static_for<l1 + 1 - kx>([&](auto kyc) {
+                    constexpr int ky = decltype(kyc)::value;
+                    XYProd<R> xy[S::VEC];
 #pragma unroll
-                  for (int v = 0; v < S::VEC; ++v) acc3(acc[k], X[kx][v], Yv[ky][v], Z[kz][v]);
+                    for (int v = 0; v < S::VEC; ++v) xy[v] = mul_xy(X[kx][v], Yv[ky][v]);
+                    static_for<l1 - l0 + 1>([&](auto lc) {
+                      constexpr int kz = l0 + decltype(lc)::value - kx - ky;
+                      if constexpr (kz >= 0) {
+                        constexpr int k = kindex(l0, kx, ky, kz);
+#pragma unroll
+                        for (int v = 0; v < S::VEC; ++v) acc_xyz(acc[k], xy[v], Z[kz][v]);
+                      }
+                    });
+                  });
                 });
               }
               if constexpr (S::REM > 0) {
