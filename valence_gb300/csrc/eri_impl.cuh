@@ -374,7 +374,7 @@ __device__ __forceinline__ df64 mad_r(df64 a, df64 b, df64 c) {
   return df_quick(s, t);
 }
 
-template <int LAB, int LCD, typename R, int STRIDE>
+template <int LAB, int LCD, typename R, int STRIDE, int ROWSTRIDE>
 __device__ __forceinline__ void rys_g(R g00, R c00, R d00, R b00, R b10, R b01, R *__restrict__ out) {
   /* integer multiples of the coefficients, formed once */
   R ib10[LAB > 1 ? LAB : 1], ib00[LAB + 1], kb01[LCD > 1 ? LCD : 1];
@@ -406,7 +406,7 @@ __device__ __forceinline__ void rys_g(R g00, R c00, R d00, R b00, R b10, R b01, 
 #pragma unroll
   for (int i = 0; i <= LAB; ++i)
 #pragma unroll
-    for (int k = 0; k <= LCD; ++k) out[(i * (LCD + 1) + k) * STRIDE] = G[i][k];
+    for (int k = 0; k <= LCD; ++k) out[i * ROWSTRIDE + k * STRIDE] = G[i][k];
 }
 
 /* vector load of V consecutive table entries (V * sizeof(R) bytes, aligned) */
@@ -454,17 +454,11 @@ struct QuartetShape {
   static constexpr int NR = (LAB + LCD) / 2 + 1;
   static constexpr int N2D = (LAB + 1) * (LCD + 1);
   /* primitive quartets processed side by side per warp iteration: each takes
-   * 3*NR lanes for its 2D tables (G2 slots).  Small blocks keep a separate
-   * accumulator per slot (NITEM = G * NCOMP items spread over the lanes);
-   * large blocks (CTA mode) keep one accumulator per component, summed over
-   * the slots, so that the registers stay bounded, and put the CTA's warps on
-   * one shell quartet */
+   * 3*NR lanes for its 2D tables (G2 slots).  Large blocks (CTA mode) put the
+   * CTA's warps on one shell quartet, each with its own partial block */
   static constexpr int G0 = 32 / (3 * NR) < 1 ? 1 : 32 / (3 * NR);
   static constexpr bool CTA = NCOMP >= 80;
-  static constexpr int G = CTA ? 1 : G0;
   static constexpr int G2 = G0;
-  static constexpr int NITEM = G * NCOMP;
-  static constexpr int PER_LANE = (NITEM + 31) / 32;
   static constexpr int JCH = 8; /* ket orbital pairs per transform chunk */
   static constexpr int NMAX = NEA > NEC ? NEA : NEC;
   /* 2D tables are stored root-innermost, [slot][dir][entry][root], each
@@ -473,13 +467,19 @@ struct QuartetShape {
   static constexpr int VEC = RB == 4 ? (NR >= 4 ? 4 : (NR >= 2 ? 2 : 1)) : (NR >= 2 ? 2 : 1);
   static constexpr int NRP = (NR + VEC - 1) / VEC * VEC;
   static constexpr int NGF = NR / VEC, REM = NR % VEC;
-  static constexpr int SM_2D = (G2 * 3 * N2D * NRP * RB + 15) / 16 * 2; /* per warp, in doubles (16-byte multiple) */
+  /* row stride RS of a direction's table (entries (i, k) at i*RS + k*NRP):
+   * padded by one vector when the rows would otherwise start 32-byte
+   * aligned, so that the lanes of line mode, which read different rows of
+   * 16-byte vectors, spread over the shared-memory banks */
+  static constexpr int RS0 = (LCD + 1) * NRP;
+  static constexpr int RS = (VEC * RB == 16 && ((RS0 * RB / 16) % 2 == 0)) ? RS0 + VEC : RS0;
+  static constexpr int DS = (LAB + 1) * RS; /* one direction's table */
+  static constexpr int SM_2D = (G2 * 3 * DS * RB + 15) / 16 * 2; /* per warp, in doubles (16-byte multiple) */
   /* per warp: roots, weights, 1/(p+q) of 32 primitive quartets, and their indices */
   static constexpr int SM_ROOT = (((2 * 32 * NR + 32) * RB + 7) / 8 + 16 + 1) / 2 * 2;
-  static constexpr int IDXD = (((NCOMP + 1) / 2 + 1) + 1) / 2 * 2; /* component index table, doubles */
-  /* staging: E[NCOMP] + max(slot buffer, transform chunk); per warp in warp
-   * mode, one per CTA in CTA mode */
-  static constexpr int SM_TR = NCOMP + (NITEM > JCH * NMAX ? NITEM : JCH * NMAX);
+  /* staging: E[NCOMP] + a transform chunk; per warp in warp mode, one per
+   * CTA in CTA mode */
+  static constexpr int SM_TR = NCOMP + JCH * NMAX;
   static constexpr int PER_WARP0 = CTA ? SM_2D + SM_ROOT : (SM_2D + SM_ROOT > SM_TR ? SM_2D + SM_ROOT : SM_TR);
   static constexpr int PER_WARP = (PER_WARP0 + 1) / 2 * 2;
   static constexpr int SHARED = CTA ? SM_TR : 0;
@@ -510,8 +510,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   constexpr bool CTA = S::CTA;
   constexpr bool DFROOT = !std::is_same<R, double>::value;
   extern __shared__ double smem[];
-  int *idx = reinterpret_cast<int *>(smem);
-  double *wbase = smem + S::IDXD;
+  double *wbase = smem;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double *ws = wbase + (size_t)warp * S::PER_WARP;
   /* staging area: per warp (warp mode) or shared by the CTA */
@@ -519,35 +518,10 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   const int tid = CTA ? (int)threadIdx.x : lane;
   const int nthr = CTA ? (int)blockDim.x : 32;
 
-  /* component c = (e, f) of the (e0|f0) block: offsets into the x, y, z 2D tables */
-  for (int c = threadIdx.x; c < S::NCOMP; c += blockDim.x) {
-    int pe[3], pf[3];
-    list_exp(LA, c / S::NEC, pe);
-    list_exp(LC, c % S::NEC, pf);
-    const int ix = pe[0] * (S::LCD + 1) + pf[0];
-    const int iy = pe[1] * (S::LCD + 1) + pf[1];
-    const int iz = pe[2] * (S::LCD + 1) + pf[2];
-    idx[c] = ix | (iy << 10) | (iz << 20);
-  }
-  __syncthreads();
-
-  /* FP32 CTA kernels keep their components' packed table offsets in
-   * registers (they have the room; the shared-memory load in front of the
-   * three dependent table loads otherwise dominates their stalls) */
-  constexpr bool LINE = true;
-  constexpr bool HOIST = CTA && std::is_same<R, float>::value && !LINE;
-  int idr[HOIST ? S::PER_LANE : 1];
   /* line mode: the lane's own function (e for ROWM, else f) and its slot */
-  const int lslot = LINE ? lane / S::NL : 0, lfun = LINE ? lane - lslot * S::NL : 0;
-  int lexp[3] = {0, 0, 0};
-  if constexpr (LINE) list_exp(S::ROWM ? LA : LC, lfun, lexp);
-  if constexpr (HOIST) {
-#pragma unroll
-    for (int m = 0; m < S::PER_LANE; ++m) {
-      const int c = lane + 32 * m;
-      idr[m] = c < S::NCOMP ? idx[c] : 0;
-    }
-  }
+  const int lslot = lane / S::NL, lfun = lane - lslot * S::NL;
+  int lexp[3];
+  list_exp(S::ROWM ? LA : LC, lfun, lexp);
   R *h2d = reinterpret_cast<R *>(ws);
   const double two_pi_25 = 34.98683665524972; /* 2 pi^(5/2) */
   const PrimT<R> *__restrict__ primR = static_cast<const PrimT<R> *>(prec_data<R>::prim(args));
@@ -559,10 +533,9 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
     const int4 pq = work[item];
     const ShellPair &P = args.pairs[pq.x];
     const ShellPair &Q = args.pairs[pq.y];
-    constexpr int NACC = LINE ? S::NK : S::PER_LANE;
-    R acc[NACC];
+    R acc[S::NK];
 #pragma unroll
-    for (int m = 0; m < NACC; ++m) acc[m] = R(0);
+    for (int m = 0; m < S::NK; ++m) acc[m] = R(0);
     /* primitive screen: pairs' primitives are sorted by their bound q0, so
      * rows ip whose q0_p q0_q(first) falls below eps end the contraction */
     const float eps = args.prim_lo, eps_hi = args.prim_hi;
@@ -728,20 +701,18 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
           const R c00 = (Pd - Ad) - qr.p * uq * PQ;
           const R d00 = (Qd - Cd) + pr.p * uq * PQ;
           const R g00 = dir == 2 ? wR : R(1);
-          rys_g<S::LAB, S::LCD, R, S::NRP>(g00, c00, d00, b00, b10, b01,
-                                           h2d + (size_t)(g * 3 + dir) * S::N2D * S::NRP + r);
+          rys_g<S::LAB, S::LCD, R, S::NRP, S::RS>(g00, c00, d00, b00, b10, b01, h2d + (size_t)(g * 3 + dir) * S::DS + r);
         }
         __syncwarp();
         const int nact = min(S::G2, nch - sub);
-        constexpr int DS = S::N2D * S::NRP; /* one direction's table */
-        if constexpr (LINE) {
+        constexpr int DS = S::DS; /* one direction's table */
+        {
           /* lane (slot lslot, function lfun): the table rows of its function
            * (one per exponent of the other side), then its line of NK
            * components, exponents known at compile time */
-          constexpr int LD1 = S::LCD + 1;
-          const int sx = S::ROWM ? lexp[0] * LD1 : lexp[0], sy = S::ROWM ? lexp[1] * LD1 : lexp[1],
-                    sz = S::ROWM ? lexp[2] * LD1 : lexp[2];
-          constexpr int KS = S::ROWM ? 1 : LD1; /* table stride between the loaded rows */
+          constexpr int KB = S::ROWM ? S::RS : S::NRP; /* the lane's own exponent: rows (e) or columns (f) */
+          constexpr int KS = S::ROWM ? S::NRP : S::RS; /* and the stride of the other side's exponent */
+          const int sx = lexp[0] * KB, sy = lexp[1] * KB, sz = lexp[2] * KB;
 #pragma unroll 1
           for (int gs = 0; gs < nact; gs += S::SL) {
             const int gg = gs + lslot;
@@ -752,9 +723,9 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
                 R X[S::KD][S::VEC], Yv[S::KD][S::VEC], Z[S::KD][S::VEC];
 #pragma unroll
                 for (int kk = 0; kk < S::KD; ++kk) {
-                  ldv<S::VEC>(hx + (sx + kk * KS) * S::NRP + rg * S::VEC, X[kk]);
-                  ldv<S::VEC>(hx + DS + (sy + kk * KS) * S::NRP + rg * S::VEC, Yv[kk]);
-                  ldv<S::VEC>(hx + 2 * DS + (sz + kk * KS) * S::NRP + rg * S::VEC, Z[kk]);
+                  ldv<S::VEC>(hx + sx + kk * KS + rg * S::VEC, X[kk]);
+                  ldv<S::VEC>(hx + DS + sy + kk * KS + rg * S::VEC, Yv[kk]);
+                  ldv<S::VEC>(hx + 2 * DS + sz + kk * KS + rg * S::VEC, Z[kk]);
                 }
                 /* the line's components by (x, y) exponent pair: the x*y
                  * product once, then one z per angular momentum */
@@ -783,9 +754,9 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
                   R X1[S::KD], Y1[S::KD], Z1[S::KD];
 #pragma unroll
                   for (int kk = 0; kk < S::KD; ++kk) {
-                    X1[kk] = hx[(sx + kk * KS) * S::NRP + rr];
-                    Y1[kk] = hx[DS + (sy + kk * KS) * S::NRP + rr];
-                    Z1[kk] = hx[2 * DS + (sz + kk * KS) * S::NRP + rr];
+                    X1[kk] = hx[sx + kk * KS + rr];
+                    Y1[kk] = hx[DS + sy + kk * KS + rr];
+                    Z1[kk] = hx[2 * DS + sz + kk * KS + rr];
                   }
                   static_for<S::NK>([&](auto kc) {
                     constexpr int k = decltype(kc)::value;
@@ -794,69 +765,6 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
                   });
                 }
               }
-            }
-          }
-        } else if constexpr (CTA) {
-          /* one (slot, root group) at a time, so that the unrolled body covers
-           * only the lane's components (instruction-cache footprint) */
-#pragma unroll 1
-          for (int t = 0; t < nact * S::NGF; ++t) {
-            const int gg = t / S::NGF, rg = t - gg * S::NGF;
-            const R *hx = h2d + (size_t)gg * 3 * DS + rg * S::VEC;
-#pragma unroll
-            for (int m = 0; m < S::PER_LANE; ++m) {
-              const int c = lane + 32 * m;
-              if (c < S::NCOMP) {
-                const int id = HOIST ? idr[HOIST ? m : 0] : idx[c];
-                R x[S::VEC], y[S::VEC], z[S::VEC];
-                ldv<S::VEC>(hx + (id & 1023) * S::NRP, x);
-                ldv<S::VEC>(hx + DS + ((id >> 10) & 1023) * S::NRP, y);
-                ldv<S::VEC>(hx + 2 * DS + (id >> 20) * S::NRP, z);
-#pragma unroll
-                for (int v = 0; v < S::VEC; ++v) acc3(acc[m], x[v], y[v], z[v]);
-              }
-            }
-          }
-          if constexpr (S::REM > 0) {
-#pragma unroll 1
-            for (int t = 0; t < nact * S::REM; ++t) {
-              const int gg = t / S::REM, rr = S::NGF * S::VEC + (t - gg * S::REM);
-              const R *hx = h2d + (size_t)gg * 3 * DS + rr;
-#pragma unroll
-              for (int m = 0; m < S::PER_LANE; ++m) {
-                const int c = lane + 32 * m;
-                if (c < S::NCOMP) {
-                  const int id = idx[c];
-                  acc3(acc[m], hx[(id & 1023) * S::NRP], hx[DS + ((id >> 10) & 1023) * S::NRP],
-                       hx[2 * DS + (id >> 20) * S::NRP]);
-                }
-              }
-            }
-          }
-        } else
-#pragma unroll
-        for (int m = 0; m < S::PER_LANE; ++m) {
-          const int it = lane + 32 * m;
-          if (it < S::NITEM) {
-            const int gg = it / S::NCOMP, c = it - gg * S::NCOMP;
-            if (gg < nact) {
-              const int id = idx[c];
-              const R *hx = h2d + (size_t)gg * 3 * DS + (id & 1023) * S::NRP;
-              const R *hy = h2d + (size_t)gg * 3 * DS + DS + ((id >> 10) & 1023) * S::NRP;
-              const R *hz = h2d + (size_t)gg * 3 * DS + 2 * DS + (id >> 20) * S::NRP;
-              R sacc = acc[m];
-#pragma unroll
-              for (int rg = 0; rg < S::NGF; ++rg) {
-                R x[S::VEC], y[S::VEC], z[S::VEC];
-                ldv<S::VEC>(hx + rg * S::VEC, x);
-                ldv<S::VEC>(hy + rg * S::VEC, y);
-                ldv<S::VEC>(hz + rg * S::VEC, z);
-#pragma unroll
-                for (int v = 0; v < S::VEC; ++v) acc3(sacc, x[v], y[v], z[v]);
-              }
-#pragma unroll
-              for (int rr = S::NGF * S::VEC; rr < S::NR; ++rr) acc3(sacc, hx[rr], hy[rr], hz[rr]);
-              acc[m] = sacc;
             }
           }
         }
@@ -875,29 +783,21 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
       else return to_double(v);
     };
     TT *E = reinterpret_cast<TT *>(stage);
+    /* the slots' partial lines to slot 0 (shuffles), then one line per lane */
+#pragma unroll
+    for (int k = 0; k < S::NK; ++k) {
+      R v = acc[k];
+#pragma unroll
+      for (int s2 = 1; s2 < S::SL; ++s2) v += shfl_down_r(acc[k], s2 * S::NL);
+      acc[k] = v;
+    }
     if (CTA) {
       /* per-warp partial blocks (in the warps' own, now idle, table
        * areas), summed in warp order: deterministic */
       TT *part = reinterpret_cast<TT *>(ws);
-      if constexpr (LINE) {
-        /* the slots' partial lines to slot 0, then one line per lane */
+      if (lslot == 0)
 #pragma unroll
-        for (int k = 0; k < S::NK; ++k) {
-          R v = acc[k];
-#pragma unroll
-          for (int s2 = 1; s2 < S::SL; ++s2) v += shfl_down_r(acc[k], s2 * S::NL);
-          acc[k] = v;
-        }
-        if (lslot == 0)
-#pragma unroll
-          for (int k = 0; k < S::NK; ++k) part[S::ROWM ? lfun * S::NEC + k : k * S::NEC + lfun] = tt(acc[k]);
-      } else {
-#pragma unroll
-        for (int m = 0; m < S::PER_LANE; ++m) {
-          const int c = lane + 32 * m;
-          if (c < S::NCOMP) part[c] = tt(acc[m]);
-        }
-      }
+        for (int k = 0; k < S::NK; ++k) part[S::ROWM ? lfun * S::NEC + k : k * S::NEC + lfun] = tt(acc[k]);
       __syncthreads();
       for (int c = tid; c < S::NCOMP; c += nthr) {
         TT sum = reinterpret_cast<const TT *>(wbase)[c];
@@ -905,39 +805,10 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         E[c] = sum;
       }
       __syncthreads();
-    } else if constexpr (LINE) {
-      /* warp mode: the slots' partial lines summed by shuffles, one line per lane */
-#pragma unroll
-      for (int k = 0; k < S::NK; ++k) {
-        R v = acc[k];
-#pragma unroll
-        for (int s2 = 1; s2 < S::SL; ++s2) v += shfl_down_r(acc[k], s2 * S::NL);
-        acc[k] = v;
-      }
+    } else {
       if (lslot == 0)
 #pragma unroll
         for (int k = 0; k < S::NK; ++k) E[S::ROWM ? lfun * S::NEC + k : k * S::NEC + lfun] = tt(acc[k]);
-      __syncwarp();
-    } else if (S::G == 1) {
-#pragma unroll
-      for (int m = 0; m < S::PER_LANE; ++m) {
-        const int c = lane + 32 * m;
-        if (c < S::NCOMP) E[c] = tt(acc[m]);
-      }
-      __syncwarp();
-    } else {
-      TT *E2 = E + S::NCOMP;
-#pragma unroll
-      for (int m = 0; m < S::PER_LANE; ++m) {
-        const int it = lane + 32 * m;
-        if (it < S::NITEM) E2[it] = tt(acc[m]);
-      }
-      __syncwarp();
-      for (int c = lane; c < S::NCOMP; c += 32) {
-        TT sum = TT(0);
-        for (int gg = 0; gg < S::G; ++gg) sum += E2[gg * S::NCOMP + c];
-        E[c] = sum;
-      }
       __syncwarp();
     }
     if (MODE == 1) {
@@ -1088,7 +959,7 @@ template <int LA, int LB, int LC, int LD, typename R, int MODE>
 int launch_one(const EriArgs &args, const int4 *work, int nwork, int max_blocks, cudaStream_t st) {
   if (nwork <= 0) return 0;
   using S = QuartetShape<LA, LB, LC, LD, sizeof(R)>;
-  size_t shm = sizeof(double) * (S::IDXD + (size_t)WARPS * S::PER_WARP + S::SHARED);
+  size_t shm = sizeof(double) * ((size_t)WARPS * S::PER_WARP + S::SHARED);
   auto kfn = eri_kernel<LA, LB, LC, LD, R, MODE>;
   static bool attr_done = false;
   if (!attr_done) {
