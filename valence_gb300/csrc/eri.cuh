@@ -20,6 +20,7 @@ struct EriArgs {
   const PrimPair *prims;
   const double *rys;       /* Chebyshev tables (device) */
   const float2 *rysdf;     /* the same coefficients as (hi, lo) FP32 pairs */
+  const float *rys32;      /* and their FP32 roundings, for the FP32 kernels */
   const int *pair_opid;    /* orbital-pair index of every pair term */
   const double *xtab;      /* transferred weight tables X' = X M (nop x ne per pair) */
   const double *hrr;       /* per-pair transfer matrices M (n_a n_b x ne) */

@@ -295,18 +295,24 @@ __device__ __forceinline__ void rys_root_df(int n, int r, int j, bool in_table, 
   }
 }
 
-/* FP32 Chebyshev sum and root for the FP32 kernels (their integrals carry
- * FP32 rounding anyway): the hi parts of the same tables */
-__device__ __forceinline__ float clenshaw12_f(const float2 *__restrict__ c, float t) {
+/* FP32 Chebyshev sum for the FP32 kernels (their integrals carry FP32
+ * rounding anyway), from the FP32 roundings of the same tables: the 12
+ * coefficients of one (interval, root) are 48 contiguous, 16-byte aligned
+ * bytes, read as three vectors */
+__device__ __forceinline__ float clenshaw12_f4(const float *__restrict__ c, float t) {
+  const float4 a = __ldg(reinterpret_cast<const float4 *>(c));
+  const float4 b = __ldg(reinterpret_cast<const float4 *>(c) + 1);
+  const float4 d = __ldg(reinterpret_cast<const float4 *>(c) + 2);
+  const float k[RYS_NCHEB_D] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, d.x, d.y, d.z, d.w};
   float b1 = 0.f, b2 = 0.f;
   const float t2 = 2.f * t;
 #pragma unroll
-  for (int k = RYS_NCHEB_D - 1; k > 0; --k) {
-    const float b0 = fmaf(t2, b1, c[k].x - b2);
+  for (int i = RYS_NCHEB_D - 1; i > 0; --i) {
+    const float b0 = fmaf(t2, b1, k[i] - b2);
     b2 = b1;
     b1 = b0;
   }
-  return fmaf(t, b1, c[0].x - b2);
+  return fmaf(t, b1, k[0] - b2);
 }
 
 __device__ __forceinline__ const PrimT<df64> *args_primdf(const EriArgs &a) {
@@ -628,11 +634,11 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
               const int j = max(0, min((int)(Tb * (float)(1.0 / RYS_H_D)), (int)(RYS_TMAX_D / RYS_H_D) - 1));
               const float t = (Tb - (float)(j * RYS_H_D)) * (float)(2.0 / RYS_H_D) - 1.f;
               const float sc = rsqrtf(1.f + Tb);
-              const float2 *c = args.rysdf + args.rc.off[S::NR - 1] + (size_t)j * (2 * S::NR) * RYS_NCHEB_D;
+              const float *c = args.rys32 + args.rc.off[S::NR - 1] + (size_t)j * (2 * S::NR) * RYS_NCHEB_D;
 #pragma unroll 1
               for (int rr = 0; rr < S::NR; ++rr) {
-                rx[lane * S::NR + rr] = clenshaw12_f(c + rr * RYS_NCHEB_D, t) * sc * sc;
-                rw[lane * S::NR + rr] = clenshaw12_f(c + (S::NR + rr) * RYS_NCHEB_D, t) * sc * pref;
+                rx[lane * S::NR + rr] = clenshaw12_f4(c + rr * RYS_NCHEB_D, t) * sc * sc;
+                rw[lane * S::NR + rr] = clenshaw12_f4(c + (S::NR + rr) * RYS_NCHEB_D, t) * sc * pref;
               }
             } else {
               const float sc = rsqrtf(Tb);

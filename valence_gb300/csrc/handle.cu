@@ -183,6 +183,7 @@ struct vsvb_gpu {
   DBuf<GShell> shells;
   DBuf<double> exps, coefs, angn, charge, axyz, rys;
   DBuf<float2> rysdf;
+  DBuf<float> rys32;
   DBuf<double> S_ao, H_ao;
   DBuf<ShellPair> pairs;
   DBuf<PrimPair> prims;
@@ -297,6 +298,7 @@ EriArgs eri_args(vsvb_gpu *h) {
   a.prims = h->prims.p;
   a.rys = h->rys.p;
   a.rysdf = h->rysdf.p;
+  a.rys32 = h->rys32.p;
   a.pair_opid = h->pair_opid.p;
   a.xtab = h->xtabh.p;
   a.hrr = h->hrr.p;
@@ -757,6 +759,9 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
       df[i] = make_float2(hi, (float)(rys_table_data[i] - (double)hi));
     }
     CK(h->rysdf.upload(df), "upload rysdf");
+    std::vector<float> f32(nt);
+    for (size_t i = 0; i < nt; ++i) f32[i] = df[i].x;
+    CK(h->rys32.upload(f32), "upload rys32");
   }
   for (int k = 0; k < 5; ++k) {
     h->rc.off[k] = rys_table_offset[k];
