@@ -260,23 +260,32 @@ __device__ __forceinline__ void rys_root(int n, int r, double T, const double *_
 /* Chebyshev sum in double-float: the high-order terms (below the FP32 noise
  * of the result) in FP32, the rest in df64.  c: (hi, lo) coefficient pairs. */
 __device__ __forceinline__ df64 clenshaw12_df(const float2 *__restrict__ c, df64 t) {
+  /* the 12 (hi, lo) pairs are 96 contiguous, 16-byte aligned bytes: six
+   * vector loads */
+  float2 k[RYS_NCHEB_D];
+#pragma unroll
+  for (int i = 0; i < RYS_NCHEB_D / 2; ++i) {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(c) + i);
+    k[2 * i] = make_float2(v.x, v.y);
+    k[2 * i + 1] = make_float2(v.z, v.w);
+  }
   float b1f = 0.f, b2f = 0.f;
   const float t2f = 2.f * t.hi;
 #pragma unroll
-  for (int k = RYS_NCHEB_D - 1; k >= RYS_DF_SPLIT; --k) {
-    const float b0 = fmaf(t2f, b1f, c[k].x - b2f);
+  for (int i = RYS_NCHEB_D - 1; i >= RYS_DF_SPLIT; --i) {
+    const float b0 = fmaf(t2f, b1f, k[i].x - b2f);
     b2f = b1f;
     b1f = b0;
   }
   df64 b1(b1f), b2(b2f);
   const df64 t2 = t + t;
 #pragma unroll
-  for (int k = RYS_DF_SPLIT - 1; k > 0; --k) {
-    const df64 b0 = t2 * b1 - b2 + df64(c[k].x, c[k].y);
+  for (int i = RYS_DF_SPLIT - 1; i > 0; --i) {
+    const df64 b0 = t2 * b1 - b2 + df64(k[i].x, k[i].y);
     b2 = b1;
     b1 = b0;
   }
-  return t * b1 - b2 + df64(c[0].x, c[0].y);
+  return t * b1 - b2 + df64(k[0].x, k[0].y);
 }
 
 /* root r in double-float; interval j, Chebyshev variable t and
