@@ -620,8 +620,15 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
               ce_c = cofactor_loc(d, q, qi, 2, Lb, lk, a.status);
             }
             if (xs) {
-              const Loc lk[2] = {Ll, Lk};
-              cx_c = cofactor_loc(d, q, qi, 2, Lb, lk, a.status);
+              if (es && ce_c.ok) {
+                /* both strikes of the direct cofactor in one spin block: the
+                 * exchanged one is its column swap, -v exactly, and only
+                 * whether it is allowed matters below (det()'s sign rule) */
+                cx_c.ok = Lb[0].spin == Ll.spin && Lb[1].spin == Lk.spin;
+              } else {
+                const Loc lk[2] = {Ll, Lk};
+                cx_c = cofactor_loc(d, q, qi, 2, Lb, lk, a.status);
+              }
             }
             double dd = 0.0, xd = 0.0;
             if (es && ce_c.ok) dd = ce_c.v;
