@@ -22,14 +22,16 @@
  * project-generated Chebyshev tables (gen_rys_tables.py).
  *
  * Work split.  Per primitive quartet, 3*n_r lanes build the x/y/z 2D tables
- * of the n_r roots in shared memory, then lanes accumulate their share of
- * the (e0|f0) components in registers.  Small blocks run G primitive
- * quartets side by side in one warp, each with its own accumulators (one
- * warp per shell quartet); blocks of >= 80 components put a whole CTA
- * on one shell quartet, its warps splitting the primitive quartets and each
- * warp building the tables of G2 primitive quartets at once into one set of
- * accumulators.  After the primitive loop the block is staged in shared
- * memory and transformed with the X' tables; U is updated with FP64 atomics.
+ * of the n_r roots in shared memory (G2 primitive quartets at once per
+ * warp).  Then, in line mode, a lane owns one function of the larger side
+ * (e or f) and accumulates its whole line of components, the function's
+ * table rows held in registers and the line's exponents compile-time
+ * constants; lines of up to 16 run two or more primitive quartets side by
+ * side.  Small blocks take one warp per shell quartet; blocks of >= 80
+ * components put a whole CTA on one shell quartet, its warps splitting the
+ * primitive quartets.  After the primitive loop the block is staged in
+ * shared memory and transformed with the X' tables; U is updated with FP64
+ * atomics.
  *
  * Arithmetic.  R = double: everything FP64.  R = double-float (df64, an
  * unevaluated sum of two FP32 numbers, ~48-bit significand): the Boys
