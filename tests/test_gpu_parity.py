@@ -99,11 +99,11 @@ def test_synthetic_water_matches_oracle(lib_built, oracle, tmp_path):
     assert abs(r["energy"] - ro.energy) < 1e-8 * max(1, abs(ro.energy))
 
 
-def test_synthetic_chain_matches_fixture(lib_built):
+def test_synthetic_chain_matches_fixture(lib_built, tmp_path):
     import json
     from valence_gb300 import configs
     fx = json.load(open(os.path.join(GOLD, "synthetic.json")))["ch_chain"]
-    p = configs.ch_chain(os.path.join(ROOT, "gpurun_out", "ch_chain.inp") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/ch_chain.inp", seed=fx["seed"])
+    p = configs.ch_chain(str(tmp_path / "ch_chain.inp"), seed=fx["seed"])
     s = lib_built.System(p)
     r = s.energy()
     assert abs(r["energy"] - fx["energy"]) < 1e-8 * max(1.0, abs(fx["energy"]))
