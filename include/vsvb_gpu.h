@@ -152,6 +152,12 @@ int vsvb_format_orbitals(const vsvb_system_desc *desc, const double *coeff, doub
 int vsvb_write_orbitals(const char *path, const vsvb_system_desc *desc, const double *coeff, double energy,
                         double etol, int done);
 
+/* The 'nelecwfn' file written beside 'orbitals' when nspinc > 1
+ * (xm_module.F90:480-505): each coupling's weight (coeff_sc, NULL: the
+ * description's) with its pairs, then the excited-state roots. */
+int vsvb_format_nelecwfn(const vsvb_system_desc *desc, const double *coeff_sc, char *buf, long cap, long *len);
+int vsvb_write_nelecwfn(const char *path, const vsvb_system_desc *desc, const double *coeff_sc);
+
 /* Build a handle: normalises primitives (norm_prim, valence.F90:2264-2305),
  * builds the shell-pair tables, AO one-electron matrices, Schwarz bounds and
  * quartet schedules on the GPU.  Replaces the set-up half of
@@ -316,6 +322,13 @@ int vsvb_opt_spin_hs(vsvb_opt *o, const double *coeff, double *ham, double *ovl)
  * roots and ptbnmax/feather (direct minimisation when ptbnmax > 0 and there
  * are no excited-state roots). */
 int vsvb_opt_minimize(vsvb_opt *o, double *coeff, double *coeff_sc, vsvb_opt_result *res);
+
+/* Files vsvb_opt_minimize writes as the reference does (xm_output 'save'
+ * after the guess energy and after every orbital or coupling update, 'done'
+ * on convergence, valence.F90:192,453,489,2823,2859,2882): the orbitals file
+ * at orbitals_path and, with more than one coupling, the coupling file at
+ * nelecwfn_path.  NULL switches a file off (the default). */
+int vsvb_opt_set_output(vsvb_opt *o, const char *orbitals_path, const char *nelecwfn_path);
 
 /* EISPACK rsg (rsg.F) on the GPU: ham w = e ovl w for symmetric ham and
  * positive-definite ovl (n x n, column-major, leading dimension ld);

@@ -214,3 +214,25 @@ def test_orbitals_writer_round_trip(lib, tmp_path):
             vals.append(float(ln[k + 5:k + 18]))
     lib.vsvb_free_desc(d)
     assert np.max(np.abs(np.array(vals) - w)) <= 5.1e-9
+
+
+def test_nelecwfn_writer_reproduces_reference_records(lib):
+    """vsvb_format_nelecwfn (xm_output's format(1x,1f13.8,7(2i3,2x)) per
+    coupling and format(1x,7(2i3,2x)) for the excited-state roots): the
+    records the reference wrote into its multi-coupling inputs, verbatim."""
+    from valence_gb300 import api
+    checked = 0
+    for name in ("be-sc", "be-scv3s+2sc", "f2-scval-p2", "n2.sc4val-b.p2"):
+        path = os.path.join(oracle_py.GOLDEN, "cases", "testing", name)
+        d = api.read_input(path)
+        if d.contents.nspinc < 2:
+            lib.vsvb_free_desc(d)
+            continue
+        txt = api.format_nelecwfn(d)
+        lib.vsvb_free_desc(d)
+        src = open(path).read().split("\n")
+        recs = [ln for ln in txt.split("\n") if ln.strip()]
+        for ln in recs:
+            assert ln in src, (name, ln)
+        checked += 1
+    assert checked >= 2

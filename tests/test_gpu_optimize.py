@@ -173,3 +173,22 @@ def test_spin_coupling_weights_per_evaluation(env):
             r, g = s.energy_grad()
         assert abs(r["energy"] - e_ref) < 1e-9
     s.close()
+
+
+def test_minimize_writes_orbitals_files(env, tmp_path):
+    """vsvb_opt_set_output: minimize writes 'orbitals' after every update and
+    with the 'converged to' record at the end, and 'nelecwfn' with the
+    optimised coupling weights."""
+    api, oracle_py = env
+    path = _path(oracle_py, "testing", "be-sc")
+    opt = api.Optimizer(path)
+    orb, wfn = tmp_path / "orbitals", tmp_path / "nelecwfn"
+    opt.set_output(str(orb), str(wfn))
+    res, c, csc = opt.minimize()
+    opt.close()
+    txt = orb.read_text()
+    line = [ln for ln in txt.split("\n") if "total energy in atomic units" in ln][0]
+    assert abs(float(line.split()[-1]) - res["energy"]) < 1e-12
+    assert "converged to" in txt
+    w = [float(ln.split()[0]) for ln in wfn.read_text().split("\n") if ln.strip() and "." in ln.split()[0]]
+    assert np.allclose(w, csc, atol=5e-9)

@@ -130,6 +130,9 @@ def lib():
         L.vsvb_opt_spin_hs.argtypes = [ctypes.c_void_p, P(D), P(D), P(D)]
         L.vsvb_opt_minimize.argtypes = [ctypes.c_void_p, P(D), P(D), P(OptResult)]
         L.vsvb_rsg.argtypes = [I, P(D), P(D), I, P(D), P(D), I]
+        L.vsvb_opt_set_output.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]
+        L.vsvb_format_nelecwfn.argtypes = [P(Desc), P(D), ctypes.c_char_p, ctypes.c_long, P(ctypes.c_long)]
+        L.vsvb_write_nelecwfn.argtypes = [ctypes.c_char_p, P(Desc), P(D)]
         _LIB = L
     return _LIB
 
@@ -148,6 +151,18 @@ def format_orbitals(desc, coeff=None, energy=0.0, etol=0.0, done=False):
                                     n.value + 1, ctypes.byref(n))
     if rc:
         raise VSVBError(f"format_orbitals failed ({rc})")
+    return buf.value.decode()
+
+
+def format_nelecwfn(desc, coeff_sc=None):
+    """The reference's 'nelecwfn' file text (xm_output with nspinc > 1)."""
+    c = None if coeff_sc is None else np.ascontiguousarray(coeff_sc, dtype=np.float64)
+    n = ctypes.c_long()
+    if lib().vsvb_format_nelecwfn(desc, None if c is None else _dptr(c), None, 0, ctypes.byref(n)):
+        raise VSVBError("format_nelecwfn failed")
+    buf = ctypes.create_string_buffer(n.value + 1)
+    if lib().vsvb_format_nelecwfn(desc, None if c is None else _dptr(c), buf, n.value + 1, ctypes.byref(n)):
+        raise VSVBError("format_nelecwfn failed")
     return buf.value.decode()
 
 
@@ -546,6 +561,12 @@ class Optimizer:
         h, s = np.zeros((n, n), order="F"), np.zeros((n, n), order="F")
         self._check(lib().vsvb_opt_spin_hs(self._o, _dptr(c), _dptr(h), _dptr(s)), "spin_hs")
         return h, s
+
+    def set_output(self, orbitals_path=None, nelecwfn_path=None):
+        """Write the 'orbitals' (and 'nelecwfn') files during minimize, as the
+        reference does after every update and on convergence."""
+        enc = lambda p: None if p is None else os.fsencode(p)
+        self._check(lib().vsvb_opt_set_output(self._o, enc(orbitals_path), enc(nelecwfn_path)), "set_output")
 
     def minimize(self, coeff=None, coeff_sc=None):
         """Returns (result dict, optimised weights, spin-coupling weights)."""

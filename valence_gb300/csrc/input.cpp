@@ -417,3 +417,65 @@ extern "C" int vsvb_write_orbitals(const char *path, const vsvb_system_desc *d, 
   const bool ok = std::fwrite(b.data(), 1, (size_t)n, f) == (size_t)n;
   return std::fclose(f) == 0 && ok ? VSVB_OK : VSVB_ERR_INPUT;
 }
+
+/* The 'nelecwfn' file xm_output writes beside 'orbitals' when there is more
+ * than one spin coupling (xm_module.F90:480-505): per coupling
+ * format(1x,1f13.8,7(2i3,2x)) with the weight and its pairs (format reversion
+ * continues past seven pairs on a record of 7(2i3,2x)), then the excited-state
+ * roots in format(1x,7(2i3,2x)) and a blank record. */
+extern "C" int vsvb_format_nelecwfn(const vsvb_system_desc *d, const double *coeff_sc, char *buf, long cap,
+                                    long *len) {
+  if (!d || !len) return VSVB_ERR_INPUT;
+  std::string o, rec;
+  const int nsc = d->nspinc > 0 ? d->nspinc : 1;
+  /* X editing at the end of a record writes nothing: records end at their
+   * last value */
+  auto flush = [&]() {
+    while (!rec.empty() && rec.back() == ' ') rec.pop_back();
+    o += rec;
+    o += '\n';
+    rec.clear();
+  };
+  for (int j = 0; j < nsc; ++j) {
+    rec = " ";
+    fort_f(rec, coeff_sc ? coeff_sc[j] : d->coeff_sc[j], 13, 8);
+    for (int k = 0; k < d->npair; ++k) {
+      if (k > 0 && k % 7 == 0) flush();
+      fort_i(rec, d->pair_sc[k + d->npair * (0 + 2 * j)], 3);
+      fort_i(rec, d->pair_sc[k + d->npair * (1 + 2 * j)], 3);
+      rec += "  ";
+    }
+    flush();
+  }
+  rec = " ";
+  for (int i = 0; i < d->nxorb; ++i) {
+    if (i > 0 && i % 7 == 0) flush();
+    fort_i(rec, d->xorb[i], 3);
+    fort_i(rec, d->root[i], 3);
+    rec += "  ";
+  }
+  flush();
+  o += '\n'; /* write(11,*) */
+  *len = (long)o.size();
+  if (buf) {
+    if (cap < (long)o.size() + 1) return VSVB_ERR_TOO_LARGE;
+    std::memcpy(buf, o.data(), o.size());
+    buf[o.size()] = 0;
+  }
+  return VSVB_OK;
+}
+
+extern "C" int vsvb_write_nelecwfn(const char *path, const vsvb_system_desc *d, const double *coeff_sc) {
+  if (!path) return VSVB_ERR_INPUT;
+  long n = 0;
+  int rc = vsvb_format_nelecwfn(d, coeff_sc, nullptr, 0, &n);
+  if (rc) return rc;
+  std::vector<char> b((size_t)n + 1);
+  rc = vsvb_format_nelecwfn(d, coeff_sc, b.data(), n + 1, &n);
+  if (rc) return rc;
+  FILE *f = std::fopen(path, "w");
+  if (!f) return VSVB_ERR_INPUT;
+  const bool ok = std::fwrite(b.data(), 1, (size_t)n, f) == (size_t)n;
+  return std::fclose(f) == 0 && ok ? VSVB_OK : VSVB_ERR_INPUT;
+}
+

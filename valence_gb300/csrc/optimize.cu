@@ -370,6 +370,8 @@ struct vsvb_opt {
   DevBuf<double> w, H, S, H2, S2, BH, BS;
   int nnd = 0, nsp = 0, nsc = 1;
   double enuc = 0.0;
+  std::string out_orbitals, out_nelecwfn; /* xm_output files (empty: off) */
+  double etol_kcal = 0.0;                 /* the loop's current tolerance, for 'done' */
   long long n_energy = 0, n_hs = 0;
   ~vsvb_opt() {
     for (auto &kv : subs) delete kv.second;
@@ -544,6 +546,20 @@ int root_of(const vsvb_system_desc &d, int iorb1) {
   return r;
 }
 
+/* xm_output (xm_module.F90:464-577): the orbitals file, and with more than
+ * one coupling the coupling file, for the current weights */
+int save_output(vsvb_opt *o, const double *coeff, double energy, bool done) {
+  if (!o->out_orbitals.empty()) {
+    int rc = vsvb_write_orbitals(o->out_orbitals.c_str(), &o->desc.d, coeff, energy, o->etol_kcal, done ? 1 : 0);
+    if (rc) return opt_fail(o, rc, "cannot write " + o->out_orbitals);
+  }
+  if (!o->out_nelecwfn.empty() && o->desc.d.nspinc > 1) {
+    int rc = vsvb_write_nelecwfn(o->out_nelecwfn.c_str(), &o->desc.d, o->csc.data());
+    if (rc) return opt_fail(o, rc, "cannot write " + o->out_nelecwfn);
+  }
+  return VSVB_OK;
+}
+
 /* first_order_opt (valence.F90:527-844) on orbital orb: the new energy */
 int first_order_opt(vsvb_opt *o, double *coeff, int orb, double *energy) {
   const vsvb_system_desc &d = o->desc.d;
@@ -593,6 +609,7 @@ int demgs_opt(vsvb_opt *o, double *coeff, int orb, double etol, double *energy) 
         if (e < eprev) {
           updated = true;
           *energy = e;
+          OK_OR_RETURN(save_output(o, coeff, e, false));
           continue;
         }
         coeff[ic] = origc - perturb;
@@ -601,6 +618,7 @@ int demgs_opt(vsvb_opt *o, double *coeff, int orb, double etol, double *energy) 
         if (e < eprev) {
           updated = true;
           *energy = e;
+          OK_OR_RETURN(save_output(o, coeff, e, false));
           continue;
         }
         coeff[ic] = origc;
@@ -687,6 +705,13 @@ int vsvb_opt_create(const vsvb_system_desc *d, const vsvb_options *opt, vsvb_opt
 
 void vsvb_opt_destroy(vsvb_opt *o) { delete o; }
 
+int vsvb_opt_set_output(vsvb_opt *o, const char *orbitals_path, const char *nelecwfn_path) {
+  if (!o) return VSVB_ERR_INPUT;
+  o->out_orbitals = orbitals_path ? orbitals_path : "";
+  o->out_nelecwfn = nelecwfn_path ? nelecwfn_path : "";
+  return VSVB_OK;
+}
+
 const char *vsvb_opt_last_error(const vsvb_opt *o) { return o ? o->err.c_str() : "null optimiser"; }
 
 int vsvb_opt_first_order_hs(vsvb_opt *o, const double *coeff, const double *coeff_sc, int iorb, double *ham,
@@ -728,11 +753,14 @@ int vsvb_opt_minimize(vsvb_opt *o, double *coeff, double *coeff_sc, vsvb_opt_res
   double energy = 0.0;
   OK_OR_RETURN(energy_of(o, coeff, &energy));
   res->guess_energy = energy;
+  o->etol_kcal = 0.0;
+  OK_OR_RETURN(save_output(o, coeff, energy, false));
   const bool dem_gs = d.ptbnmax > 0.0 && d.nxorb == 0;
   int num_iter = 0;
   double eprv_sc = 0.0, eprv_orb = 0.0, etol = 1.0;
   for (int ntol = d.ntol_e_min; ntol <= d.ntol_e_max; ++ntol) {
     etol = std::pow(10.0, -ntol);
+    o->etol_kcal = etol;
     bool finished = false;
     while (!finished) {
       eprv_sc = energy;
@@ -747,8 +775,12 @@ int vsvb_opt_minimize(vsvb_opt *o, double *coeff, double *coeff_sc, vsvb_opt_res
             const double eprv_set = energy;
             ++num_iter;
             for (int iorb = lo; iorb <= hi; ++iorb) {
-              if (dem_gs) OK_OR_RETURN(demgs_opt(o, coeff, iorb - 1, etol, &energy));
-              else OK_OR_RETURN(first_order_opt(o, coeff, iorb - 1, &energy));
+              if (dem_gs) {
+                OK_OR_RETURN(demgs_opt(o, coeff, iorb - 1, etol, &energy));
+              } else {
+                OK_OR_RETURN(first_order_opt(o, coeff, iorb - 1, &energy));
+                OK_OR_RETURN(save_output(o, coeff, energy, false));
+              }
             }
             setcnv = std::fabs(energy - eprv_set) * kTokcal < etol;
             if (lo == hi && dem_gs) setcnv = true;
@@ -763,6 +795,7 @@ int vsvb_opt_minimize(vsvb_opt *o, double *coeff, double *coeff_sc, vsvb_opt_res
       if (d.nspinc > 1) {
         ++num_iter;
         OK_OR_RETURN(spin_opt(o, coeff, &energy));
+        OK_OR_RETURN(save_output(o, coeff, energy, false));
         finished = std::fabs(energy - eprv_sc) * kTokcal < etol;
       } else {
         finished = true;
@@ -774,6 +807,7 @@ int vsvb_opt_minimize(vsvb_opt *o, double *coeff, double *coeff_sc, vsvb_opt_res
   res->energy = energy;
   res->iterations = num_iter;
   res->converged = num_iter < d.max_iter && std::fabs(energy - eprev) * kTokcal < etol;
+  if (res->converged) OK_OR_RETURN(save_output(o, coeff, energy, true));
   res->etol = etol;
   res->n_energy_evals = o->n_energy;
   res->n_hs_builds = o->n_hs;
