@@ -192,3 +192,15 @@ def test_minimize_writes_orbitals_files(env, tmp_path):
     assert "converged to" in txt
     w = [float(ln.split()[0]) for ln in wfn.read_text().split("\n") if ln.strip() and "." in ln.split()[0]]
     assert np.allclose(w, csc, atol=5e-9)
+
+
+@pytest.mark.parametrize("name", ["h2o-vdz", "lih-sv", "be-sc", "c2-pt-vshf-p2"])
+def test_minimize_on_the_mixed_path(env, name):
+    """The optimiser on the double-float mixed path (FP32 below the Schwarz
+    bound 1e-6) lands on the reference's optimised energy within 1e-6 Eh."""
+    api, oracle_py = env
+    case = [c for c in oracle_py.goldens()["cases"] if c["converged"] and c["name"] == name][0]
+    opt = api.Optimizer(os.path.join(oracle_py.GOLDEN, case["input"]), precision=api.MIXED_DF64)
+    res, c, csc = opt.minimize()
+    opt.close()
+    assert abs(res["energy"] - case["total_energy"]) < 1e-6, (res["energy"], case["total_energy"])
