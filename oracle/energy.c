@@ -1527,3 +1527,30 @@ void vo_ao_eri_block(vo_input *in, int ga, int gb, int gc, int gd, double *out) 
   if (!st) return;
   eri_block(st, ga, gb, gc, gd, out);
 }
+
+/* normal(iorb, iorb) (valence.F90:2157-2182) on the weights as set:
+ * coeff_raw of orbital iorb scaled to unit self-overlap (derived basis
+ * functions normalised first, as the energy path does) */
+int vo_normal(vo_input *in, int iorb) {
+  if (iorb < 1 || iorb > in->norbs) return 1;
+  if (g_last_state) {
+    state_free(g_last_state);
+    g_last_state = NULL;
+  }
+  memcpy(in->coeff, in->coeff_raw, sizeof(double) * in->totlen);
+  vo_state *st = state_new(in);
+  vo_ctx *c0 = ctx_new(st);
+  int nfirst = 2 * in->npair + in->nunpd + in->ndocc + 1;
+  for (int i = nfirst; i <= in->norbs; ++i) {
+    ovint(c0, i, i);
+    double s = pow(c0->sint, -0.5);
+    for (int j = in->map_orbs[i - 1]; j <= in->map_orbs[i] - 1; ++j) in->coeff[j - 1] *= s;
+  }
+  ovint(c0, iorb, iorb);
+  double s = pow(c0->sint, -0.5);
+  for (int j = in->map_orbs[iorb - 1]; j <= in->map_orbs[iorb] - 1; ++j) in->coeff_raw[j - 1] *= s;
+  ctx_free(c0);
+  state_free(st);
+  return 0;
+}
+

@@ -106,6 +106,8 @@ int vo_first_order_hs(vo_input *in, int iorb, double *ham, double *ovl, int nthr
 /* spin_opt's (valence.F90:850-897): nspinc x nspinc over the couplings. */
 int vo_spin_hs(vo_input *in, double *ham, double *ovl, int nthreads);
 double vo_nuclear_repulsion(vo_input *in);
+/* normal(iorb, iorb) (valence.F90:2157-2182) applied to coeff_raw */
+int vo_normal(vo_input *in, int iorb);
 
 /* Orbital-level integrals after vo_guess_energy's normalisation:
  * (io ko | jo lo) over the screened LCAO weights (1-based orbitals). */

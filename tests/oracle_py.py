@@ -136,6 +136,7 @@ class OptOracle(Oracle):
                                  ctypes.c_int]
         L.vo_nuclear_repulsion.argtypes = [ctypes.c_void_p]
         L.vo_nuclear_repulsion.restype = ctypes.c_double
+        L.vo_normal.argtypes = [ctypes.c_void_p, ctypes.c_int]
         self.inp = ctypes.cast(self.h, ctypes.POINTER(VoInput)).contents
 
     def coeff_raw(self):
@@ -188,6 +189,50 @@ class OptOracle(Oracle):
         self.set_coeff(c)
         return eig[r] + self.enucrep()
 
+    def demgs_opt(self, iorb, etol, energy, nthreads=0):
+        """demgs_opt (valence.F90:350-524): coordinate-wise perturbation of
+        the orbital's normalised weights, largest step first, feathered down
+        until tokcal * perturb^2 < etol.  normal() follows every change, and
+        a rejected +step leaves the other weights at their +step scale, as in
+        the reference."""
+        inp = self.inp
+        j0 = inp.map_orbs[iorb - 1] - 1
+        nb = self.norbas(iorb)
+        perturb = inp.ptbnmax
+
+        def trial(i, value):
+            c = self.coeff_raw()
+            c[j0 + i] = value
+            self.set_coeff(c)
+            lib().vo_normal(self.h, iorb)
+            return self.guess_energy(nthreads).energy
+
+        while TOKCAL * perturb * perturb >= etol:
+            lock = [False] * nb
+            updated = True
+            while updated:
+                updated = False
+                for i in range(nb):
+                    if lock[i]:
+                        continue
+                    origc, eprev = self.coeff_raw()[j0 + i], energy
+                    e = trial(i, origc + perturb)
+                    if e < eprev:
+                        updated, energy = True, e
+                        continue
+                    e = trial(i, origc - perturb)
+                    if e < eprev:
+                        updated, energy = True, e
+                        continue
+                    c = self.coeff_raw()
+                    c[j0 + i] = origc
+                    self.set_coeff(c)
+                    lib().vo_normal(self.h, iorb)
+                    lock[i] = True
+                    energy = eprev
+            perturb *= inp.feather
+        return energy
+
     def spin_opt(self, nthreads=0):
         """valence.F90:850-936: lowest root into coeff_sc (not normalised)."""
         import scipy.linalg
@@ -197,12 +242,15 @@ class OptOracle(Oracle):
         return eig[0] + self.enucrep()
 
     def minimize_energy(self, nthreads=0):
-        """minimize_energy (valence.F90:2744-2885) after guess_energy; the
-        first-order method only (dem_gs inputs raise).  Returns the final
-        energy and the number of iterations."""
+        """minimize_energy (valence.F90:2744-2885) after guess_energy, with
+        first_order_opt, or demgs_opt when ptbnmax > 0 and there are no
+        excited-state roots.  Returns the final energy and the number of
+        iterations."""
         inp = self.inp
-        if inp.ptbnmax > 0.0 and inp.nxorb == 0:
-            raise NotImplementedError("direct energy minimisation (demgs_opt)")
+        dem_gs = inp.ptbnmax > 0.0 and inp.nxorb == 0
+        # calculate_vsvb_energy normalises the weights before anything else
+        for iorb in range(1, inp.norbs - inp.ndf + 1):
+            lib().vo_normal(self.h, iorb)
         energy = self.guess_energy(nthreads).energy
         num_iter = 0
         eprv_sc = eprv_orb = 0.0
@@ -221,8 +269,13 @@ class OptOracle(Oracle):
                             eprv_set = energy
                             num_iter += 1
                             for iorb in range(lo, hi + 1):
-                                energy = self.first_order_opt(iorb, nthreads)
+                                if dem_gs:
+                                    energy = self.demgs_opt(iorb, etol, energy, nthreads)
+                                else:
+                                    energy = self.first_order_opt(iorb, nthreads)
                             setcnv = abs(energy - eprv_set) * TOKCAL < etol
+                            if lo == hi and dem_gs:
+                                setcnv = True
                     orbconv = abs(energy - eprv_orb) * TOKCAL < etol
                     if len(sets) == 1:
                         orbconv = True

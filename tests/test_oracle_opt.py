@@ -1,6 +1,6 @@
 """The oracle's restatement of the reference optimiser (minimize_energy with
-first_order_opt and spin_opt, valence.F90:527-936, 2744-2885) against the
-optimised total energies the reference's own test suite pins
+first_order_opt, demgs_opt and spin_opt, valence.F90:350-936, 2744-2885)
+against the optimised total energies the reference's own test suite pins
 (testing/testing.py:69-151, examples/test_examples.py: 'True' entries,
 1e-6 Eh).  The H/S builds are the oracle's literal transition energies over
 the reference's dummy orbitals; rsg is scipy's generalised eigensolver."""
@@ -11,19 +11,16 @@ import pytest
 
 from tests import oracle_py
 
-# inputs the oracle optimises in seconds; c2-pt-vshf-p2 (about 15 minutes
-# here) and the direct-minimisation inputs (demgs_opt) are left out
-FAST = ["be", "be+ndf", "cu+", "h", "h2-dz", "h2-sz", "he", "h+ndf", "h2o-vdz", "h2o-vdz-sc1", "lih-sv", "be-sc",
-        "be-scv3s+2sc", "be3s2", "he1s2s", "he3s-1s3s", "li_opt"]
+# inputs the oracle optimises in seconds (c2-pt-vshf-p2, about 15 minutes
+# here, is left out); h2o-vdz-dem and the testing li_opt run demgs_opt
+FAST = ["be", "be+ndf", "cu+", "h", "h2-dz", "h2-sz", "he", "h+ndf", "h2o-vdz", "h2o-vdz-sc1", "h2o-vdz-dem", "lih-sv",
+        "be-sc", "be-scv3s+2sc", "be3s2", "he1s2s", "he3s-1s3s", "li_opt"]
 
 
 def _cases():
     out = []
     for c in oracle_py.goldens()["cases"]:
         if c["converged"] and c["name"] in FAST:
-            o = oracle_py.OptOracle(os.path.join(oracle_py.GOLDEN, c["input"]))
-            if o.inp.ptbnmax > 0.0 and o.inp.nxorb == 0:
-                continue
             out.append(pytest.param(c, id=f'{c["suite"]}-{c["name"]}'))
     return out
 
