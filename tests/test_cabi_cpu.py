@@ -236,3 +236,32 @@ def test_nelecwfn_writer_reproduces_reference_records(lib):
             assert ln in src, (name, ln)
         checked += 1
     assert checked >= 2
+
+
+def test_plain_c_host_compiles_links_and_runs(lib, tmp_path):
+    """include/vsvb_gpu.h is a C header: a C99 host (tests/c_host/host.c)
+    compiles against it with warnings as errors, links the library and runs
+    the input reader and writers; handle creation returns a status code."""
+    import shutil
+    import torch
+    from valence_gb300 import api
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    exe = str(tmp_path / "host")
+    libdir = os.path.dirname(api.library_path())
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "c_host", "host.c"), "-L", libdir, "-lvsvb_gb300",
+                        "-Wl,-rpath," + libdir, "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    inp = os.path.join(oracle_py.GOLDEN, "cases", "testing", "be-sc")
+    r = subprocess.run([exe, inp], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    out = dict((ln.split()[0], ln.split()[1:]) for ln in r.stdout.splitlines())
+    assert out["read"][0] == "0" and out["read"][8] == "2"
+    assert out["orbitals"][0] == "0" and int(out["orbitals"][1]) > 0
+    assert out["nelecwfn"][0] == "0"
+    if not torch.cuda.is_available():
+        assert out["create"][0] != "0" and out["opt_create"][0] != "0"
+    else:
+        assert out["create"][0] == "0" and out["opt_create"][0] == "0"
