@@ -460,8 +460,12 @@ def run_batch(a, timed, world):
             seed += 1
             try:
                 s = vg.System(p, precision=vg.MIXED_DF64)
-                s.energy_grad()
+                r, _ = s.energy_grad()
             except vg.VSVBError:
+                skipped += 1
+                continue
+            if r["n_singular_pairs"]:
+                s.close()
                 skipped += 1
                 continue
             systems.append((s, p))

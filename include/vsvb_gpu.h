@@ -42,7 +42,7 @@ typedef enum vsvb_status {
   VSVB_ERR_INPUT = 1,       /* malformed input / inconsistent dimensions */
   VSVB_ERR_UNSUPPORTED = 2, /* e.g. angular momentum above d on the GPU */
   VSVB_ERR_CUDA = 3,        /* a CUDA runtime call failed */
-  VSVB_ERR_SINGULAR = 4,    /* gradient requested through a singular determinant pair */
+  VSVB_ERR_SINGULAR = 4,    /* a determinant-pair block singular even when shifted (gradient), or rsg's overlap not positive definite */
   VSVB_ERR_NOMEM = 5,
   VSVB_ERR_TIMEOUT = 6,     /* a bounded device-side wait gave up */
   VSVB_ERR_NOT_NORMALISABLE = 7, /* an orbital has non-positive self-overlap */

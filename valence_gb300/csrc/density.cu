@@ -16,7 +16,12 @@
  * with T = A^-1.  Blocks whose pivots fall below 1e-7 of their largest entry
  * (exact rank deficiency from molecular symmetry, e.g. pi pairs) take the
  * exact path: the struck matrix is built and its determinant taken by LU,
- * which is what the reference's givdr computes.
+ * which is what the reference's givdr computes.  For the adjoint such a
+ * block also keeps det and inverse of A + delta I (delta = 1e-8 of its
+ * largest entry): every struck determinant is a polynomial in A, so the
+ * derivative taken through the shifted pair is within about 5 delta
+ * (relative) of the exact one at any rank deficiency, where det(A) A^-1
+ * itself does not exist.
  *
  * The task loop keeps the reference's arithmetic: the same triangular task
  * enumeration (xm_dtriang8, xm_module.F90:969-991), the Schwarz screens on
@@ -83,6 +88,7 @@ struct QInfo {
   /* after the determinant pairs are factorised (load_dets) */
   double da, db; /* det of the alpha / beta block */
   double wdd;    /* w * da * db */
+  double wddr;   /* w * det(A + delta I) per block: wdd unless a block is flagged */
   int sing;      /* exact-minor flags per spin block */
 };
 
@@ -96,7 +102,7 @@ __device__ __forceinline__ QInfo decode_q(const DetCtx &d, long long q) {
   r.isc = (int)(sp / d.ds.nsc);
   r.jsc = (int)(sp % d.ds.nsc);
   r.w = d.coeff_sc[r.isc] * d.coeff_sc[r.jsc];
-  r.da = r.db = r.wdd = 0.0;
+  r.da = r.db = r.wdd = r.wddr = 0.0;
   r.sing = 0;
   return r;
 }
@@ -106,6 +112,7 @@ __device__ __forceinline__ void load_dets(const DetCtx &d, long long q, QInfo &q
   qi.db = d.det_b[q];
   qi.wdd = qi.w * qi.da * qi.db;
   qi.sing = d.sing[q];
+  qi.wddr = qi.sing ? qi.w * d.detr_a[q] * d.detr_b[q] : qi.wdd;
 }
 
 /* exact determinant of spin block sp of pair q with up to two strikes, by LU
@@ -158,6 +165,8 @@ __device__ __noinline__ double struck_det_exact(const DetCtx &d, const QInfo &qi
 struct Cof {
   bool ok;        /* spin integration non-zero */
   double v;       /* w * det_a * det_b * J_a * J_b */
+  double vr;      /* the same from A + delta I on a flagged block (the
+                   * adjoint's value; v elsewhere) */
   int na_s, nb_s; /* strikes per spin */
   int ra[2], ca[2], rb[2], cb[2];
   double Ja, Jb;  /* reduced factors */
@@ -170,11 +179,10 @@ struct Loc {
 
 /* cofactor of determinant pair q for up to two strikes (bra slot -> ket
  * slot), given their locations */
-__device__ Cof cofactor_loc(const DetCtx &d, long long q, const QInfo &qi, int nst, const Loc *lb, const Loc *lk,
-                            int *status) {
+__device__ Cof cofactor_loc(const DetCtx &d, long long q, const QInfo &qi, int nst, const Loc *lb, const Loc *lk) {
   Cof c;
   c.ok = false;
-  c.v = 0.0;
+  c.v = c.vr = 0.0;
   c.na_s = c.nb_s = 0;
   c.Ja = c.Jb = 1.0;
   for (int t = 0; t < nst; ++t) {
@@ -193,31 +201,24 @@ __device__ Cof cofactor_loc(const DetCtx &d, long long q, const QInfo &qi, int n
   c.ok = true;
   const int na = d.ds.nalpha, nb = d.ds.nbeta;
   const int sing = qi.sing;
-  double fa, fb;
-  if ((sing & 1) && c.na_s > 0) {
-    fa = struck_det_exact(d, qi, 0, c.na_s, c.ra, c.ca);
-    c.Ja = 0.0;
-    if (status) atomicOr(status, 2);
-  } else {
-    const double *Ta = d.Ta + (size_t)q * na * na;
-    if (c.na_s == 1) c.Ja = Ta[c.ca[0] * na + c.ra[0]];
-    else if (c.na_s == 2)
-      c.Ja = Ta[c.ca[0] * na + c.ra[0]] * Ta[c.ca[1] * na + c.ra[1]] - Ta[c.ca[0] * na + c.ra[1]] * Ta[c.ca[1] * na + c.ra[0]];
-    fa = qi.da * c.Ja;
+  /* J from the stored inverse: A^-1, or (A + delta I)^-1 on a flagged block */
+  const double *Ta = d.Ta + (size_t)q * na * na;
+  if (c.na_s == 1) c.Ja = Ta[c.ca[0] * na + c.ra[0]];
+  else if (c.na_s == 2)
+    c.Ja = Ta[c.ca[0] * na + c.ra[0]] * Ta[c.ca[1] * na + c.ra[1]] - Ta[c.ca[0] * na + c.ra[1]] * Ta[c.ca[1] * na + c.ra[0]];
+  const double *Tb = d.Tb + (size_t)q * nb * nb;
+  if (c.nb_s == 1) c.Jb = Tb[c.cb[0] * nb + c.rb[0]];
+  else if (c.nb_s == 2)
+    c.Jb = Tb[c.cb[0] * nb + c.rb[0]] * Tb[c.cb[1] * nb + c.rb[1]] - Tb[c.cb[0] * nb + c.rb[1]] * Tb[c.cb[1] * nb + c.rb[0]];
+  if (!(sing & 3)) {
+    c.v = c.vr = qi.wdd * (c.Ja * c.Jb);
+    return c;
   }
-  if ((sing & 2) && c.nb_s > 0) {
-    fb = struck_det_exact(d, qi, 1, c.nb_s, c.rb, c.cb);
-    c.Jb = 0.0;
-    if (status) atomicOr(status, 2);
-  } else {
-    const double *Tb = d.Tb + (size_t)q * nb * nb;
-    if (c.nb_s == 1) c.Jb = Tb[c.cb[0] * nb + c.rb[0]];
-    else if (c.nb_s == 2)
-      c.Jb = Tb[c.cb[0] * nb + c.rb[0]] * Tb[c.cb[1] * nb + c.rb[1]] - Tb[c.cb[0] * nb + c.rb[1]] * Tb[c.cb[1] * nb + c.rb[0]];
-    fb = qi.db * c.Jb;
-  }
-  /* on the inverse path fa * fb = da * db * Ja * Jb */
-  c.v = (sing & 3) ? qi.w * fa * fb : qi.wdd * (c.Ja * c.Jb);
+  /* a flagged block: the value from exact struck determinants */
+  const double fa = (sing & 1) && c.na_s > 0 ? struck_det_exact(d, qi, 0, c.na_s, c.ra, c.ca) : qi.da * c.Ja;
+  const double fb = (sing & 2) && c.nb_s > 0 ? struck_det_exact(d, qi, 1, c.nb_s, c.rb, c.cb) : qi.db * c.Jb;
+  c.v = qi.w * fa * fb;
+  c.vr = qi.wddr * (c.Ja * c.Jb);
   return c;
 }
 
@@ -234,13 +235,13 @@ __device__ __forceinline__ Loc loc_ket(const DetCtx &d, const QInfo &qi, int s) 
 
 /* cofactor of determinant pair q for up to two (bra slot, ket slot) strikes */
 __device__ __forceinline__ Cof cofactor(const DetCtx &d, long long q, const QInfo &qi, int nst, const int *sb,
-                                        const int *sk, int *status) {
+                                        const int *sk) {
   Loc lb[2], lk[2];
   for (int t = 0; t < nst; ++t) {
     lb[t] = loc_bra(d, qi, sb[t]);
     lk[t] = loc_ket(d, qi, sk[t]);
   }
-  return cofactor_loc(d, q, qi, nst, lb, lk, status);
+  return cofactor_loc(d, q, qi, nst, lb, lk);
 }
 
 /* dJ/dT accumulation for one cofactor with coefficient coef on v */
@@ -248,7 +249,7 @@ __device__ void accum_G(const DetCtx &d, long long q, const QInfo &qi, const Cof
                         int lda, int ldb) {
   if (!c.ok || coef == 0.0) return;
   const int na = d.ds.nalpha, nb = d.ds.nbeta;
-  const double dd = qi.wdd;
+  const double dd = qi.wddr;
   if (c.na_s > 0) {
     const double *Ta = d.Ta + (size_t)q * na * na;
     const double f = coef * dd * c.Jb;
@@ -319,99 +320,132 @@ __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
     const int n = sp == 0 ? d.ds.nalpha : d.ds.nbeta;
     double *Tout = (sp == 0 ? d.Ta : d.Tb) + (size_t)q * n * n;
     if (n == 0) {
-      if (threadIdx.x == 0) (sp == 0 ? d.det_a : d.det_b)[q] = 1.0;
+      if (threadIdx.x == 0) (sp == 0 ? d.det_a : d.det_b)[q] = (sp == 0 ? d.detr_a : d.detr_b)[q] = 1.0;
       continue;
     }
     const int n2 = 2 * n;
-    /* W = [A | I] */
-    double mx = 0.0;
-    for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
-      int r = t / n2, c = t - r * n2;
-      double v;
-      if (c < n) {
-        int sb = spat(d, pos_slot(d, qi.isc, qi.bb, sp, r));
-        int sk = spat(d, pos_slot(d, qi.jsc, qi.kb, sp, c));
-        v = d.So[sb * d.ds.nsp + sk];
-        mx = fmax(mx, fabs(v));
-      } else {
-        v = (c - n == r) ? 1.0 : 0.0;
-      }
-      W[t] = v;
-    }
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double m = 0.0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
-      red[0] = m;
-      sdet = 1.0;
-      ssing = 0;
-    }
-    __syncthreads();
-    const double amax = red[0];
-    __syncthreads();
-    for (int k = 0; k < n; ++k) {
-      /* pivot search */
-      double best = -1.0;
-      int bi = k;
-      for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
-        double v = fabs(W[i * n2 + k]);
-        if (v > best) {
-          best = v;
-          bi = i;
+    double amax = 0.0;
+    /* pass 0 factorises A; a block whose pivots fall below 1e-7 of its
+     * largest entry takes its exact determinant by LU instead and then
+     * pass 1 factorises A + delta I (delta = 1e-8 of that entry): the
+     * adjoint walks take the determinant and inverse of the shifted matrix
+     * together, which gives the derivative of every struck determinant of
+     * A to about 5 delta relative, whatever the block's rank deficiency */
+    for (int pass = 0; pass < 2; ++pass) {
+      const double shift = pass == 0 ? 0.0 : 1e-8 * amax;
+      /* W = [A + shift I | I] */
+      double mx = 0.0;
+      for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
+        int r = t / n2, c = t - r * n2;
+        double v;
+        if (c < n) {
+          int sb = spat(d, pos_slot(d, qi.isc, qi.bb, sp, r));
+          int sk = spat(d, pos_slot(d, qi.jsc, qi.kb, sp, c));
+          v = d.So[sb * d.ds.nsp + sk];
+          mx = fmax(mx, fabs(v));
+          if (c == r) v += shift;
+        } else {
+          v = (c - n == r) ? 1.0 : 0.0;
         }
+        W[t] = v;
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        double ob = __shfl_xor_sync(0xffffffffu, best, o);
-        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ob > best || (ob == best && oi < bi)) {
-          best = ob;
-          bi = oi;
-        }
-      }
-      if ((threadIdx.x & 31) == 0) {
-        red[threadIdx.x >> 5] = best;
-        redi[threadIdx.x >> 5] = bi;
-      }
+      for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
       __syncthreads();
       if (threadIdx.x == 0) {
-        double b = -1.0;
-        int p = k;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-          if (red[w] > b || (red[w] == b && redi[w] < p)) {
-            b = red[w];
-            p = redi[w];
+        double m = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+        red[0] = m;
+        sdet = 1.0;
+        ssing = 0;
+      }
+      __syncthreads();
+      if (pass == 0) amax = red[0];
+      /* pass 0 flags small pivots; pass 1 fails only on a zero pivot */
+      const double pmin = pass == 0 ? 1e-7 * amax : 0.0;
+      __syncthreads();
+      for (int k = 0; k < n; ++k) {
+        /* pivot search */
+        double best = -1.0;
+        int bi = k;
+        for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
+          double v = fabs(W[i * n2 + k]);
+          if (v > best) {
+            best = v;
+            bi = i;
           }
-        spiv = p;
-        if (!(b > 1e-7 * amax)) ssing = 1;
-      }
-      __syncthreads();
-      if (ssing) break;
-      const int p = spiv;
-      if (p != k) {
-        for (int j = threadIdx.x; j < n2; j += blockDim.x) {
-          double t = W[k * n2 + j];
-          W[k * n2 + j] = W[p * n2 + j];
-          W[p * n2 + j] = t;
         }
+        for (int o = 16; o > 0; o >>= 1) {
+          double ob = __shfl_xor_sync(0xffffffffu, best, o);
+          int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+          if (ob > best || (ob == best && oi < bi)) {
+            best = ob;
+            bi = oi;
+          }
+        }
+        if ((threadIdx.x & 31) == 0) {
+          red[threadIdx.x >> 5] = best;
+          redi[threadIdx.x >> 5] = bi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double b = -1.0;
+          int p = k;
+          for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+            if (red[w] > b || (red[w] == b && redi[w] < p)) {
+              b = red[w];
+              p = redi[w];
+            }
+          spiv = p;
+          if (!(b > pmin)) ssing = 1;
+        }
+        __syncthreads();
+        if (ssing) break;
+        const int p = spiv;
+        if (p != k) {
+          for (int j = threadIdx.x; j < n2; j += blockDim.x) {
+            double t = W[k * n2 + j];
+            W[k * n2 + j] = W[p * n2 + j];
+            W[p * n2 + j] = t;
+          }
+        }
+        __syncthreads();
+        const double piv = W[k * n2 + k];
+        if (threadIdx.x == 0) sdet *= (p != k ? -piv : piv);
+        __syncthreads();
+        for (int j = threadIdx.x; j < n2; j += blockDim.x) W[k * n2 + j] /= piv;
+        __syncthreads();
+        for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
+          int i = t / n2, j = t - i * n2;
+          if (i != k && j != k) W[t] -= W[i * n2 + k] * W[k * n2 + j];
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+          if (i != k) W[i * n2 + k] = 0.0;
+        __syncthreads();
       }
-      __syncthreads();
-      const double piv = W[k * n2 + k];
-      if (threadIdx.x == 0) sdet *= (p != k ? -piv : piv);
-      __syncthreads();
-      for (int j = threadIdx.x; j < n2; j += blockDim.x) W[k * n2 + j] /= piv;
-      __syncthreads();
-      for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
-        int i = t / n2, j = t - i * n2;
-        if (i != k && j != k) W[t] -= W[i * n2 + k] * W[k * n2 + j];
+      if (!ssing) {
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+          int r = t / n, c = t - r * n;
+          Tout[t] = W[r * n2 + n + c];
+        }
+        if (threadIdx.x == 0) {
+          if (pass == 0) (sp == 0 ? d.det_a : d.det_b)[q] = sdet;
+          (sp == 0 ? d.detr_a : d.detr_b)[q] = sdet;
+        }
+        __syncthreads();
+        break;
       }
-      __syncthreads();
-      for (int i = threadIdx.x; i < n; i += blockDim.x)
-        if (i != k) W[i * n2 + k] = 0.0;
-      __syncthreads();
-    }
-    if (ssing) {
+      if (pass == 1) {
+        /* A + delta I is singular too: no inverse for the adjoint */
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) Tout[t] = 0.0;
+        if (threadIdx.x == 0) {
+          (sp == 0 ? d.detr_a : d.detr_b)[q] = 0.0;
+          if (d.status) atomicOr(d.status, 2);
+        }
+        __syncthreads();
+        break;
+      }
       /* exact-minor path: the unstruck determinant by LU on a fresh copy */
       if (threadIdx.x == 0) {
         double det = 1.0;
@@ -452,13 +486,6 @@ __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
         atomicOr(&d.sing[q], 1 << sp);
       }
       __syncthreads();
-      for (int t = threadIdx.x; t < n * n; t += blockDim.x) Tout[t] = 0.0;
-    } else {
-      for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
-        int r = t / n, c = t - r * n;
-        Tout[t] = W[r * n2 + n + c];
-      }
-      if (threadIdx.x == 0) (sp == 0 ? d.det_a : d.det_b)[q] = sdet;
     }
     __syncthreads();
   }
@@ -522,7 +549,7 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
     /* 1-based parity as in the reference: slots i+1, j+1 */
     if (idocc && jdocc && ((i + 1) & 1) != ((j + 1) & 1)) continue;
     int sb[1] = {i}, sk[1] = {j};
-    Cof c = cofactor(d, q, qi, 1, sb, sk, a.status);
+    Cof c = cofactor(d, q, qi, 1, sb, sk);
     if (!c.ok) continue;
     const int si = spat(d, i), sj = spat(d, j);
     const double h = d.Ho[si * nsp + sj], s = d.So[si * nsp + sj];
@@ -531,15 +558,15 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
     if (UNSC) {
       /* dE/dh part (scaled by 1/W later) and dE/dS part (scaled by
        * -E_num/(W^2 nelec) later) kept apart */
-      vtot += h * c.v;
-      vtot_s += s * c.v;
+      vtot += h * c.vr;
+      vtot_s += s * c.vr;
       accum_G(d, q, qi, c, h, Ga, Gb, lda, ldb);
       double *Gsa = a.Gs + (size_t)q * (na * na + nb * nb);
       accum_G(d, q, qi, c, s, Gsa, Gsa + na * na, na, nb);
       atomicAdd(a.D1 + si * nsp + sj, c.v);
     } else if (GRAD) {
       const double coef = h * inv_w + dw_coef * s;
-      vtot += coef * c.v;
+      vtot += coef * c.vr;
       accum_G(d, q, qi, c, coef, Ga, Gb, lda, ldb);
       atomicAdd(a.Hbar + si * nsp + sj, c.v * inv_w);
       atomicAdd(a.Sbar + si * nsp + sj, c.v * dw_coef);
@@ -617,7 +644,7 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
             cx_c.ok = false;
             if (es) {
               const Loc lk[2] = {Lk, Ll};
-              ce_c = cofactor_loc(d, q, qi, 2, Lb, lk, a.status);
+              ce_c = cofactor_loc(d, q, qi, 2, Lb, lk);
             }
             if (xs) {
               if (es && ce_c.ok) {
@@ -627,7 +654,7 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
                 cx_c.ok = Lb[0].spin == Ll.spin && Lb[1].spin == Lk.spin;
               } else {
                 const Loc lk[2] = {Ll, Lk};
-                cx_c = cofactor_loc(d, q, qi, 2, Lb, lk, a.status);
+                cx_c = cofactor_loc(d, q, qi, 2, Lb, lk);
               }
             }
             double dd = 0.0, xd = 0.0;
@@ -649,11 +676,11 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
               cve *= fw;
               cvx *= fw;
               if (ce_c.ok && cve != 0.0) {
-                vtot += cve * ce_c.v;
+                vtot += cve * ce_c.vr;
                 accum_G(d, q, qi, ce_c, cve, Ga, Gb, lda, ldb);
               }
               if (cx_c.ok && cvx != 0.0) {
-                vtot += cvx * cx_c.v;
+                vtot += cvx * cx_c.vr;
                 accum_G(d, q, qi, cx_c, cvx, Ga, Gb, lda, ldb);
               }
             }

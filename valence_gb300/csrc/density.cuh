@@ -12,10 +12,12 @@ struct DetCtx {
   const int *slot_which;  /* [nsc][2*npair]: 0 if the slot is pair_sc(k,1), 1 if (k,2) */
   const double *coeff_sc; /* [nsc] (1.0 when nspinc == 0) */
   const double *So, *Ho;  /* nsp x nsp orbital overlap / core Hamiltonian */
-  double *det_a, *det_b;  /* [nq] */
-  double *Ta, *Tb;        /* [nq][n*n] inverses (zero on the exact-minor path) */
+  double *det_a, *det_b;  /* [nq] determinants (exact LU on the exact-minor path) */
+  double *detr_a, *detr_b; /* [nq] det(A + delta I) of a flagged block, det(A) elsewhere */
+  double *Ta, *Tb;        /* [nq][n*n] inverses, of A + delta I on a flagged block */
   int *sing;              /* [nq] bit0 alpha, bit1 beta on the exact-minor path */
   int *nsing;             /* count of determinant pairs with a bit set (optional) */
+  int *status;            /* bit 1 (value 2): a flagged block whose shift is singular too */
 };
 
 struct AsmArgs {

@@ -205,7 +205,7 @@ struct vsvb_gpu {
   DBuf<int> obs_n, obs_ao, term0, term_slot, term_j, term_m, term_f, ndf_orb;
   DBuf<double> coeff_d, ndf_scale, orb_scale, Craw, C, So, Ho, xtab, T, sqT, qmax, q0max;
   DBuf<int> pair_slot, slot_pair, slot_which, sing, status, nsing;
-  DBuf<double> coeff_sc, det_a, det_b, Ta, Tb, scratch;
+  DBuf<double> coeff_sc, det_a, det_b, detr_a, detr_b, Ta, Tb, scratch;
   int ld_scratch = 0;
   DBuf<double> part_e1, part_wf, part_e2, result;
   /* adjoint */
@@ -327,10 +327,13 @@ DetCtx det_ctx(vsvb_gpu *h) {
   d.Ho = h->Ho.p;
   d.det_a = h->det_a.p;
   d.det_b = h->det_b.p;
+  d.detr_a = h->detr_a.p;
+  d.detr_b = h->detr_b.p;
   d.Ta = h->Ta.p;
   d.Tb = h->Tb.p;
   d.sing = h->sing.p;
   d.nsing = h->nsing.p;
+  d.status = h->status.p;
   return d;
 }
 
@@ -1058,6 +1061,8 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   const int na = ds.nalpha, nb = ds.nbeta;
   CK(h->det_a.alloc(nq), "alloc det");
   CK(h->det_b.alloc(nq), "alloc det");
+  CK(h->detr_a.alloc(nq), "alloc det");
+  CK(h->detr_b.alloc(nq), "alloc det");
   CK(h->Ta.alloc(std::max<long long>(nq * na * na, 1)), "alloc Ta");
   CK(h->Tb.alloc(std::max<long long>(nq * nb * nb, 1)), "alloc Tb");
   CK(h->sing.alloc(nq), "alloc sing");
@@ -1556,7 +1561,7 @@ static int energy_grad_common(vsvb_gpu *h, vsvb_energy_result *out, double *grad
   int status = 0;
   CK(cudaMemcpy(&status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost), "status");
   if (status & 2) {
-    h->err = "gradient through a singular determinant pair is not implemented";
+    h->err = "gradient through a determinant pair whose overlap block stays singular when shifted";
     return VSVB_ERR_SINGULAR;
   }
   if (out) *out = r;
@@ -1738,7 +1743,7 @@ int vsvb_batch_energy_grad(vsvb_batch *b, const double *const *weights_dev, doub
       return VSVB_ERR_NOT_NORMALISABLE;
     }
     if (stat[i] & 2) {
-      b->err = "molecule " + std::to_string(i) + ": gradient through a singular determinant pair";
+      b->err = "molecule " + std::to_string(i) + ": gradient through a determinant pair whose overlap block stays singular when shifted";
       return VSVB_ERR_SINGULAR;
     }
     if (results) {
@@ -1953,7 +1958,7 @@ int gpu_hs_columns(vsvb_gpu *h, const double *w_dev, const int *src_dev, int j0,
     return VSVB_ERR_NOT_NORMALISABLE;
   }
   if (flag & 2) {
-    h->err = "first_order_opt matrices through a singular determinant pair are not implemented";
+    h->err = "first_order_opt matrices through a determinant pair whose overlap block stays singular when shifted";
     return VSVB_ERR_SINGULAR;
   }
   return VSVB_OK;
