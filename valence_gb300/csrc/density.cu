@@ -119,6 +119,11 @@ __device__ __forceinline__ void load_dets(const DetCtx &d, long long q, QInfo &q
  * with partial pivoting on the struck matrix (n <= VSVB_MAXN) */
 __device__ __noinline__ double struck_det_exact(const DetCtx &d, const QInfo &qi, int sp, int ns, const int *rr, const int *cc) {
   const int n = sp == 0 ? d.ds.nalpha : d.ds.nbeta;
+  if (n > VSVB_MAXN) {
+    /* larger than the local matrix: reported, not computed */
+    if (d.status) atomicOr(d.status, 4);
+    return 0.0;
+  }
   double M[VSVB_MAXN * VSVB_MAXN];
   for (int r = 0; r < n; ++r) {
     int sb = spat(d, pos_slot(d, qi.isc, qi.bb, sp, r));

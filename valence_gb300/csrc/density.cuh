@@ -17,7 +17,8 @@ struct DetCtx {
   double *Ta, *Tb;        /* [nq][n*n] inverses, of A + delta I on a flagged block */
   int *sing;              /* [nq] bit0 alpha, bit1 beta on the exact-minor path */
   int *nsing;             /* count of determinant pairs with a bit set (optional) */
-  int *status;            /* bit 1 (value 2): a flagged block whose shift is singular too */
+  int *status;            /* value 2: a flagged block whose shift is singular too;
+                           * value 4: a flagged block above VSVB_MAXN electrons of one spin */
 };
 
 struct AsmArgs {

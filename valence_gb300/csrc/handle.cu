@@ -1276,6 +1276,10 @@ int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
     h->err = "an orbital has non-positive self-overlap";
     return VSVB_ERR_NOT_NORMALISABLE;
   }
+  if (status & 4) {
+    h->err = "a singular determinant block with more than " + std::to_string(VSVB_MAXN) + " electrons of one spin";
+    return VSVB_ERR_UNSUPPORTED;
+  }
   if (out) {
     fill_result(h, r, out);
     out->n_singular_pairs = nsing;
@@ -1742,6 +1746,11 @@ int vsvb_batch_energy_grad(vsvb_batch *b, const double *const *weights_dev, doub
       b->err = "molecule " + std::to_string(i) + ": an orbital has non-positive self-overlap";
       return VSVB_ERR_NOT_NORMALISABLE;
     }
+    if (stat[i] & 4) {
+      b->err = "molecule " + std::to_string(i) + ": a singular determinant block with more than " +
+               std::to_string(VSVB_MAXN) + " electrons of one spin";
+      return VSVB_ERR_UNSUPPORTED;
+    }
     if (stat[i] & 2) {
       b->err = "molecule " + std::to_string(i) + ": gradient through a determinant pair whose overlap block stays singular when shifted";
       return VSVB_ERR_SINGULAR;
@@ -1956,6 +1965,10 @@ int gpu_hs_columns(vsvb_gpu *h, const double *w_dev, const int *src_dev, int j0,
   if (flag & 1) {
     h->err = "an orbital has non-positive self-overlap";
     return VSVB_ERR_NOT_NORMALISABLE;
+  }
+  if (flag & 4) {
+    h->err = "a singular determinant block with more than " + std::to_string(VSVB_MAXN) + " electrons of one spin";
+    return VSVB_ERR_UNSUPPORTED;
   }
   if (flag & 2) {
     h->err = "first_order_opt matrices through a determinant pair whose overlap block stays singular when shifted";
