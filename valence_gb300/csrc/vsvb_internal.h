@@ -14,7 +14,9 @@
  *   C_obs       double[norb*maxobs]  per evaluation: normalised orbital weights
  *   T           double[np*np]        per evaluation: orbital-pair ERIs
  *                                    (i k | j l), np = n(n+1)/2
- *   det data    per determinant pair q: det, inverse (n x n) per spin
+ *   det data    per determinant pair q: det, inverse (n x n) per spin; a
+ *               block flagged singular keeps det(A + delta I) and that
+ *               matrix's inverse for the adjoint
  */
 #ifndef VSVB_INTERNAL_H
 #define VSVB_INTERNAL_H
