@@ -207,8 +207,11 @@ extern "C" int vsvb_det_factor(const double *a_dev, int n, int nmat, double *det
  *    needs 2*n*n*nmat of them and is rejected with VSVB_ERR_TOO_LARGE beyond
  *    that;
  *  - the first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress) with that device current; make that first call
- *    before any stream capture;
+ *    (cudaGetSymbolAddress) with that device current and keeps it for the
+ *    life of the process: a cudaDeviceReset may move the array, so the
+ *    library must not be used across one;
+ *  - every call synchronises its stream before returning, so none may be
+ *    made while that stream is capturing a CUDA graph;
  *  - every call shares the one array, which keeps the previous call's
  *    contents (each call rewrites all the scratch it reads); calls whose
  *    work overlaps on the GPU race on it, so serialise them (one stream, or
