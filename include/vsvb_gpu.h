@@ -17,7 +17,7 @@
  * orbital integrals, the Schwarz table, every screened orbital-quartet ERI and
  * its contraction with the spin-coupled cofactor densities, and returns the
  * same energy/wfnorm pair.  The Fortran side binds these entry points with
- * ISO_C_BINDING (see INTEGRATION.md); nothing here takes a torch type.
+ * ISO_C_BINDING; nothing here takes a torch type.
  *
  * Conventions: all arrays are plain host pointers unless a name ends in
  * _dev.  Index arrays keep the reference's 1-based Fortran values exactly as
@@ -110,6 +110,12 @@ typedef struct vsvb_options {
                            * whole evaluation from the second call on (default 1) */
   int autotune;           /* pick the ERI grid caps and assembly task splits by timing them on
                            * this device at create (default 0: fixed heuristics) */
+  int block_mode;         /* orbital-pair ERIs per atom quartet (s and p shells only): each
+                           * shell quartet's (ab|cd) block is staged per atom quartet and
+                           * transformed once per atom quartet.  0 (default): on for large
+                           * s/p systems (more than 5e7 candidate shell quartets), 1: on,
+                           * -1: off.  Energies only; a gradient call returns
+                           * VSVB_ERR_UNSUPPORTED on a block-mode handle */
 } vsvb_options;
 
 typedef struct vsvb_energy_result {
@@ -275,7 +281,9 @@ int vsvb_det_factor(const double *a_dev, int n, int nmat, double *det_dev, doubl
  * counterpart in the reference.  Scratch is a fixed 4 MiB device array per
  * device (2*n*n*nmat doubles at most, else VSVB_ERR_TOO_LARGE) held for the
  * life of the process; the first call on a device resolves that array's
- * address and should come before any stream capture; concurrent calls share
+ * address once and keeps it, so the library must not be used across a
+ * cudaDeviceReset.  Every call synchronises its stream before returning, so
+ * no call may be made while that stream is capturing.  Concurrent calls share
  * the array and must not overlap on the GPU.  Arguments and results as
  * vsvb_det_factor. */
 int vsvb_det_factor_noalloc(const double *a_dev, int n, int nmat, double *det_dev, double *inv_dev, int *sing_dev,
@@ -346,6 +354,17 @@ int vsvb_gpu_num_orbitals(const vsvb_gpu *h);
  * index i*(i+1)/2+k) of the last evaluation, np = n(n+1)/2, n = spatial
  * orbitals.  Returns np, or a negative vsvb_status. */
 int vsvb_gpu_debug_orbital_eri(vsvb_gpu *h, double *out, size_t cap);
+/* Sampled entries of the same matrix: out[i] = T[idx[i]] (idx[i] < np*np),
+ * for systems whose T is too large to copy whole.  Returns np, or a
+ * negative vsvb_status. */
+int vsvb_gpu_debug_orbital_eri_at(vsvb_gpu *h, const long long *idx, int n, double *out);
+/* Block mode (vsvb_options.block_mode) figures of one energy evaluation:
+ * algorithmic FLOPs of the ERI launches per kind (FP64, FP32, double-float;
+ * primitive-quartet work as in vsvb_gpu_eri_profile plus the transfer to
+ * (ab|cd)), of the per-atom-quartet transforms (FP64, FP32, double-float),
+ * and counts: atom quartets, chunks, kernel launches of the sweep.  Returns
+ * 1 when the handle runs in block mode, 0 when not. */
+int vsvb_gpu_block_stats(const vsvb_gpu *h, double *eri_flops3, double *transform_flops3, long long *counts3);
 /* Orbital overlap and core-Hamiltonian matrices of the last evaluation
  * (n x n, row-major). */
 int vsvb_gpu_debug_orbital_1e(vsvb_gpu *h, double *s, double *hcore, size_t cap);

@@ -2,7 +2,9 @@
 synthetic workloads (valence_gb300.configs), used as fixtures by the GPU
 parity tests.  Run from the repository root:
 
-    python tests/golden/make_synthetic.py
+    python tests/golden/make_synthetic.py [case ...]
+
+(with case names, only those entries are recomputed).
 """
 import json
 import os
@@ -15,16 +17,20 @@ sys.path.insert(0, ROOT)
 
 from valence_gb300 import configs  # noqa: E402
 
-CASES = {"ch_chain": dict(fn=configs.ch_chain, seed=2), "lif_cluster_small": dict(fn=configs.lif_cluster_small, seed=3)}
+CASES = {"ch_chain": dict(fn=configs.ch_chain, seed=2), "lif_cluster_small": dict(fn=configs.lif_cluster_small, seed=3),
+         "singular_pair_large": dict(fn=configs.singular_pair_large, seed=5)}
 
 
-def main():
+def main(only=None):
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
     exe = os.path.join(ROOT, "oracle", "_build", "vsvb_oracle")
     nthreads = os.cpu_count() or 1
-    out = {}
+    fx = os.path.join(ROOT, "tests", "golden", "synthetic.json")
+    out = json.load(open(fx)) if only and os.path.exists(fx) else {}
     with tempfile.TemporaryDirectory() as d:
         for name, c in CASES.items():
+            if only and name not in only:
+                continue
             path = c["fn"](os.path.join(d, name + ".inp"), seed=c["seed"])
             txt = subprocess.run([exe, path, str(nthreads)], capture_output=True, text=True, check=True).stdout
             e = float([ln for ln in txt.splitlines() if "guess energy" in ln][0].split()[2])
@@ -37,4 +43,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

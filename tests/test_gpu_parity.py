@@ -96,7 +96,7 @@ def test_synthetic_water_matches_oracle(lib_built, oracle, tmp_path):
     _orbital_checks(s, o, 5)
     assert abs(r["e1"] - ro.e1) < 1e-8 * max(1, abs(ro.e1))
     assert abs(r["e2"] - ro.e2) < 1e-8 * max(1, abs(ro.e2))
-    assert abs(r["energy"] - ro.energy) < 1e-8 * max(1, abs(ro.energy))
+    assert abs(r["energy"] - ro.energy) < 1e-8  # Eh, absolute
 
 
 def test_synthetic_chain_matches_fixture(lib_built, tmp_path):
@@ -106,7 +106,7 @@ def test_synthetic_chain_matches_fixture(lib_built, tmp_path):
     p = configs.ch_chain(str(tmp_path / "ch_chain.inp"), seed=fx["seed"])
     s = lib_built.System(p)
     r = s.energy()
-    assert abs(r["energy"] - fx["energy"]) < 1e-8 * max(1.0, abs(fx["energy"]))
+    assert abs(r["energy"] - fx["energy"]) < 1e-8  # Eh, absolute
     assert abs(r["wfnorm"] - fx["wfnorm"]) < 1e-10 * max(1.0, abs(fx["wfnorm"]))
 
 
@@ -114,7 +114,7 @@ def test_synthetic_chain_matches_fixture(lib_built, tmp_path):
 def test_synthetic_cluster_matches_fixture(lib_built, tmp_path, precision):
     """The Li/F cluster workload's geometry and basis family at 2x2x2 (72
     functions, 12 DOCC, wfnorm 0.16) against the oracle fixture: FP64 within
-    1e-8 relative, the mixed paths within 1e-6 Eh and their own estimate."""
+    1e-8 Eh, the mixed paths within 1e-6 Eh and their own estimate."""
     import json
     from valence_gb300 import configs
     fx = json.load(open(os.path.join(GOLD, "synthetic.json")))["lif_cluster_small"]
@@ -123,7 +123,7 @@ def test_synthetic_cluster_matches_fixture(lib_built, tmp_path, precision):
     r = s.energy()
     d = abs(r["energy"] - fx["energy"])
     if precision == "FP64":
-        assert d < 1e-8 * max(1.0, abs(fx["energy"]))
+        assert d < 1e-8  # Eh, absolute
         assert abs(r["wfnorm"] - fx["wfnorm"]) < 1e-10
     else:
         assert d < 1e-6, d

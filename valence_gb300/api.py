@@ -52,7 +52,8 @@ class Desc(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("mixed_threshold", ctypes.c_double), ("ao_screen", ctypes.c_double),
                 ("device", ctypes.c_int), ("grad_mode", ctypes.c_int), ("prim_screen", ctypes.c_double),
-                ("prim_split", ctypes.c_int), ("cuda_graph", ctypes.c_int), ("autotune", ctypes.c_int)]
+                ("prim_split", ctypes.c_int), ("cuda_graph", ctypes.c_int), ("autotune", ctypes.c_int),
+                ("block_mode", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -99,6 +100,8 @@ def lib():
         L.vsvb_gpu_num_orbitals.argtypes = [ctypes.c_void_p]
         L.vsvb_gpu_debug_orbital_eri.argtypes = [ctypes.c_void_p, P(D), ctypes.c_size_t]
         L.vsvb_gpu_debug_orbital_1e.argtypes = [ctypes.c_void_p, P(D), P(D), ctypes.c_size_t]
+        L.vsvb_gpu_debug_orbital_eri_at.argtypes = [ctypes.c_void_p, P(ctypes.c_longlong), I, P(D)]
+        L.vsvb_gpu_block_stats.argtypes = [ctypes.c_void_p, P(D), P(D), P(ctypes.c_longlong)]
         L.vsvb_gpu_batch_energy_grad.argtypes = [P(ctypes.c_void_p), I, P(P(D)), P(Result), P(P(D))]
         L.vsvb_gpu_set_stream.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.vsvb_gpu_set_spin_coeffs.argtypes = [ctypes.c_void_p, P(D)]
@@ -181,7 +184,7 @@ def read_input(path):
 
 
 def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, grad_mode=0, prim_screen=None,
-                 prim_split=None, cuda_graph=None, autotune=None):
+                 prim_split=None, cuda_graph=None, autotune=None, block_mode=None):
     o = Options()
     lib().vsvb_default_options(ctypes.byref(o))
     o.precision = precision
@@ -197,6 +200,8 @@ def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0
         o.cuda_graph = int(cuda_graph)
     if autotune is not None:
         o.autotune = int(autotune)
+    if block_mode is not None:
+        o.block_mode = int(block_mode)
     return o
 
 
@@ -204,7 +209,7 @@ class System:
     """One molecule on the GPU: a parsed input plus a device handle."""
 
     def __init__(self, path, precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, coords_angstrom=None,
-                 grad_mode=0, prim_screen=None, prim_split=None, cuda_graph=None, autotune=None):
+                 grad_mode=0, prim_screen=None, prim_split=None, cuda_graph=None, autotune=None, block_mode=None):
         self.path = path
         self._desc = read_input(path)
         d = self._desc.contents
@@ -215,7 +220,7 @@ class System:
         if coords_angstrom is not None:
             self._coords_bohr[:] = np.asarray(coords_angstrom, dtype=np.float64).ravel() * 1.889725987722
         self.opt = make_options(precision, mixed_threshold, ao_screen, device, grad_mode, prim_screen, prim_split,
-                                cuda_graph, autotune)
+                                cuda_graph, autotune, block_mode)
         self._h = ctypes.c_void_p()
         rc = lib().vsvb_gpu_create(self._desc, ctypes.byref(self.opt), ctypes.byref(self._h))
         if rc:
@@ -329,6 +334,31 @@ class System:
         if rc < 0:
             raise VSVBError("debug_orbital_eri failed")
         return out.reshape(np_, np_)
+
+    def orbital_eri_at(self, p, q):
+        """Entries T[p[i], q[i]] of the orbital-pair ERI matrix of the last
+        evaluation (orbital-pair indices i*(i+1)/2+k, i >= k)."""
+        n = lib().vsvb_gpu_num_orbitals(self._h)
+        np_ = n * (n + 1) // 2
+        idx = np.ascontiguousarray(np.asarray(p, dtype=np.int64) * np_ + np.asarray(q, dtype=np.int64))
+        out = np.zeros(idx.size)
+        rc = lib().vsvb_gpu_debug_orbital_eri_at(self._h, idx.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                                 int(idx.size), _dptr(out))
+        if rc < 0 or rc > 0 and rc != np_:
+            raise VSVBError(f"debug_orbital_eri_at failed ({rc}): {lib().vsvb_gpu_last_error(self._h).decode()}")
+        return out
+
+    def block_stats(self):
+        """Block-mode figures: whether the handle runs in block mode, the
+        algorithmic FLOPs of one sweep per ERI kind and of the transforms, and
+        the atom quartets, chunks and launches of the sweep."""
+        ef = (ctypes.c_double * 3)()
+        tf = (ctypes.c_double * 3)()
+        cn = (ctypes.c_longlong * 3)()
+        on = lib().vsvb_gpu_block_stats(self._h, ef, tf, cn)
+        return {"on": bool(on), "eri_flops": {"fp64": ef[0], "fp32": ef[1], "df64": ef[2]},
+                "transform_flops": {"fp64": tf[0], "fp32": tf[1], "df64": tf[2]},
+                "atom_quartets": cn[0], "chunks": cn[1], "launches": cn[2]}
 
     def orbital_1e(self):
         n = lib().vsvb_gpu_num_orbitals(self._h)

@@ -172,5 +172,26 @@ def lif_cluster_small(path, seed=3):
     return lif_cluster(path, seed=seed, n=2, ndocc=12)
 
 
+def singular_pair_large(path, seed=5, natom=32, ndocc=32):
+    """A spin-coupled pair whose first orbital sits on an atom 25 A away from
+    a chain of natom Z=1 atoms (s, s, p shells, 5 functions each) that
+    carries the second orbital and ndocc doubly occupied orbitals on 1-2
+    atoms: every transition determinant pair that moves the far orbital into
+    the other spin block has an exactly singular overlap block (a row of
+    zeros up to exp(-300)), here with ndocc + 1 = 33 electrons of one spin."""
+    rng = np.random.default_rng(seed)
+    hsh = _shells(rng, [0, 0, 1], 0.3, 30.0, (3, 3))
+    atoms = [(1, 0.0, 0.0, 1.4 * i) for i in range(natom)] + [(1, 25.0, 0.0, 0.0)]
+    nf = _nfun(hsh)
+    far = natom + 1
+    orbs = [([far], rng.uniform(-1, 1, nf)), ([1, 2], rng.uniform(-1, 1, 2 * nf))]
+    for k in range(ndocc):
+        a = k % natom
+        atl = [a + 1] if k < natom else [a + 1, (a + 1) % natom + 1]
+        orbs.append((atl, rng.uniform(-1, 1, nf * len(atl))))
+    write_input(path, atoms, [(1.0, hsh)], orbs, npair=1, pairs=[(1, 2)])
+    return path
+
+
 WORKLOADS = {"water_vshf": water_vshf, "ch_chain": ch_chain, "lif_cluster": lif_cluster,
-             "lif_cluster_small": lif_cluster_small}
+             "lif_cluster_small": lif_cluster_small, "singular_pair_large": singular_pair_large}

@@ -15,8 +15,17 @@
  *                                                      - T[c1][r2] T[c2][r1])
  * with T = A^-1.  Blocks whose pivots fall below 1e-7 of their largest entry
  * (exact rank deficiency from molecular symmetry, e.g. pi pairs) take the
- * exact path: the struck matrix is built and its determinant taken by LU,
- * which is what the reference's givdr computes.  For the adjoint such a
+ * exact path, which gives what the reference's givdr computes for any rank
+ * of A: with P a fixed rank-2 matrix, every struck determinant of A + t P
+ * (at most two strikes) is a polynomial of degree <= 2 in t -- the strikes
+ * replace rows, so the struck matrix is A_struck + t P' with P' of rank <= 2
+ * -- whose value at t = 0 is the struck determinant of A:
+ *   f(0) = 3 f(1) - 3 f(2) + f(3),  f(k) = det(A + kP) J_k,
+ * J_k from the inverse of A + kP by Jacobi's identity as above.  A + kP is
+ * well conditioned for rank deficiency up to 2; at 3 or more it stays
+ * singular and every struck determinant with at most two strikes is exactly
+ * zero.  Three extra factorisations per flagged block make each struck
+ * determinant O(1) at any block size.  For the adjoint such a
  * block also keeps det and inverse of A + delta I (delta = 1e-8 of its
  * largest entry): every struck determinant is a polynomial in A, so the
  * derivative taken through the shifted pair is within about 5 delta
@@ -115,56 +124,25 @@ __device__ __forceinline__ void load_dets(const DetCtx &d, long long q, QInfo &q
   qi.wddr = qi.sing ? qi.w * d.detr_a[q] * d.detr_b[q] : qi.wdd;
 }
 
-/* exact determinant of spin block sp of pair q with up to two strikes, by LU
- * with partial pivoting on the struck matrix (n <= VSVB_MAXN) */
-__device__ __noinline__ double struck_det_exact(const DetCtx &d, const QInfo &qi, int sp, int ns, const int *rr, const int *cc) {
-  const int n = sp == 0 ? d.ds.nalpha : d.ds.nbeta;
-  if (n > VSVB_MAXN) {
-    /* larger than the local matrix: reported, not computed */
-    if (d.status) atomicOr(d.status, 4);
-    return 0.0;
+/* exact determinant of spin block sp of pair q with up to two strikes, from
+ * the three perturbed factorisations of its slot (detpair_kernel) */
+__device__ __forceinline__ double struck_det_exact(const DetCtx &d, long long q, int sp, int ns, const int *rr,
+                                                   const int *cc) {
+  const int slot = d.xslot[q];
+  if (slot < 0 || slot >= d.xcap) return 0.0;
+  const int na = d.ds.nalpha, nb = d.ds.nbeta, n = sp == 0 ? na : nb;
+  const double *X = d.xinv + (size_t)slot * 3 * (na * na + nb * nb) + (sp == 0 ? 0 : 3 * (size_t)na * na);
+  const double *dk = d.xdet + (size_t)slot * 6 + sp * 3;
+  double f[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double *T = X + (size_t)k * n * n;
+    double J = 1.0;
+    if (ns == 1) J = T[cc[0] * n + rr[0]];
+    else if (ns == 2) J = T[cc[0] * n + rr[0]] * T[cc[1] * n + rr[1]] - T[cc[0] * n + rr[1]] * T[cc[1] * n + rr[0]];
+    f[k] = dk[k] * J;
   }
-  double M[VSVB_MAXN * VSVB_MAXN];
-  for (int r = 0; r < n; ++r) {
-    int sb = spat(d, pos_slot(d, qi.isc, qi.bb, sp, r));
-    for (int c = 0; c < n; ++c) {
-      int sk = spat(d, pos_slot(d, qi.jsc, qi.kb, sp, c));
-      M[r * n + c] = d.So[sb * d.ds.nsp + sk];
-    }
-  }
-  for (int t = 0; t < ns; ++t) {
-    for (int i = 0; i < n; ++i) {
-      M[rr[t] * n + i] = 0.0;
-      M[i * n + cc[t]] = 0.0;
-    }
-    M[rr[t] * n + cc[t]] = 1.0;
-  }
-  double det = 1.0;
-  for (int k = 0; k < n; ++k) {
-    int p = k;
-    double mx = fabs(M[k * n + k]);
-    for (int i = k + 1; i < n; ++i)
-      if (fabs(M[i * n + k]) > mx) {
-        mx = fabs(M[i * n + k]);
-        p = i;
-      }
-    if (mx == 0.0) return 0.0;
-    if (p != k) {
-      for (int j = 0; j < n; ++j) {
-        double t = M[k * n + j];
-        M[k * n + j] = M[p * n + j];
-        M[p * n + j] = t;
-      }
-      det = -det;
-    }
-    double piv = M[k * n + k];
-    det *= piv;
-    for (int i = k + 1; i < n; ++i) {
-      double f = M[i * n + k] / piv;
-      for (int j = k + 1; j < n; ++j) M[i * n + j] -= f * M[k * n + j];
-    }
-  }
-  return det;
+  return 3.0 * f[0] - 3.0 * f[1] + f[2];
 }
 
 struct Cof {
@@ -220,8 +198,8 @@ __device__ Cof cofactor_loc(const DetCtx &d, long long q, const QInfo &qi, int n
     return c;
   }
   /* a flagged block: the value from exact struck determinants */
-  const double fa = (sing & 1) && c.na_s > 0 ? struck_det_exact(d, qi, 0, c.na_s, c.ra, c.ca) : qi.da * c.Ja;
-  const double fb = (sing & 2) && c.nb_s > 0 ? struck_det_exact(d, qi, 1, c.nb_s, c.rb, c.cb) : qi.db * c.Jb;
+  const double fa = (sing & 1) && c.na_s > 0 ? struck_det_exact(d, q, 0, c.na_s, c.ra, c.ca) : qi.da * c.Ja;
+  const double fb = (sing & 2) && c.nb_s > 0 ? struck_det_exact(d, q, 1, c.nb_s, c.rb, c.cb) : qi.db * c.Jb;
   c.v = qi.w * fa * fb;
   c.vr = qi.wddr * (c.Ja * c.Jb);
   return c;
@@ -313,14 +291,26 @@ __device__ __forceinline__ void dtriang(long long ij, int &i, int &j) {
 }  // namespace
 
 /* ---- determinant pairs: one block per q, Gauss-Jordan per spin block ---- */
+namespace {
+/* the fixed rank-2 matrix of the exact-minor path: P[r][c] = s (w1_r z1_c +
+ * w2_r z2_c), entries of w and z from sin / cos of irrational steps */
+__device__ __forceinline__ double pert_entry(int r, int c, double s) {
+  const double w1 = sin(1.0 + 0.7548776662466927 * r), w2 = sin(2.0 + 0.5698402909980532 * r);
+  const double z1 = cos(0.5 + 0.6180339887498949 * c), z2 = cos(1.5 + 0.4142135623730950 * c);
+  return s * (w1 * z1 + w2 * z2);
+}
+}  // namespace
+
 __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
   __shared__ double red[8];
   __shared__ int redi[8];
   __shared__ double sdet;
-  __shared__ int ssing, spiv;
+  __shared__ int ssing, spiv, sslot;
   const long long q = blockIdx.x;
   const QInfo qi = decode_q(d, q);
   double *W = scratch + (size_t)blockIdx.x * ld_scratch;
+  if (threadIdx.x == 0) sslot = -1;
+  __syncthreads();
   for (int sp = 0; sp < 2; ++sp) {
     const int n = sp == 0 ? d.ds.nalpha : d.ds.nbeta;
     double *Tout = (sp == 0 ? d.Ta : d.Tb) + (size_t)q * n * n;
@@ -329,16 +319,8 @@ __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
       continue;
     }
     const int n2 = 2 * n;
-    double amax = 0.0;
-    /* pass 0 factorises A; a block whose pivots fall below 1e-7 of its
-     * largest entry takes its exact determinant by LU instead and then
-     * pass 1 factorises A + delta I (delta = 1e-8 of that entry): the
-     * adjoint walks take the determinant and inverse of the shifted matrix
-     * together, which gives the derivative of every struck determinant of
-     * A to about 5 delta relative, whatever the block's rank deficiency */
-    for (int pass = 0; pass < 2; ++pass) {
-      const double shift = pass == 0 ? 0.0 : 1e-8 * amax;
-      /* W = [A + shift I | I] */
+    /* W = [A + shift I + kp P | I]; returns max |A| over the block */
+    auto fill = [&](double shift, double kp) -> double {
       double mx = 0.0;
       for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
         int r = t / n2, c = t - r * n2;
@@ -349,6 +331,7 @@ __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
           v = d.So[sb * d.ds.nsp + sk];
           mx = fmax(mx, fabs(v));
           if (c == r) v += shift;
+          if (kp != 0.0) v += pert_entry(r, c, kp);
         } else {
           v = (c - n == r) ? 1.0 : 0.0;
         }
@@ -361,16 +344,21 @@ __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
         double m = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
         red[0] = m;
+      }
+      __syncthreads();
+      const double amax = red[0];
+      __syncthreads();
+      return amax;
+    };
+    /* Gauss-Jordan with partial pivoting on W; false (and no inverse) when
+     * a pivot is not above pmin; sdet holds the determinant */
+    auto gj = [&](double pmin) -> bool {
+      if (threadIdx.x == 0) {
         sdet = 1.0;
         ssing = 0;
       }
       __syncthreads();
-      if (pass == 0) amax = red[0];
-      /* pass 0 flags small pivots; pass 1 fails only on a zero pivot */
-      const double pmin = pass == 0 ? 1e-7 * amax : 0.0;
-      __syncthreads();
       for (int k = 0; k < n; ++k) {
-        /* pivot search */
         double best = -1.0;
         int bi = k;
         for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
@@ -429,72 +417,84 @@ __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
           if (i != k) W[i * n2 + k] = 0.0;
         __syncthreads();
       }
-      if (!ssing) {
-        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
-          int r = t / n, c = t - r * n;
-          Tout[t] = W[r * n2 + n + c];
-        }
-        if (threadIdx.x == 0) {
-          if (pass == 0) (sp == 0 ? d.det_a : d.det_b)[q] = sdet;
-          (sp == 0 ? d.detr_a : d.detr_b)[q] = sdet;
-        }
-        __syncthreads();
-        break;
-      }
-      if (pass == 1) {
-        /* A + delta I is singular too: no inverse for the adjoint */
-        for (int t = threadIdx.x; t < n * n; t += blockDim.x) Tout[t] = 0.0;
-        if (threadIdx.x == 0) {
-          (sp == 0 ? d.detr_a : d.detr_b)[q] = 0.0;
-          if (d.status) atomicOr(d.status, 2);
-        }
-        __syncthreads();
-        break;
-      }
-      /* exact-minor path: the unstruck determinant by LU on a fresh copy */
-      if (threadIdx.x == 0) {
-        double det = 1.0;
-        double *M = W;
-        for (int r = 0; r < n; ++r)
-          for (int c = 0; c < n; ++c) {
-            int sb = spat(d, pos_slot(d, qi.isc, qi.bb, sp, r));
-            int sk = spat(d, pos_slot(d, qi.jsc, qi.kb, sp, c));
-            M[r * n + c] = d.So[sb * d.ds.nsp + sk];
-          }
-        for (int k = 0; k < n && det != 0.0; ++k) {
-          int p = k;
-          double m = fabs(M[k * n + k]);
-          for (int i = k + 1; i < n; ++i)
-            if (fabs(M[i * n + k]) > m) {
-              m = fabs(M[i * n + k]);
-              p = i;
-            }
-          if (m == 0.0) {
-            det = 0.0;
-            break;
-          }
-          if (p != k) {
-            for (int j = 0; j < n; ++j) {
-              double t = M[k * n + j];
-              M[k * n + j] = M[p * n + j];
-              M[p * n + j] = t;
-            }
-            det = -det;
-          }
-          det *= M[k * n + k];
-          for (int i = k + 1; i < n; ++i) {
-            double f = M[i * n + k] / M[k * n + k];
-            for (int j = k + 1; j < n; ++j) M[i * n + j] -= f * M[k * n + j];
-          }
-        }
-        (sp == 0 ? d.det_a : d.det_b)[q] = det;
-        atomicOr(&d.sing[q], 1 << sp);
-      }
+      const bool ok = !ssing;
       __syncthreads();
+      return ok;
+    };
+    auto store_inverse = [&](double *dst) {
+      for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        int r = t / n, c = t - r * n;
+        dst[t] = W[r * n2 + n + c];
+      }
+    };
+    const double amax = fill(0.0, 0.0);
+    if (gj(1e-7 * amax)) {
+      store_inverse(Tout);
+      if (threadIdx.x == 0) (sp == 0 ? d.det_a : d.det_b)[q] = (sp == 0 ? d.detr_a : d.detr_b)[q] = sdet;
+      __syncthreads();
+      continue;
+    }
+    /* a flagged block: pivots below 1e-7 of its largest entry */
+    if (threadIdx.x == 0) {
+      atomicOr(&d.sing[q], 1 << sp);
+      if (sslot < 0) {
+        const int sl = atomicAdd(d.xcount, 1);
+        sslot = sl < d.xcap ? sl : d.xcap;
+      }
+    }
+    __syncthreads();
+    const int slot = sslot;
+    double det0 = 0.0;
+    if (slot < d.xcap) {
+      const int na = d.ds.nalpha, nb = d.ds.nbeta;
+      double *X = d.xinv + (size_t)slot * 3 * (na * na + nb * nb) + (sp == 0 ? 0 : 3 * (size_t)na * na);
+      const double ps = 0.1 * amax * rsqrt((double)n);
+      double f[3];
+      for (int k = 0; k < 3; ++k) {
+        fill(0.0, (k + 1) * ps);
+        double *Xk = X + (size_t)k * n * n;
+        if (gj(1e-11 * amax)) {
+          store_inverse(Xk);
+          f[k] = sdet;
+        } else {
+          /* rank deficiency of 3 or more: every struck determinant with at
+           * most two strikes is zero */
+          for (int t = threadIdx.x; t < n * n; t += blockDim.x) Xk[t] = 0.0;
+          f[k] = 0.0;
+        }
+        if (threadIdx.x == 0) d.xdet[(size_t)slot * 6 + sp * 3 + k] = f[k];
+        __syncthreads();
+      }
+      det0 = 3.0 * f[0] - 3.0 * f[1] + f[2];
+    } else if (threadIdx.x == 0 && d.status) {
+      atomicOr(d.status, 4);
+    }
+    if (threadIdx.x == 0) (sp == 0 ? d.det_a : d.det_b)[q] = det0;
+    /* the adjoint's pair: det and inverse of A + delta I (delta = 1e-8 of
+     * the largest entry) -- the derivative of every struck determinant of A
+     * to about 5 delta relative, whatever the rank deficiency.  Only an
+     * exactly zero pivot is reported (status 2): on transition blocks whose
+     * left and right null vectors are nearly orthogonal the shifted pivots
+     * fall to about 1e-8 of delta, and the derivative taken through det and
+     * inverse together still matches central differences there */
+    const double shift = 1e-8 * amax;
+    fill(shift, 0.0);
+    if (gj(0.0)) {
+      store_inverse(Tout);
+      if (threadIdx.x == 0) (sp == 0 ? d.detr_a : d.detr_b)[q] = sdet;
+    } else {
+      for (int t = threadIdx.x; t < n * n; t += blockDim.x) Tout[t] = 0.0;
+      if (threadIdx.x == 0) {
+        (sp == 0 ? d.detr_a : d.detr_b)[q] = 0.0;
+        if (d.status) atomicOr(d.status, 2);
+      }
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0 && d.nsing && d.sing[q]) atomicAdd(d.nsing, 1);
+  if (threadIdx.x == 0) {
+    d.xslot[q] = sslot < d.xcap ? sslot : -1;
+    if (d.nsing && d.sing[q]) atomicAdd(d.nsing, 1);
+  }
 }
 
 /* ---- energy (and adjoint) assembly: grid (nq, nsplit) ---- */

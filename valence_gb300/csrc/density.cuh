@@ -18,7 +18,15 @@ struct DetCtx {
   int *sing;              /* [nq] bit0 alpha, bit1 beta on the exact-minor path */
   int *nsing;             /* count of determinant pairs with a bit set (optional) */
   int *status;            /* value 2: a flagged block whose shift is singular too;
-                           * value 4: a flagged block above VSVB_MAXN electrons of one spin */
+                           * value 4: more flagged determinant pairs than the pool holds */
+  /* exact-minor pool: per flagged determinant pair one slot holding, per
+   * spin block, inverse and determinant of A + k P (k = 1, 2, 3; P a fixed
+   * rank-2 matrix), from which every struck determinant of A follows */
+  double *xinv;           /* [xcap][3 (na*na + nb*nb)] */
+  double *xdet;           /* [xcap][2][3] */
+  int *xslot;             /* [nq] slot of pair q, -1 when none */
+  int *xcount;            /* slots taken (reset per evaluation) */
+  int xcap;
 };
 
 struct AsmArgs {

@@ -102,6 +102,16 @@ double eri_flops(int mode, int cp, int cq, double nprimq, int nopP, int nopQ) {
   return nprimq * prim + tr;
 }
 
+double eri_block_hrr_flops(int cp, int cq) {
+  /* (ab| = sum_e M(ab, e) (e0|: one term per function pair of an s or p
+   * pair without a p on B, two with one (the transfer adds A-B times the
+   * lower function); per block element the product of the two counts, 2
+   * flops each */
+  static const int nab_[3] = {1, 3, 9}, nt_[3] = {1, 1, 2};
+  if (cp > 2 || cq > 2) return 0.0;
+  return 2.0 * nab_[cp] * nab_[cq] * nt_[cp] * nt_[cq];
+}
+
 int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int4 *work, int nwork, int max_blocks,
                cudaStream_t st) {
   /* the Schwarz pass and the separate adjoint sweep (grad_mode 1) always run

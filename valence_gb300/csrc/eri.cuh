@@ -34,6 +34,13 @@ struct EriArgs {
   float prim_lo, prim_hi;  /* evaluate the primitive quartets with prim_lo <= q0_p q0_q < prim_hi */
   const double *Tbar;      /* mode 2: dE/dT */
   double *xbar;            /* mode 2: dE/dX' */
+  /* mode 4 (block mode): per shell pair its place in its atom pair's block
+   * (off of shell A's functions in its atom, off of shell B's, flags: 1 shell
+   * A on the pair's second atom, 2 both shells on one atom, 4 one shell;
+   * functions of the pair's second atom), and the staging buffer of the
+   * current chunk of atom quartets */
+  const int4 *pair_blk;
+  double *G;
 };
 
 /* arithmetic kinds of the ERI kernels */
@@ -43,7 +50,12 @@ enum { ERI_F64 = 0, ERI_F32 = 1, ERI_DF64 = 2 };
  * 2 adjoint, 3 forward + adjoint.  Work items (P, Q, r0, r1): shell pairs P
  * (class cp) and Q, and the rows r0 <= ip < r1 of P's primitive pairs to
  * evaluate (a large quartet is split into row ranges).  max_blocks caps the
- * grid (the blocks then stride over the work list). */
+ * grid (the blocks then stride over the work list).
+ * Mode 4 (block mode, classes 0..2): the transferred block (ab|cd) is added
+ * into the staging buffer of its atom quartet; items (P, Q, g, w) with g the
+ * block's offset in G, w = columns of the block | 1<<20 when P belongs to the
+ * quartet's ket atom pair | 1<<21 when both atom pairs are the same (the
+ * transposed block is added too). */
 int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int4 *work, int nwork, int max_blocks,
                cudaStream_t st);
 int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st);
@@ -52,6 +64,9 @@ int eri_dispatch_df64(int mode, int cp, int cq, const EriArgs &a, const int4 *w,
                       cudaStream_t st);
 double eri_flops(int mode, int cp, int cq, double nprimq, int nopP, int nopQ);
 int eri_symmetrize(double *T, int np, double *sq, cudaStream_t st);
+/* block mode: algorithmic FLOPs of the transfer (ab|cd) = M_P (e0|f0) M_Q^T
+ * of one shell quartet (its non-zero terms) */
+double eri_block_hrr_flops(int cp, int cq);
 /* out[i] = (float)in[i] */
 int eri_to_float(const double *in, float *out, size_t n, cudaStream_t st);
 #endif

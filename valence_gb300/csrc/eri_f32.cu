@@ -7,5 +7,6 @@
 int eri_dispatch_f32(int mode, int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st) {
   if (mode == 0) return dispatch<float, 0>(cp, cq, a, w, n, max_blocks, st);
   if (mode == 3) return dispatch<float, 3>(cp, cq, a, w, n, max_blocks, st);
+  if (mode == 4) return dispatch_blk<float>(cp, cq, a, w, n, max_blocks, st);
   return 3;
 }

@@ -9,5 +9,6 @@ int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int4 *w, 
   if (mode == 1) return dispatch<double, 1>(cp, cq, a, w, n, max_blocks, st);
   if (mode == 2) return dispatch<double, 2>(cp, cq, a, w, n, max_blocks, st);
   if (mode == 3) return dispatch<double, 3>(cp, cq, a, w, n, max_blocks, st);
+  if (mode == 4) return dispatch_blk<double>(cp, cq, a, w, n, max_blocks, st);
   return 3;
 }

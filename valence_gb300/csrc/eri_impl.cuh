@@ -461,6 +461,21 @@ __device__ __forceinline__ void ldv(const df64 *p, df64 (&o)[V]) {
 
 constexpr int WARPS = 4;
 
+/* block mode: the places of pair function (a of shell A, b of shell B) in
+ * its atom pair's rows, row = f1 * nf2 + f2 with f1 a function of the pair's
+ * first atom and f2 of its second (bp: off A, off B, flags, nf2) */
+__device__ __forceinline__ int blk_places(int4 bp, int a, int b, int *pos) {
+  const int fa = bp.x + a, fb = bp.y + b;
+  if (bp.z & 2) {
+    pos[0] = fa * bp.w + fb;
+    if (bp.z & 4) return 1;
+    pos[1] = fb * bp.w + fa;
+    return 2;
+  }
+  pos[0] = (bp.z & 1) ? fb * bp.w + fa : fa * bp.w + fb;
+  return 1;
+}
+
 /* RB: bytes of one element of the arithmetic type (2D tables, roots) */
 template <int LA, int LB, int LC, int LD, int RB = 8>
 struct QuartetShape {
@@ -568,9 +583,11 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         }
       }
     }
-    /* this item's rows of P's primitive pairs */
-    const int r1 = min(pq.w, nrow), pq_begin = pq.z * Q.nprim;
-    const int npq = r1 > pq.z ? (r1 - pq.z) * Q.nprim : 0;
+    /* this item's rows of P's primitive pairs (block-mode items carry their
+     * staging place instead: every row) */
+    const int row0 = MODE == 4 ? 0 : pq.z, rowe = MODE == 4 ? nrow : pq.w;
+    const int r1 = min(rowe, nrow), pq_begin = row0 * Q.nprim;
+    const int npq = r1 > row0 ? (r1 - row0) * Q.nprim : 0;
     /* lane roles in the 2D phase: slot g, root r, direction dir */
     const int g = lane / (3 * S::NR), rem = lane - g * (3 * S::NR);
     const int r = rem / 3, dir = rem - 3 * (rem / 3);
@@ -861,6 +878,59 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
       continue;
     }
 
+    if constexpr (MODE == 4) {
+      /* block mode: (ab|cd) = M_P E M_Q^T (the sparse transfer rows) added
+       * into the atom quartet's staging block at every place the pair
+       * functions take there: both orders of two shells on one atom, and the
+       * transposed block when bra and ket are the same atom pair */
+      constexpr int NCB = NC<LB>::v, NDD = NC<LD>::v, NCDF = NC<LC>::v * NC<LD>::v;
+      const int4 bp = __ldg(args.pair_blk + pq.x), bq = __ldg(args.pair_blk + pq.y);
+      const int ncol = pq.w & 0xFFFFF;
+      const bool swp = (pq.w >> 20) & 1, dg = ((pq.w >> 21) & 1) && pq.x != pq.y;
+      double *Gq = args.G + (unsigned)pq.z;
+      const double *MP = args.hrr + P.m0, *MQ = args.hrr + Q.m0;
+      /* the ket transfer first, Y[e][cd] = sum_f E[e][f] M_Q[cd][f], in the
+       * idle table area (warp 1's in CTA mode, past E in warp mode) */
+      constexpr int EW = (S::NCOMP * (int)sizeof(TT) + 7) / 8; /* E's doubles in warp mode */
+      static_assert(CTA ? S::NEA * NCDF <= S::PER_WARP : EW + S::NEA * NCDF <= S::PER_WARP,
+                    "block-mode transfer area too small");
+      double *Yt = CTA ? wbase + S::PER_WARP : ws + EW;
+      for (int o = tid; o < S::NEA * NCDF; o += nthr) {
+        const int e = o / NCDF, cd = o - e * NCDF;
+        double t = 0.0;
+        for (int f = 0; f < S::NEC; ++f) {
+          const double mq = __ldg(MQ + cd * S::NEC + f);
+          if (mq != 0.0) t = fma((double)E[e * S::NEC + f], mq, t);
+        }
+        Yt[o] = t;
+      }
+      if (CTA) __syncthreads();
+      else __syncwarp();
+      for (int o = tid; o < S::NAB * NCDF; o += nthr) {
+        const int ab = o / NCDF, cd = o - ab * NCDF;
+        double v = 0.0;
+        for (int e = 0; e < S::NEA; ++e) {
+          const double mp = __ldg(MP + ab * S::NEA + e);
+          if (mp != 0.0) v = fma(mp, Yt[e * NCDF + cd], v);
+        }
+        int rows[2], cols[2];
+        const int nr = blk_places(bp, ab / NCB, ab - (ab / NCB) * NCB, rows);
+        const int nc = blk_places(bq, cd / NDD, cd - (cd / NDD) * NDD, cols);
+        /* (P|Q) at [P's place][Q's place] when P is on the bra atom pair of
+         * the quartet, else transposed; and the other orientation too when
+         * bra and ket are the same atom pair */
+        for (int i = 0; i < nr; ++i)
+          for (int j = 0; j < nc; ++j) {
+            const size_t pq_at = (size_t)rows[i] * ncol + cols[j], qp_at = (size_t)cols[j] * ncol + rows[i];
+            atomicAdd(Gq + (swp ? qp_at : pq_at), v);
+            if (dg) atomicAdd(Gq + (swp ? pq_at : qp_at), v);
+          }
+      }
+      if (CTA) __syncthreads();
+      else __syncwarp();
+      continue;
+    }
+
     TT *Y = E + S::NCOMP;
     const TT *xtT;
     const TT *TbarT;
@@ -1003,6 +1073,16 @@ template <> struct ClsL<5> { static constexpr int a = 2, b = 2; };
 template <int CP, int CQ, typename R, int MODE>
 int launch_cls(const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st) {
   return launch_one<ClsL<CP>::a, ClsL<CP>::b, ClsL<CQ>::a, ClsL<CQ>::b, R, MODE>(a, w, n, max_blocks, st);
+}
+
+/* block mode: s and p pair classes only */
+template <typename R>
+int dispatch_blk(int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st) {
+#define CASE(X, Y) \
+  if (cp == X && cq == Y) return launch_cls<X, Y, R, 4>(a, w, n, max_blocks, st);
+  CASE(0, 0) CASE(1, 0) CASE(1, 1) CASE(2, 0) CASE(2, 1) CASE(2, 2)
+#undef CASE
+  return 2;
 }
 
 template <typename R, int MODE>

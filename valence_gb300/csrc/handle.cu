@@ -28,9 +28,11 @@
 #include <map>
 #include <set>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/vsvb_gpu.h"
+#include "block.cuh"
 #include "density.cuh"
 #include "eri.cuh"
 #include "handle_internal.h"
@@ -204,7 +206,9 @@ struct vsvb_gpu {
   int nxterm = 0;
   DBuf<int> obs_n, obs_ao, term0, term_slot, term_j, term_m, term_f, ndf_orb;
   DBuf<double> coeff_d, ndf_scale, orb_scale, Craw, C, So, Ho, xtab, T, sqT, qmax, q0max;
-  DBuf<int> pair_slot, slot_pair, slot_which, sing, status, nsing;
+  DBuf<int> pair_slot, slot_pair, slot_which, sing, status, nsing, xslot, xcount;
+  DBuf<double> xinv, xdet; /* exact-minor pool of flagged determinant pairs */
+  int xcap = 0;
   DBuf<double> coeff_sc, det_a, det_b, detr_a, detr_b, Ta, Tb, scratch;
   int ld_scratch = 0;
   DBuf<double> part_e1, part_wf, part_e2, result;
@@ -221,6 +225,31 @@ struct vsvb_gpu {
   int hs_split = 0, hs_sub = -1;
   DBuf<int> hs_flag;
   std::vector<double> csc_h; /* the spin-coupling weights in use */
+  /* block mode (block.cu): atom quartets in chunks whose staging blocks fit
+   * one of two alternating buffers of blk_gsize doubles */
+  bool blk_on = false;
+  struct BlkLaunch {
+    long long off; /* into blk_work */
+    int n, kind, cp, cq;
+    float lo, hi;
+  };
+  struct BlkChunk {
+    int aq0, naq, tt; /* atom quartets, transform arithmetic (0 FP64, 1 FP32) */
+    int l0, nl;       /* its ERI launches in blk_launch */
+  };
+  std::vector<BlkLaunch> blk_launch;
+  std::vector<BlkChunk> blk_chunk;
+  size_t blk_gsize = 0;
+  int blk_nfmax = 1, blk_nomax = 1, blk_ncoef = 0;
+  size_t blk_smem[3] = {0, 0, 0};
+  double blk_eri_flops[3] = {0, 0, 0};  /* per ERI kind, one sweep */
+  double blk_tr_flops[3] = {0, 0, 0};   /* transform, FP64 / FP32 / double-float */
+  long long blk_naq = 0;
+  DBuf<int4> blk_pair, blk_aq, blk_ap, blk_work, blk_csrc;
+  DBuf<int2> blk_atom_orb;
+  DBuf<int> blk_atom_nf, blk_atom_c0, blk_orb, blk_cao;
+  DBuf<double> blk_catom, blk_G;
+  cudaEvent_t blk_done[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -333,6 +362,11 @@ DetCtx det_ctx(vsvb_gpu *h) {
   d.Tb = h->Tb.p;
   d.sing = h->sing.p;
   d.nsing = h->nsing.p;
+  d.xinv = h->xinv.p;
+  d.xdet = h->xdet.p;
+  d.xslot = h->xslot.p;
+  d.xcount = h->xcount.p;
+  d.xcap = h->xcap;
   d.status = h->status.p;
   return d;
 }
@@ -401,6 +435,279 @@ int upload_prims(vsvb_gpu *h, const std::vector<PrimPair> &prims) {
   CK(h->prim64.upload(p64), "upload prim64");
   CK(h->prim32.upload(p32), "upload prim32");
   CK(h->primdf.upload(pdf), "upload primdf");
+  return VSVB_OK;
+}
+
+/* Block-mode set-up (block.cu): atom pairs and their shell pairs, the
+ * per-atom orbital weight tables, the atom quartets above the AO screen
+ * sorted by bound (largest first) and cut into chunks whose staging blocks
+ * fit one buffer, and per chunk the shell-quartet lists of every (bra class,
+ * ket class, precision), built by worker threads straight into device
+ * memory. */
+int build_block(vsvb_gpu *h, const vsvb_system_desc *d, const std::vector<GShell> &sh, const std::vector<int> &first_sh,
+                const std::vector<std::vector<int>> &orbs_on_atom, const std::vector<std::vector<int>> &slot_of_shell,
+                const std::vector<ShellPair> &pairs, const std::vector<float> &q0f, const std::vector<double> &q0,
+                const std::vector<double> &amp) {
+  const int nat = d->natom;
+  std::vector<int> atom_nf(nat), atom_c0(nat), borb, cao;
+  std::vector<int2> atom_orb(nat);
+  std::vector<int4> csrc;
+  int nfmax = 1, nomax = 1;
+  for (int a = 0; a < nat; ++a) {
+    int nf = 0;
+    for (int g = first_sh[a]; g < first_sh[a + 1]; ++g) nf += ncart(sh[g].l);
+    atom_nf[a] = nf;
+    nfmax = std::max(nfmax, nf);
+    atom_orb[a] = make_int2((int)borb.size(), 0);
+    atom_c0[a] = (int)csrc.size();
+    for (int o : orbs_on_atom[a]) {
+      borb.push_back(o);
+      atom_orb[a].y++;
+      for (int g = first_sh[a]; g < first_sh[a + 1]; ++g) {
+        const int slot = slot_of_shell[o][g], nc = ncart(sh[g].l);
+        for (int c = 0; c < nc; ++c) {
+          csrc.push_back(make_int4(o, slot < 0 ? -1 : slot + c, slot, nc));
+          cao.push_back(sh[g].ao0 + c);
+        }
+      }
+    }
+    nomax = std::max(nomax, atom_orb[a].y);
+  }
+  h->blk_nfmax = nfmax;
+  h->blk_nomax = nomax;
+  h->blk_smem[0] = blk_transform_smem(nfmax, nomax, 0);
+  h->blk_smem[1] = blk_transform_smem(nfmax, nomax, 1);
+  h->blk_smem[2] = blk_transform_smem(nfmax, nomax, 2);
+  if (h->blk_smem[0] > 227 * 1024) {
+    h->err = "block mode: an atom's functions and orbitals exceed the transform's shared memory";
+    return VSVB_ERR_UNSUPPORTED;
+  }
+  h->blk_ncoef = (int)csrc.size();
+  CK(h->blk_atom_nf.upload(atom_nf), "upload blk");
+  CK(h->blk_atom_c0.upload(atom_c0), "upload blk");
+  CK(h->blk_atom_orb.upload(atom_orb), "upload blk");
+  CK(h->blk_orb.upload(borb.empty() ? std::vector<int>(1, 0) : borb), "upload blk");
+  CK(h->blk_csrc.upload(csrc.empty() ? std::vector<int4>(1, make_int4(0, -1, 0, 0)) : csrc), "upload blk");
+  CK(h->blk_cao.upload(cao.empty() ? std::vector<int>(1, 0) : cao), "upload blk");
+  CK(h->blk_catom.alloc(std::max<size_t>(csrc.size(), 1)), "alloc blk");
+  /* atom pairs (first atom >= second) and each shell pair's place */
+  std::vector<int> ap_of(nat * nat, -1);
+  std::vector<int4> aps;
+  std::vector<std::vector<int>> ap_pairs;
+  std::vector<double> ap_q;
+  std::vector<int4> pblk(pairs.size());
+  for (size_t p = 0; p < pairs.size(); ++p) {
+    const int sA = pairs[p].shA, sB = pairs[p].shB, aA = sh[sA].atom, aB = sh[sB].atom;
+    const int X = std::max(aA, aB), Y = std::min(aA, aB);
+    int &ap = ap_of[X * nat + Y];
+    if (ap < 0) {
+      ap = (int)aps.size();
+      aps.push_back(make_int4(X, Y, atom_nf[X] * atom_nf[Y], 0));
+      ap_pairs.emplace_back();
+      ap_q.push_back(0.0);
+    }
+    ap_pairs[ap].push_back((int)p);
+    ap_q[ap] = std::max(ap_q[ap], pairs[p].qmax);
+    const int offA = sh[sA].ao0 - sh[first_sh[aA]].ao0, offB = sh[sB].ao0 - sh[first_sh[aB]].ao0;
+    const int flags = (X != Y && aA == Y ? 1 : 0) | (X == Y ? 2 : 0) | (sA == sB ? 4 : 0);
+    pblk[p] = make_int4(offA, offB, flags, atom_nf[Y]);
+  }
+  CK(h->blk_pair.upload(pblk.empty() ? std::vector<int4>(1, make_int4(0, 0, 0, 0)) : pblk), "upload blk");
+  CK(h->blk_ap.upload(aps.empty() ? std::vector<int4>(1, make_int4(0, 0, 0, 0)) : aps), "upload blk");
+  /* atom quartets above the screen, largest bound first */
+  struct AQ {
+    int i, j;
+    double b;
+  };
+  std::vector<AQ> aqs;
+  for (int i = 0; i < (int)aps.size(); ++i)
+    for (int j = 0; j <= i; ++j) {
+      const double b = ap_q[i] * ap_q[j];
+      if (b >= h->opt.ao_screen) aqs.push_back({i, j, b});
+    }
+  std::stable_sort(aqs.begin(), aqs.end(), [](const AQ &x, const AQ &y) { return x.b > y.b; });
+  h->blk_naq = (long long)aqs.size();
+  /* chunks: staging blocks of one chunk fit blk_gsize doubles */
+  const size_t gbudget = (size_t)1 << 24; /* 128 MiB of FP64 per buffer */
+  size_t gmax = 0;
+  std::vector<int4> aqd(aqs.size());
+  {
+    size_t off = 0;
+    int c0 = 0;
+    for (size_t k = 0; k < aqs.size(); ++k) {
+      const size_t sz = (size_t)aps[aqs[k].i].z * aps[aqs[k].j].z;
+      if (off > 0 && off + sz > gbudget) {
+        h->blk_chunk.push_back({c0, (int)k - c0, 0, 0, 0});
+        c0 = (int)k;
+        off = 0;
+      }
+      aqd[k] = make_int4(aqs[k].i, aqs[k].j, (int)off, aqs[k].i == aqs[k].j ? 1 : 0);
+      off += sz;
+      gmax = std::max(gmax, off);
+    }
+    if (!aqs.empty()) h->blk_chunk.push_back({c0, (int)aqs.size() - c0, 0, 0, 0});
+  }
+  h->blk_gsize = std::max<size_t>(gmax, 1);
+  CK(h->blk_aq.upload(aqd.empty() ? std::vector<int4>(1, make_int4(0, 0, 0, 0)) : aqd), "upload blk");
+  CK(h->blk_G.alloc(2 * h->blk_gsize), "alloc blk G");
+  CK(cudaMemset(h->blk_G.p, 0, sizeof(double) * h->blk_G.n), "memset blk G");
+  const bool mixed = h->opt.precision == VSVB_MIXED || h->opt.precision == VSVB_MIXED_DF64;
+  const float eps = (float)h->opt.prim_screen, tau = (float)h->opt.mixed_threshold;
+  const bool split = mixed && h->opt.prim_split;
+  const int kind64 = eri_kind(h, 0);
+  auto window = [&](int P, int Q, float lo, float hi, double &sum) -> double {
+    const float *a = q0f.data() + pairs[P].prim0, *b = q0f.data() + pairs[Q].prim0;
+    const int na = pairs[P].nprim, nb = pairs[Q].nprim;
+    double n = 0.0;
+    sum = 0.0;
+    int jlo = nb, jhi = nb;
+    for (int i = 0; i < na; ++i) {
+      if (!(a[i] * b[0] >= lo)) break;
+      while (jlo > 0 && !(a[i] * b[jlo - 1] >= lo)) --jlo;
+      while (jhi > 0 && !(a[i] * b[jhi - 1] >= hi)) --jhi;
+      n += jlo - jhi;
+      for (int j = jhi; j < jlo; ++j) sum += (double)a[i] * b[j];
+    }
+    return n;
+  };
+  /* per chunk: the quartet lists of each (cp, cq, precision), counted in a
+   * first pass and written in a second, both over worker threads */
+  const int nch = (int)h->blk_chunk.size();
+  struct ChunkStat {
+    long long cnt[3][3][2];
+    long long nq64, nq32;
+    double nprim_all, nprim32, errb, ball;
+    double prim[3][3][2][2]; /* primitive quartets per (cp, cq, precision, main / FP32 tail) */
+  };
+  std::vector<ChunkStat> cs(nch);
+  for (auto &c : cs) std::memset(&c, 0, sizeof(c));
+  auto for_quartets = [&](int c, auto &&f) {
+    const auto &ch = h->blk_chunk[c];
+    for (int k = ch.aq0; k < ch.aq0 + ch.naq; ++k) {
+      const AQ &q = aqs[k];
+      const int ncol = aps[q.j].z;
+      for (int P : ap_pairs[q.i])
+        for (int Q : ap_pairs[q.j]) {
+          if (q.i == q.j && Q > P) continue;
+          const double b = pairs[P].qmax * pairs[Q].qmax;
+          if (b < h->opt.ao_screen) continue;
+          int a = P, cc = Q, swp = 0;
+          if (pairs[a].cls < pairs[cc].cls) {
+            std::swap(a, cc);
+            swp = 1;
+          }
+          const int prec = (mixed && b < h->opt.mixed_threshold) ? 1 : 0;
+          f(pairs[a].cls, pairs[cc].cls, prec, make_int4(a, cc, aqd[k].z, ncol | (swp << 20) | ((q.i == q.j) << 21)), b,
+            P, Q);
+        }
+    }
+  };
+  const int nthr = std::max(1, std::min<int>(16, (int)std::thread::hardware_concurrency()));
+  auto run_threads = [&](auto &&job) {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthr; ++t) th.emplace_back([&, t]() {
+      for (int c = t; c < nch; c += nthr) job(c);
+    });
+    for (auto &x : th) x.join();
+  };
+  run_threads([&](int c) {
+    ChunkStat &st = cs[c];
+    for_quartets(c, [&](int cp, int cq, int prec, int4, double b, int P, int Q) {
+      st.cnt[cp][cq][prec]++;
+      int a = P, cc = Q;
+      if (pairs[a].cls < pairs[cc].cls) std::swap(a, cc);
+      double sb = 0.0;
+      const double nall = window(a, cc, eps, INFINITY, sb);
+      st.ball += b;
+      st.nprim_all += nall;
+      if (prec) {
+        st.nq32++;
+        st.nprim32 += nall;
+        st.errb += amp[P] * amp[Q];
+        st.prim[cp][cq][1][0] += nall;
+      } else {
+        st.nq64++;
+        if (split) {
+          const double nt = window(a, cc, eps, tau, sb);
+          st.nprim32 += nt;
+          st.errb += sb * (amp[P] / std::max(q0[P], 1e-300)) * (amp[Q] / std::max(q0[Q], 1e-300));
+          st.prim[cp][cq][0][1] += nt;
+          st.prim[cp][cq][0][0] += nall - nt;
+        } else {
+          st.prim[cp][cq][0][0] += nall;
+        }
+      }
+    });
+  });
+  /* offsets, launches and totals */
+  long long total = 0;
+  std::vector<long long> off((size_t)nch * 18, 0);
+  for (int c = 0; c < nch; ++c) {
+    auto &ch = h->blk_chunk[c];
+    const ChunkStat &st = cs[c];
+    h->nq_fp64 += st.nq64;
+    h->nq_fp32 += st.nq32;
+    h->nprimq_all += st.nprim_all;
+    h->nprimq_fp32 += st.nprim32;
+    h->err_bound += st.errb;
+    h->bound_all += st.ball;
+    ch.l0 = (int)h->blk_launch.size();
+    /* transform in FP32 when every quartet of the chunk is FP32-class; the
+     * others in the FP64-class arithmetic of the handle (double-float on
+     * VSVB_MIXED_DF64) */
+    ch.tt = (mixed && aqs[ch.aq0].b < h->opt.mixed_threshold) ? 1 : (kind64 == ERI_DF64 ? 2 : 0);
+    for (int a = 0; a < 3; ++a)
+      for (int cq = 0; cq <= a; ++cq)
+        for (int prec = 0; prec < 2; ++prec) {
+          const long long n = st.cnt[a][cq][prec];
+          off[(size_t)c * 18 + (a * 3 + cq) * 2 + prec] = total;
+          if (n == 0) continue;
+          const double hf = (double)n * eri_block_hrr_flops(a, cq);
+          if (prec == 1) {
+            h->blk_launch.push_back({total, (int)n, ERI_F32, a, cq, eps, INFINITY});
+            h->blk_eri_flops[ERI_F32] += eri_flops(1, a, cq, st.prim[a][cq][1][0], 0, 0) + hf;
+          } else {
+            h->blk_launch.push_back({total, (int)n, kind64, a, cq, split ? std::max(eps, tau) : eps, INFINITY});
+            h->blk_eri_flops[kind64] += eri_flops(1, a, cq, st.prim[a][cq][0][0], 0, 0) + hf;
+            if (split) {
+              h->blk_launch.push_back({total, (int)n, ERI_F32, a, cq, eps, tau});
+              h->blk_eri_flops[ERI_F32] += eri_flops(1, a, cq, st.prim[a][cq][0][1], 0, 0);
+            }
+          }
+          total += n;
+        }
+    ch.nl = (int)h->blk_launch.size() - ch.l0;
+    for (int k = ch.aq0; k < ch.aq0 + ch.naq; ++k) {
+      const int4 p1 = aps[aqs[k].i], p2 = aps[aqs[k].j];
+      h->blk_tr_flops[ch.tt] += blk_transform_flops(atom_nf[p1.x], atom_nf[p1.y], atom_nf[p2.x], atom_nf[p2.y],
+                                                    atom_orb[p1.x].y, atom_orb[p1.y].y, atom_orb[p2.x].y,
+                                                    atom_orb[p2.y].y);
+    }
+  }
+  CK(h->blk_work.alloc(std::max<long long>(total, 1)), "alloc blk work");
+  int fill_err = 0;
+  run_threads([&](int c) {
+    if (cudaSetDevice(h->dev) != cudaSuccess) {
+      fill_err = 1;
+      return;
+    }
+    std::vector<int4> lst[3][3][2];
+    for_quartets(c, [&](int cp, int cq, int prec, int4 item, double, int, int) { lst[cp][cq][prec].push_back(item); });
+    for (int a = 0; a < 3; ++a)
+      for (int cq = 0; cq <= a; ++cq)
+        for (int prec = 0; prec < 2; ++prec) {
+          const auto &v = lst[a][cq][prec];
+          if (v.empty()) continue;
+          const long long o = off[(size_t)c * 18 + (a * 3 + cq) * 2 + prec];
+          if (cudaMemcpy(h->blk_work.p + o, v.data(), sizeof(int4) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            fill_err = 1;
+        }
+  });
+  if (fill_err) {
+    h->err = "block mode: upload of the quartet lists failed";
+    return VSVB_ERR_CUDA;
+  }
+  for (int k = 0; k < 2; ++k) CK(cudaEventCreateWithFlags(&h->blk_done[k], cudaEventDisableTiming), "cudaEventCreate");
   return VSVB_OK;
 }
 
@@ -922,99 +1229,121 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   };
   h->err_bound = 0.0;
   h->bound_all = 0.0;
-  for (size_t P = 0; P < pairs.size(); ++P)
-    for (size_t Q = 0; Q <= P; ++Q) {
-      double b = pairs[P].qmax * pairs[Q].qmax;
-      if (b < h->opt.ao_screen) continue;
-      int a = (int)P, c = (int)Q;
-      if (pairs[a].cls < pairs[c].cls) std::swap(a, c);
-      int prec = (mixed && b < h->opt.mixed_threshold) ? 1 : 0;
-      h->bound_all += b;
-      double sb = 0.0;
-      const double nall = window(a, c, eps, INFINITY, sb);
-      h->nprimq_all += nall;
-      if (prec) {
-        h->nq_fp32++;
-        h->nprimq_fp32 += nall;
-        h->err_bound += amp[P] * amp[Q];
-      } else {
-        h->nq_fp64++;
-        if (split) {
-          /* the FP32 tail: its bound mass in units of the pair bounds, with
-           * the transfer norms of both pairs */
-          const double nt = window(a, c, eps, tau, sb);
-          h->nprimq_fp32 += nt;
-          h->err_bound += sb * (amp[P] / std::max(q0[P], 1e-300)) * (amp[Q] / std::max(q0[Q], 1e-300));
-        }
-      }
-      h->work_h[prec][pairs[a].cls][pairs[c].cls].push_back(make_int2(a, c));
-    }
   {
-    std::vector<std::vector<int4>> iwl;
-    /* a quartet with more than this many primitive quartets in a launch's
-     * window is split into row ranges of P's primitives, so that the largest
-     * quartets do not leave a tail of lone CTAs at the end of the launch */
-    constexpr int SPLIT_PRIMQ = 512;
-    std::vector<int> rows;
-    for (int p = 0; p < 2; ++p)
-      for (int a = 0; a < 6; ++a)
-        for (int c = 0; c < 6; ++c) {
-          const auto &w = h->work_h[p][a][c];
-          if (w.empty()) continue;
-          /* launches over this list: FP32-class lists in FP32; FP64-class
-           * lists in the handle's FP64-class arithmetic, and with the split
-           * their primitive quartets below tau in FP32 */
-          std::vector<vsvb_gpu::SweepItem> items;
-          if (p == 1) {
-            items.push_back({p, ERI_F32, a, c, eps, INFINITY, 0, 0, 0, 100 * ERI_F32 + 10 * a + c});
-          } else if (split) {
-            items.push_back({p, eri_kind(h, 0), a, c, std::max(eps, tau), INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
-            items.push_back({p, ERI_F32, a, c, eps, tau, 0, 0, 0, 300 + 10 * a + c});
-          } else {
-            items.push_back({p, eri_kind(h, 0), a, c, eps, INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
-          }
-          for (auto &it : items) {
-            std::vector<std::pair<double, int4>> kept;
-            for (const int2 &q : w) {
-              window_rows(q.x, q.y, it.lo, it.hi, rows);
-              double n = 0.0;
-              for (int r : rows) n += r;
-              if (n <= 0.0) continue;
-              const int parts = (int)std::ceil(n / SPLIT_PRIMQ);
-              const double target = n / parts;
-              int r0 = 0;
-              double acc = 0.0;
-              for (int r = 0; r < (int)rows.size(); ++r) {
-                acc += rows[r];
-                const bool last = r + 1 == (int)rows.size();
-                if (acc > 0.0 && (acc >= target || last)) {
-                  kept.push_back({acc, make_int4(q.x, q.y, r0, last ? 1 << 30 : r + 1)});
-                  it.flops_fwd += eri_flops(0, a, c, acc, pairs[q.x].nop, pairs[q.y].nop);
-                  it.flops_grad += eri_flops(3, a, c, acc, pairs[q.x].nop, pairs[q.y].nop);
-                  r0 = r + 1;
-                  acc = 0.0;
-                } else if (acc == 0.0) {
-                  r0 = r + 1;
-                }
-              }
-              it.nprimq += n;
-            }
-            if (kept.empty()) continue;
-            std::stable_sort(kept.begin(), kept.end(), [](const std::pair<double, int4> &x,
-                                                          const std::pair<double, int4> &y) { return x.first > y.first; });
-            std::vector<int4> lst(kept.size());
-            for (size_t k = 0; k < kept.size(); ++k) lst[k] = kept[k].second;
-            it.wl = (int)iwl.size();
-            iwl.push_back(std::move(lst));
-            h->sweep.push_back(it);
+    /* block mode: s and p shells only, not for first_order_opt's handles */
+    bool sp_only = true;
+    for (const GShell &g : sh) sp_only = sp_only && g.l <= 1;
+    const double ncand = 0.5 * (double)pairs.size() * ((double)pairs.size() + 1.0);
+    const bool want = h->opt.block_mode > 0 || (h->opt.block_mode == 0 && ncand > 5e7);
+    if (want && (!sp_only || h->hs_split)) {
+      if (h->opt.block_mode > 0) {
+        h->err = "block mode needs s and p shells only";
+        return VSVB_ERR_UNSUPPORTED;
+      }
+    } else if (want) {
+      h->blk_on = true;
+    }
+  }
+  if (h->blk_on) {
+    int rc = build_block(h, d, sh, first_sh, orbs_on_atom, slot_of_shell, pairs, q0f, q0, amp);
+    if (rc) return rc;
+  } else {
+    h->err_bound = 0.0;
+    h->bound_all = 0.0;
+    for (size_t P = 0; P < pairs.size(); ++P)
+      for (size_t Q = 0; Q <= P; ++Q) {
+        double b = pairs[P].qmax * pairs[Q].qmax;
+        if (b < h->opt.ao_screen) continue;
+        int a = (int)P, c = (int)Q;
+        if (pairs[a].cls < pairs[c].cls) std::swap(a, c);
+        int prec = (mixed && b < h->opt.mixed_threshold) ? 1 : 0;
+        h->bound_all += b;
+        double sb = 0.0;
+        const double nall = window(a, c, eps, INFINITY, sb);
+        h->nprimq_all += nall;
+        if (prec) {
+          h->nq_fp32++;
+          h->nprimq_fp32 += nall;
+          h->err_bound += amp[P] * amp[Q];
+        } else {
+          h->nq_fp64++;
+          if (split) {
+            /* the FP32 tail: its bound mass in units of the pair bounds, with
+             * the transfer norms of both pairs */
+            const double nt = window(a, c, eps, tau, sb);
+            h->nprimq_fp32 += nt;
+            h->err_bound += sb * (amp[P] / std::max(q0[P], 1e-300)) * (amp[Q] / std::max(q0[Q], 1e-300));
           }
         }
-    std::sort(h->sweep.begin(), h->sweep.end(), [](const vsvb_gpu::SweepItem &x, const vsvb_gpu::SweepItem &y) {
-      return x.flops_fwd > y.flops_fwd;
-    });
-    h->item_wh = std::move(iwl);
-    h->item_wd = std::vector<DBuf<int4>>(h->item_wh.size());
-    for (size_t k = 0; k < h->item_wh.size(); ++k) CK(h->item_wd[k].upload(h->item_wh[k]), "upload item work");
+        h->work_h[prec][pairs[a].cls][pairs[c].cls].push_back(make_int2(a, c));
+      }
+    {
+      std::vector<std::vector<int4>> iwl;
+      /* a quartet with more than this many primitive quartets in a launch's
+       * window is split into row ranges of P's primitives, so that the largest
+       * quartets do not leave a tail of lone CTAs at the end of the launch */
+      constexpr int SPLIT_PRIMQ = 512;
+      std::vector<int> rows;
+      for (int p = 0; p < 2; ++p)
+        for (int a = 0; a < 6; ++a)
+          for (int c = 0; c < 6; ++c) {
+            const auto &w = h->work_h[p][a][c];
+            if (w.empty()) continue;
+            /* launches over this list: FP32-class lists in FP32; FP64-class
+             * lists in the handle's FP64-class arithmetic, and with the split
+             * their primitive quartets below tau in FP32 */
+            std::vector<vsvb_gpu::SweepItem> items;
+            if (p == 1) {
+              items.push_back({p, ERI_F32, a, c, eps, INFINITY, 0, 0, 0, 100 * ERI_F32 + 10 * a + c});
+            } else if (split) {
+              items.push_back({p, eri_kind(h, 0), a, c, std::max(eps, tau), INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
+              items.push_back({p, ERI_F32, a, c, eps, tau, 0, 0, 0, 300 + 10 * a + c});
+            } else {
+              items.push_back({p, eri_kind(h, 0), a, c, eps, INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
+            }
+            for (auto &it : items) {
+              std::vector<std::pair<double, int4>> kept;
+              for (const int2 &q : w) {
+                window_rows(q.x, q.y, it.lo, it.hi, rows);
+                double n = 0.0;
+                for (int r : rows) n += r;
+                if (n <= 0.0) continue;
+                const int parts = (int)std::ceil(n / SPLIT_PRIMQ);
+                const double target = n / parts;
+                int r0 = 0;
+                double acc = 0.0;
+                for (int r = 0; r < (int)rows.size(); ++r) {
+                  acc += rows[r];
+                  const bool last = r + 1 == (int)rows.size();
+                  if (acc > 0.0 && (acc >= target || last)) {
+                    kept.push_back({acc, make_int4(q.x, q.y, r0, last ? 1 << 30 : r + 1)});
+                    it.flops_fwd += eri_flops(0, a, c, acc, pairs[q.x].nop, pairs[q.y].nop);
+                    it.flops_grad += eri_flops(3, a, c, acc, pairs[q.x].nop, pairs[q.y].nop);
+                    r0 = r + 1;
+                    acc = 0.0;
+                  } else if (acc == 0.0) {
+                    r0 = r + 1;
+                  }
+                }
+                it.nprimq += n;
+              }
+              if (kept.empty()) continue;
+              std::stable_sort(kept.begin(), kept.end(), [](const std::pair<double, int4> &x,
+                                                            const std::pair<double, int4> &y) { return x.first > y.first; });
+              std::vector<int4> lst(kept.size());
+              for (size_t k = 0; k < kept.size(); ++k) lst[k] = kept[k].second;
+              it.wl = (int)iwl.size();
+              iwl.push_back(std::move(lst));
+              h->sweep.push_back(it);
+            }
+          }
+      std::sort(h->sweep.begin(), h->sweep.end(), [](const vsvb_gpu::SweepItem &x, const vsvb_gpu::SweepItem &y) {
+        return x.flops_fwd > y.flops_fwd;
+      });
+      h->item_wh = std::move(iwl);
+      h->item_wd = std::vector<DBuf<int4>>(h->item_wh.size());
+      for (size_t k = 0; k < h->item_wh.size(); ++k) CK(h->item_wd[k].upload(h->item_wh[k]), "upload item work");
+    }
   }
 
   /* determinant pairs */
@@ -1066,6 +1395,16 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   CK(h->Ta.alloc(std::max<long long>(nq * na * na, 1)), "alloc Ta");
   CK(h->Tb.alloc(std::max<long long>(nq * nb * nb, 1)), "alloc Tb");
   CK(h->sing.alloc(nq), "alloc sing");
+  {
+    /* exact-minor pool: one slot per flagged determinant pair, up to 1 GiB */
+    const size_t per = (size_t)3 * ((size_t)na * na + (size_t)nb * nb);
+    const size_t cap = std::max<size_t>(1, ((size_t)1 << 27) / std::max<size_t>(per, 1));
+    h->xcap = (int)std::min<size_t>(std::min<size_t>((size_t)nq, cap), (size_t)1 << 30);
+    CK(h->xinv.alloc(std::max<size_t>((size_t)h->xcap * per, 1)), "alloc exact-minor pool");
+    CK(h->xdet.alloc((size_t)h->xcap * 6), "alloc exact-minor pool");
+    CK(h->xslot.alloc(nq), "alloc exact-minor pool");
+    CK(h->xcount.alloc(1), "alloc exact-minor pool");
+  }
   CK(h->nsing.alloc(1), "alloc nsing");
   h->ld_scratch = 2 * std::max(na, nb) * std::max(std::max(na, nb), 1);
   CK(h->scratch.alloc(std::max<long long>(nq * h->ld_scratch, 1)), "alloc scratch");
@@ -1161,6 +1500,91 @@ int eri_sweep(vsvb_gpu *h, int mode) {
   return VSVB_OK;
 }
 
+/* block mode: the orbital-pair matrix U (into T) chunk by chunk.  The ERI
+ * launches of chunk c run on the side streams into staging buffer c % 2
+ * (after the transform of chunk c - 2 has freed it); the handle's stream
+ * joins them and transforms the chunk, so the integrals of chunk c + 1 run
+ * while chunk c is transformed. */
+int block_sweep(vsvb_gpu *h) {
+  cudaStream_t st = h->st;
+  {
+    BlkCoefArgs ca{};
+    ca.src = h->blk_csrc.p;
+    ca.ao = h->blk_cao.p;
+    ca.n = h->blk_ncoef;
+    ca.C = h->C.p;
+    ca.maxobs = h->maxobs;
+    ca.angn = h->angn.p;
+    ca.dtol = h->dtol;
+    ca.catom = h->blk_catom.p;
+    if (blk_coef(ca, st)) {
+      h->err = "block weight launch failed";
+      return VSVB_ERR_CUDA;
+    }
+    h->launches++;
+  }
+  if (h->sweep_timing && !h->sweep_t0) {
+    CK(cudaEventCreate(&h->sweep_t0), "cudaEventCreate");
+    CK(cudaEventCreate(&h->sweep_t1), "cudaEventCreate");
+  }
+  if (h->sweep_timing) CK(cudaEventRecord(h->sweep_t0, st), "event record");
+  /* the transforms leave the staging buffers cleared; clearing them here as
+   * well keeps an evaluation correct after one that stopped part-way */
+  CK(cudaMemsetAsync(h->blk_G.p, 0, sizeof(double) * h->blk_G.n, st), "memset staging");
+  CK(cudaEventRecord(h->ev_fork, st), "event record");
+  for (int k = 0; k < vsvb_gpu::NAUX; ++k) CK(cudaStreamWaitEvent(h->aux[k], h->ev_fork, 0), "stream wait");
+  EriArgs ea = eri_args(h);
+  ea.pair_blk = h->blk_pair.p;
+  BlkArgs ba{};
+  ba.aq = h->blk_aq.p;
+  ba.ap = h->blk_ap.p;
+  ba.atom_orb = h->blk_atom_orb.p;
+  ba.atom_nf = h->blk_atom_nf.p;
+  ba.atom_c0 = h->blk_atom_c0.p;
+  ba.orb = h->blk_orb.p;
+  ba.catom = h->blk_catom.p;
+  ba.U = h->T.p;
+  ba.np = h->np;
+  ba.nfmax = h->blk_nfmax;
+  ba.nomax = h->blk_nomax;
+  ba.r1n = blk_r1(h->blk_nfmax, h->blk_nomax);
+  int rr = 0;
+  for (size_t c = 0; c < h->blk_chunk.size(); ++c) {
+    const auto &ch = h->blk_chunk[c];
+    const int buf = (int)(c & 1);
+    double *G = h->blk_G.p + (size_t)buf * h->blk_gsize;
+    if (c >= 2)
+      for (int k = 0; k < vsvb_gpu::NAUX; ++k) CK(cudaStreamWaitEvent(h->aux[k], h->blk_done[buf], 0), "stream wait");
+    ea.G = G;
+    for (int l = ch.l0; l < ch.l0 + ch.nl; ++l) {
+      const auto &L = h->blk_launch[l];
+      ea.prim_lo = L.lo;
+      ea.prim_hi = L.hi;
+      cudaStream_t sa = h->aux[rr++ % vsvb_gpu::NAUX];
+      if (eri_launch(4, L.kind, L.cp, L.cq, ea, h->blk_work.p + L.off, L.n, h->nsm * 16, sa)) {
+        h->err = "block ERI launch failed";
+        return VSVB_ERR_CUDA;
+      }
+      h->launches++;
+    }
+    for (int k = 0; k < vsvb_gpu::NAUX; ++k) {
+      CK(cudaEventRecord(h->ev_join[k], h->aux[k]), "event record");
+      CK(cudaStreamWaitEvent(st, h->ev_join[k], 0), "stream wait");
+    }
+    ba.G = G;
+    ba.G_clear = G;
+    if (blk_transform(ba, ch.aq0, ch.naq, ch.tt, h->blk_smem[ch.tt], st)) {
+      h->err = "block transform launch failed";
+      return VSVB_ERR_CUDA;
+    }
+    h->launches++;
+    CK(cudaEventRecord(h->blk_done[buf], st), "event record");
+  }
+  h->sweep_mode = 4;
+  if (h->sweep_timing) CK(cudaEventRecord(h->sweep_t1, st), "event record");
+  return VSVB_OK;
+}
+
 /* forward pass on coeff_d; leaves E in result[0..4] (device).  With fused,
  * the ERI sweep also accumulates the (unscaled) adjoint dE/dX from the
  * unscreened cofactor densities. */
@@ -1180,7 +1604,7 @@ int forward(vsvb_gpu *h, bool fused = false) {
   orb_1e_kernel<<<dim3(h->nsp, h->nsp), 128, 0, st>>>(oa, h->So.p, h->Ho.p);
   CK(cudaGetLastError(), "orb_1e");
   h->launches += 2;
-  if (h->nxelem > 0) {
+  if (h->nxelem > 0 && !h->blk_on) {
     XtabArgs xa = xtab_args(h);
     xtab_kernel<<<(unsigned)((h->nxelem + 255) / 256), 256, 0, st>>>(xa);
     CK(cudaGetLastError(), "xtab");
@@ -1189,6 +1613,7 @@ int forward(vsvb_gpu *h, bool fused = false) {
     h->launches += 2;
   }
   CK(cudaMemsetAsync(h->sing.p, 0, sizeof(int) * h->sing.n, st), "memset sing");
+  CK(cudaMemsetAsync(h->xcount.p, 0, sizeof(int), st), "memset pool count");
   CK(cudaMemsetAsync(h->nsing.p, 0, sizeof(int), st), "memset nsing");
   DetCtx dc = det_ctx(h);
   detpair_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, h->scratch.p, h->ld_scratch);
@@ -1209,7 +1634,7 @@ int forward(vsvb_gpu *h, bool fused = false) {
   }
   CK(cudaMemsetAsync(h->T.p, 0, sizeof(double) * h->T.n, st), "memset T");
   {
-    int rc = eri_sweep(h, fused ? 3 : 0);
+    int rc = h->blk_on ? block_sweep(h) : eri_sweep(h, fused ? 3 : 0);
     if (rc) return rc;
   }
   if (eri_symmetrize(h->T.p, h->np, h->sqT.p, st)) {
@@ -1277,7 +1702,7 @@ int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
     return VSVB_ERR_NOT_NORMALISABLE;
   }
   if (status & 4) {
-    h->err = "a singular determinant block with more than " + std::to_string(VSVB_MAXN) + " electrons of one spin";
+    h->err = "more singular determinant pairs than the exact-minor pool holds";
     return VSVB_ERR_UNSUPPORTED;
   }
   if (out) {
@@ -1296,7 +1721,7 @@ int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
  * Each candidate runs 3 times on the handle's own data (min taken); the
  * choice changes launch shapes only, never the arithmetic. */
 int autotune(vsvb_gpu *h) {
-  if (h->sweep.empty() && h->ntasks == 0) return VSVB_OK;
+  if ((h->sweep.empty() && h->ntasks == 0) || h->blk_on) return VSVB_OK;
   int rc = forward(h); /* weight tables, T and determinant pairs for the timed launches */
   if (rc) return rc;
   CK(cudaStreamSynchronize(h->st), "autotune sync");
@@ -1452,6 +1877,7 @@ void vsvb_default_options(vsvb_options *o) {
   o->prim_split = 1;
   o->cuda_graph = 1;
   o->autotune = 0;
+  o->block_mode = 0;
 }
 
 int vsvb_gpu_create(const vsvb_system_desc *d, const vsvb_options *opt, vsvb_gpu **out) {
@@ -1481,6 +1907,8 @@ void vsvb_gpu_destroy(vsvb_gpu *h) {
   for (cudaEvent_t e : h->sweep_ev) cudaEventDestroy(e);
   if (h->sweep_t0) cudaEventDestroy(h->sweep_t0);
   if (h->sweep_t1) cudaEventDestroy(h->sweep_t1);
+  for (int k = 0; k < 2; ++k)
+    if (h->blk_done[k]) cudaEventDestroy(h->blk_done[k]);
   delete h;
   if (st) cudaStreamDestroy(st);
 }
@@ -1553,6 +1981,10 @@ static int enqueue_eval(vsvb_gpu *h, bool fused) {
 }
 
 static int energy_grad_common(vsvb_gpu *h, vsvb_energy_result *out, double *grad, bool grad_on_device) {
+  if (h->blk_on) {
+    h->err = "the gradient is not available on a block-mode handle";
+    return VSVB_ERR_UNSUPPORTED;
+  }
   const bool fused = h->opt.grad_mode == 0;
   int rc = enqueue_eval(h, fused);
   if (rc) return rc;
@@ -1747,8 +2179,7 @@ int vsvb_batch_energy_grad(vsvb_batch *b, const double *const *weights_dev, doub
       return VSVB_ERR_NOT_NORMALISABLE;
     }
     if (stat[i] & 4) {
-      b->err = "molecule " + std::to_string(i) + ": a singular determinant block with more than " +
-               std::to_string(VSVB_MAXN) + " electrons of one spin";
+      b->err = "molecule " + std::to_string(i) + ": more singular determinant pairs than the exact-minor pool holds";
       return VSVB_ERR_UNSUPPORTED;
     }
     if (stat[i] & 2) {
@@ -1893,6 +2324,35 @@ int vsvb_gpu_debug_orbital_eri(vsvb_gpu *h, double *out, size_t cap) {
   return h->np;
 }
 
+int vsvb_gpu_debug_orbital_eri_at(vsvb_gpu *h, const long long *idx, int n, double *out) {
+  if (!h || (n > 0 && (!idx || !out))) return VSVB_ERR_INPUT;
+  CK(cudaSetDevice(h->dev), "cudaSetDevice");
+  CK(cudaStreamSynchronize(h->st), "sync");
+  const long long nt = (long long)h->np * h->np;
+  for (int i = 0; i < n; ++i) {
+    if (idx[i] < 0 || idx[i] >= nt) {
+      h->err = "orbital-pair ERI index out of range";
+      return VSVB_ERR_INPUT;
+    }
+    CK(cudaMemcpy(out + i, h->T.p + idx[i], sizeof(double), cudaMemcpyDeviceToHost), "copy T entry");
+  }
+  return h->np;
+}
+
+int vsvb_gpu_block_stats(const vsvb_gpu *h, double *eri_flops3, double *transform_flops2, long long *counts3) {
+  if (!h) return -VSVB_ERR_INPUT;
+  if (eri_flops3)
+    for (int k = 0; k < 3; ++k) eri_flops3[k] = h->blk_eri_flops[k];
+  if (transform_flops2)
+    for (int k = 0; k < 3; ++k) transform_flops2[k] = h->blk_tr_flops[k];
+  if (counts3) {
+    counts3[0] = h->blk_naq;
+    counts3[1] = (long long)h->blk_chunk.size();
+    counts3[2] = (long long)h->blk_launch.size() + (long long)h->blk_chunk.size();
+  }
+  return h->blk_on ? 1 : 0;
+}
+
 int vsvb_gpu_debug_orbital_1e(vsvb_gpu *h, double *s, double *hc, size_t cap) {
   if (!h) return -VSVB_ERR_INPUT;
   size_t n = (size_t)h->nsp * h->nsp;
@@ -1967,7 +2427,7 @@ int gpu_hs_columns(vsvb_gpu *h, const double *w_dev, const int *src_dev, int j0,
     return VSVB_ERR_NOT_NORMALISABLE;
   }
   if (flag & 4) {
-    h->err = "a singular determinant block with more than " + std::to_string(VSVB_MAXN) + " electrons of one spin";
+    h->err = "more singular determinant pairs than the exact-minor pool holds";
     return VSVB_ERR_UNSUPPORTED;
   }
   if (flag & 2) {

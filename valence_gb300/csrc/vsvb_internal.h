@@ -16,7 +16,8 @@
  *                                    (i k | j l), np = n(n+1)/2
  *   det data    per determinant pair q: det, inverse (n x n) per spin; a
  *               block flagged singular keeps det(A + delta I) and that
- *               matrix's inverse for the adjoint
+ *               matrix's inverse for the adjoint, and its pair takes a slot
+ *               of the exact-minor pool: inverse and det of A + k P, k = 1..3
  */
 #ifndef VSVB_INTERNAL_H
 #define VSVB_INTERNAL_H
@@ -25,7 +26,6 @@
 
 #define VSVB_LMAX 2     /* highest angular momentum on the GPU */
 #define VSVB_NCLS 6     /* shell-pair classes (la>=lb): 00 10 11 20 21 22 */
-#define VSVB_MAXN 32    /* largest spin block handled by the exact-minor path */
 
 struct GShell {
   int l, nprim, prim0, atom; /* prim0 indexes the global exponent/coef arrays */
