@@ -90,6 +90,8 @@ __global__ void blk_coef_kernel(BlkCoefArgs a) {
   a.catom[e] = v;
 }
 
+constexpr int OB = 8; /* output orbitals per thread pass: independent accumulators */
+
 template <typename TT>
 __global__ void __launch_bounds__(256) blk_transform_kernel(BlkArgs a, int aq0) {
   extern __shared__ double sm_raw[];
@@ -100,74 +102,119 @@ __global__ void __launch_bounds__(256) blk_transform_kernel(BlkArgs a, int aq0) 
   const int nfA = a.atom_nf[XA], nfB = a.atom_nf[XB], nfC = a.atom_nf[XC], nfD = a.atom_nf[XD];
   const int2 oA = a.atom_orb[XA], oB = a.atom_orb[XB], oC = a.atom_orb[XC], oD = a.atom_orb[XD];
   const int nA = oA.y, nB = oB.y, nC = oC.y, nD = oD.y;
-  const int cw = a.nomax * a.nfmax;
+  /* weight blocks [orbital][function], orbital rows zero-padded to a
+   * multiple of OB so that the blocked passes need no guards */
+  const int cw = a.nomaxp * a.nfmax;
   TT *CA = sm, *CB = CA + cw, *CC = CB + cw, *CD = CC + cw;
   TT *R1 = CD + cw;
   TT *R2 = R1 + a.r1n;
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int t = tid; t < nA * nfA; t += nt) to_t(a.catom[a.atom_c0[XA] + t], CA[t]);
-  for (int t = tid; t < nB * nfB; t += nt) to_t(a.catom[a.atom_c0[XB] + t], CB[t]);
-  for (int t = tid; t < nC * nfC; t += nt) to_t(a.catom[a.atom_c0[XC] + t], CC[t]);
-  for (int t = tid; t < nD * nfD; t += nt) to_t(a.catom[a.atom_c0[XD] + t], CD[t]);
+  auto load_c = [&](TT *dst, int atom, int n, int nf) {
+    for (int t = tid; t < a.nomaxp * nf; t += nt) {
+      if (t < n * nf) to_t(a.catom[a.atom_c0[atom] + t], dst[t]);
+      else zero_t(dst[t]);
+    }
+  };
+  load_c(CA, XA, nA, nfA);
+  load_c(CB, XB, nB, nfB);
+  load_c(CC, XC, nC, nfC);
+  load_c(CD, XD, nD, nfD);
   __syncthreads();
   const int nAB = nfA * nfB, ncol = nfC * nfD, nCD = nC * nD;
   const double *G = a.G + (unsigned)q.z;
-  /* 1: the d index */
-  for (int idx = tid; idx < nAB * nfC * nD; idx += nt) {
-    const int v = idx % nD, t = idx / nD, c = t % nfC, ab = t / nfC;
-    const double *g = G + (size_t)ab * ncol + c * nfD;
-    const TT *cd = CD + v * nfD;
-    TT s;
-    zero_t(s);
-    for (int d = 0; d < nfD; ++d) {
-      TT gv;
-      to_t(g[d], gv);
-      mac(s, gv, cd[d]);
+  /* 1: the d index -- item (ab, c), outputs v */
+  for (int it = tid; it < nAB * nfC; it += nt) {
+    const double *g = G + (size_t)(it / nfC) * ncol + (it % nfC) * nfD;
+    for (int v0 = 0; v0 < nD; v0 += OB) {
+      TT acc[OB];
+#pragma unroll
+      for (int k = 0; k < OB; ++k) zero_t(acc[k]);
+      for (int d = 0; d < nfD; ++d) {
+        TT x;
+        to_t(g[d], x);
+        const TT *cd = CD + v0 * nfD + d;
+#pragma unroll
+        for (int k = 0; k < OB; ++k) mac(acc[k], x, cd[k * nfD]);
+      }
+#pragma unroll
+      for (int k = 0; k < OB; ++k)
+        if (v0 + k < nD) R1[(size_t)it * nD + v0 + k] = acc[k];
     }
-    R1[idx] = s;
   }
   __syncthreads();
   /* the block has been read: clear it for the chunk that reuses the buffer */
   for (int idx = tid; idx < nAB * ncol; idx += nt) a.G_clear[(unsigned)q.z + idx] = 0.0;
-  /* 2: the c index */
-  for (int idx = tid; idx < nAB * nCD; idx += nt) {
-    const int v = idx % nD, t = idx / nD, u = t % nC, ab = t / nC;
+  /* 2: the c index -- item (ab, v), outputs u */
+  for (int it = tid; it < nAB * nD; it += nt) {
+    const int ab = it / nD, v = it - ab * nD;
     const TT *y = R1 + (size_t)ab * nfC * nD + v;
-    const TT *cc = CC + u * nfC;
-    TT s;
-    zero_t(s);
-    for (int c = 0; c < nfC; ++c) mac(s, cc[c], y[c * nD]);
-    R2[idx] = s;
+    for (int u0 = 0; u0 < nC; u0 += OB) {
+      TT acc[OB];
+#pragma unroll
+      for (int k = 0; k < OB; ++k) zero_t(acc[k]);
+      for (int c = 0; c < nfC; ++c) {
+        const TT x = y[c * nD];
+        const TT *cc = CC + u0 * nfC + c;
+#pragma unroll
+        for (int k = 0; k < OB; ++k) mac(acc[k], x, cc[k * nfC]);
+      }
+#pragma unroll
+      for (int k = 0; k < OB; ++k)
+        if (u0 + k < nC) R2[((size_t)ab * nC + u0 + k) * nD + v] = acc[k];
+    }
   }
   __syncthreads();
-  /* 3: the b index */
-  for (int idx = tid; idx < nfA * nB * nCD; idx += nt) {
-    const int uv = idx % nCD, t2 = idx / nCD, t = t2 % nB, aa = t2 / nB;
+  /* 3: the b index -- item (a, uv), outputs t */
+  for (int it = tid; it < nfA * nCD; it += nt) {
+    const int aa = it / nCD, uv = it - aa * nCD;
     const TT *z = R2 + (size_t)aa * nfB * nCD + uv;
-    const TT *cb = CB + t * nfB;
-    TT s;
-    zero_t(s);
-    for (int b = 0; b < nfB; ++b) mac(s, cb[b], z[(size_t)b * nCD]);
-    R1[idx] = s;
+    for (int t0 = 0; t0 < nB; t0 += OB) {
+      TT acc[OB];
+#pragma unroll
+      for (int k = 0; k < OB; ++k) zero_t(acc[k]);
+      for (int b = 0; b < nfB; ++b) {
+        const TT x = z[(size_t)b * nCD];
+        const TT *cb = CB + t0 * nfB + b;
+#pragma unroll
+        for (int k = 0; k < OB; ++k) mac(acc[k], x, cb[k * nfB]);
+      }
+#pragma unroll
+      for (int k = 0; k < OB; ++k)
+        if (t0 + k < nB) R1[((size_t)aa * nB + t0 + k) * nCD + uv] = acc[k];
+    }
   }
   __syncthreads();
-  /* 4: the a index, and the orbital-pair scatter */
+  /* 4: the a index -- item (t, uv), outputs s -- and the orbital-pair scatter */
   const double wgt = q.w & 1 ? 0.5 : 1.0;
-  for (int idx = tid; idx < nA * nB * nCD; idx += nt) {
-    const int uv = idx % nCD, t2 = idx / nCD, t = t2 % nB, s = t2 / nB;
+  for (int it = tid; it < nB * nCD; it += nt) {
+    const int t = it / nCD, uv = it - t * nCD;
     const int u = uv / nD, v = uv - u * nD;
-    const int os = a.orb[oA.x + s], ot = a.orb[oB.x + t], ou = a.orb[oC.x + u], ov = a.orb[oD.x + v];
-    if (XA == XB && os < ot) continue;
+    const int ot = a.orb[oB.x + t], ou = a.orb[oC.x + u], ov = a.orb[oD.x + v];
     if (XC == XD && ou < ov) continue;
-    /* across two atoms an orbital paired with itself takes both orders of
-     * its weight product, C_i(a) C_i(b) + C_i(b) C_i(a): weight 2 */
-    const double w2 = (XA != XB && os == ot ? 2.0 : 1.0) * (XC != XD && ou == ov ? 2.0 : 1.0);
+    const int qcol = opidx_b(ou, ov);
+    const double wq = wgt * (XC != XD && ou == ov ? 2.0 : 1.0);
     const TT *y = R1 + (size_t)t * nCD + uv;
-    const TT *ca = CA + s * nfA;
-    TT acc;
-    zero_t(acc);
-    for (int aa = 0; aa < nfA; ++aa) mac(acc, ca[aa], y[(size_t)aa * nB * nCD]);
-    if (nonzero_t(acc)) atomicAdd(a.U + (size_t)opidx_b(os, ot) * a.np + opidx_b(ou, ov), wgt * w2 * dbl(acc));
+    for (int s0 = 0; s0 < nA; s0 += OB) {
+      TT acc[OB];
+#pragma unroll
+      for (int k = 0; k < OB; ++k) zero_t(acc[k]);
+      for (int aa = 0; aa < nfA; ++aa) {
+        const TT x = y[(size_t)aa * nB * nCD];
+        const TT *ca = CA + s0 * nfA + aa;
+#pragma unroll
+        for (int k = 0; k < OB; ++k) mac(acc[k], x, ca[k * nfA]);
+      }
+#pragma unroll
+      for (int k = 0; k < OB; ++k) {
+        if (s0 + k >= nA) continue;
+        const int os = a.orb[oA.x + s0 + k];
+        if (XA == XB && os < ot) continue;
+        /* across two atoms an orbital paired with itself takes both orders
+         * of its weight product, C_i(a) C_i(b) + C_i(b) C_i(a): weight 2 */
+        const double w2 = wq * (XA != XB && os == ot ? 2.0 : 1.0);
+        if (nonzero_t(acc[k])) atomicAdd(a.U + (size_t)opidx_b(os, ot) * a.np + qcol, w2 * dbl(acc[k]));
+      }
+    }
   }
 }
 
@@ -187,7 +234,8 @@ int blk_r1(int nfmax, int nomax) {
 size_t blk_transform_smem(int nfmax, int nomax, int tt) {
   const size_t r1 = (size_t)blk_r1(nfmax, nomax);
   const size_t r2 = (size_t)nfmax * nfmax * nomax * nomax;
-  const size_t n = 4 * (size_t)nomax * nfmax + r1 + r2;
+  const size_t nomaxp = (size_t)(nomax + 7) / 8 * 8;
+  const size_t n = 4 * nomaxp * nfmax + r1 + r2;
   return n * (tt == 1 ? sizeof(float) : sizeof(double)); /* double-float: two FP32 */
 }
 

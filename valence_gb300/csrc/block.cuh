@@ -33,6 +33,7 @@ struct BlkArgs {
   int np;
   int nfmax, nomax;     /* largest functions / orbitals on an atom (shared-memory layout) */
   int r1n;              /* blk_r1(nfmax, nomax) */
+  int nomaxp;           /* nomax rounded up to a multiple of 8 */
 };
 
 int blk_coef(const BlkCoefArgs &a, cudaStream_t st);

@@ -301,9 +301,9 @@ __device__ __forceinline__ double pert_entry(int r, int c, double s) {
 }
 }  // namespace
 
-__global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
-  __shared__ double red[8];
-  __shared__ int redi[8];
+__global__ void __launch_bounds__(512) detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
+  __shared__ double red[32];
+  __shared__ int redi[32];
   __shared__ double sdet;
   __shared__ int ssing, spiv, sslot;
   const long long q = blockIdx.x;
@@ -319,6 +319,24 @@ __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
       continue;
     }
     const int n2 = 2 * n;
+    if (sp == 1 && n == d.ds.nalpha) {
+      /* a beta block with the same orbitals as the unflagged alpha block
+       * (doubly occupied orbitals only) takes its factorisation */
+      int same = !(d.sing[q] & 1);
+      for (int r = threadIdx.x; r < n && same; r += blockDim.x)
+        same = spat(d, pos_slot(d, qi.isc, qi.bb, 0, r)) == spat(d, pos_slot(d, qi.isc, qi.bb, 1, r)) &&
+               spat(d, pos_slot(d, qi.jsc, qi.kb, 0, r)) == spat(d, pos_slot(d, qi.jsc, qi.kb, 1, r));
+      if (__syncthreads_and(same)) {
+        const double *Ta = d.Ta + (size_t)q * n * n;
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) Tout[t] = Ta[t];
+        if (threadIdx.x == 0) {
+          d.det_b[q] = d.det_a[q];
+          d.detr_b[q] = d.detr_a[q];
+        }
+        __syncthreads();
+        continue;
+      }
+    }
     /* W = [A + shift I + kp P | I]; returns max |A| over the block */
     auto fill = [&](double shift, double kp) -> double {
       double mx = 0.0;
@@ -408,13 +426,20 @@ __global__ void detpair_kernel(DetCtx d, double *scratch, int ld_scratch) {
         __syncthreads();
         for (int j = threadIdx.x; j < n2; j += blockDim.x) W[k * n2 + j] /= piv;
         __syncthreads();
-        for (int t = threadIdx.x; t < n * n2; t += blockDim.x) {
-          int i = t / n2, j = t - i * n2;
-          if (i != k && j != k) W[t] -= W[i * n2 + k] * W[k * n2 + j];
+        /* rows to warps, columns to lanes; the pivot column becomes exactly
+         * zero (f - f * 1) */
+        {
+          const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+          const double *prow = W + (size_t)k * n2;
+          for (int i = threadIdx.x >> 5; i < n; i += nw) {
+            if (i == k) continue;
+            double *row = W + (size_t)i * n2;
+            const double f = row[k];
+            __syncwarp();
+            if (f != 0.0)
+              for (int j = lane; j < n2; j += 32) row[j] -= f * prow[j];
+          }
         }
-        __syncthreads();
-        for (int i = threadIdx.x; i < n; i += blockDim.x)
-          if (i != k) W[i * n2 + k] = 0.0;
         __syncthreads();
       }
       const bool ok = !ssing;

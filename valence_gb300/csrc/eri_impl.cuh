@@ -530,6 +530,97 @@ struct QuartetShape {
   static_assert(!CTA || PER_WARP * 8 >= NCOMP * (RB == 4 ? 4 : 8), "per-warp area too small for the partial block");
 };
 
+/* Rys roots rx and scaled weights rw (2 pi^(5/2) Kp Kq / sqrt(p+q) folded
+ * in) of the primitive quartet of primitive pairs pi, qi, and 1/(p+q), in
+ * the kernel arithmetic R: FP64 from the FP64 tables; FP32 from their FP32
+ * roundings; double-float with no FP64 instruction.  UR: unroll count of the
+ * loops over roots (1 keeps the code small where rx, rw live in shared
+ * memory; full unrolling keeps them in registers). */
+template <typename R, int NR, int UR>
+__device__ __forceinline__ void prim_roots(const EriArgs &args, const PrimT<R> *__restrict__ primR, int pi, int qi,
+                                           R *rx, R *rw, R &ripq) {
+  if constexpr (std::is_same<R, double>::value) {
+    const double two_pi_25 = 34.98683665524972; /* 2 pi^(5/2) */
+    const PrimPair &pp = args.prims[pi];
+    const PrimPair &qq = args.prims[qi];
+    const double p = pp.p, q = qq.p;
+    const double ipq = 1.0 / (p + q);
+    const double dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
+    const double Tb = p * q * ipq * (dx * dx + dy * dy + dz * dz);
+    const double pref = two_pi_25 * pp.Kp * qq.Kp * sqrt(ipq);
+#pragma unroll UR
+    for (int rr = 0; rr < NR; ++rr) {
+      double u, w;
+      rys_root(NR, rr, Tb, args.rys, args.rc, u, w);
+      rx[rr] = R(u);
+      rw[rr] = R(w * pref);
+    }
+    ripq = R(ipq);
+  } else if constexpr (std::is_same<R, float>::value) {
+    /* FP32 kernels: roots, weights and prefactor in FP32 */
+    const PrimT<float> &pp = primR[pi];
+    const PrimT<float> &qq = primR[qi];
+    const float ipq = 1.f / (pp.p + qq.p);
+    const float dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
+    const float Tb = pp.p * qq.p * ipq * (dx * dx + dy * dy + dz * dz);
+    const float pref = 34.98683665f /* 2 pi^(5/2) */ * pp.Kp * qq.Kp * sqrtf(ipq);
+    if (Tb < (float)RYS_TMAX_D) {
+      const int j = max(0, min((int)(Tb * (float)(1.0 / RYS_H_D)), (int)(RYS_TMAX_D / RYS_H_D) - 1));
+      const float t = (Tb - (float)(j * RYS_H_D)) * (float)(2.0 / RYS_H_D) - 1.f;
+      const float sc = rsqrtf(1.f + Tb);
+      const float *c = args.rys32 + args.rc.off[NR - 1] + (size_t)j * (2 * NR) * RYS_NCHEB_D;
+#pragma unroll UR
+      for (int rr = 0; rr < NR; ++rr) {
+        rx[rr] = clenshaw12_f4(c + rr * RYS_NCHEB_D, t) * sc * sc;
+        rw[rr] = clenshaw12_f4(c + (NR + rr) * RYS_NCHEB_D, t) * sc * pref;
+      }
+    } else {
+      const float sc = rsqrtf(Tb);
+#pragma unroll UR
+      for (int rr = 0; rr < NR; ++rr) {
+        rx[rr] = args.rc.axf[NR - 1][rr].x * sc * sc;
+        rw[rr] = args.rc.awf[NR - 1][rr].x * sc * pref;
+      }
+    }
+    ripq = ipq;
+  } else {
+    /* double-float throughout: no FP64 instruction on this path */
+    const PrimT<df64> &pp = args_primdf(args)[pi];
+    const PrimT<df64> &qq = args_primdf(args)[qi];
+    const df64 pq = pp.p + qq.p;
+    const df64 ipq = df_recip(pq);
+    const df64 dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
+    const df64 Tb = pp.p * qq.p * ipq * (dx * dx + dy * dy + dz * dz);
+    const df64 pref = df64(34.98683547973633f, 1.1755134e-06f) /* 2 pi^(5/2) */ * pp.Kp * qq.Kp * df_sqrt(ipq);
+    const float Tf = Tb.hi;
+    df64 t(0.f), sc(0.f);
+    int j = 0;
+    if (Tf < (float)RYS_TMAX_D) {
+      j = (int)(Tf * (float)(1.0 / RYS_H_D));
+      /* guard the interval choice against hi-part rounding at its edge */
+      const df64 tj = Tb - df64((float)(j * RYS_H_D));
+      if (tj.hi < 0.f) {
+        --j;
+      } else if (tj.hi >= (float)RYS_H_D) {
+        ++j;
+      }
+      j = max(0, min(j, (int)(RYS_TMAX_D / RYS_H_D) - 1));
+      t = (Tb - df64((float)(j * RYS_H_D))) * df64((float)(2.0 / RYS_H_D)) - df64(1.f);
+      sc = df_rsqrt(Tb + df64(1.f));
+    } else {
+      sc = df_rsqrt(Tb);
+    }
+#pragma unroll UR
+    for (int rr = 0; rr < NR; ++rr) {
+      df64 x, w;
+      rys_root_df(NR, rr, j, Tf < (float)RYS_TMAX_D, t, sc, args.rysdf, args.rc, x, w);
+      rx[rr] = from_df<R>(x);
+      rw[rr] = from_df<R>(w * pref);
+    }
+    ripq = from_df<R>(ipq);
+  }
+}
+
 /*
  * MODE 0: forward transform into U.
  * MODE 1: Schwarz diagonal -- qmax_out[P] = sqrt(max_ab |(ab|ab)|).
@@ -540,7 +631,6 @@ template <int LA, int LB, int LC, int LD, typename R, int MODE>
 __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int4 *__restrict__ work, int nwork) {
   using S = QuartetShape<LA, LB, LC, LD, sizeof(R)>;
   constexpr bool CTA = S::CTA;
-  constexpr bool DFROOT = !std::is_same<R, double>::value;
   extern __shared__ double smem[];
   double *wbase = smem;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -555,7 +645,6 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   int lexp[3];
   list_exp(S::ROWM ? LA : LC, lfun, lexp);
   R *h2d = reinterpret_cast<R *>(ws);
-  const double two_pi_25 = 34.98683665524972; /* 2 pi^(5/2) */
   const PrimT<R> *__restrict__ primR = static_cast<const PrimT<R> *>(prec_data<R>::prim(args));
   const GeomT<R> *__restrict__ geomR = static_cast<const GeomT<R> *>(prec_data<R>::geom(args));
 
@@ -634,85 +723,8 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
         if (lane < nch) {
           const int pqi = plist[lane];
           const int ip = pqi / Q.nprim, iq = pqi - ip * Q.nprim;
-          if constexpr (!DFROOT) {
-            const PrimPair &pp = args.prims[P.prim0 + ip];
-            const PrimPair &qq = args.prims[Q.prim0 + iq];
-            const double p = pp.p, q = qq.p;
-            const double ipq = 1.0 / (p + q);
-            const double dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
-            const double Tb = p * q * ipq * (dx * dx + dy * dy + dz * dz);
-            const double pref = two_pi_25 * pp.Kp * qq.Kp * sqrt(ipq);
-#pragma unroll 1
-            for (int rr = 0; rr < S::NR; ++rr) {
-              double u, w;
-              rys_root(S::NR, rr, Tb, args.rys, args.rc, u, w);
-              rx[lane * S::NR + rr] = R(u);
-              rw[lane * S::NR + rr] = R(w * pref);
-            }
-            ripq[lane] = R(ipq);
-          } else if constexpr (std::is_same<R, float>::value) {
-            /* FP32 kernels: roots, weights and prefactor in FP32 */
-            const PrimT<float> &pp = primR[P.prim0 + ip];
-            const PrimT<float> &qq = primR[Q.prim0 + iq];
-            const float ipq = 1.f / (pp.p + qq.p);
-            const float dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
-            const float Tb = pp.p * qq.p * ipq * (dx * dx + dy * dy + dz * dz);
-            const float pref = 34.98683665f /* 2 pi^(5/2) */ * pp.Kp * qq.Kp * sqrtf(ipq);
-            if (Tb < (float)RYS_TMAX_D) {
-              const int j = max(0, min((int)(Tb * (float)(1.0 / RYS_H_D)), (int)(RYS_TMAX_D / RYS_H_D) - 1));
-              const float t = (Tb - (float)(j * RYS_H_D)) * (float)(2.0 / RYS_H_D) - 1.f;
-              const float sc = rsqrtf(1.f + Tb);
-              const float *c = args.rys32 + args.rc.off[S::NR - 1] + (size_t)j * (2 * S::NR) * RYS_NCHEB_D;
-#pragma unroll 1
-              for (int rr = 0; rr < S::NR; ++rr) {
-                rx[lane * S::NR + rr] = clenshaw12_f4(c + rr * RYS_NCHEB_D, t) * sc * sc;
-                rw[lane * S::NR + rr] = clenshaw12_f4(c + (S::NR + rr) * RYS_NCHEB_D, t) * sc * pref;
-              }
-            } else {
-              const float sc = rsqrtf(Tb);
-#pragma unroll 1
-              for (int rr = 0; rr < S::NR; ++rr) {
-                rx[lane * S::NR + rr] = args.rc.axf[S::NR - 1][rr].x * sc * sc;
-                rw[lane * S::NR + rr] = args.rc.awf[S::NR - 1][rr].x * sc * pref;
-              }
-            }
-            ripq[lane] = ipq;
-          } else {
-            /* double-float throughout: no FP64 instruction on this path */
-            const PrimT<df64> &pp = args_primdf(args)[P.prim0 + ip];
-            const PrimT<df64> &qq = args_primdf(args)[Q.prim0 + iq];
-            const df64 pq = pp.p + qq.p;
-            const df64 ipq = df_recip(pq);
-            const df64 dx = pp.P[0] - qq.P[0], dy = pp.P[1] - qq.P[1], dz = pp.P[2] - qq.P[2];
-            const df64 Tb = pp.p * qq.p * ipq * (dx * dx + dy * dy + dz * dz);
-            const df64 pref = df64(34.98683547973633f, 1.1755134e-06f) /* 2 pi^(5/2) */ * pp.Kp * qq.Kp * df_sqrt(ipq);
-            const float Tf = Tb.hi;
-            df64 t(0.f), sc(0.f);
-            int j = 0;
-            if (Tf < (float)RYS_TMAX_D) {
-              j = (int)(Tf * (float)(1.0 / RYS_H_D));
-              /* guard the interval choice against hi-part rounding at its edge */
-              const df64 tj = Tb - df64((float)(j * RYS_H_D));
-              if (tj.hi < 0.f) {
-                --j;
-              } else if (tj.hi >= (float)RYS_H_D) {
-                ++j;
-              }
-              j = max(0, min(j, (int)(RYS_TMAX_D / RYS_H_D) - 1));
-              t = (Tb - df64((float)(j * RYS_H_D))) * df64((float)(2.0 / RYS_H_D)) - df64(1.f);
-              sc = df_rsqrt(Tb + df64(1.f));
-            } else {
-              sc = df_rsqrt(Tb);
-            }
-#pragma unroll 1
-            for (int rr = 0; rr < S::NR; ++rr) {
-              df64 x, w;
-              rys_root_df(S::NR, rr, j, Tf < (float)RYS_TMAX_D, t, sc, args.rysdf, args.rc, x, w);
-              rx[lane * S::NR + rr] = from_df<R>(x);
-              rw[lane * S::NR + rr] = from_df<R>(w * pref);
-            }
-            ripq[lane] = from_df<R>(ipq);
-          }
+          prim_roots<R, S::NR, 1>(args, primR, P.prim0 + ip, Q.prim0 + iq, rx + lane * S::NR, rw + lane * S::NR,
+                                  ripq[lane]);
         }
       }
       __syncwarp();
@@ -1042,6 +1054,148 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   }
 }
 
+
+/*
+ * Block mode, low classes (s and p pairs with at most 27 (e0|f0)
+ * components): one lane per shell quartet.  The lane walks the quartet's
+ * primitive quartets inside [prim_lo, prim_hi) of the primitive bound
+ * (smallest bounds first in FP32), with roots, 2D tables and the component
+ * sums in registers; then the transfer to (ab|cd) in closed form for s and
+ * p, (a b| = (a+b, 0| + (A-B)_b (a 0| (Head-Gordon & Pople), and the block
+ * is added into the atom quartet's staging block as mode 4 does.  Against
+ * the warp kernels this drops the shared-memory tables, the compaction
+ * ballots and the warp synchronisation that dominate these small classes.
+ */
+template <int LA, int LB>
+struct LanePair {
+  static constexpr int NE = ne_c(LA, LB);
+};
+
+/* (ab| from the (e0| list of a pair (la >= lb, both <= 1): e indexes the
+ * functions of angular momentum la .. la+lb in CCA order */
+template <int LA, int LB>
+__device__ __forceinline__ double lane_hrr(int a, int b, const double *e, const double AB[3]) {
+  if constexpr (LB == 0) {
+    return e[a];
+  } else {
+    /* la = lb = 1: (a b| = (a+b, 0| + AB_b (a 0|, the 6 d functions after the 3 p */
+    constexpr int dix[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    return e[3 + dix[a][b]] + AB[b] * e[a];
+  }
+}
+
+template <int LA, int LB, int LC, int LD, typename R>
+__global__ void __launch_bounds__(128) eri_lane_kernel(EriArgs args, const int4 *__restrict__ work, int nwork) {
+  constexpr int LAB = LA + LB, LCD = LC + LD, NR = (LAB + LCD) / 2 + 1;
+  constexpr int NEA = LanePair<LA, LB>::NE, NEC = LanePair<LC, LD>::NE;
+  constexpr bool ASC = std::is_same<R, float>::value;
+  const PrimT<R> *__restrict__ primR = static_cast<const PrimT<R> *>(prec_data<R>::prim(args));
+  const GeomT<R> *__restrict__ geomR = static_cast<const GeomT<R> *>(prec_data<R>::geom(args));
+  const float eps = args.prim_lo, eps_hi = args.prim_hi;
+  for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < nwork; item += gridDim.x * blockDim.x) {
+    const int4 pq = work[item];
+    const ShellPair &P = args.pairs[pq.x];
+    const ShellPair &Q = args.pairs[pq.y];
+    const int np_ = P.nprim, nq_ = Q.nprim;
+    const float *q0p = args.prim_q0 + P.prim0, *q0q = args.prim_q0 + Q.prim0;
+    R acc[NEA][NEC];
+#pragma unroll
+    for (int e = 0; e < NEA; ++e)
+#pragma unroll
+      for (int f = 0; f < NEC; ++f) acc[e][f] = R(0);
+    R Ad[3], Cd[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      Ad[k] = geomR[pq.x].A[k];
+      Cd[k] = geomR[pq.y].A[k];
+    }
+    for (int k0 = 0; k0 < np_ * nq_; ++k0) {
+      /* FP32: smallest bounds (highest indices of the sorted primitives) first */
+      const int k = ASC ? np_ * nq_ - 1 - k0 : k0;
+      const int ip = k / nq_, iq = k - ip * nq_;
+      const float b = q0p[ip] * q0q[iq];
+      if (!(b >= eps && b < eps_hi)) continue;
+      R rx[NR], rw[NR], ipq;
+      prim_roots<R, NR, NR>(args, primR, P.prim0 + ip, Q.prim0 + iq, rx, rw, ipq);
+      const PrimT<R> &pr = primR[P.prim0 + ip], &qr = primR[Q.prim0 + iq];
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const R uq = rx[r] * ipq;
+        const R b00 = R(0.5f) * uq;
+        const R b10 = R(0.5f) * pr.inv_p * (R(1) - qr.p * uq);
+        const R b01 = R(0.5f) * qr.inv_p * (R(1) - pr.p * uq);
+        R G[3][(LAB + 1) * (LCD + 1)];
+#pragma unroll
+        for (int dir = 0; dir < 3; ++dir) {
+          const R Pd = pr.P[dir], Qd = qr.P[dir], PQ = Pd - Qd;
+          const R c00 = (Pd - Ad[dir]) - qr.p * uq * PQ;
+          const R d00 = (Qd - Cd[dir]) + pr.p * uq * PQ;
+          rys_g<LAB, LCD, R, 1, LCD + 1>(dir == 2 ? rw[r] : R(1), c00, d00, b00, b10, b01, G[dir]);
+        }
+        static_for<NEA>([&](auto ec) {
+          constexpr int e = decltype(ec)::value;
+          constexpr int ex = cexp(LA, e, 0), ey = cexp(LA, e, 1), ez = cexp(LA, e, 2);
+          static_for<NEC>([&](auto fc) {
+            constexpr int f = decltype(fc)::value;
+            constexpr int fx = cexp(LC, f, 0), fy = cexp(LC, f, 1), fz = cexp(LC, f, 2);
+            acc3(acc[e][f], G[0][ex * (LCD + 1) + fx], G[1][ey * (LCD + 1) + fy], G[2][ez * (LCD + 1) + fz]);
+          });
+        });
+      }
+    }
+    /* transfer to (ab|cd) and the staging block (mode 4 places) */
+    double E[NEA * NEC];
+#pragma unroll
+    for (int e = 0; e < NEA; ++e)
+#pragma unroll
+      for (int f = 0; f < NEC; ++f) E[e * NEC + f] = to_double(acc[e][f]);
+    double ABp[3], ABq[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      ABp[k] = P.A[k] - P.B[k];
+      ABq[k] = Q.A[k] - Q.B[k];
+    }
+    const int4 bp = __ldg(args.pair_blk + pq.x), bq = __ldg(args.pair_blk + pq.y);
+    const int ncol = pq.w & 0xFFFFF;
+    const bool swp = (pq.w >> 20) & 1, dg = ((pq.w >> 21) & 1) && pq.x != pq.y;
+    double *Gq = args.G + (unsigned)pq.z;
+#pragma unroll
+    for (int c = 0; c < NC<LC>::v; ++c)
+#pragma unroll
+      for (int d = 0; d < NC<LD>::v; ++d) {
+        /* the ket transfer: Y[e] = (e0|cd) */
+        double Y[NEA];
+#pragma unroll
+        for (int e = 0; e < NEA; ++e) Y[e] = lane_hrr<LC, LD>(c, d, E + e * NEC, ABq);
+        int cols[2];
+        const int nc = blk_places(bq, c, d, cols);
+#pragma unroll
+        for (int a = 0; a < NC<LA>::v; ++a)
+#pragma unroll
+          for (int bb = 0; bb < NC<LB>::v; ++bb) {
+            const double v = lane_hrr<LA, LB>(a, bb, Y, ABp);
+            int rows[2];
+            const int nr = blk_places(bp, a, bb, rows);
+            for (int i = 0; i < nr; ++i)
+              for (int j = 0; j < nc; ++j) {
+                const size_t pq_at = (size_t)rows[i] * ncol + cols[j], qp_at = (size_t)cols[j] * ncol + rows[i];
+                atomicAdd(Gq + (swp ? qp_at : pq_at), v);
+                if (dg) atomicAdd(Gq + (swp ? pq_at : qp_at), v);
+              }
+          }
+      }
+  }
+}
+
+template <int LA, int LB, int LC, int LD, typename R>
+int launch_lane(const EriArgs &args, const int4 *work, int nwork, int max_blocks, cudaStream_t st) {
+  if (nwork <= 0) return 0;
+  int blocks = (nwork + 127) / 128;
+  if (blocks > max_blocks) blocks = max_blocks;
+  eri_lane_kernel<LA, LB, LC, LD, R><<<blocks, 128, 0, st>>>(args, work, nwork);
+  return cudaGetLastError() != cudaSuccess;
+}
+
 template <int LA, int LB, int LC, int LD, typename R, int MODE>
 int launch_one(const EriArgs &args, const int4 *work, int nwork, int max_blocks, cudaStream_t st) {
   if (nwork <= 0) return 0;
@@ -1075,13 +1229,16 @@ int launch_cls(const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStrea
   return launch_one<ClsL<CP>::a, ClsL<CP>::b, ClsL<CQ>::a, ClsL<CQ>::b, R, MODE>(a, w, n, max_blocks, st);
 }
 
-/* block mode: s and p pair classes only */
+/* block mode: s and p pair classes only; up to 27 (e0|f0) components one
+ * lane per shell quartet, (pp|pp) on the CTA kernel */
 template <typename R>
 int dispatch_blk(int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st) {
-#define CASE(X, Y) \
-  if (cp == X && cq == Y) return launch_cls<X, Y, R, 4>(a, w, n, max_blocks, st);
-  CASE(0, 0) CASE(1, 0) CASE(1, 1) CASE(2, 0) CASE(2, 1) CASE(2, 2)
-#undef CASE
+  if (cp == 0 && cq == 0) return launch_lane<0, 0, 0, 0, R>(a, w, n, max_blocks, st);
+  if (cp == 1 && cq == 0) return launch_lane<1, 0, 0, 0, R>(a, w, n, max_blocks, st);
+  if (cp == 1 && cq == 1) return launch_lane<1, 0, 1, 0, R>(a, w, n, max_blocks, st);
+  if (cp == 2 && cq == 0) return launch_lane<1, 1, 0, 0, R>(a, w, n, max_blocks, st);
+  if (cp == 2 && cq == 1) return launch_lane<1, 1, 1, 0, R>(a, w, n, max_blocks, st);
+  if (cp == 2 && cq == 2) return launch_cls<2, 2, R, 4>(a, w, n, max_blocks, st);
   return 2;
 }
 

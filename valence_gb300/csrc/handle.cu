@@ -696,8 +696,13 @@ int build_block(vsvb_gpu *h, const vsvb_system_desc *d, const std::vector<GShell
     for (int a = 0; a < 3; ++a)
       for (int cq = 0; cq <= a; ++cq)
         for (int prec = 0; prec < 2; ++prec) {
-          const auto &v = lst[a][cq][prec];
+          auto &v = lst[a][cq][prec];
           if (v.empty()) continue;
+          /* most primitive quartets first: neighbouring lanes of the
+           * one-lane-per-quartet kernels get similar work */
+          std::stable_sort(v.begin(), v.end(), [&](const int4 &x, const int4 &y) {
+            return pairs[x.x].nprim * pairs[x.y].nprim > pairs[y.x].nprim * pairs[y.y].nprim;
+          });
           const long long o = off[(size_t)c * 18 + (a * 3 + cq) * 2 + prec];
           if (cudaMemcpy(h->blk_work.p + o, v.data(), sizeof(int4) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess)
             fill_err = 1;
@@ -1548,6 +1553,7 @@ int block_sweep(vsvb_gpu *h) {
   ba.nfmax = h->blk_nfmax;
   ba.nomax = h->blk_nomax;
   ba.r1n = blk_r1(h->blk_nfmax, h->blk_nomax);
+  ba.nomaxp = (h->blk_nomax + 7) / 8 * 8;
   int rr = 0;
   for (size_t c = 0; c < h->blk_chunk.size(); ++c) {
     const auto &ch = h->blk_chunk[c];
@@ -1616,7 +1622,8 @@ int forward(vsvb_gpu *h, bool fused = false) {
   CK(cudaMemsetAsync(h->xcount.p, 0, sizeof(int), st), "memset pool count");
   CK(cudaMemsetAsync(h->nsing.p, 0, sizeof(int), st), "memset nsing");
   DetCtx dc = det_ctx(h);
-  detpair_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, h->scratch.p, h->ld_scratch);
+  detpair_kernel<<<(unsigned)h->ds.nq, std::max(h->ds.nalpha, h->ds.nbeta) > 64 ? 512 : 128, 0, st>>>(
+      dc, h->scratch.p, h->ld_scratch);
   CK(cudaGetLastError(), "detpair");
   h->launches++;
   if (fused) {
