@@ -1,34 +1,43 @@
-"""Benchmark: VSVB energy+gradient evaluations per second on one GB300.
+"""Benchmark: VSVB evaluations per second on one GB300, mixed precision
+against plain FP64.
 
-Workload (default): the spin-coupled C/H chain -- 8 atoms alternating Z=6/1
-at 1.1 A, 4 Rumer-coupled pairs (16 determinants per side, 256 determinant
-pairs) + 8 DOCC, s/p/d basis of 104 Cartesian functions, 3-6 primitives per
-shell; seeded synthetic weights (valence_gb300.configs.ch_chain, seed 2).
-A step is one energy + adjoint gradient with respect to all 416 orbital
-weights.  The headline value uses the mixed path (VSVB_MIXED_DF64: FP32 for
-shell quartets whose Schwarz bound is below 1e-6, double-float -- pairs of
-FP32 numbers, ~48-bit -- for the rest, Rys roots in double-float); the plain
-FP64 path and the FP32 + native-FP64 split (VSVB_MIXED) are timed beside it,
-and |dE| of each against FP64 is reported.
+Workload (default, the largest configuration that runs on one GPU): the
+64-atom Li/F cluster -- a 4x4x4 grid of alternating Z=3/Z=9 atoms at 2.0 A,
+s/p basis of 576 Cartesian functions (3s 2p per atom, 3-6 primitives,
+exponents log-uniform in [0.05, 1e4]), 304 doubly occupied orbitals on 1-2
+atoms with seeded uniform(-1, 1) weights, integral screen 1e-12
+(valence_gb300.configs.lif_cluster, seed 3).  That configuration defines an
+energy evaluation (no gradient), so a step is one guess energy: 1.07e9
+orbital-quartet tasks over a 46,360 x 46,360 orbital-pair ERI matrix built in
+block mode (vsvb_options.block_mode).  --workload ch_chain runs the
+spin-coupled C/H chain (104 functions, 4 Rumer pairs, 256 determinant pairs)
+with a step of one energy + adjoint gradient; its figures are also reported
+under "ch_chain" in the default line.
 
-  value          device-resident weights (vsvb_gpu_energy_grad_device)
-  e2e            public host API (vsvb_gpu_energy_grad): pinned host weights
-                 copied in and the energy + gradient copied out every step
-  roofline       dominant ERI class launch of the headline steps: algorithmic
-                 FLOPs / its CUDA-event time inside the timed steps (events
-                 on the side stream it runs on), against the FP64 or FP32 FMA
-                 rate measured on this device by vsvb_gpu_fma_peak
-                 (MEASURED_PEAKS.json carries only HBM and bf16 figures); for
-                 a double-float launch the roofline is that FP32 instruction
-                 rate x 3 flops / 16 instructions per component update
+The headline value is the mixed path (VSVB_MIXED_DF64: FP32 for shell
+quartets whose Schwarz bound is below 1e-6, double-float -- pairs of FP32
+numbers, ~48-bit -- for the rest); the plain FP64 path and the FP32 +
+native-FP64 split (VSVB_MIXED) are timed beside it, and |dE| of each against
+FP64 is reported.
+
+  value          device-resident weights
+  e2e            public host API (vsvb_gpu_energy / vsvb_gpu_energy_grad):
+                 pinned host weights copied in and the results copied out
+                 every step
+  roofline       block mode: the ERI launches and atom-quartet transforms of
+                 the step (fork to join, CUDA events on the stream the
+                 library launches on), algorithmic FLOPs per kind against the
+                 FMA rates measured on this device (vsvb_gpu_fma_peak);
+                 per-quartet mode: the ERI sweep's class launches
   cpu_baseline   the CPU oracle (a literal C restatement of the reference,
-                 energy only -- the reference has no gradient) on all host
-                 cores, one full evaluation
+                 energy only) on all host cores: one full evaluation where it
+                 finishes in seconds; on the cluster a bounded sample of every
+                 phase (Schwarz table, one-electron loop, task loop),
+                 extrapolated phase by phase and labelled so
 
 --impl reference times that CPU restatement on the same workload and prints
-the same metric (energy evaluations per second).
-Multi-GPU (torchrun): independent replicas, one per rank ("weak" scaling);
-the path needs no collective.
+the same metric.  Multi-GPU (torchrun): independent replicas, one per rank
+("weak" scaling); the path needs no collective.
 """
 import argparse
 import json
@@ -44,6 +53,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "VSVB energy+grad evals/s, mixed vs plain FP64 on 1 GB300 at |ΔE|<=1e-6 Eh"
+# workloads whose configuration defines an energy evaluation only (block mode)
+ENERGY_ONLY = {"lif_cluster"}
+# bounded CPU-oracle samples per phase (Schwarz entries, one-electron terms,
+# two-electron tasks) for workloads whose full CPU evaluation takes hours
+CPU_SAMPLE = {"lif_cluster": (16, 16, 12)}
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the ERI class
@@ -117,7 +131,7 @@ def _args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ch_chain")
+    ap.add_argument("--workload", default="lif_cluster")
     ap.add_argument("--mixed-threshold", type=float, default=1e-6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
@@ -197,55 +211,130 @@ def _oracle_energy_time(path, nthreads):
     return dt, e
 
 
+def _oracle_sampled_time(path, nthreads, samples):
+    """Extrapolated CPU-oracle seconds of one full evaluation from bounded
+    samples of every phase: every k-th Schwarz entry, one-electron term and
+    two-electron task (vo_guess_energy_timed); each phase's time is scaled by
+    its own sampling factor, the set-up counts once."""
+    import math
+
+    from tests import oracle_py
+    from valence_gb300 import configs
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    dsc = configs.describe(path)
+    nsp = dsc["spatial_orbitals"]
+    nelec = 2 * (dsc["coupled_pairs"] + dsc["docc"]) + dsc["unpaired"]
+    npairs = nsp * (nsp + 1) // 2
+    n1, ntasks = nelec * nelec, npairs * (npairs + 1) // 2
+    totals = (npairs, n1, ntasks)
+    strides = tuple(max(1, n // k) for n, k in zip(totals, samples))
+    o = oracle_py.Oracle(path)
+    t = time.perf_counter()
+    _, ph = o.guess_energy_timed(nthreads, *strides)
+    wall = time.perf_counter() - t
+    visited = [math.ceil(n / st) for n, st in zip(totals, strides)]
+    full = ph[0] + sum(ph[k + 1] * totals[k] / visited[k] for k in range(3))
+    sample = (f"extrapolated: the CPU oracle (literal C restatement of valence.F90's guess energy, energy only) "
+              f"timed on every {strides[0]}th Schwarz entry ({visited[0]} of {npairs}), every {strides[1]}th "
+              f"one-electron term ({visited[1]} of {n1}) and every {strides[2]}th task ({visited[2]} of {ntasks}); "
+              f"each phase scaled by its sampling factor, set-up once; phase seconds {[round(x, 3) for x in ph]}, "
+              f"sample wall {wall:.1f} s")
+    return full, wall, sample
+
+
+def _cpu_seconds(workload, path, cores):
+    """(seconds of one full CPU-oracle evaluation, sample description)."""
+    if workload in CPU_SAMPLE:
+        full, _, sample = _oracle_sampled_time(path, cores, CPU_SAMPLE[workload])
+        return full, sample
+    dt, _ = _oracle_energy_time(path, cores)
+    return dt, ("one full energy evaluation of the same workload by the CPU oracle (literal C restatement of "
+                "valence.F90's guess energy, cached AO shell-quartet blocks); energy only, the reference has no "
+                "gradient")
+
+
+def _config(a, workload, path, world):
+    import inspect
+
+    from valence_gb300 import configs
+    c = {"workload": workload,
+         "seed": inspect.signature(configs.WORKLOADS[workload]).parameters["seed"].default}
+    c.update(configs.describe(path))
+    c["step"] = ("one guess energy (the configuration defines no gradient)" if workload in ENERGY_ONLY
+                 else "one energy + adjoint gradient with respect to every weight")
+    c.update({"mixed_threshold": a.mixed_threshold, "l2": "flushed (256 MB write) between timed steps",
+              "replicas": world})
+    return c
+
+
 def run_reference(a, rank, world):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    steps = max(1, min(a.steps, 3))
+    steps = max(1, min(a.steps, 2 if a.workload in CPU_SAMPLE else 3))
     with tempfile.TemporaryDirectory() as d:
         path = _workload(a.workload, d)
         times = []
         for _ in range(steps):
-            dt, e = _oracle_energy_time(path, cores)
+            dt, sample = _cpu_seconds(a.workload, path, cores)
             times.append(dt)
+        cfg = _config(a, a.workload, path, world)
     v = 1.0 / statistics.mean(times)
-    sample = (f"{steps} full energy evaluation(s) of the {a.workload} workload by the CPU oracle "
-              f"(literal C restatement of valence.F90's guess energy with cached AO shell-quartet blocks; "
-              f"energy only, the reference has no gradient); steps capped at 3")
+    sample = f"{steps} step(s), each: " + sample + f"; steps capped at {steps}"
     print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world,
                       "steps": steps, "warmup": 0, "ms_per_step": 1e3 * statistics.mean(times),
                       "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                      "data": "synthetic", "config": {"workload": a.workload, "seed": 2},
+                      "data": "synthetic", "config": cfg,
                       "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
                                        "sample": sample},
                       "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
-def run_ours(a, rank, world):
-    import numpy as np
+def block_roofline(stats, block_ms, fp64_peak, fp32_peak, step_ms):
+    """Roofline of block mode: the ERI launches (one lane per shell quartet
+    for the small s/p classes, the CTA kernel for (pp|pp)) and the
+    per-atom-quartet transforms of one step, chunk after chunk, on 6 side
+    streams and the handle's stream, timed fork to join by CUDA events on
+    those streams (block_ms per step).  Per kind the bound rate for the
+    algorithmic FLOPs: ERIs as in eri_roofline (FMA instruction rate x 3
+    flops per component update / 2 instructions, 16 in double-float);
+    transforms FP64 / FP32 at the FMA FLOP rate, double-float at 2 flops per
+    multiply-add of 12 FP32 instructions.  T* = sum W_kind / P_kind,
+    frac = T* / T_block."""
+    rate = {("eri", "fp64"): fp64_peak / 2 * 3 / 2, ("eri", "fp32"): fp32_peak / 2 * 3 / 2,
+            ("eri", "df64"): fp32_peak / 2 * 3 / 16, ("transform", "fp64"): fp64_peak,
+            ("transform", "fp32"): fp32_peak, ("transform", "df64"): fp32_peak / 12}
+    W = {("eri", k): v for k, v in stats["eri_flops"].items()}
+    W.update({("transform", k): v for k, v in stats["transform_flops"].items()})
+    t_star = sum(W[k] / rate[k] for k in W)
+    t_block = statistics.mean(block_ms) * 1e-3
+    w_tot = sum(W.values())
+    return {"bound": "fp32_pipe",
+            "kernel": "block mode: eri_lane_kernel / eri_kernel<1,1,1,1,*,4> ERI launches and "
+                      "blk_transform_kernel per chunk of atom quartets (one step: "
+                      f"{stats['chunks']} chunks, {stats['launches']} launches)",
+            "achieved": w_tot / t_block / 1e12, "peak": w_tot / t_star / 1e12, "unit": "TFLOP/s",
+            "frac": t_star / t_block,
+            "achieved_unit_note": "algorithmic FLOPs (eri_flops per primitive quartet + transfer; four quarter "
+                                  "transforms per atom quartet) per second of the block phase",
+            "peak_basis": "T* = sum over kinds of W_kind / P_kind with the FMA rates of vsvb_gpu_fma_peak",
+            "flops_per_step": {f"{a}_{b}": v for (a, b), v in W.items()},
+            "block_phase_ms": t_block * 1e3, "share_of_step": t_block * 1e3 / step_ms,
+            "traffic": PROFILED_TRAFFIC.get(("lif_cluster", "transform_df64")),
+            "traffic_note": "dram read+write bytes per launch of blk_transform_kernel<df64> (one chunk of atom "
+                            "quartets), from the ncu capture summarised in profiles/",
+            "fp64_fma_tflops": fp64_peak / 1e12, "fp32_fma_tflops": fp32_peak / 1e12}
+
+
+def measure(a, workload, world, dev, stream, flush, steps, warmup, side_steps, side_warmup):
+    """One workload: the mixed (double-float) arm over exactly `steps` timed
+    steps with its roofline timing, then the FP64 and VSVB_MIXED arms
+    (side_steps each) and the host-API arm (steps), one handle at a time."""
     import torch
 
     import valence_gb300 as vg
     from valence_gb300 import api
-
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 126 MB L2
-
-    with tempfile.TemporaryDirectory() as d:
-        path = _workload(a.workload, d)
-        s64 = vg.System(path, precision=vg.FP64, device=dev)
-        smx = vg.System(path, precision=vg.MIXED_DF64, mixed_threshold=a.mixed_threshold, device=dev)
-        smn = vg.System(path, precision=vg.MIXED, mixed_threshold=a.mixed_threshold, device=dev)
-    n = s64.totlen
-    w_dev = torch.from_numpy(s64.coeff0.copy()).to("cuda")
-    g_dev = torch.zeros(n, dtype=torch.float64, device="cuda")
-    w_pin = torch.from_numpy(s64.coeff0.copy()).pin_memory()
-    g_pin = torch.zeros(n, dtype=torch.float64).pin_memory()
-    for s in (s64, smx, smn):
-        s.set_stream(stream.cuda_stream)
+    grad = workload not in ENERGY_ONLY
 
     def timed(fn, steps, warmup, after_step=None):
         for _ in range(warmup):
@@ -271,98 +360,170 @@ def run_ours(a, rank, world):
             torch.distributed.barrier()
         return ms, launches, last
 
-    dev_step = lambda s: (lambda: s.energy_grad_device(w_dev.data_ptr(), g_dev.data_ptr()))
-
-    def host_step(s):
-        def f():
-            r = api.Result()
-            rc = api.lib().vsvb_gpu_energy_grad(s._h, w_pin.numpy().ctypes.data_as(api.ctypes.POINTER(api.ctypes.c_double)),
-                                                api.ctypes.byref(r),
-                                                g_pin.numpy().ctypes.data_as(api.ctypes.POINTER(api.ctypes.c_double)))
-            if rc:
-                raise api.VSVBError(api.lib().vsvb_gpu_last_error(s._h).decode())
-            return r.as_dict()
-        return f
-
-    # per-class ERI launch times inside the timed steps (CUDA events on the
-    # side stream each class runs on, read back after each step)
-    sweep = {}
-    sweep_wall = []
-
-    def collect():
-        for x in smx.sweep_times():
-            acc = sweep.setdefault(x["cls"], [0.0, 0.0, 0])
-            acc[0] += x["ms"]
-            acc[1] += x["flops"]
-            acc[2] += 1
-        sweep_wall.append(smx.sweep_wall_ms())
-
-    smx.set_sweep_timing(True)
-    clk = Clocks(dev)
-    clk.start()
-    ms_mx, launches_mx, r_mx = timed(dev_step(smx), a.steps, a.warmup, after_step=collect)
-    clocks = clk.stop()
-    smx.set_sweep_timing(False)
-    if a.headline_only:
-        ms_64, r_64, ms_mn, r_mn, ms_e2e = ms_mx, r_mx, ms_mx, r_mx, ms_mx
-    else:
-        ms_64, _, r_64 = timed(dev_step(s64), a.steps, a.warmup)
-        ms_mn, _, r_mn = timed(dev_step(smn), a.steps, a.warmup)
-        ms_e2e, _, r_e2e = timed(host_step(smx), a.steps, a.warmup)
-
     def agg(ms):
         t = torch.tensor([sum(ms)], dtype=torch.float64, device="cuda")
         if world > 1:
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         return t.item()
 
-    t_mx, t_64, t_e2e, t_mn = agg(ms_mx), agg(ms_64), agg(ms_e2e), agg(ms_mn)
-    value = world * a.steps / (t_mx * 1e-3)
-    v64 = world * a.steps / (t_64 * 1e-3)
-    ve2e = world * a.steps / (t_e2e * 1e-3)
-    dE = abs(r_mx["energy"] - r_64["energy"])
-    vmn = world * a.steps / (t_mn * 1e-3)
+    with tempfile.TemporaryDirectory() as d:
+        path = _workload(workload, d)
+        cfg = _config(a, workload, path, world)
 
+        def system(prec):
+            s = vg.System(path, precision=prec, mixed_threshold=a.mixed_threshold, device=dev)
+            s.set_stream(stream.cuda_stream)
+            return s
+
+        def dev_step(s, w_dev, g_dev):
+            if grad:
+                return lambda: s.energy_grad_device(w_dev.data_ptr(), g_dev.data_ptr())
+            return lambda: s.energy_device(w_dev.data_ptr())
+
+        def host_step(s, w_pin, g_pin):
+            P = api.ctypes.POINTER(api.ctypes.c_double)
+
+            def f():
+                r = api.Result()
+                if grad:
+                    rc = api.lib().vsvb_gpu_energy_grad(s._h, w_pin.numpy().ctypes.data_as(P), api.ctypes.byref(r),
+                                                        g_pin.numpy().ctypes.data_as(P))
+                else:
+                    rc = api.lib().vsvb_gpu_energy(s._h, w_pin.numpy().ctypes.data_as(P), api.ctypes.byref(r))
+                if rc:
+                    raise api.VSVBError(api.lib().vsvb_gpu_last_error(s._h).decode())
+                return r.as_dict()
+            return f
+
+        out = {"config": cfg}
+        smx = system(vg.MIXED_DF64)
+        n = smx.totlen
+        w_dev = torch.from_numpy(smx.coeff0.copy()).to("cuda")
+        g_dev = torch.zeros(n, dtype=torch.float64, device="cuda")
+        w_pin = torch.from_numpy(smx.coeff0.copy()).pin_memory()
+        g_pin = torch.zeros(n, dtype=torch.float64).pin_memory()
+        stats = smx.block_stats()
+        sweep, sweep_wall = {}, []
+
+        def collect():
+            if not stats["on"]:
+                for x in smx.sweep_times():
+                    acc = sweep.setdefault(x["cls"], [0.0, 0.0, 0])
+                    acc[0] += x["ms"]
+                    acc[1] += x["flops"]
+                    acc[2] += 1
+            sweep_wall.append(smx.sweep_wall_ms())
+
+        smx.set_sweep_timing(True)
+        clk = Clocks(dev)
+        clk.start()
+        ms_mx, launches_mx, r_mx = timed(dev_step(smx, w_dev, g_dev), steps, warmup, after_step=collect)
+        out["clocks"] = clk.stop()
+        smx.set_sweep_timing(False)
+        out["ms_mx"], out["launches"], out["r_mx"] = ms_mx, launches_mx, r_mx
+        out["value"] = world * steps / (agg(ms_mx) * 1e-3)
+        fp64_peak, fp32_peak = api.fma_peak(dev)
+        if stats["on"]:
+            out["roofline"] = block_roofline(stats, sweep_wall, fp64_peak, fp32_peak, statistics.mean(ms_mx))
+        else:
+            out["roofline"] = eri_roofline(sweep, sweep_wall, fp64_peak, fp32_peak, statistics.mean(ms_mx), workload)
+        if a.headline_only:
+            smx.close()
+            return out
+        ms_e2e, _, _ = timed(host_step(smx, w_pin, g_pin), steps, warmup)
+        out["e2e"] = {"value": world * steps / (agg(ms_e2e) * 1e-3), "unit": "evals/s",
+                      "h2d_bytes_per_step": 8 * n,
+                      "d2h_bytes_per_step": (8 * n if grad else 0) + 8 * 7 + 8 * 5 + 4 * 2}
+        smx.close()
+        for name, prec in (("fp64", vg.FP64), ("mixed_native_fp64", vg.MIXED)):
+            s = system(prec)
+            ms_s, _, r_s = timed(dev_step(s, w_dev, g_dev), side_steps, side_warmup)
+            out[name] = {"value": world * side_steps / (agg(ms_s) * 1e-3), "unit": "evals/s",
+                         "ms_per_step": statistics.mean(ms_s), "steps": side_steps, "warmup": side_warmup,
+                         "energy": r_s["energy"], "err_est": r_s["err_est"]}
+            s.close()
+        e64 = out["fp64"]["energy"]
+        out["mixed_native_fp64"]["abs_dE_vs_fp64"] = abs(out["mixed_native_fp64"]["energy"] - e64)
+        out["mixed_over_fp64"] = out["value"] / out["fp64"]["value"]
+        out["mixed_native_over_fp64"] = out["mixed_native_fp64"]["value"] / out["fp64"]["value"]
+        out["abs_dE_mixed_vs_fp64"] = abs(r_mx["energy"] - e64)
+        out["err_est_mixed"] = r_mx["err_est"]
+        if world == 1 and not a.no_cpu_baseline:
+            cores = os.cpu_count() or 1
+            dt, sample = _cpu_seconds(workload, path, cores)
+            out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "evals/s", "cores": cores, "kind": "port",
+                                   "sample": sample}
+    return out
+
+
+def run_ours(a, rank, world):
+    import torch
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 126 MB L2
+    energy_only = a.workload in ENERGY_ONLY
+    # the FP64 and FP32 + native FP64 arms of an energy-only (large) workload
+    # are timed on fewer steps than the headline arm: they are reported beside
+    # it, not as the headline
+    side_steps = min(a.steps, 2) if energy_only else a.steps
+    side_warmup = 1 if energy_only else a.warmup
+    m = measure(a, a.workload, world, dev, stream, flush, a.steps, a.warmup, side_steps, side_warmup)
     if rank != 0:
         return
-    # roofline of the dominant ERI launch of the headline (mixed) run
-    fp64_peak, fp32_peak = api.fma_peak(dev)
-    roofline = eri_roofline(sweep, sweep_wall, fp64_peak, fp32_peak, statistics.mean(ms_mx), a.workload)
-    cpu = None
-    if world == 1 and not a.no_cpu_baseline:
-        with tempfile.TemporaryDirectory() as d:
-            path = _workload(a.workload, d)
-            cores = os.cpu_count() or 1
-            dt, e_cpu = _oracle_energy_time(path, cores)
-        cpu = {"value": 1.0 / dt, "unit": "evals/s", "cores": cores, "kind": "port",
-               "sample": "one full energy evaluation of the same workload by the CPU oracle (literal C restatement "
-                         "of valence.F90, cached AO blocks); energy only -- the reference has no gradient",
-               "dE_vs_gpu_fp64": abs(e_cpu - r_64["energy"])}
-    nq = r_mx["n_quartets_fp64"] + r_mx["n_quartets_fp32"]
-    out = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": a.steps,
-           "warmup": a.warmup, "ms_per_step": t_mx / a.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32 (Schwarz < 1e-6) + double-float (2xf32) elsewhere", "data": "synthetic",
-           "config": {"workload": a.workload, "seed": 2, "atoms": 8, "functions": 104, "coupled_pairs": 4,
-                      "docc": 8, "determinant_pairs": 256, "weights": n, "mixed_threshold": a.mixed_threshold,
-                      "l2": "flushed (256 MB write) between timed steps", "replicas": world},
-           "fp64": {"value": v64, "unit": "evals/s", "ms_per_step": t_64 / a.steps},
-           "mixed_native_fp64": {"value": vmn, "unit": "evals/s", "ms_per_step": t_mn / a.steps,
-                                 "abs_dE_vs_fp64": abs(r_mn["energy"] - r_64["energy"])},
-           "mixed_over_fp64": value / v64, "abs_dE_mixed_vs_fp64": dE, "energy_fp64": r_64["energy"],
-           "quartets": {"fp64": r_mx["n_quartets_fp64"], "fp32": r_mx["n_quartets_fp32"], "total": nq},
-           "e2e": {"value": ve2e, "unit": "evals/s", "h2d_bytes_per_step": 8 * n,
-                   "d2h_bytes_per_step": 8 * n + 5 * 8 + 2 * 4},
-           "gpu_launches": launches_mx, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks}
+    r = m["r_mx"]
+    out = {"metric": METRIC, "value": m["value"], "unit": "evals/s", "n_gpus": world, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": statistics.mean(m["ms_mx"]), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": ("f32 (Schwarz < 1e-6) + double-float (2xf32) elsewhere; f64 determinants and reductions"),
+           "data": "synthetic", "config": m["config"], "gpu_launches": m["launches"],
+           "roofline": m["roofline"], "clocks": m["clocks"],
+           "quartets": {"fp64": r["n_quartets_fp64"], "fp32": r["n_quartets_fp32"],
+                        "total": r["n_quartets_fp64"] + r["n_quartets_fp32"],
+                        "primitive": r["n_prim_quartets"], "primitive_fp32": r["n_prim_quartets_fp32"]},
+           "tasks": r["n_tasks"], "energy_mixed": r["energy"]}
     if a.headline_only:
-        for k in ("fp64", "mixed_native_fp64", "mixed_over_fp64", "abs_dE_mixed_vs_fp64", "energy_fp64", "e2e"):
-            out[k] = None
         out["note"] = "headline mixed arm only (per-kernel launch-list run)"
-    else:
-        out["water"] = run_water(a, timed, dev)
-        if a.batch > 0:
-            out["batch"] = run_batch(a, timed, world)
-        if not a.no_optimizer:
-            out["optimizer"] = run_optimizer(a, dev)
+        print(json.dumps(out))
+        return
+    for k in ("e2e", "fp64", "mixed_native_fp64", "mixed_over_fp64", "mixed_native_over_fp64",
+              "abs_dE_mixed_vs_fp64", "err_est_mixed", "cpu_baseline"):
+        out[k] = m.get(k)
+    if a.workload != "ch_chain":
+        c = measure(a, "ch_chain", world, dev, stream, flush, a.steps, a.warmup, a.steps, a.warmup)
+        out["ch_chain"] = {"config": c["config"], "value": c["value"], "unit": "energy+grad evals/s",
+                           "ms_per_step": statistics.mean(c["ms_mx"]), "e2e": c["e2e"], "fp64": c["fp64"],
+                           "mixed_native_fp64": c["mixed_native_fp64"], "mixed_over_fp64": c["mixed_over_fp64"],
+                           "mixed_native_over_fp64": c["mixed_native_over_fp64"],
+                           "abs_dE_mixed_vs_fp64": c["abs_dE_mixed_vs_fp64"], "roofline": c["roofline"],
+                           "cpu_baseline": c.get("cpu_baseline"), "gpu_launches": c["launches"]}
+
+    def timed_simple(fn, steps, warmup):
+        import torch
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms, launches, last = [], 0, None
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            last = fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            launches += last["n_kernel_launches"]
+        torch.cuda.synchronize()
+        return ms, launches, last
+
+    out["water"] = run_water(a, timed_simple, dev)
+    if a.batch > 0:
+        out["batch"] = run_batch(a, timed_simple, world)
+    if not a.no_optimizer:
+        out["optimizer"] = run_optimizer(a, dev)
     print(json.dumps(out))
 
 
@@ -403,15 +564,15 @@ def run_optimizer(a, dev):
            "minimize_abs_dE": abs(res["energy"] - case["total_energy"]), "iterations": res["iterations"],
            "hs_builds": res["n_hs_builds"]}
     with tempfile.TemporaryDirectory() as d:
-        wpath = _workload(a.workload, d)
+        wpath = _workload("ch_chain", d)
         for name, prec in (("fp64", api.FP64), ("double_float", api.MIXED_DF64)):
             opt = api.Optimizer(wpath, precision=prec, device=dev)
             iorb = opt.desc_counts()["nnd"] + 1  # the first DOCC orbital
             opt.first_order_hs(iorb)
             t = time.perf_counter()
             opt.first_order_hs(iorb)
-            out[f"{a.workload}_hs_{name}_ms"] = 1e3 * (time.perf_counter() - t)
-            out[f"{a.workload}_hs_order"] = int(opt.map_orbs[iorb] - opt.map_orbs[iorb - 1])
+            out[f"ch_chain_hs_{name}_ms"] = 1e3 * (time.perf_counter() - t)
+            out["ch_chain_hs_order"] = int(opt.map_orbs[iorb] - opt.map_orbs[iorb - 1])
             opt.close()
     return out
 
@@ -447,27 +608,21 @@ def run_water(a, timed, dev):
 def run_batch(a, timed, world):
     """Batched energy + gradient: a.batch independent random molecules (2-12
     atoms, Z in {1,3,6,7,8,9}, 4-80 functions, 0-2 coupled pairs; seeds from
-    1000, draws whose determinant pairs are singular skipped) on the mixed
-    path, all evaluated by one CUDA-graph launch per step (vsvb_batch)."""
+    1000, every draw kept -- those with singular determinant pairs counted)
+    on the mixed path, all evaluated by one CUDA-graph launch per step
+    (vsvb_batch)."""
     import torch
 
     import valence_gb300 as vg
     from valence_gb300 import configs
-    systems, skipped, seed = [], 0, 1000
+    systems, singular, seed = [], 0, 1000
     with tempfile.TemporaryDirectory() as d:
         while len(systems) < a.batch:
             p = configs.random_molecule(os.path.join(d, f"m{seed}.inp"), seed)
             seed += 1
-            try:
-                s = vg.System(p, precision=vg.MIXED_DF64)
-                r, _ = s.energy_grad()
-            except vg.VSVBError:
-                skipped += 1
-                continue
-            if r["n_singular_pairs"]:
-                s.close()
-                skipped += 1
-                continue
+            s = vg.System(p, precision=vg.MIXED_DF64)
+            r, _ = s.energy_grad()
+            singular += r["n_singular_pairs"] > 0
             systems.append((s, p))
         # CPU baseline: the oracle on every 16th molecule, all host cores
         cpu_s, sample = 0.0, systems[::16]
@@ -490,7 +645,7 @@ def run_batch(a, timed, world):
     nf = [s.totlen for s in systems]
     out = {"workload": f"{len(systems)} random molecules, 4-80 functions, mixed path, one CUDA graph per step",
            "value": world * len(systems) / (t * 1e-3), "unit": "molecule energy+grad evals/s",
-           "ms_per_step": t, "kernels_per_graph_launch": b.launches, "skipped_draws": skipped,
+           "ms_per_step": t, "kernels_per_graph_launch": b.launches, "molecules_with_singular_pairs": singular,
            "weights_total": int(sum(nf))}
     if cpu_s > 0:
         out["cpu_baseline"] = {"value": len(sample) / cpu_s, "unit": "molecule energy evals/s",

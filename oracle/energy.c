@@ -933,7 +933,17 @@ static vo_state *state_new(vo_input *in) {
   return st;
 }
 
+static double omp_wtime_or_zero(void) {
+#ifdef _OPENMP
+  return omp_get_wtime();
+#else
+  return 0.0;
+#endif
+}
+
 static long long g_task_stride = 1;
+static long long g_schw_stride = 1, g_e1_stride = 1; /* timing mode only (vo_guess_energy_timed) */
+static double g_phase_t[4];
 
 /* Timing aid for the CPU baseline: only every stride-th 2e task is evaluated
  * (the others are skipped), so a bounded sample of the reference's task list
@@ -1029,6 +1039,11 @@ static void schwarz_ints(vo_state *st, int nspat, int nsd, int nth) {
       j = (int)(t + 1 - (ii * ii - ii) / 2);
       int ie = i > nsd ? 2 * i - nsd : i;
       int je = j > nsd ? 2 * j - nsd : j;
+      if (g_schw_stride > 1 && t % g_schw_stride) {
+        /* timing mode: entries outside the sample pass every screen */
+        st->schwarz[indx(i, j)] = 1.0;
+        continue;
+      }
       int2e(cx, st->bra[ie], st->ket[je], st->bra[ie], st->ket[je]);
       st->schwarz[indx(i, j)] = sqrt(cx->gint);
     }
@@ -1086,6 +1101,7 @@ static void vsvb_energy_core(vo_state *st, int nsd, int nspat, int sym, int jorb
       double le = 0.0, lw = 0.0;
 #pragma omp for schedule(dynamic, 1)
       for (int t = 0; t < nelec * nelec; ++t) {
+        if (g_e1_stride > 1 && t % g_e1_stride) continue;
         int i = t / nelec + 1, j = t % nelec + 1;
         int i_docc = i > nsd, j_docc = j > nsd;
         if (i_docc && j_docc && (i % 2) != (j % 2)) continue;
@@ -1114,6 +1130,7 @@ static void vsvb_energy_core(vo_state *st, int nsd, int nspat, int sym, int jorb
     free(pw);
   }
   wfnorm /= (double)nelec;
+  g_phase_t[2] = omp_wtime_or_zero();
   long long ntij = ((long long)nspat * nspat + nspat) / 2;
   long long ntasks = sym ? (ntij * ntij + ntij) / 2 : ntij * ntij;
   double itol = in->itol;
@@ -1246,6 +1263,7 @@ static void vsvb_energy_core(vo_state *st, int nsd, int nspat, int sym, int jorb
 }
 
 int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
+  g_phase_t[0] = omp_wtime_or_zero();
   memset(res, 0, sizeof(*res));
   double nre = 0.0;
   vo_state *st = prepare(in, &nre);
@@ -1255,7 +1273,9 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
   vo_ctx *c0 = ctx_new(st);
   wfndet(st, c0);
   ctx_free(c0);
+  g_phase_t[1] = omp_wtime_or_zero();
   schwarz_ints(st, st->nsp, st->nnd, nth);
+  g_phase_t[3] = omp_wtime_or_zero(); /* one-electron loop starts */
   long long ntij = ((long long)st->nsp * st->nsp + st->nsp) / 2;
   res->ntasks = (ntij * ntij + ntij) / 2;
   /* vsvb_energy with iorb = 0, spinav = .false., ijkl symmetry enabled */
@@ -1267,7 +1287,28 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads) {
   /* guess_energy tail (valence.F90:342-344) */
   res->energy = (e1 + e2) / wfnorm + nre;
   g_last_state = st;
+  {
+    /* phase times: set-up, Schwarz table, one-electron loop, task loop */
+    const double t_end = omp_wtime_or_zero();
+    const double t0 = g_phase_t[0], t1 = g_phase_t[1], t2 = g_phase_t[3], t3 = g_phase_t[2];
+    g_phase_t[0] = t1 - t0;
+    g_phase_t[1] = t2 - t1;
+    g_phase_t[2] = t3 - t2;
+    g_phase_t[3] = t_end - t3;
+  }
   return 0;
+}
+
+int vo_guess_energy_timed(vo_input *in, vo_result *res, int nthreads, long long schw_stride, long long e1_stride,
+                          long long task_stride, double *phase_seconds) {
+  g_schw_stride = schw_stride > 0 ? schw_stride : 1;
+  g_e1_stride = e1_stride > 0 ? e1_stride : 1;
+  g_task_stride = task_stride > 0 ? task_stride : 1;
+  int rc = vo_guess_energy(in, res, nthreads);
+  g_schw_stride = g_e1_stride = g_task_stride = 1;
+  if (phase_seconds)
+    for (int k = 0; k < 4; ++k) phase_seconds[k] = g_phase_t[k];
+  return rc;
 }
 
 /* first_order_opt's dummy orbitals (valence.F90:609-672): orbital

@@ -94,6 +94,15 @@ int vo_guess_energy(vo_input *in, vo_result *res, int nthreads);
 /* Same with only every stride-th two-electron task evaluated (CPU-baseline
  * timing on a bounded sample; the energy is then not the full energy). */
 int vo_guess_energy_sampled(vo_input *in, vo_result *res, int nthreads, long long stride);
+/* CPU-baseline timing on bounded samples of every phase: only every
+ * schw_stride-th Schwarz-table entry (the others set so that they pass every
+ * screen), every e1_stride-th one-electron term and every task_stride-th
+ * two-electron task are evaluated.  phase_seconds[4]: set-up (normalisation,
+ * orbital overlaps), Schwarz table, one-electron loop, task loop; each
+ * extrapolates to the full run by its stride.  The energy is not the full
+ * energy. */
+int vo_guess_energy_timed(vo_input *in, vo_result *res, int nthreads, long long schw_stride, long long e1_stride,
+                          long long task_stride, double *phase_seconds);
 
 /* first_order_opt's Hamiltonian and overlap matrices (valence.F90:527-758)
  * for orbital iorb (1-based) of the wave function with the weights as set

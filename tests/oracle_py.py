@@ -38,6 +38,9 @@ def lib():
         _lib.vo_boys.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
         _lib.vo_guess_energy_sampled.argtypes = [ctypes.c_void_p, ctypes.POINTER(VoResult), ctypes.c_int,
                                                  ctypes.c_longlong]
+        _lib.vo_guess_energy_timed.argtypes = [ctypes.c_void_p, ctypes.POINTER(VoResult), ctypes.c_int,
+                                               ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong,
+                                               ctypes.POINTER(ctypes.c_double)]
     return _lib
 
 
@@ -72,6 +75,14 @@ class Oracle:
         r = VoResult()
         lib().vo_guess_energy_sampled(self.h, ctypes.byref(r), nthreads, stride)
         return r
+
+    def guess_energy_timed(self, nthreads=0, schw_stride=1, e1_stride=1, task_stride=1):
+        """Phase times (set-up, Schwarz table, one-electron loop, task loop)
+        of a run that evaluates only every stride-th item of each phase."""
+        r = VoResult()
+        t = (ctypes.c_double * 4)()
+        lib().vo_guess_energy_timed(self.h, ctypes.byref(r), nthreads, schw_stride, e1_stride, task_stride, t)
+        return r, list(t)
 
     def int2e(self, io, ko, jo, lo):
         return lib().vo_int2e(self.h, io, ko, jo, lo)

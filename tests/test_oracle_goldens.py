@@ -65,3 +65,16 @@ def test_translation_invariance(oracle):
     o.set_coords_angstrom((xyz + np.array([0.3, -1.1, 2.0])).ravel())
     e1 = o.guess_energy().energy
     assert abs(e1 - e0) < 1e-10
+
+
+def test_timed_mode_at_stride_one_is_the_full_run():
+    """vo_guess_energy_timed (the bench's bounded CPU samples) evaluates
+    everything at stride 1: the same energy as vo_guess_energy, and phase
+    times that are non-negative."""
+    from tests import oracle_py
+    p = os.path.join(oracle_py.GOLDEN, "cases", "testing", "be-sc")
+    o = oracle_py.Oracle(p)
+    full = o.guess_energy(2).energy
+    r, ph = oracle_py.Oracle(p).guess_energy_timed(2, 1, 1, 1)
+    assert abs(r.energy - full) < 1e-12 * max(1.0, abs(full))
+    assert len(ph) == 4 and min(ph) >= 0.0

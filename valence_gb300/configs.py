@@ -193,5 +193,41 @@ def singular_pair_large(path, seed=5, natom=32, ndocc=32):
     return path
 
 
+def describe(path):
+    """Counts of an input in VALENCE's format (line A of xm_input and the
+    basis records): atoms, shells, Cartesian functions, highest angular
+    momentum, orbitals by kind, spin couplings, determinant pairs and
+    weights -- the configuration fields of a benchmark line."""
+    toks = open(path).read().split()
+    it = iter(toks)
+    a = [int(next(it)) for _ in range(15)]
+    natom, natom_t, npair, nunpd, ndocc, totlen, _, nspinc = a[:8]
+    for _ in range(8):
+        next(it)
+    types = []
+    for _ in range(natom):
+        types.append(int(next(it)))
+        for _ in range(3):
+            next(it)
+    nfun_t, nsh_t, lmax = [], [], 0
+    for _ in range(natom_t):
+        next(it)
+        ns = int(next(it))
+        nf = 0
+        for _ in range(ns):
+            l, npr = int(next(it)), int(next(it))
+            lmax = max(lmax, l)
+            nf += (l + 1) * (l + 2) // 2
+            for _ in range(npr if npr == 1 else 2 * npr):
+                next(it)
+        nfun_t.append(nf)
+        nsh_t.append(ns)
+    nsc = max(nspinc, 1)
+    return {"atoms": natom, "shells": sum(nsh_t[t - 1] for t in types),
+            "functions": sum(nfun_t[t - 1] for t in types), "max_l": lmax, "coupled_pairs": npair,
+            "unpaired": nunpd, "docc": ndocc, "spatial_orbitals": 2 * npair + nunpd + ndocc,
+            "spin_couplings": nsc, "determinant_pairs": nsc * nsc * 4 ** npair, "weights": totlen}
+
+
 WORKLOADS = {"water_vshf": water_vshf, "ch_chain": ch_chain, "lif_cluster": lif_cluster,
              "lif_cluster_small": lif_cluster_small, "singular_pair_large": singular_pair_large}
