@@ -21,6 +21,9 @@ CASES = {"ch_chain": dict(fn=configs.ch_chain, seed=2), "lif_cluster_small": dic
          "singular_pair_large": dict(fn=configs.singular_pair_large, seed=5)}
 
 
+N_BATCH = 16
+
+
 def main(only=None):
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
     exe = os.path.join(ROOT, "oracle", "_build", "vsvb_oracle")
@@ -38,6 +41,18 @@ def main(only=None):
             out[name] = {"seed": c["seed"], "energy": e, "wfnorm": float(f[5]), "e1": float(f[1]), "e2": float(f[3]),
                          "source": f"oracle/_build/vsvb_oracle on valence_gb300.configs.{c['fn'].__name__}"
                                    f"(seed={c['seed']}), {nthreads} threads"}
+        if not only or "batch_molecules" in only:
+            # the batched configuration's random molecules (seeds 1000 ...)
+            mols = []
+            for seed in range(1000, 1000 + N_BATCH):
+                path = configs.random_molecule(os.path.join(d, f"m{seed}.inp"), seed)
+                txt = subprocess.run([exe, path, str(nthreads)], capture_output=True, text=True, check=True).stdout
+                e = float([ln for ln in txt.splitlines() if "guess energy" in ln][0].split()[2])
+                f = [ln for ln in txt.splitlines() if ln.strip().startswith("e1")][0].split()
+                mols.append({"seed": seed, "energy": e, "wfnorm": float(f[5])})
+            out["batch_molecules"] = {"molecules": mols,
+                                      "source": f"oracle/_build/vsvb_oracle on valence_gb300.configs.random_molecule"
+                                                f"(seed), {nthreads} threads"}
     with open(os.path.join(ROOT, "tests", "golden", "synthetic.json"), "w") as fh:
         json.dump(out, fh, indent=1)
 

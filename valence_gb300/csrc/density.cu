@@ -99,6 +99,7 @@ struct QInfo {
   double wdd;    /* w * da * db */
   double wddr;   /* w * det(A + delta I) per block: wdd unless a block is flagged */
   int sing;      /* exact-minor flags per spin block */
+  int abeq;      /* the beta block equals the alpha block (DetCtx.abeq) */
 };
 
 __device__ __forceinline__ QInfo decode_q(const DetCtx &d, long long q) {
@@ -113,6 +114,7 @@ __device__ __forceinline__ QInfo decode_q(const DetCtx &d, long long q) {
   r.w = d.coeff_sc[r.isc] * d.coeff_sc[r.jsc];
   r.da = r.db = r.wdd = r.wddr = 0.0;
   r.sing = 0;
+  r.abeq = 0;
   return r;
 }
 
@@ -122,6 +124,7 @@ __device__ __forceinline__ void load_dets(const DetCtx &d, long long q, QInfo &q
   qi.wdd = qi.w * qi.da * qi.db;
   qi.sing = d.sing[q];
   qi.wddr = qi.sing ? qi.w * d.detr_a[q] * d.detr_b[q] : qi.wdd;
+  qi.abeq = d.abeq ? d.abeq[q] : 0;
 }
 
 /* exact determinant of spin block sp of pair q with up to two strikes, from
@@ -309,7 +312,10 @@ __global__ void __launch_bounds__(512) detpair_kernel(DetCtx d, double *scratch,
   const long long q = blockIdx.x;
   const QInfo qi = decode_q(d, q);
   double *W = scratch + (size_t)blockIdx.x * ld_scratch;
-  if (threadIdx.x == 0) sslot = -1;
+  if (threadIdx.x == 0) {
+    sslot = -1;
+    if (d.abeq) d.abeq[q] = 0;
+  }
   __syncthreads();
   for (int sp = 0; sp < 2; ++sp) {
     const int n = sp == 0 ? d.ds.nalpha : d.ds.nbeta;
@@ -332,6 +338,7 @@ __global__ void __launch_bounds__(512) detpair_kernel(DetCtx d, double *scratch,
         if (threadIdx.x == 0) {
           d.det_b[q] = d.det_a[q];
           d.detr_b[q] = d.detr_a[q];
+          if (d.abeq) d.abeq[q] = d.ds.nunpd == 0;
         }
         __syncthreads();
         continue;
@@ -647,6 +654,60 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
     const bool id = io >= nnd, jd = jo >= nnd, kd = ko >= nnd, ld = lo >= nnd;
     const int iso = id ? 2 : 1, jso = jd ? 2 : 1, kso = kd ? 2 : 1, lso = ld ? 2 : 1;
     double esum = 0.0, xsum = 0.0, dsum_e = 0.0, dsum_x = 0.0;
+    if (MODE == 0 && qi.abeq && id && jd && kd && ld) {
+      /* four doubly occupied orbitals and one factorisation for both spin
+       * blocks: every cofactor of the 16 spin terms comes from the four
+       * inverse entries T[k][i], T[l][j], T[l][i], T[k][j] (block positions
+       * do not depend on the spin without unpaired electrons); the terms,
+       * their order and the sign rule are those of the general loop below */
+      const int ia = 2 * (io + 1) - nnd - 2, ja = 2 * (jo + 1) - nnd - 2;
+      const int ka = 2 * (ko + 1) - nnd - 2, la = 2 * (lo + 1) - nnd - 2;
+      const int pi_ = loc_bra(d, qi, ia).pos, pj_ = loc_bra(d, qi, ja).pos;
+      const int pk_ = loc_ket(d, qi, ka).pos, pl_ = loc_ket(d, qi, la).pos;
+      const double *Tq = d.Ta + (size_t)q * na * na;
+      const double tki = Tq[pk_ * na + pi_], tlj = Tq[pl_ * na + pj_];
+      const double tli = Tq[pl_ * na + pi_], tkj = Tq[pk_ * na + pj_];
+      for (int is = 0; is < 2; ++is) {
+        const int i = ia + is;
+        const int si = loc_bra(d, qi, i).spin;
+        for (int js = 0; js < 2; ++js) {
+          const int j = ja + js;
+          if (!(j < i)) continue;
+          const int sj = loc_bra(d, qi, j).spin;
+          for (int ks = 0; ks < 2; ++ks) {
+            const int k = ka + ks;
+            const int sk = loc_ket(d, qi, k).spin;
+            for (int ls = 0; ls < 2; ++ls) {
+              const int l = la + ls;
+              if (!(l < k)) continue;
+              const int sl = loc_ket(d, qi, l).spin;
+              const bool ik0 = ((i + 1) & 1) != ((k + 1) & 1), jl0 = ((j + 1) & 1) != ((l + 1) & 1);
+              const bool il0 = ((i + 1) & 1) != ((l + 1) & 1), jk0 = ((j + 1) & 1) != ((k + 1) & 1);
+              const bool ce = !(ik0 || jl0), cx = !(il0 || jk0);
+              if (!((ce && es) || (cx && xs))) continue;
+              /* direct cofactor: strikes i -> k, j -> l */
+              const bool eok = es && si == sk && sj == sl;
+              double ev = 0.0;
+              if (eok) ev = qi.wdd * (si == sj ? tki * tlj - tkj * tli : tki * tlj);
+              double dd = 0.0, xd = 0.0;
+              if (eok) dd = ev;
+              if (xs) {
+                if (eok) {
+                  /* the exchanged cofactor is the direct one's column swap */
+                  if (si == sl && sj == sk) xd = ev;
+                } else if (si == sl && sj == sk) {
+                  /* strikes i -> l, j -> k */
+                  const double xv = qi.wdd * (si == sj ? tli * tkj - tlj * tki : tli * tkj);
+                  xd = -xv;
+                }
+              }
+              if (es) dsum_e += dd;
+              if (xs) dsum_x += xd;
+            }
+          }
+        }
+      }
+    } else
     for (int is = 0; is < iso; ++is) {
       /* 0-based slot; 1-based formula 2*io - nnd + is - 2 with 1-based io */
       const int i = id ? 2 * (io + 1) - nnd + (is + 1) - 2 - 1 : io;

@@ -27,6 +27,8 @@ struct DetCtx {
   int *xslot;             /* [nq] slot of pair q, -1 when none */
   int *xcount;            /* slots taken (reset per evaluation) */
   int xcap;
+  int *abeq;              /* [nq] 1 when the beta block has the alpha block's orbitals and
+                           * factorisation (doubly occupied orbitals, no unpaired ones) */
 };
 
 struct AsmArgs {

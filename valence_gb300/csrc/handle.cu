@@ -206,7 +206,7 @@ struct vsvb_gpu {
   int nxterm = 0;
   DBuf<int> obs_n, obs_ao, term0, term_slot, term_j, term_m, term_f, ndf_orb;
   DBuf<double> coeff_d, ndf_scale, orb_scale, Craw, C, So, Ho, xtab, T, sqT, qmax, q0max;
-  DBuf<int> pair_slot, slot_pair, slot_which, sing, status, nsing, xslot, xcount;
+  DBuf<int> pair_slot, slot_pair, slot_which, sing, status, nsing, xslot, xcount, abeq;
   DBuf<double> xinv, xdet; /* exact-minor pool of flagged determinant pairs */
   int xcap = 0;
   DBuf<double> coeff_sc, det_a, det_b, detr_a, detr_b, Ta, Tb, scratch;
@@ -367,6 +367,7 @@ DetCtx det_ctx(vsvb_gpu *h) {
   d.xslot = h->xslot.p;
   d.xcount = h->xcount.p;
   d.xcap = h->xcap;
+  d.abeq = h->abeq.p;
   d.status = h->status.p;
   return d;
 }
@@ -1409,6 +1410,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     CK(h->xdet.alloc((size_t)h->xcap * 6), "alloc exact-minor pool");
     CK(h->xslot.alloc(nq), "alloc exact-minor pool");
     CK(h->xcount.alloc(1), "alloc exact-minor pool");
+    CK(h->abeq.alloc(nq), "alloc block flags");
   }
   CK(h->nsing.alloc(1), "alloc nsing");
   h->ld_scratch = 2 * std::max(na, nb) * std::max(std::max(na, nb), 1);
