@@ -658,8 +658,7 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
       /* four doubly occupied orbitals and one factorisation for both spin
        * blocks: every cofactor of the 16 spin terms comes from the four
        * inverse entries T[k][i], T[l][j], T[l][i], T[k][j] (block positions
-       * do not depend on the spin without unpaired electrons); the terms,
-       * their order and the sign rule are those of the general loop below */
+       * do not depend on the spin without unpaired electrons) */
       const int ia = 2 * (io + 1) - nnd - 2, ja = 2 * (jo + 1) - nnd - 2;
       const int ka = 2 * (ko + 1) - nnd - 2, la = 2 * (lo + 1) - nnd - 2;
       const int pi_ = loc_bra(d, qi, ia).pos, pj_ = loc_bra(d, qi, ja).pos;
@@ -667,46 +666,29 @@ __global__ void assemble_kernel(DetCtx d, AsmArgs a) {
       const double *Tq = d.Ta + (size_t)q * na * na;
       const double tki = Tq[pk_ * na + pi_], tlj = Tq[pl_ * na + pj_];
       const double tli = Tq[pl_ * na + pi_], tkj = Tq[pk_ * na + pj_];
-      for (int is = 0; is < 2; ++is) {
-        const int i = ia + is;
-        const int si = loc_bra(d, qi, i).spin;
-        for (int js = 0; js < 2; ++js) {
-          const int j = ja + js;
-          if (!(j < i)) continue;
-          const int sj = loc_bra(d, qi, j).spin;
-          for (int ks = 0; ks < 2; ++ks) {
-            const int k = ka + ks;
-            const int sk = loc_ket(d, qi, k).spin;
-            for (int ls = 0; ls < 2; ++ls) {
-              const int l = la + ls;
-              if (!(l < k)) continue;
-              const int sl = loc_ket(d, qi, l).spin;
-              const bool ik0 = ((i + 1) & 1) != ((k + 1) & 1), jl0 = ((j + 1) & 1) != ((l + 1) & 1);
-              const bool il0 = ((i + 1) & 1) != ((l + 1) & 1), jk0 = ((j + 1) & 1) != ((k + 1) & 1);
-              const bool ce = !(ik0 || jl0), cx = !(il0 || jk0);
-              if (!((ce && es) || (cx && xs))) continue;
-              /* direct cofactor: strikes i -> k, j -> l */
-              const bool eok = es && si == sk && sj == sl;
-              double ev = 0.0;
-              if (eok) ev = qi.wdd * (si == sj ? tki * tlj - tkj * tli : tki * tlj);
-              double dd = 0.0, xd = 0.0;
-              if (eok) dd = ev;
-              if (xs) {
-                if (eok) {
-                  /* the exchanged cofactor is the direct one's column swap */
-                  if (si == sl && sj == sk) xd = ev;
-                } else if (si == sl && sj == sk) {
-                  /* strikes i -> l, j -> k */
-                  const double xv = qi.wdd * (si == sj ? tli * tkj - tlj * tki : tli * tkj);
-                  xd = -xv;
-                }
-              }
-              if (es) dsum_e += dd;
-              if (xs) dsum_x += xd;
-            }
-          }
-        }
+      /* The 16 spin terms in closed form.  Slot parity is spin, so the
+       * DOCC parity skips (:1352-1375) keep the terms whose strikes stay in
+       * one spin block; with the slot orders j < i, l < k of the task loop:
+       *   io > jo, ko > lo: (aa|aa), (bb|bb) give J2 direct and exchanged
+       *     (the column-swap rule of det(), :2041-2054), (ab|ab), (ba|ba)
+       *     t_ki t_lj direct, (ab|ba), (ba|ab) -t_li t_kj exchanged;
+       *   one of io = jo, ko = lo: one direct t_ki t_lj, one exchanged
+       *     -t_li t_kj;  both: one direct t_ki t_lj,
+       * J2 = t_ki t_lj - t_kj t_li, each term times w det_a det_b. */
+      const double a = tki * tlj, x = tli * tkj, j2 = a - tkj * tli;
+      double de, dx;
+      if (io != jo && ko != lo) {
+        de = 2.0 * qi.wdd * (j2 + a);
+        dx = 2.0 * qi.wdd * (j2 - x);
+      } else if (io != jo || ko != lo) {
+        de = qi.wdd * a;
+        dx = -qi.wdd * x;
+      } else {
+        de = qi.wdd * a;
+        dx = 0.0;
       }
+      if (es) dsum_e = de;
+      if (xs) dsum_x = dx;
     } else
     for (int is = 0; is < iso; ++is) {
       /* 0-based slot; 1-based formula 2*io - nnd + is - 2 with 1-based io */

@@ -529,7 +529,9 @@ int build_block(vsvb_gpu *h, const vsvb_system_desc *d, const std::vector<GShell
   std::stable_sort(aqs.begin(), aqs.end(), [](const AQ &x, const AQ &y) { return x.b > y.b; });
   h->blk_naq = (long long)aqs.size();
   /* chunks: staging blocks of one chunk fit blk_gsize doubles */
-  const size_t gbudget = (size_t)1 << 24; /* 128 MiB of FP64 per buffer */
+  /* 512 MiB of FP64 per buffer: enough shell quartets per class launch to
+   * fill the GPU with the one-lane-per-quartet kernels */
+  const size_t gbudget = (size_t)1 << 26;
   size_t gmax = 0;
   std::vector<int4> aqd(aqs.size());
   {
