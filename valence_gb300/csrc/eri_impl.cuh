@@ -1238,7 +1238,12 @@ int dispatch_blk(int cp, int cq, const EriArgs &a, const int4 *w, int n, int max
   if (cp == 1 && cq == 1) return launch_lane<1, 0, 1, 0, R>(a, w, n, max_blocks, st);
   if (cp == 2 && cq == 0) return launch_lane<1, 1, 0, 0, R>(a, w, n, max_blocks, st);
   if (cp == 2 && cq == 1) return launch_lane<1, 1, 1, 0, R>(a, w, n, max_blocks, st);
-  if (cp == 2 && cq == 2) return launch_cls<2, 2, R, 4>(a, w, n, max_blocks, st);
+  if (cp == 2 && cq == 2) {
+    /* (pp|pp): 81 components -- in registers one lane per quartet in FP32,
+     * the CTA kernel in the wider arithmetics */
+    if constexpr (std::is_same<R, float>::value) return launch_lane<1, 1, 1, 1, R>(a, w, n, max_blocks, st);
+    else return launch_cls<2, 2, R, 4>(a, w, n, max_blocks, st);
+  }
   return 2;
 }
 
