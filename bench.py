@@ -53,11 +53,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "VSVB energy+grad evals/s, mixed vs plain FP64 on 1 GB300 at |ΔE|<=1e-6 Eh"
-# workloads whose configuration defines an energy evaluation only (block mode)
-ENERGY_ONLY = {"lif_cluster"}
+# workloads whose configuration defines an energy evaluation only; any
+# workload run in block mode is timed as energy evaluations as well
+ENERGY_ONLY = {"lif_cluster", "lif_cluster_3"}
 # bounded CPU-oracle samples per phase (Schwarz entries, one-electron terms,
 # two-electron tasks) for workloads whose full CPU evaluation takes hours
-CPU_SAMPLE = {"lif_cluster": (16, 16, 12)}
+CPU_SAMPLE = {"lif_cluster": (16, 16, 12), "lif_cluster_3": (16, 16, 12)}
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the ERI class
@@ -137,6 +138,8 @@ def _args():
     ap.add_argument("--headline-only", action="store_true",
                     help="time only the headline mixed arm (used for per-kernel launch lists)")
     ap.add_argument("--no-optimizer", action="store_true", help="skip the optimiser-path figures")
+    ap.add_argument("--block-mode", default="auto", choices=["auto", "on", "off"],
+                    help="vsvb_options.block_mode of the headline workload (auto: on for large s/p systems)")
     ap.add_argument("--batch", type=int, default=256,
                     help="molecules in the batched (one CUDA graph) measurement; 0 skips it")
     return ap.parse_args()
@@ -253,15 +256,17 @@ def _cpu_seconds(workload, path, cores):
                 "gradient")
 
 
-def _config(a, workload, path, world):
+def _config(a, workload, path, world, grad=None):
     import inspect
 
     from valence_gb300 import configs
     c = {"workload": workload,
          "seed": inspect.signature(configs.WORKLOADS[workload]).parameters["seed"].default}
     c.update(configs.describe(path))
-    c["step"] = ("one guess energy (the configuration defines no gradient)" if workload in ENERGY_ONLY
-                 else "one energy + adjoint gradient with respect to every weight")
+    if grad is None:
+        grad = workload not in ENERGY_ONLY
+    c["step"] = ("one energy + adjoint gradient with respect to every weight" if grad
+                 else "one guess energy (the configuration defines no gradient)")
     c.update({"mixed_threshold": a.mixed_threshold, "l2": "flushed (256 MB write) between timed steps",
               "replicas": world})
     return c
@@ -334,7 +339,8 @@ def measure(a, workload, world, dev, stream, flush, steps, warmup, side_steps, s
 
     import valence_gb300 as vg
     from valence_gb300 import api
-    grad = workload not in ENERGY_ONLY
+    bm = {"auto": 0, "on": 1, "off": -1}[a.block_mode] if workload == a.workload else 0
+    grad = workload not in ENERGY_ONLY and bm != 1
 
     def timed(fn, steps, warmup, after_step=None):
         for _ in range(warmup):
@@ -368,10 +374,10 @@ def measure(a, workload, world, dev, stream, flush, steps, warmup, side_steps, s
 
     with tempfile.TemporaryDirectory() as d:
         path = _workload(workload, d)
-        cfg = _config(a, workload, path, world)
+        cfg = _config(a, workload, path, world, grad)
 
         def system(prec):
-            s = vg.System(path, precision=prec, mixed_threshold=a.mixed_threshold, device=dev)
+            s = vg.System(path, precision=prec, mixed_threshold=a.mixed_threshold, device=dev, block_mode=bm)
             s.set_stream(stream.cuda_stream)
             return s
 
@@ -464,7 +470,7 @@ def run_ours(a, rank, world):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 126 MB L2
-    energy_only = a.workload in ENERGY_ONLY
+    energy_only = a.workload in ENERGY_ONLY or a.block_mode == "on"
     # the FP64 and FP32 + native FP64 arms of an energy-only (large) workload
     # are timed on fewer steps than the headline arm: they are reported beside
     # it, not as the headline

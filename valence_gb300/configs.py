@@ -172,6 +172,13 @@ def lif_cluster_small(path, seed=3):
     return lif_cluster(path, seed=seed, n=2, ndocc=12)
 
 
+def lif_cluster_3(path, seed=3):
+    """The cluster workload at 3x3x3 (27 atoms, 243 functions, 108 DOCC): the
+    block-mode kernels at the full cluster's chunk size, small enough for a
+    detailed profile."""
+    return lif_cluster(path, seed=seed, n=3, ndocc=108)
+
+
 def singular_pair_large(path, seed=5, natom=32, ndocc=32):
     """A spin-coupled pair whose first orbital sits on an atom 25 A away from
     a chain of natom Z=1 atoms (s, s, p shells, 5 functions each) that
@@ -230,4 +237,5 @@ def describe(path):
 
 
 WORKLOADS = {"water_vshf": water_vshf, "ch_chain": ch_chain, "lif_cluster": lif_cluster,
-             "lif_cluster_small": lif_cluster_small, "singular_pair_large": singular_pair_large}
+             "lif_cluster_small": lif_cluster_small, "lif_cluster_3": lif_cluster_3,
+             "singular_pair_large": singular_pair_large}
