@@ -30,25 +30,45 @@
 
 namespace {
 
+/* T = U + U^T in 32 x 32 tiles (i-tile >= j-tile), the transposed tile
+ * staged in shared memory so that both reads and both writes are coalesced;
+ * the diagonal tiles also store the Schwarz factors sqrt(T[p][p]) of
+ * schwarz_ints (valence.F90:1516) */
 __global__ void symmetrize_kernel(double *T, int np, double *sq) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long n = (long long)np * (np + 1) / 2;
-  if (t >= n) return;
-  long long i = (long long)((sqrt(8.0 * t + 1.0) - 1.0) / 2.0);
-  while ((i + 1) * (i + 2) / 2 <= t) ++i;
-  while (i * (i + 1) / 2 > t) --i;
-  long long j = t - i * (i + 1) / 2;
-  double *a = T + i * np + j, *b = T + j * np + i;
-  double v = *a + *b;
-  if (i == j) {
-    v = 2.0 * (*a);
-    sq[i] = sqrt(fmax(v, 0.0)); /* Schwarz factor of orbital pair i (schwarz_ints, valence.F90:1516) */
+  __shared__ double tl[32][33];
+  const long long tile = blockIdx.x;
+  long long ti = (long long)((sqrtf(8.0f * (float)tile + 1.0f) - 1.0f) * 0.5f);
+  while ((ti + 1) * (ti + 2) / 2 <= tile) ++ti;
+  while (ti * (ti + 1) / 2 > tile) --ti;
+  const long long tj = tile - ti * (ti + 1) / 2;
+  const int tx = threadIdx.x, ty = threadIdx.y; /* 32 x 8 */
+  /* the mirror tile (rows of tile j, columns of tile i), read coalesced */
+  for (int r = ty; r < 32; r += 8) {
+    const long long row = tj * 32 + r, col = ti * 32 + tx;
+    tl[r][tx] = row < np && col < np ? T[row * np + col] : 0.0;
   }
-  *a = v;
-  *b = v;
+  __syncthreads();
+  double v[4];
+  for (int k = 0, r = ty; r < 32; r += 8, ++k) {
+    const long long row = ti * 32 + r, col = tj * 32 + tx;
+    v[k] = row < np && col < np ? T[row * np + col] + tl[tx][r] : 0.0;
+  }
+  __syncthreads();
+  for (int k = 0, r = ty; r < 32; r += 8, ++k) {
+    const long long row = ti * 32 + r, col = tj * 32 + tx;
+    if (row < np && col < np) {
+      T[row * np + col] = v[k];
+      if (row == col) sq[row] = sqrt(fmax(v[k], 0.0));
+    }
+    tl[r][tx] = v[k];
+  }
+  __syncthreads();
+  if (ti != tj)
+    for (int r = ty; r < 32; r += 8) {
+      const long long row = tj * 32 + r, col = ti * 32 + tx;
+      if (row < np && col < np) T[row * np + col] = tl[tx][r];
+    }
 }
-
-
 
 __global__ void to_float_kernel(const double *in, float *out, size_t n) {
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
@@ -67,9 +87,9 @@ int eri_to_float(const double *in, float *out, size_t n, cudaStream_t st) {
 /* T = U + U^T after the forward pass (the kernels accumulate one
  * orientation); sq[p] = sqrt(max(T[p][p], 0)) */
 int eri_symmetrize(double *T, int np, double *sq, cudaStream_t st) {
-  long long n = (long long)np * (np + 1) / 2;
-  if (n == 0) return 0;
-  symmetrize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(T, np, sq);
+  if (np == 0) return 0;
+  const long long nt = (np + 31) / 32;
+  symmetrize_kernel<<<(unsigned)(nt * (nt + 1) / 2), dim3(32, 8), 0, st>>>(T, np, sq);
   return cudaGetLastError() != cudaSuccess;
 }
 

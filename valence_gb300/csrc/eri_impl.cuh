@@ -1109,12 +1109,11 @@ __global__ void __launch_bounds__(128) eri_lane_kernel(EriArgs args, const int4 
       Ad[k] = geomR[pq.x].A[k];
       Cd[k] = geomR[pq.y].A[k];
     }
-    for (int k0 = 0; k0 < np_ * nq_; ++k0) {
-      /* FP32: smallest bounds (highest indices of the sorted primitives) first */
-      const int k = ASC ? np_ * nq_ - 1 - k0 : k0;
-      const int ip = k / nq_, iq = k - ip * nq_;
-      const float b = q0p[ip] * q0q[iq];
-      if (!(b >= eps && b < eps_hi)) continue;
+    /* the window's primitive quartets only: the primitives of both pairs are
+     * sorted by bound, descending, so row ip keeps the columns [jhi, jlo)
+     * with q0_p q0_q >= eps for iq < jlo and < eps_hi from jhi on, both ends
+     * monotone over the rows */
+    auto body = [&](int ip, int iq) {
       R rx[NR], rw[NR], ipq;
       prim_roots<R, NR, NR>(args, primR, P.prim0 + ip, Q.prim0 + iq, rx, rw, ipq);
       const PrimT<R> &pr = primR[P.prim0 + ip], &qr = primR[Q.prim0 + iq];
@@ -1141,6 +1140,24 @@ __global__ void __launch_bounds__(128) eri_lane_kernel(EriArgs args, const int4 
             acc3(acc[e][f], G[0][ex * (LCD + 1) + fx], G[1][ey * (LCD + 1) + fy], G[2][ez * (LCD + 1) + fz]);
           });
         });
+      }
+    };
+    int nrow = 0;
+    while (nrow < np_ && q0p[nrow] * q0q[0] >= eps) ++nrow;
+    if constexpr (ASC) {
+      /* FP32: smallest bounds first -- rows from the last, columns down */
+      int jlo = 0, jhi = 0;
+      for (int ip = nrow - 1; ip >= 0; --ip) {
+        while (jlo < nq_ && q0p[ip] * q0q[jlo] >= eps) ++jlo;
+        while (jhi < nq_ && q0p[ip] * q0q[jhi] >= eps_hi) ++jhi;
+        for (int iq = jlo - 1; iq >= jhi; --iq) body(ip, iq);
+      }
+    } else {
+      int jlo = nq_, jhi = nq_;
+      for (int ip = 0; ip < nrow; ++ip) {
+        while (jlo > 0 && !(q0p[ip] * q0q[jlo - 1] >= eps)) --jlo;
+        while (jhi > 0 && !(q0p[ip] * q0q[jhi - 1] >= eps_hi)) --jhi;
+        for (int iq = jhi; iq < jlo; ++iq) body(ip, iq);
       }
     }
     /* transfer to (ab|cd) and the staging block (mode 4 places) */
