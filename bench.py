@@ -61,25 +61,13 @@ ENERGY_ONLY = {"lif_cluster", "lif_cluster_3"}
 CPU_SAMPLE = {"lif_cluster": (16, 16, 12), "lif_cluster_3": (16, 16, 12)}
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum per launch of the ERI class
-# launches, from the ncu capture summarised in profiles/ (keys: workload,
-# 100*kind + 10*bra pair class + ket pair class; kind 1 = FP32 class, 2 =
-# double-float, 3 = FP32 tail; pair classes ss ps pp ds dp dd = 0..5)
-PROFILED_TRAFFIC = {
-    ("ch_chain", 100): 484096, ("ch_chain", 110): 840704, ("ch_chain", 111): 616064, ("ch_chain", 120): 636416,
-    ("ch_chain", 121): 708864, ("ch_chain", 122): 413824, ("ch_chain", 130): 904448, ("ch_chain", 131): 1027200,
-    ("ch_chain", 132): 829696, ("ch_chain", 133): 688640, ("ch_chain", 140): 899968, ("ch_chain", 141): 1005824,
-    ("ch_chain", 142): 811776, ("ch_chain", 143): 1057920, ("ch_chain", 144): 663040, ("ch_chain", 150): 711296,
-    ("ch_chain", 151): 813440, ("ch_chain", 152): 720896, ("ch_chain", 153): 883200, ("ch_chain", 154): 924160,
-    ("ch_chain", 155): 493312, ("ch_chain", 200): 632064, ("ch_chain", 210): 1007360, ("ch_chain", 211): 748032,
-    ("ch_chain", 220): 807936, ("ch_chain", 221): 894720, ("ch_chain", 222): 580096, ("ch_chain", 230): 1172736,
-    ("ch_chain", 231): 1286656, ("ch_chain", 232): 1090048, ("ch_chain", 233): 935424, ("ch_chain", 240): 1179648,
-    ("ch_chain", 241): 1285632, ("ch_chain", 242): 1079552, ("ch_chain", 243): 1408768, ("ch_chain", 244): 973568,
-    ("ch_chain", 250): 998400, ("ch_chain", 251): 1112064, ("ch_chain", 252): 991744, ("ch_chain", 253): 1255424,
-    ("ch_chain", 254): 1281024, ("ch_chain", 255): 844544,
-}
-# FP32 tail launches (code 3xx) run the same kernels as the FP32 class launches (1xx)
-PROFILED_TRAFFIC.update({(w, 300 + c % 100): v for (w, c), v in list(PROFILED_TRAFFIC.items()) if c < 200})
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
+# kernel, from the ncu captures summarised in profiles/.  Block mode: one
+# blk_transform_kernel<df64> launch (a chunk of atom quartets) of the 4x4x4
+# cluster, scaled from the 3x3x3 cluster's capture (149 KB per atom quartet,
+# profiles/transform_lif_cluster_3.md) by the 15,570 atom quartets of a
+# chunk.  Per-quartet path: keys (workload, class code).
+PROFILED_TRAFFIC = {("lif_cluster", "transform_df64"): 2322444656}
 
 
 def eri_roofline(sweep, sweep_wall, fp64_peak, fp32_peak, step_ms, workload):
