@@ -67,7 +67,9 @@ CPU_SAMPLE = {"lif_cluster": (16, 16, 12), "lif_cluster_3": (16, 16, 12)}
 # cluster, scaled from the 3x3x3 cluster's capture (149 KB per atom quartet,
 # profiles/transform_lif_cluster_3.md) by the 15,570 atom quartets of a
 # chunk.  Per-quartet path: keys (workload, class code).
-PROFILED_TRAFFIC = {("lif_cluster", "transform_df64"): 2322444656}
+PROFILED_TRAFFIC = {("lif_cluster", "transform_df64"): 2322444656,
+                    # eri_kernel<2,2,2,1,df64,3> on the chain (profiles/eri_ch_chain.md)
+                    ("ch_chain", 254): 1279232}
 
 
 def eri_roofline(sweep, sweep_wall, fp64_peak, fp32_peak, step_ms, workload):

@@ -1073,8 +1073,8 @@ struct LanePair {
 
 /* (ab| from the (e0| list of a pair (la >= lb, both <= 1): e indexes the
  * functions of angular momentum la .. la+lb in CCA order */
-template <int LA, int LB>
-__device__ __forceinline__ double lane_hrr(int a, int b, const double *e, const double AB[3]) {
+template <int LA, int LB, typename TT>
+__device__ __forceinline__ TT lane_hrr(int a, int b, const TT *e, const TT AB[3]) {
   if constexpr (LB == 0) {
     return e[a];
   } else {
@@ -1160,17 +1160,28 @@ __global__ void __launch_bounds__(128) eri_lane_kernel(EriArgs args, const int4 
         for (int iq = jhi; iq < jlo; ++iq) body(ip, iq);
       }
     }
-    /* transfer to (ab|cd) and the staging block (mode 4 places) */
-    double E[NEA * NEC];
+    /* transfer to (ab|cd) and the staging block (mode 4 places): in FP32
+     * for the FP32 quartets (whose integrals carry FP32 rounding anyway),
+     * in FP64 otherwise */
+    using TT = typename std::conditional<std::is_same<R, float>::value, float, double>::type;
+    TT E[NEA * NEC];
 #pragma unroll
     for (int e = 0; e < NEA; ++e)
 #pragma unroll
-      for (int f = 0; f < NEC; ++f) E[e * NEC + f] = to_double(acc[e][f]);
-    double ABp[3], ABq[3];
+      for (int f = 0; f < NEC; ++f) {
+        if constexpr (std::is_same<R, float>::value) E[e * NEC + f] = acc[e][f];
+        else E[e * NEC + f] = to_double(acc[e][f]);
+      }
+    TT ABp[3], ABq[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      ABp[k] = P.A[k] - P.B[k];
-      ABq[k] = Q.A[k] - Q.B[k];
+      if constexpr (std::is_same<R, float>::value) {
+        ABp[k] = geomR[pq.x].AB[k];
+        ABq[k] = geomR[pq.y].AB[k];
+      } else {
+        ABp[k] = P.A[k] - P.B[k];
+        ABq[k] = Q.A[k] - Q.B[k];
+      }
     }
     const int4 bp = __ldg(args.pair_blk + pq.x), bq = __ldg(args.pair_blk + pq.y);
     const int ncol = pq.w & 0xFFFFF;
@@ -1181,16 +1192,16 @@ __global__ void __launch_bounds__(128) eri_lane_kernel(EriArgs args, const int4 
 #pragma unroll
       for (int d = 0; d < NC<LD>::v; ++d) {
         /* the ket transfer: Y[e] = (e0|cd) */
-        double Y[NEA];
+        TT Y[NEA];
 #pragma unroll
-        for (int e = 0; e < NEA; ++e) Y[e] = lane_hrr<LC, LD>(c, d, E + e * NEC, ABq);
+        for (int e = 0; e < NEA; ++e) Y[e] = lane_hrr<LC, LD, TT>(c, d, E + e * NEC, ABq);
         int cols[2];
         const int nc = blk_places(bq, c, d, cols);
 #pragma unroll
         for (int a = 0; a < NC<LA>::v; ++a)
 #pragma unroll
           for (int bb = 0; bb < NC<LB>::v; ++bb) {
-            const double v = lane_hrr<LA, LB>(a, bb, Y, ABp);
+            const double v = (double)lane_hrr<LA, LB, TT>(a, bb, Y, ABp);
             int rows[2];
             const int nr = blk_places(bp, a, bb, rows);
             for (int i = 0; i < nr; ++i)
