@@ -307,18 +307,21 @@ __device__ __forceinline__ void rys_root_df(int n, int r, int j, bool in_table, 
 }
 
 /* FP32 Chebyshev sum for the FP32 kernels (their integrals carry FP32
- * rounding anyway), from the FP32 roundings of the same tables: the 12
- * coefficients of one (interval, root) are 48 contiguous, 16-byte aligned
- * bytes, read as three vectors */
-__device__ __forceinline__ float clenshaw12_f4(const float *__restrict__ c, float t) {
+ * rounding anyway), from the FP32 roundings of the same tables.  Only the
+ * first 8 of the 12 coefficients of one (interval, root): the dropped tail
+ * is below 1.3e-9 of the value for the weights and 5e-13 for the roots on
+ * every interval of the 1-5 root rules, far under FP32 rounding (6e-8).
+ * They are 32 contiguous, 16-byte aligned bytes (each 12-coefficient block
+ * starts on a 48-byte boundary), read as two vectors. */
+constexpr int RYS_NCHEB_F = 8;
+__device__ __forceinline__ float clenshaw8_f4(const float *__restrict__ c, float t) {
   const float4 a = __ldg(reinterpret_cast<const float4 *>(c));
   const float4 b = __ldg(reinterpret_cast<const float4 *>(c) + 1);
-  const float4 d = __ldg(reinterpret_cast<const float4 *>(c) + 2);
-  const float k[RYS_NCHEB_D] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, d.x, d.y, d.z, d.w};
+  const float k[RYS_NCHEB_F] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
   float b1 = 0.f, b2 = 0.f;
   const float t2 = 2.f * t;
 #pragma unroll
-  for (int i = RYS_NCHEB_D - 1; i > 0; --i) {
+  for (int i = RYS_NCHEB_F - 1; i > 0; --i) {
     const float b0 = fmaf(t2, b1, k[i] - b2);
     b2 = b1;
     b1 = b0;
@@ -571,8 +574,8 @@ __device__ __forceinline__ void prim_roots(const EriArgs &args, const PrimT<R> *
       const float *c = args.rys32 + args.rc.off[NR - 1] + (size_t)j * (2 * NR) * RYS_NCHEB_D;
 #pragma unroll UR
       for (int rr = 0; rr < NR; ++rr) {
-        rx[rr] = clenshaw12_f4(c + rr * RYS_NCHEB_D, t) * sc * sc;
-        rw[rr] = clenshaw12_f4(c + (NR + rr) * RYS_NCHEB_D, t) * sc * pref;
+        rx[rr] = clenshaw8_f4(c + rr * RYS_NCHEB_D, t) * sc * sc;
+        rw[rr] = clenshaw8_f4(c + (NR + rr) * RYS_NCHEB_D, t) * sc * pref;
       }
     } else {
       const float sc = rsqrtf(Tb);
