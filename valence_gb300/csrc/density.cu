@@ -129,8 +129,8 @@ __device__ __forceinline__ void load_dets(const DetCtx &d, long long q, QInfo &q
 
 /* exact determinant of spin block sp of pair q with up to two strikes, from
  * the three perturbed factorisations of its slot (detpair_kernel) */
-__device__ __forceinline__ double struck_det_exact(const DetCtx &d, long long q, int sp, int ns, const int *rr,
-                                                   const int *cc) {
+__device__ __noinline__ double struck_det_exact(const DetCtx &d, long long q, int sp, int ns, const int *rr,
+                                                const int *cc) {
   const int slot = d.xslot[q];
   if (slot < 0 || slot >= d.xcap) return 0.0;
   const int na = d.ds.nalpha, nb = d.ds.nbeta, n = sp == 0 ? na : nb;
