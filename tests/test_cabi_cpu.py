@@ -265,3 +265,18 @@ def test_plain_c_host_compiles_links_and_runs(lib, tmp_path):
         assert out["create"][0] != "0" and out["opt_create"][0] != "0"
     else:
         assert out["create"][0] == "0" and out["opt_create"][0] == "0"
+
+
+@pytest.mark.parametrize("name", ["water_vshf", "ch_chain", "lif_cluster", "lif_cluster_small", "lif_cluster_3",
+                                  "singular_pair_large", "alkane_chain"])
+def test_workload_generators_parse(lib, tmp_path, name):
+    """Every seeded benchmark workload is a valid VALENCE input for the
+    library's reader, with the counts configs.describe reports."""
+    from valence_gb300 import api, configs
+    p = configs.WORKLOADS[name](str(tmp_path / (name + ".inp")))
+    d = api.read_input(p)
+    c = d.contents
+    dsc = configs.describe(p)
+    assert (c.natom, c.npair, c.nunpd, c.ndocc, c.totlen) == (dsc["atoms"], dsc["coupled_pairs"], dsc["unpaired"],
+                                                             dsc["docc"], dsc["weights"])
+    lib.vsvb_free_desc(d)

@@ -172,6 +172,41 @@ def lif_cluster_small(path, seed=3):
     return lif_cluster(path, seed=seed, n=2, ndocc=12)
 
 
+def alkane_chain(path, seed=4, ncarbon=42, nh=86, npair=8, ndocc=117):
+    """The large optimisation loop's geometry: a zigzag chain of ncarbon Z=6
+    atoms at 1.54 A with nh Z=1 atoms at 1.09 A (two per carbon, one more on
+    each end carbon), s/p/d basis (C: 3s 2p 1d, H: 2s 1p 1d; 3-6 primitives,
+    exponents log-uniform in [0.08, 3000]), npair Rumer pairs on
+    neighbouring carbons and ndocc doubly occupied orbitals on 1-2 atoms.
+    Defined for completeness: its size (about 1,500 functions, 65,536
+    determinant pairs) is beyond what the GPU path runs."""
+    rng = np.random.default_rng(seed)
+    c = _shells(rng, [0, 0, 0, 1, 1, 2], 0.08, 3000.0, (3, 6))
+    h = _shells(rng, [0, 0, 1, 2], 0.08, 3000.0, (3, 6))
+    th = math.radians(109.5) / 2
+    atoms = []
+    for i in range(ncarbon):
+        atoms.append((1, 1.54 * math.sin(th) * i, 0.0, (0.0 if i % 2 == 0 else 1.54 * math.cos(th))))
+    hpos = []
+    for i in range(ncarbon):
+        x, y, z = atoms[i][1:]
+        zd = -1.0 if i % 2 == 0 else 1.0
+        for sgn in (1, -1):
+            hpos.append((x, sgn * 1.09 * math.sin(th), z + zd * 1.09 * math.cos(th)))
+    hpos.append((atoms[0][1] - 1.09, 0.0, atoms[0][3]))
+    hpos.append((atoms[-1][1] + 1.09, 0.0, atoms[-1][3]))
+    atoms += [(2, *p) for p in hpos[:nh]]
+    nf = {1: _nfun(c), 2: _nfun(h)}
+    orbs = []
+    for k in range(2 * npair + ndocc):
+        a = k % (ncarbon - 1)
+        atl = [a + 1, a + 2] if k < 2 * npair or k % 2 == 0 else [a + 1]
+        orbs.append((atl, rng.uniform(-1, 1, sum(nf[atoms[j - 1][0]] for j in atl))))
+    pairs = [(2 * k + 1, 2 * k + 2) for k in range(npair)]
+    write_input(path, atoms, [(6.0, c), (1.0, h)], orbs, npair=npair, pairs=pairs)
+    return path
+
+
 def lif_cluster_3(path, seed=3):
     """The cluster workload at 3x3x3 (27 atoms, 243 functions, 108 DOCC): the
     block-mode kernels at the full cluster's chunk size, small enough for a
@@ -237,5 +272,5 @@ def describe(path):
 
 
 WORKLOADS = {"water_vshf": water_vshf, "ch_chain": ch_chain, "lif_cluster": lif_cluster,
-             "lif_cluster_small": lif_cluster_small, "lif_cluster_3": lif_cluster_3,
+             "lif_cluster_small": lif_cluster_small, "lif_cluster_3": lif_cluster_3, "alkane_chain": alkane_chain,
              "singular_pair_large": singular_pair_large}
