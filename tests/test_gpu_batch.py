@@ -73,6 +73,9 @@ def test_batch_matches_individual(vg, tmp_path, precision):
             assert abs(r["energy"] - r0["energy"]) < 1e-9 * max(1.0, abs(r0["energy"]))
             assert np.max(np.abs(g.cpu().numpy() - g0)) < 1e-9 * max(1.0, np.abs(g0).max())
     assert b.launches > 0
+    # one merged ERI sweep for all molecules: fewer launches than the
+    # molecules' own evaluations together
+    assert b.launches < sum(r0["n_kernel_launches"] for r0, _ in ref)
     # new weights for one molecule, same pointers: replay sees them
     ws[0].mul_(0.5)
     res = b.energy_grad_device([w.data_ptr() for w in ws], [g.data_ptr() for g in gs])

@@ -140,3 +140,10 @@ int eri_launch(int mode, int kind, int cp, int cq, const EriArgs &a, const int4 
   if (kind == ERI_F32) return eri_dispatch_f32(mode, cp, cq, a, work, nwork, max_blocks, st);
   return eri_dispatch_df64(mode, cp, cq, a, work, nwork, max_blocks, st);
 }
+
+int eri_launch_tab(int kind, int cp, int cq, const EriArgs &a, const int4 *work, int nwork, int max_blocks,
+                   cudaStream_t st, const EriArgs *tab, const int *wmol) {
+  if (kind == ERI_F64) return eri_dispatch_tab_f64(cp, cq, a, work, nwork, max_blocks, st, tab, wmol);
+  if (kind == ERI_F32) return eri_dispatch_tab_f32(cp, cq, a, work, nwork, max_blocks, st, tab, wmol);
+  return eri_dispatch_tab_df64(cp, cq, a, work, nwork, max_blocks, st, tab, wmol);
+}

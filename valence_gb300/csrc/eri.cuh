@@ -62,6 +62,17 @@ int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int4 *w, 
 int eri_dispatch_f32(int mode, int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st);
 int eri_dispatch_df64(int mode, int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks,
                       cudaStream_t st);
+/* A forward + adjoint (mode 3) launch over the quartets of many molecules:
+ * work item i belongs to molecule wmol[i] with arguments tab[wmol[i]]
+ * (device arrays); a gives the primitive window of the launch. */
+int eri_launch_tab(int kind, int cp, int cq, const EriArgs &a, const int4 *work, int nwork, int max_blocks,
+                   cudaStream_t st, const EriArgs *tab, const int *wmol);
+int eri_dispatch_tab_f64(int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st,
+                         const EriArgs *tab, const int *wmol);
+int eri_dispatch_tab_f32(int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st,
+                         const EriArgs *tab, const int *wmol);
+int eri_dispatch_tab_df64(int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st,
+                          const EriArgs *tab, const int *wmol);
 double eri_flops(int mode, int cp, int cq, double nprimq, int nopP, int nopQ);
 int eri_symmetrize(double *T, int np, double *sq, cudaStream_t st);
 /* block mode: algorithmic FLOPs of the transfer (ab|cd) = M_P (e0|f0) M_Q^T

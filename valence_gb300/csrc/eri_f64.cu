@@ -12,3 +12,8 @@ int eri_dispatch_f64(int mode, int cp, int cq, const EriArgs &a, const int4 *w, 
   if (mode == 4) return dispatch_blk<double>(cp, cq, a, w, n, max_blocks, st);
   return 3;
 }
+
+int eri_dispatch_tab_f64(int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st,
+                          const EriArgs *tab, const int *wmol) {
+  return dispatch_tab<double>(cp, cq, a, w, n, max_blocks, st, tab, wmol);
+}

@@ -630,8 +630,12 @@ __device__ __forceinline__ void prim_roots(const EriArgs &args, const PrimT<R> *
  * MODE 2: adjoint -- accumulate dE/dX for both pairs from Tbar.
  * MODE 3: forward and adjoint from one evaluation of each quartet.
  */
-template <int LA, int LB, int LC, int LD, typename R, int MODE>
-__global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int4 *__restrict__ work, int nwork) {
+/* TAB: a batch launch over the quartets of many molecules -- item i of the
+ * work list belongs to molecule wmol[i], whose arguments are tab[wmol[i]];
+ * the launch's own arguments give only the primitive window */
+template <int LA, int LB, int LC, int LD, typename R, int MODE, bool TAB = false>
+__global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args0, const int4 *__restrict__ work, int nwork,
+                                                         const EriArgs *__restrict__ tab, const int *__restrict__ wmol) {
   using S = QuartetShape<LA, LB, LC, LD, sizeof(R)>;
   constexpr bool CTA = S::CTA;
   extern __shared__ double smem[];
@@ -648,12 +652,13 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
   int lexp[3];
   list_exp(S::ROWM ? LA : LC, lfun, lexp);
   R *h2d = reinterpret_cast<R *>(ws);
-  const PrimT<R> *__restrict__ primR = static_cast<const PrimT<R> *>(prec_data<R>::prim(args));
-  const GeomT<R> *__restrict__ geomR = static_cast<const GeomT<R> *>(prec_data<R>::geom(args));
 
   const int item0 = CTA ? (int)blockIdx.x : (int)blockIdx.x * WARPS + warp;
   const int istep = CTA ? (int)gridDim.x : (int)gridDim.x * WARPS;
   for (int item = item0; item < nwork; item += istep) {
+    const EriArgs &args = TAB ? tab[wmol[item]] : args0;
+    const PrimT<R> *__restrict__ primR = static_cast<const PrimT<R> *>(prec_data<R>::prim(args));
+    const GeomT<R> *__restrict__ geomR = static_cast<const GeomT<R> *>(prec_data<R>::geom(args));
     const int4 pq = work[item];
     const ShellPair &P = args.pairs[pq.x];
     const ShellPair &Q = args.pairs[pq.y];
@@ -662,7 +667,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args, const int
     for (int m = 0; m < S::NK; ++m) acc[m] = R(0);
     /* primitive screen: pairs' primitives are sorted by their bound q0, so
      * rows ip whose q0_p q0_q(first) falls below eps end the contraction */
-    const float eps = args.prim_lo, eps_hi = args.prim_hi;
+    const float eps = args0.prim_lo, eps_hi = args0.prim_hi;
     int nrow = P.nprim;
     if (eps > 0.f) {
       const float qtop = args.prim_q0[Q.prim0];
@@ -1227,12 +1232,13 @@ int launch_lane(const EriArgs &args, const int4 *work, int nwork, int max_blocks
   return cudaGetLastError() != cudaSuccess;
 }
 
-template <int LA, int LB, int LC, int LD, typename R, int MODE>
-int launch_one(const EriArgs &args, const int4 *work, int nwork, int max_blocks, cudaStream_t st) {
+template <int LA, int LB, int LC, int LD, typename R, int MODE, bool TAB = false>
+int launch_one(const EriArgs &args, const int4 *work, int nwork, int max_blocks, cudaStream_t st,
+               const EriArgs *tab = nullptr, const int *wmol = nullptr) {
   if (nwork <= 0) return 0;
   using S = QuartetShape<LA, LB, LC, LD, sizeof(R)>;
   size_t shm = sizeof(double) * ((size_t)WARPS * S::PER_WARP + S::SHARED);
-  auto kfn = eri_kernel<LA, LB, LC, LD, R, MODE>;
+  auto kfn = eri_kernel<LA, LB, LC, LD, R, MODE, TAB>;
   static bool attr_done = false;
   if (!attr_done) {
     if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess) return 1;
@@ -1241,7 +1247,7 @@ int launch_one(const EriArgs &args, const int4 *work, int nwork, int max_blocks,
   const int per_block = S::CTA ? 1 : WARPS;
   int blocks = (nwork + per_block - 1) / per_block;
   if (blocks > max_blocks) blocks = max_blocks; /* grid-stride beyond this */
-  kfn<<<blocks, WARPS * 32, shm, st>>>(args, work, nwork);
+  kfn<<<blocks, WARPS * 32, shm, st>>>(args, work, nwork, tab, wmol);
   return cudaGetLastError() != cudaSuccess;
 }
 
@@ -1255,9 +1261,25 @@ template <> struct ClsL<3> { static constexpr int a = 2, b = 0; };
 template <> struct ClsL<4> { static constexpr int a = 2, b = 1; };
 template <> struct ClsL<5> { static constexpr int a = 2, b = 2; };
 
-template <int CP, int CQ, typename R, int MODE>
-int launch_cls(const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st) {
-  return launch_one<ClsL<CP>::a, ClsL<CP>::b, ClsL<CQ>::a, ClsL<CQ>::b, R, MODE>(a, w, n, max_blocks, st);
+template <int CP, int CQ, typename R, int MODE, bool TAB = false>
+int launch_cls(const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st, const EriArgs *tab = nullptr,
+               const int *wmol = nullptr) {
+  return launch_one<ClsL<CP>::a, ClsL<CP>::b, ClsL<CQ>::a, ClsL<CQ>::b, R, MODE, TAB>(a, w, n, max_blocks, st, tab,
+                                                                                     wmol);
+}
+
+/* batch launches (forward + adjoint, mode 3) over the quartets of many
+ * molecules, per-item arguments from tab[wmol[item]] */
+template <typename R>
+int dispatch_tab(int cp, int cq, const EriArgs &a, const int4 *w, int n, int max_blocks, cudaStream_t st,
+                 const EriArgs *tab, const int *wmol) {
+#define CASE(X, Y) \
+  if (cp == X && cq == Y) return launch_cls<X, Y, R, 3, true>(a, w, n, max_blocks, st, tab, wmol);
+  CASE(0, 0) CASE(1, 0) CASE(1, 1) CASE(2, 0) CASE(2, 1) CASE(2, 2)
+  CASE(3, 0) CASE(3, 1) CASE(3, 2) CASE(3, 3) CASE(4, 0) CASE(4, 1) CASE(4, 2) CASE(4, 3) CASE(4, 4)
+  CASE(5, 0) CASE(5, 1) CASE(5, 2) CASE(5, 3) CASE(5, 4) CASE(5, 5)
+#undef CASE
+  return 2;
 }
 
 /* block mode: s and p pair classes only; up to 27 (e0|f0) components one

@@ -29,6 +29,7 @@
 #include <set>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "../../include/vsvb_gpu.h"
@@ -1598,7 +1599,20 @@ int block_sweep(vsvb_gpu *h) {
 /* forward pass on coeff_d; leaves E in result[0..4] (device).  With fused,
  * the ERI sweep also accumulates the (unscaled) adjoint dE/dX from the
  * unscreened cofactor densities. */
+/* the forward pass in two halves around the ERI sweep, so that a batch can
+ * run one sweep for all its molecules between them */
+int forward_pre(vsvb_gpu *h, bool fused);
+int forward_post(vsvb_gpu *h, bool fused);
+
 int forward(vsvb_gpu *h, bool fused = false) {
+  int rc = forward_pre(h, fused);
+  if (rc) return rc;
+  rc = h->blk_on ? block_sweep(h) : eri_sweep(h, fused ? 3 : 0);
+  if (rc) return rc;
+  return forward_post(h, fused); /* launches keep counting across the three */
+}
+
+int forward_pre(vsvb_gpu *h, bool fused) {
   cudaStream_t st = h->st;
   h->launches = 0;
   CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), st), "memset status");
@@ -1644,10 +1658,12 @@ int forward(vsvb_gpu *h, bool fused = false) {
     h->launches += 2;
   }
   CK(cudaMemsetAsync(h->T.p, 0, sizeof(double) * h->T.n, st), "memset T");
-  {
-    int rc = h->blk_on ? block_sweep(h) : eri_sweep(h, fused ? 3 : 0);
-    if (rc) return rc;
-  }
+  return VSVB_OK;
+}
+
+int forward_post(vsvb_gpu *h, bool fused) {
+  cudaStream_t st = h->st;
+  DetCtx dc = det_ctx(h);
   if (eri_symmetrize(h->T.p, h->np, h->sqT.p, st)) {
     h->err = "symmetrize launch failed";
     return VSVB_ERR_CUDA;
@@ -2057,6 +2073,23 @@ struct vsvb_batch {
   DBuf<double> res; /* [n][5] */
   DBuf<int> stat;   /* [n] */
   int launches = 0;
+  /* one ERI sweep for every molecule (all handles per quartet, fused
+   * gradient): the molecules' class launches merged per (arithmetic, bra
+   * class, ket class, primitive window), each item tagged with its molecule */
+  bool merged = false;
+  struct Group {
+    int kind, a, c, n;
+    float lo, hi;
+    long long off;
+  };
+  std::vector<Group> groups;
+  DBuf<int4> gwork;
+  DBuf<int> gmol;
+  DBuf<EriArgs> etab;
+  static constexpr int NAUX = 6;
+  cudaStream_t aux[NAUX] = {};
+  cudaEvent_t sfork = nullptr, sjoin[NAUX] = {};
+  std::vector<cudaEvent_t> pre; /* per molecule: its half before the sweep is done */
 };
 
 namespace {
@@ -2071,9 +2104,78 @@ int batch_fail(vsvb_batch *b, cudaError_t e, const char *what) {
     if (e_ != cudaSuccess) return batch_fail(b, e_, what); \
   } while (0)
 
+/* the merged evaluation on the batch's streams: per molecule (on its own
+ * stream) weights in and the forward half before the sweep; one sweep of
+ * merged class launches over every molecule's quartets on the side streams;
+ * per molecule the rest of the forward pass, the adjoint and the results */
+int batch_enqueue_merged(vsvb_batch *b, const double *const *w, double *const *g, int &launches) {
+  const int n = (int)b->hs.size();
+  launches = 0;
+  BCK(cudaEventRecord(b->fork, b->st), "event record");
+  int rc = VSVB_OK;
+  for (int i = 0; i < n && !rc; ++i) {
+    vsvb_gpu *h = b->hs[i];
+    cudaStream_t saved = h->st;
+    h->st = h->own_st;
+    if (cudaStreamWaitEvent(h->st, b->fork, 0) != cudaSuccess ||
+        cudaMemcpyAsync(h->coeff_d.p, w[i], sizeof(double) * h->totlen, cudaMemcpyDeviceToDevice, h->st) != cudaSuccess)
+      rc = VSVB_ERR_CUDA;
+    if (!rc) rc = forward_pre(h, true);
+    launches += h->launches;
+    if (!rc && (cudaEventRecord(b->pre[i], h->st) != cudaSuccess ||
+                cudaStreamWaitEvent(b->st, b->pre[i], 0) != cudaSuccess))
+      rc = VSVB_ERR_CUDA;
+    if (rc && h->err.size()) b->err = "molecule " + std::to_string(i) + ": " + h->err;
+    h->st = saved;
+  }
+  if (rc) return rc;
+  BCK(cudaEventRecord(b->sfork, b->st), "event record");
+  for (int k = 0; k < vsvb_batch::NAUX; ++k) BCK(cudaStreamWaitEvent(b->aux[k], b->sfork, 0), "stream wait");
+  EriArgs a0 = eri_args(b->hs[0]);
+  for (size_t k = 0; k < b->groups.size(); ++k) {
+    const auto &G = b->groups[k];
+    a0.prim_lo = G.lo;
+    a0.prim_hi = G.hi;
+    if (eri_launch_tab(G.kind, G.a, G.c, a0, b->gwork.p + G.off, G.n, b->hs[0]->nsm * 16,
+                       b->aux[k % vsvb_batch::NAUX], b->etab.p, b->gmol.p + G.off)) {
+      b->err = "merged ERI launch failed";
+      return VSVB_ERR_CUDA;
+    }
+    ++launches;
+  }
+  for (int k = 0; k < vsvb_batch::NAUX; ++k) {
+    BCK(cudaEventRecord(b->sjoin[k], b->aux[k]), "event record");
+    BCK(cudaStreamWaitEvent(b->st, b->sjoin[k], 0), "stream wait");
+  }
+  BCK(cudaEventRecord(b->sfork, b->st), "event record");
+  for (int i = 0; i < n && !rc; ++i) {
+    vsvb_gpu *h = b->hs[i];
+    cudaStream_t saved = h->st;
+    h->st = h->own_st;
+    if (cudaStreamWaitEvent(h->st, b->sfork, 0) != cudaSuccess) rc = VSVB_ERR_CUDA;
+    h->launches = 0;
+    if (!rc) rc = forward_post(h, true);
+    const int nl = h->launches;
+    if (!rc) rc = backward(h, true);
+    launches += nl + h->launches;
+    if (!rc && (cudaMemcpyAsync(g[i], h->coeff_bar.p, sizeof(double) * h->totlen, cudaMemcpyDeviceToDevice,
+                                h->st) != cudaSuccess ||
+                cudaMemcpyAsync(b->res.p + 5 * i, h->result.p, sizeof(double) * 5, cudaMemcpyDeviceToDevice,
+                                h->st) != cudaSuccess ||
+                cudaMemcpyAsync(b->stat.p + i, h->status.p, sizeof(int), cudaMemcpyDeviceToDevice, h->st) != cudaSuccess ||
+                cudaEventRecord(b->join[i], h->st) != cudaSuccess ||
+                cudaStreamWaitEvent(b->st, b->join[i], 0) != cudaSuccess))
+      rc = VSVB_ERR_CUDA;
+    if (rc && h->err.size()) b->err = "molecule " + std::to_string(i) + ": " + h->err;
+    h->st = saved;
+  }
+  return rc;
+}
+
 /* capture every handle's evaluation (copy weights in, forward + adjoint,
- * copy gradient and result out) as one graph, each handle on its own stream
- * forked from and joined into the batch stream */
+ * copy gradient and result out) as one graph: merged (one sweep for all
+ * molecules) when the batch allows it, otherwise each handle on its own
+ * stream branch forked from and joined into the batch stream */
 int batch_capture(vsvb_batch *b, const double *const *w, double *const *g) {
   if (b->exec) {
     cudaGraphExecDestroy(b->exec);
@@ -2081,8 +2183,29 @@ int batch_capture(vsvb_batch *b, const double *const *w, double *const *g) {
   }
   const int n = (int)b->hs.size();
   BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal), "begin capture");
-  BCK(cudaEventRecord(b->fork, b->st), "event record");
   int rc = VSVB_OK, launches = 0;
+  if (b->merged) {
+    rc = batch_enqueue_merged(b, w, g, launches);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->st, &graph);
+    if (rc || e != cudaSuccess || !graph) {
+      if (graph) cudaGraphDestroy(graph);
+      (void)cudaGetLastError();
+      if (b->err.empty()) b->err = "batch capture failed";
+      return rc ? rc : VSVB_ERR_CUDA;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+      b->exec = nullptr;
+      return batch_fail(b, ei, "graph instantiate");
+    }
+    b->w.assign(w, w + n);
+    b->g.assign(g, g + n);
+    b->launches = launches;
+    return VSVB_OK;
+  }
+  BCK(cudaEventRecord(b->fork, b->st), "event record");
   for (int i = 0; i < n && !rc; ++i) {
     vsvb_gpu *h = b->hs[i];
     cudaStream_t saved = h->st;
@@ -2163,6 +2286,63 @@ int vsvb_batch_create(vsvb_gpu *const *handles, int n, vsvb_batch **out) {
       return rc;
     }
   }
+  /* merged sweep: every handle on the per-quartet path with the fused
+   * gradient (one ERI sweep per evaluation) */
+  b->merged = true;
+  for (vsvb_gpu *h : b->hs) b->merged = b->merged && !h->blk_on && h->opt.grad_mode == 0;
+  if (b->merged) {
+    std::map<std::tuple<int, int, int, float, float>, std::vector<std::pair<int, int>>> key;
+    for (int i = 0; i < n; ++i)
+      for (const auto &it : b->hs[i]->sweep) key[std::make_tuple(it.kind, it.a, it.c, it.lo, it.hi)].push_back({i, it.wl});
+    std::vector<int4> work;
+    std::vector<int> mol;
+    for (const auto &kv : key) {
+      vsvb_batch::Group G{};
+      G.kind = std::get<0>(kv.first);
+      G.a = std::get<1>(kv.first);
+      G.c = std::get<2>(kv.first);
+      G.lo = std::get<3>(kv.first);
+      G.hi = std::get<4>(kv.first);
+      G.off = (long long)work.size();
+      for (const auto &m : kv.second) {
+        const auto &lst = b->hs[m.first]->item_wh[m.second];
+        work.insert(work.end(), lst.begin(), lst.end());
+        mol.insert(mol.end(), lst.size(), m.first);
+      }
+      G.n = (int)(work.size() - G.off);
+      if (G.n > 0) b->groups.push_back(G);
+    }
+    /* most work first over the side streams */
+    std::stable_sort(b->groups.begin(), b->groups.end(),
+                     [](const vsvb_batch::Group &x, const vsvb_batch::Group &y) { return x.n > y.n; });
+    std::vector<EriArgs> tab;
+    for (vsvb_gpu *h : b->hs) tab.push_back(eri_args(h));
+    BCK(b->gwork.upload(work.empty() ? std::vector<int4>(1, make_int4(0, 0, 0, 0)) : work), "upload merged work");
+    BCK(b->gmol.upload(mol.empty() ? std::vector<int>(1, 0) : mol), "upload merged work");
+    BCK(b->etab.upload(tab), "upload argument table");
+    for (int k = 0; k < vsvb_batch::NAUX; ++k) {
+      BCK(cudaStreamCreateWithFlags(&b->aux[k], cudaStreamNonBlocking), "cudaStreamCreate");
+      BCK(cudaEventCreateWithFlags(&b->sjoin[k], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    BCK(cudaEventCreateWithFlags(&b->sfork, cudaEventDisableTiming), "cudaEventCreate");
+    b->pre.assign(n, nullptr);
+    for (int i = 0; i < n; ++i) BCK(cudaEventCreateWithFlags(&b->pre[i], cudaEventDisableTiming), "cudaEventCreate");
+    /* one eager merged evaluation: sets the merged kernels' attributes
+     * outside any capture */
+    std::vector<DBuf<double>> wd(n), gd(n);
+    std::vector<const double *> wp(n);
+    std::vector<double *> gp(n);
+    for (int i = 0; i < n; ++i) {
+      BCK(wd[i].upload(b->hs[i]->coeff0), "upload weights");
+      BCK(gd[i].alloc(b->hs[i]->totlen), "alloc gradient");
+      wp[i] = wd[i].p;
+      gp[i] = gd[i].p;
+    }
+    int launches = 0;
+    int rc = batch_enqueue_merged(b, wp.data(), gp.data(), launches);
+    if (rc) return rc;
+    BCK(cudaStreamSynchronize(b->st), "merged warm-up");
+  }
   return VSVB_OK;
 }
 
@@ -2216,6 +2396,13 @@ void vsvb_batch_destroy(vsvb_batch *b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   for (cudaEvent_t e : b->join)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->pre)
+    if (e) cudaEventDestroy(e);
+  for (int k = 0; k < vsvb_batch::NAUX; ++k) {
+    if (b->aux[k]) cudaStreamDestroy(b->aux[k]);
+    if (b->sjoin[k]) cudaEventDestroy(b->sjoin[k]);
+  }
+  if (b->sfork) cudaEventDestroy(b->sfork);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
