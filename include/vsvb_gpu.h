@@ -116,6 +116,14 @@ typedef struct vsvb_options {
                            * s/p systems (more than 5e7 candidate shell quartets), 1: on,
                            * -1: off.  Energies only; a gradient call returns
                            * VSVB_ERR_UNSUPPORTED on a block-mode handle */
+  int core_mode;          /* the determinant-pair sum over the doubly occupied core shared by
+                           * every determinant, in closed form: one P x P factorisation per
+                           * pair and spin (P coupled pairs) and one pass over the orbital-pair
+                           * ERIs, in place of the per-pair task loop (valence.F90:1153-1433).
+                           * Needs 1-10 spin-coupled pairs and no unpaired orbitals.
+                           * 0 (default): on from 4096 determinant pairs, 1: on (else
+                           * VSVB_ERR_UNSUPPORTED at create), -1: off.  Gradients with
+                           * grad_mode 0 only (VSVB_ERR_UNSUPPORTED otherwise) */
 } vsvb_options;
 
 typedef struct vsvb_energy_result {
@@ -365,6 +373,10 @@ int vsvb_gpu_debug_orbital_eri_at(vsvb_gpu *h, const long long *idx, int n, doub
  * and counts: atom quartets, chunks, kernel launches of the sweep.  Returns
  * 1 when the handle runs in block mode, 0 when not. */
 int vsvb_gpu_block_stats(const vsvb_gpu *h, double *eri_flops3, double *transform_flops3, long long *counts3);
+/* Core mode (vsvb_options.core_mode): FMAs of the pair-summed density GEMM
+ * of one energy evaluation, and counts2 = {determinant pairs, coupled
+ * orbitals}.  Returns 1 on a core-mode handle, 0 otherwise, negative on error. */
+int vsvb_gpu_core_stats(const vsvb_gpu *h, double *gemm_fma, long long *counts2);
 /* Orbital overlap and core-Hamiltonian matrices of the last evaluation
  * (n x n, row-major). */
 int vsvb_gpu_debug_orbital_1e(vsvb_gpu *h, double *s, double *hcore, size_t cap);

@@ -53,7 +53,7 @@ class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("mixed_threshold", ctypes.c_double), ("ao_screen", ctypes.c_double),
                 ("device", ctypes.c_int), ("grad_mode", ctypes.c_int), ("prim_screen", ctypes.c_double),
                 ("prim_split", ctypes.c_int), ("cuda_graph", ctypes.c_int), ("autotune", ctypes.c_int),
-                ("block_mode", ctypes.c_int)]
+                ("block_mode", ctypes.c_int), ("core_mode", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -102,6 +102,7 @@ def lib():
         L.vsvb_gpu_debug_orbital_1e.argtypes = [ctypes.c_void_p, P(D), P(D), ctypes.c_size_t]
         L.vsvb_gpu_debug_orbital_eri_at.argtypes = [ctypes.c_void_p, P(ctypes.c_longlong), I, P(D)]
         L.vsvb_gpu_block_stats.argtypes = [ctypes.c_void_p, P(D), P(D), P(ctypes.c_longlong)]
+        L.vsvb_gpu_core_stats.argtypes = [ctypes.c_void_p, P(D), P(ctypes.c_longlong)]
         L.vsvb_gpu_batch_energy_grad.argtypes = [P(ctypes.c_void_p), I, P(P(D)), P(Result), P(P(D))]
         L.vsvb_gpu_set_stream.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.vsvb_gpu_set_spin_coeffs.argtypes = [ctypes.c_void_p, P(D)]
@@ -184,7 +185,7 @@ def read_input(path):
 
 
 def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, grad_mode=0, prim_screen=None,
-                 prim_split=None, cuda_graph=None, autotune=None, block_mode=None):
+                 prim_split=None, cuda_graph=None, autotune=None, block_mode=None, core_mode=None):
     o = Options()
     lib().vsvb_default_options(ctypes.byref(o))
     o.precision = precision
@@ -202,6 +203,8 @@ def make_options(precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0
         o.autotune = int(autotune)
     if block_mode is not None:
         o.block_mode = int(block_mode)
+    if core_mode is not None:
+        o.core_mode = int(core_mode)
     return o
 
 
@@ -209,7 +212,8 @@ class System:
     """One molecule on the GPU: a parsed input plus a device handle."""
 
     def __init__(self, path, precision=FP64, mixed_threshold=1e-6, ao_screen=1e-15, device=0, coords_angstrom=None,
-                 grad_mode=0, prim_screen=None, prim_split=None, cuda_graph=None, autotune=None, block_mode=None):
+                 grad_mode=0, prim_screen=None, prim_split=None, cuda_graph=None, autotune=None, block_mode=None,
+                 core_mode=None):
         self.path = path
         self._desc = read_input(path)
         d = self._desc.contents
@@ -220,7 +224,7 @@ class System:
         if coords_angstrom is not None:
             self._coords_bohr[:] = np.asarray(coords_angstrom, dtype=np.float64).ravel() * 1.889725987722
         self.opt = make_options(precision, mixed_threshold, ao_screen, device, grad_mode, prim_screen, prim_split,
-                                cuda_graph, autotune, block_mode)
+                                cuda_graph, autotune, block_mode, core_mode)
         self._h = ctypes.c_void_p()
         rc = lib().vsvb_gpu_create(self._desc, ctypes.byref(self.opt), ctypes.byref(self._h))
         if rc:
@@ -359,6 +363,17 @@ class System:
         return {"on": bool(on), "eri_flops": {"fp64": ef[0], "fp32": ef[1], "df64": ef[2]},
                 "transform_flops": {"fp64": tf[0], "fp32": tf[1], "df64": tf[2]},
                 "atom_quartets": cn[0], "chunks": cn[1], "launches": cn[2]}
+
+    def core_stats(self):
+        """Core-mode figures: whether the handle sums the determinant pairs
+        over the shared core, the FMAs of its pair-summed density GEMM per
+        evaluation, the determinant pairs and the coupled orbitals."""
+        f = ctypes.c_double()
+        cn = (ctypes.c_longlong * 2)()
+        on = lib().vsvb_gpu_core_stats(self._h, ctypes.byref(f), cn)
+        if on < 0:
+            raise VSVBError("core_stats failed")
+        return {"on": bool(on), "gemm_fma": f.value, "determinant_pairs": cn[0], "coupled_orbitals": cn[1]}
 
     def orbital_1e(self):
         n = lib().vsvb_gpu_num_orbitals(self._h)

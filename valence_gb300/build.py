@@ -16,7 +16,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libvsvb_gb300.so")
 CU = ["eri.cu", "eri_f64.cu", "eri_f32.cu", "eri_df64.cu", "density.cu", "onee.cu", "handle.cu", "peak.cu",
-      "detfactor.cu", "optimize.cu", "block.cu"]
+      "detfactor.cu", "optimize.cu", "block.cu", "core.cu"]
 CPP = ["input.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -34,6 +34,7 @@
 
 #include "../../include/vsvb_gpu.h"
 #include "block.cuh"
+#include "core.cuh"
 #include "density.cuh"
 #include "eri.cuh"
 #include "handle_internal.h"
@@ -251,6 +252,20 @@ struct vsvb_gpu {
   DBuf<int> blk_atom_nf, blk_atom_c0, blk_orb, blk_cao;
   DBuf<double> blk_catom, blk_G;
   cudaEvent_t blk_done[2] = {nullptr, nullptr};
+  /* core mode (core.cu): the determinant-pair sum over the shared doubly
+   * occupied core in closed form */
+  bool core_on = false;
+  int core_nt = 0;
+  DBuf<unsigned char> core_detorb, core_detpos;
+  DBuf<int> core_lst1, core_off1, core_lst2, core_off2, core_pslot, core_pcount;
+  DBuf<int2> core_pik;
+  DBuf<double> core_fw, core_G, core_Y, core_M, core_P0, core_U, core_s0, core_dd, core_L, core_pool;
+  DBuf<double> core_A0, core_A1, core_A2, core_A2x, core_R1, core_Wv, core_X, core_part;
+  int core_cap = 0;
+  /* core-mode adjoint (core.cu CoreGrad) */
+  static constexpr int CORE_NCHUNK = 64;
+  DBuf<double> cg_Yg, cg_Axp, cg_Ax, cg_Wvb, cg_KP, cg_KR, cg_R1b, cg_P0b, cg_A1b, cg_Ub, cg_Mbp, cg_lam, cg_Mb, cg_sc,
+      cg_t1, cg_t2;
 };
 
 namespace {
@@ -400,6 +415,89 @@ AsmArgs asm_args(vsvb_gpu *h) {
     a.g_in_smem = 4 * gbytes <= 40 * 1024 ? 4 : (gbytes <= 40 * 1024 ? 1 : 0);
   }
   return a;
+}
+
+int setup_core(vsvb_gpu *h, const std::vector<int> &pslot);
+
+CoreGrad core_grad(vsvb_gpu *h) {
+  CoreGrad g{};
+  g.Gam = h->Tbar.p;
+  g.Yg = h->cg_Yg.p;
+  g.Axp = h->cg_Axp.p;
+  g.nchunk = vsvb_gpu::CORE_NCHUNK;
+  g.Ax = h->cg_Ax.p;
+  g.Wvb = h->cg_Wvb.p;
+  g.KP = h->cg_KP.p;
+  g.KR = h->cg_KR.p;
+  g.R1b = h->cg_R1b.p;
+  g.P0b = h->cg_P0b.p;
+  g.A1b = h->cg_A1b.p;
+  g.Ub = h->cg_Ub.p;
+  g.Mbp = h->cg_Mbp.p;
+  g.lam = h->cg_lam.p;
+  g.Mb = h->cg_Mb.p;
+  g.sc = h->cg_sc.p;
+  g.t1 = h->cg_t1.p;
+  g.t2 = h->cg_t2.p;
+  g.Sbar = h->Sbar.p;
+  g.Hbar = h->Hbar.p;
+  return g;
+}
+
+CoreArgs core_args(vsvb_gpu *h) {
+  CoreArgs c{};
+  const DetSetup &ds = h->ds;
+  c.nsp = ds.nsp;
+  c.P = ds.npair;
+  c.nC = 2 * ds.npair;
+  c.nD = ds.nsp - c.nC;
+  c.nsc = ds.nsc;
+  c.ndet = ds.nsc << ds.npair;
+  c.nelec = ds.nelec;
+  c.nq = ds.nq;
+  c.np = h->np;
+  c.ncp = c.nC * (c.nC + 1) / 2;
+  c.kx = c.ncp + 2;
+  c.So = h->So.p;
+  c.Ho = h->Ho.p;
+  c.csc = h->coeff_sc.p;
+  c.detorb = h->core_detorb.p;
+  c.detpos = h->core_detpos.p;
+  c.lst1 = h->core_lst1.p;
+  c.off1 = h->core_off1.p;
+  c.lst2 = h->core_lst2.p;
+  c.off2 = h->core_off2.p;
+  c.pik = h->core_pik.p;
+  c.fw = h->core_fw.p;
+  c.G = h->core_G.p;
+  c.Y = h->core_Y.p;
+  c.M = h->core_M.p;
+  c.P0 = h->core_P0.p;
+  c.U = h->core_U.p;
+  c.s0 = h->core_s0.p;
+  c.dd = h->core_dd.p;
+  c.L = h->core_L.p;
+  c.pslot = h->core_pslot.p;
+  c.pool = h->core_pool.p;
+  c.pcount = h->core_pcount.p;
+  c.cap = h->core_cap;
+  c.status = h->status.p;
+  c.A0 = h->core_A0.p;
+  c.A1 = h->core_A1.p;
+  c.A2 = h->core_A2.p;
+  c.A2x = h->core_A2x.p;
+  c.R1 = h->core_R1.p;
+  c.Wv = h->core_Wv.p;
+  c.X = h->core_X.p;
+  c.T = h->T.p;
+  c.sq = h->sqT.p;
+  c.itol = h->itol;
+  c.part = h->core_part.p;
+  c.ntile = h->core_nt;
+  c.enuc = h->enuc;
+  c.out = h->result.p;
+  c.nsing = h->nsing.p;
+  return c;
 }
 
 /* arithmetic of a schedule: list 1 holds the quartets below the mixed
@@ -1395,7 +1493,24 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   CK(h->slot_which.upload(swhich.empty() ? std::vector<int>(1, 0) : swhich), "upload sc");
   CK(h->coeff_sc.upload(csc), "upload coeff_sc");
   h->csc_h = csc;
-  const long long nq = ds.nq;
+  const long long nq_all = ds.nq;
+  {
+    /* core mode: every determinant pair shares the doubly occupied core
+     * (no unpaired orbitals, the usual slot layout); automatic from 4096
+     * determinant pairs */
+    const bool fits = d->nunpd == 0 && !h->hs_split && d->npair >= 1 && d->npair <= 10;
+    if (h->opt.core_mode > 0 && !fits) {
+      h->err = "core mode needs spin-coupled pairs (at most 10) and no unpaired orbitals";
+      return VSVB_ERR_UNSUPPORTED;
+    }
+    h->core_on = fits && (h->opt.core_mode > 0 || (h->opt.core_mode == 0 && nq_all >= 4096));
+  }
+  if (h->core_on) {
+    int rc = setup_core(h, pslot);
+    if (rc) return rc;
+  }
+  /* per-pair buffers of the factorised path (one element in core mode) */
+  const long long nq = h->core_on ? 1 : nq_all;
   const int na = ds.nalpha, nb = ds.nbeta;
   CK(h->det_a.alloc(nq), "alloc det");
   CK(h->det_b.alloc(nq), "alloc det");
@@ -1421,11 +1536,11 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   long long ntij = (long long)nsp * (nsp + 1) / 2;
   h->ntasks = ntij * (ntij + 1) / 2;
   long long work = std::max<long long>(h->ntasks, (long long)ds.nelec * ds.nelec);
-  long long want = (16LL * h->nsm + nq - 1) / nq;
+  long long want = (16LL * h->nsm + nq_all - 1) / nq_all;
   long long maxs = (work + 127) / 128;
   h->nsplit = (int)std::max<long long>(1, std::min(want, maxs));
   h->nsplit_max = (int)std::max<long long>(1, std::min(4 * want, maxs)); /* autotuner range */
-  size_t nslot = (size_t)nq * h->nsplit_max;
+  size_t nslot = (size_t)nq_all * h->nsplit_max;
   CK(h->part_e1.alloc(nslot), "alloc parts");
   CK(h->part_wf.alloc(nslot), "alloc parts");
   CK(h->part_e2.alloc(nslot), "alloc parts");
@@ -1443,6 +1558,80 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   return VSVB_OK;
 }
 
+/* core-mode tables: per determinant (coupling, spin-flip bits) the coupled
+ * orbital at each block position of each spin and the reverse map, the
+ * determinants grouped by the spins of one or two coupled orbitals, the
+ * orbital-pair index map; and the buffers of core.cu */
+int setup_core(vsvb_gpu *h, const std::vector<int> &pslot) {
+  const DetSetup &ds = h->ds;
+  const int P = ds.npair, nC = 2 * P, nsc = ds.nsc, nsp = ds.nsp, nD = nsp - nC;
+  const int ndet = nsc << P;
+  std::vector<unsigned char> orb((size_t)ndet * 2 * P), pos((size_t)ndet * nC);
+  for (int dt = 0; dt < ndet; ++dt) {
+    const int sc = dt >> P, bits = dt & ((1 << P) - 1);
+    for (int sp = 0; sp < 2; ++sp)
+      for (int r = 0; r < P; ++r) {
+        const int o = pslot[((size_t)sc * P + r) * 2 + (sp ^ ((bits >> r) & 1))];
+        orb[((size_t)dt * 2 + sp) * P + r] = (unsigned char)o;
+        pos[(size_t)dt * nC + o] = (unsigned char)((sp << 5) | r);
+      }
+  }
+  auto spin = [&](int dt, int o) { return pos[(size_t)dt * nC + o] >> 5; };
+  std::vector<int> l1, o1(2 * nC + 1), l2, o2(4 * nC * nC + 1);
+  for (int x = 0; x < nC; ++x)
+    for (int sp = 0; sp < 2; ++sp) {
+      o1[2 * x + sp] = (int)l1.size();
+      for (int dt = 0; dt < ndet; ++dt)
+        if (spin(dt, x) == sp) l1.push_back(dt);
+    }
+  o1[2 * nC] = (int)l1.size();
+  for (int x = 0; x < nC; ++x)
+    for (int y = 0; y < nC; ++y)
+      for (int g = 0; g < 4; ++g) {
+        o2[4 * (x * nC + y) + g] = (int)l2.size();
+        for (int dt = 0; dt < ndet; ++dt)
+          if (2 * spin(dt, x) + spin(dt, y) == g) l2.push_back(dt);
+      }
+  o2[4 * nC * nC] = (int)l2.size();
+  std::vector<int2> pik((size_t)h->np);
+  for (int i = 0; i < nsp; ++i)
+    for (int k = 0; k <= i; ++k) pik[(size_t)i * (i + 1) / 2 + k] = make_int2(i, k);
+  CK(h->core_detorb.upload(orb), "upload core tables");
+  CK(h->core_detpos.upload(pos), "upload core tables");
+  CK(h->core_lst1.upload(l1), "upload core tables");
+  CK(h->core_off1.upload(o1), "upload core tables");
+  CK(h->core_lst2.upload(l2), "upload core tables");
+  CK(h->core_off2.upload(o2), "upload core tables");
+  CK(h->core_pik.upload(pik), "upload core tables");
+  const long long nq = ds.nq;
+  const int P2 = P * P, ncp = nC * (nC + 1) / 2, kx = ncp + 2;
+  CK(h->core_fw.alloc(std::max<size_t>((size_t)nD * (2 * nD + nC), 1)), "alloc core");
+  CK(h->core_G.alloc(std::max<size_t>((size_t)nD * nD, 1)), "alloc core");
+  CK(h->core_Y.alloc(std::max<size_t>((size_t)nD * nC, 1)), "alloc core");
+  CK(h->core_M.alloc((size_t)nC * nC), "alloc core");
+  CK(h->core_P0.alloc((size_t)nsp * nsp), "alloc core");
+  CK(h->core_U.alloc((size_t)nsp * nC), "alloc core");
+  CK(h->core_s0.alloc(1), "alloc core");
+  CK(h->core_dd.alloc((size_t)nq * 2), "alloc core");
+  CK(h->core_L.alloc((size_t)nq * 2 * P2), "alloc core");
+  CK(h->core_pslot.alloc((size_t)nq), "alloc core");
+  CK(h->core_pcount.alloc(1), "alloc core");
+  /* flagged-pair pool: three perturbed factorisations per spin, up to 512 MiB */
+  const size_t per = (size_t)6 * (1 + P2);
+  h->core_cap = (int)std::min<size_t>((size_t)nq, ((size_t)1 << 26) / per);
+  CK(h->core_pool.alloc(std::max<size_t>((size_t)h->core_cap * per, 1)), "alloc core");
+  CK(h->core_A0.alloc(1), "alloc core");
+  CK(h->core_A1.alloc((size_t)nC * nC), "alloc core");
+  CK(h->core_A2.alloc((size_t)nC * nC * nC * nC), "alloc core");
+  CK(h->core_A2x.alloc((size_t)kx * kx), "alloc core");
+  CK(h->core_R1.alloc((size_t)nsp * nsp), "alloc core");
+  CK(h->core_Wv.alloc((size_t)h->np * kx), "alloc core");
+  CK(h->core_X.alloc((size_t)h->np * kx), "alloc core");
+  h->core_nt = (h->np + 63) / 64;
+  CK(h->core_part.alloc((size_t)h->core_nt * h->core_nt), "alloc core");
+  return VSVB_OK;
+}
+
 int alloc_grad(vsvb_gpu *h) {
   if (h->grad_ready) return VSVB_OK;
   const long long nq = h->ds.nq;
@@ -1454,10 +1643,32 @@ int alloc_grad(vsvb_gpu *h) {
   CK(h->xbar.alloc(std::max<long long>(h->nxelem, 1)), "alloc xbar");
   CK(h->xbarh.alloc(std::max<long long>(h->nxh, 1)), "alloc xbarh");
   CK(h->Cbar.alloc((size_t)h->norb_all * h->maxobs), "alloc Cbar");
-  CK(h->vtot.alloc((size_t)nq * h->nsplit_max), "alloc vtot");
-  CK(h->Gglob.alloc(std::max<long long>(nq * (na * na + nb * nb), 1)), "alloc G");
-  CK(h->Gs.alloc(std::max<long long>(nq * (na * na + nb * nb), 1)), "alloc Gs");
-  CK(h->vtot_s.alloc((size_t)nq * h->nsplit_max), "alloc vtot_s");
+  if (h->core_on) {
+    /* the pair sums' adjoint instead of the per-pair walk buffers */
+    const int P = h->ds.npair, nC = 2 * P, kx = nC * (nC + 1) / 2 + 2, n = h->nsp;
+    const size_t nn = (size_t)n * n;
+    CK(h->cg_Yg.alloc((size_t)h->np * kx), "alloc core adjoint");
+    CK(h->cg_Axp.alloc((size_t)vsvb_gpu::CORE_NCHUNK * kx * kx), "alloc core adjoint");
+    CK(h->cg_Ax.alloc((size_t)kx * kx), "alloc core adjoint");
+    CK(h->cg_Wvb.alloc((size_t)h->np * kx), "alloc core adjoint");
+    CK(h->cg_KP.alloc(nn), "alloc core adjoint");
+    CK(h->cg_KR.alloc(nn), "alloc core adjoint");
+    CK(h->cg_R1b.alloc(nn), "alloc core adjoint");
+    CK(h->cg_P0b.alloc(nn), "alloc core adjoint");
+    CK(h->cg_A1b.alloc((size_t)nC * nC), "alloc core adjoint");
+    CK(h->cg_Ub.alloc((size_t)n * nC), "alloc core adjoint");
+    CK(h->cg_Mbp.alloc((size_t)h->ds.nq * 2 * P * P), "alloc core adjoint");
+    CK(h->cg_lam.alloc((size_t)h->ds.nq), "alloc core adjoint");
+    CK(h->cg_Mb.alloc((size_t)nC * nC), "alloc core adjoint");
+    CK(h->cg_sc.alloc(4), "alloc core adjoint");
+    CK(h->cg_t1.alloc(nn), "alloc core adjoint");
+    CK(h->cg_t2.alloc(nn), "alloc core adjoint");
+  }
+  const long long nqw = h->core_on ? 1 : nq;
+  CK(h->vtot.alloc((size_t)nqw * h->nsplit_max), "alloc vtot");
+  CK(h->Gglob.alloc(std::max<long long>(nqw * (na * na + nb * nb), 1)), "alloc G");
+  CK(h->Gs.alloc(std::max<long long>(nqw * (na * na + nb * nb), 1)), "alloc Gs");
+  CK(h->vtot_s.alloc((size_t)nqw * h->nsplit_max), "alloc vtot_s");
   CK(h->D1.alloc((size_t)h->nsp * h->nsp), "alloc D1");
   CK(h->coeff_bar.alloc(h->totlen), "alloc coeff_bar");
   CK(h->ndf_bar.alloc(std::max(h->ndf, 1)), "alloc ndf_bar");
@@ -1639,6 +1850,28 @@ int forward_pre(vsvb_gpu *h, bool fused) {
   CK(cudaMemsetAsync(h->sing.p, 0, sizeof(int) * h->sing.n, st), "memset sing");
   CK(cudaMemsetAsync(h->xcount.p, 0, sizeof(int), st), "memset pool count");
   CK(cudaMemsetAsync(h->nsing.p, 0, sizeof(int), st), "memset nsing");
+  if (h->core_on) {
+    /* the pair sums over the shared core need the overlaps only */
+    const int nl = core_pre(core_args(h), st);
+    if (nl < 0) {
+      h->err = "core-mode launch failed";
+      return VSVB_ERR_CUDA;
+    }
+    h->launches += nl;
+    if (fused) {
+      /* Gamma is the sweep's dE_num/dT */
+      int rc = alloc_grad(h);
+      if (rc) return rc;
+      CK(cudaMemsetAsync(h->xbarh.p, 0, sizeof(double) * h->xbarh.n, st), "memset xbarh");
+      if (core_gamma(core_args(h), h->Tbar.p, st) < 0 || eri_to_float(h->Tbar.p, h->Tbar32.p, h->Tbar.n, st)) {
+        h->err = "core-mode launch failed";
+        return VSVB_ERR_CUDA;
+      }
+      h->launches += 2;
+    }
+    CK(cudaMemsetAsync(h->T.p, 0, sizeof(double) * h->T.n, st), "memset T");
+    return VSVB_OK;
+  }
   DetCtx dc = det_ctx(h);
   detpair_kernel<<<(unsigned)h->ds.nq, std::max(h->ds.nalpha, h->ds.nbeta) > 64 ? 512 : 128, 0, st>>>(
       dc, h->scratch.p, h->ld_scratch);
@@ -1669,6 +1902,15 @@ int forward_post(vsvb_gpu *h, bool fused) {
     return VSVB_ERR_CUDA;
   }
   h->launches++;
+  if (h->core_on) {
+    const int nl = core_post(core_args(h), fused ? h->Tbar.p : nullptr, st);
+    if (nl < 0) {
+      h->err = "core-mode launch failed";
+      return VSVB_ERR_CUDA;
+    }
+    h->launches += nl;
+    return VSVB_OK;
+  }
   AsmArgs aa = asm_args(h);
   if (fused) {
     /* one walk for the energy sums and the (unscaled) adjoint quantities */
@@ -1732,6 +1974,10 @@ int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
     h->err = "more singular determinant pairs than the exact-minor pool holds";
     return VSVB_ERR_UNSUPPORTED;
   }
+  if (status & 8) {
+    h->err = "the doubly occupied orbitals' overlap block is singular";
+    return VSVB_ERR_SINGULAR;
+  }
   if (out) {
     fill_result(h, r, out);
     out->n_singular_pairs = nsing;
@@ -1748,7 +1994,7 @@ int finish_result(vsvb_gpu *h, vsvb_energy_result *out) {
  * Each candidate runs 3 times on the handle's own data (min taken); the
  * choice changes launch shapes only, never the arithmetic. */
 int autotune(vsvb_gpu *h) {
-  if ((h->sweep.empty() && h->ntasks == 0) || h->blk_on) return VSVB_OK;
+  if ((h->sweep.empty() && h->ntasks == 0) || h->blk_on || h->core_on) return VSVB_OK;
   int rc = forward(h); /* weight tables, T and determinant pairs for the timed launches */
   if (rc) return rc;
   CK(cudaStreamSynchronize(h->st), "autotune sync");
@@ -1845,7 +2091,15 @@ int backward(vsvb_gpu *h, bool fused) {
   AsmArgs aa = asm_args(h);
   aa.status = h->status.p;
   aa.res = h->result.p;
-  if (fused) {
+  if (h->core_on) {
+    /* dE/dS_orb and dE/dh_orb of the pair sums; dE/dT went into the sweep */
+    const int nl = core_adjoint(core_args(h), core_grad(h), st);
+    if (nl < 0) {
+      h->err = "core-mode adjoint launch failed";
+      return VSVB_ERR_CUDA;
+    }
+    h->launches += nl;
+  } else if (fused) {
     /* the forward walk accumulated the adjoint quantities unscaled */
     grad_scale_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, aa, h->nsplit);
     CK(cudaGetLastError(), "grad scale");
@@ -1857,8 +2111,10 @@ int backward(vsvb_gpu *h, bool fused) {
     size_t gsh = sizeof(double) * (size_t)(na * na + nb * nb) * aa.g_in_smem;
     CK(launch_assemble(1, dim3((unsigned)h->ds.nq, h->nsplit), 128, gsh, st, dc, aa), "assemble grad");
   }
-  detpair_adjoint_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, aa, h->nsplit);
-  CK(cudaGetLastError(), "detpair adjoint");
+  if (!h->core_on) {
+    detpair_adjoint_kernel<<<(unsigned)h->ds.nq, 128, 0, st>>>(dc, aa, h->nsplit);
+    CK(cudaGetLastError(), "detpair adjoint");
+  }
   if (!fused) {
     int rc2 = eri_sweep(h, 2);
     if (rc2) return rc2;
@@ -1905,6 +2161,7 @@ void vsvb_default_options(vsvb_options *o) {
   o->cuda_graph = 1;
   o->autotune = 0;
   o->block_mode = 0;
+  o->core_mode = 0;
 }
 
 int vsvb_gpu_create(const vsvb_system_desc *d, const vsvb_options *opt, vsvb_gpu **out) {
@@ -2010,6 +2267,10 @@ static int enqueue_eval(vsvb_gpu *h, bool fused) {
 static int energy_grad_common(vsvb_gpu *h, vsvb_energy_result *out, double *grad, bool grad_on_device) {
   if (h->blk_on) {
     h->err = "the gradient is not available on a block-mode handle";
+    return VSVB_ERR_UNSUPPORTED;
+  }
+  if (h->core_on && h->opt.grad_mode != 0) {
+    h->err = "a core-mode handle takes the fused gradient (grad_mode 0) only";
     return VSVB_ERR_UNSUPPORTED;
   }
   const bool fused = h->opt.grad_mode == 0;
@@ -2549,6 +2810,19 @@ int vsvb_gpu_block_stats(const vsvb_gpu *h, double *eri_flops3, double *transfor
     counts3[2] = (long long)h->blk_launch.size() + (long long)h->blk_chunk.size();
   }
   return h->blk_on ? 1 : 0;
+}
+
+int vsvb_gpu_core_stats(const vsvb_gpu *h, double *gemm_fma, long long *counts2) {
+  if (!h) return -VSVB_ERR_INPUT;
+  if (!h->core_on) return 0;
+  vsvb_gpu *hh = const_cast<vsvb_gpu *>(h);
+  const CoreArgs c = core_args(hh);
+  if (gemm_fma) *gemm_fma = core_gemm_fma(c);
+  if (counts2) {
+    counts2[0] = c.nq;
+    counts2[1] = (long long)c.nC;
+  }
+  return 1;
 }
 
 int vsvb_gpu_debug_orbital_1e(vsvb_gpu *h, double *s, double *hc, size_t cap) {
