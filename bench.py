@@ -2,17 +2,20 @@
 against plain FP64.
 
 Workload (default, the largest configuration that runs on one GPU): the
-64-atom Li/F cluster -- a 4x4x4 grid of alternating Z=3/Z=9 atoms at 2.0 A,
-s/p basis of 576 Cartesian functions (3s 2p per atom, 3-6 primitives,
-exponents log-uniform in [0.05, 1e4]), 304 doubly occupied orbitals on 1-2
-atoms with seeded uniform(-1, 1) weights, integral screen 1e-12
-(valence_gb300.configs.lif_cluster, seed 3).  That configuration defines an
-energy evaluation (no gradient), so a step is one guess energy: 1.07e9
-orbital-quartet tasks over a 46,360 x 46,360 orbital-pair ERI matrix built in
-block mode (vsvb_options.block_mode).  --workload ch_chain runs the
-spin-coupled C/H chain (104 functions, 4 Rumer pairs, 256 determinant pairs)
-with a step of one energy + adjoint gradient; its figures are also reported
-under "ch_chain" in the default line.
+128-atom alkane-like chain -- 42 Z=6 atoms in a zigzag at 1.54 A with 86 Z=1
+atoms at 1.09 A, s/p/d basis of 1,576 Cartesian functions (C: 3s 2p 1d, H:
+2s 1p 1d; 3-6 primitives, exponents log-uniform in [0.08, 3000]), 8 Rumer
+spin-coupled pairs on neighbouring carbons (256 determinants per side,
+65,536 determinant pairs) and 117 doubly occupied orbitals on 1-2 atoms with
+seeded uniform(-1, 1) weights (valence_gb300.configs.alkane_chain, seed 4).
+A step is one energy + adjoint gradient with respect to all 3,120 weights;
+the determinant pairs are summed over their shared doubly occupied core in
+closed form (vsvb_options.core_mode).  The same line reports the optimisation
+loop that configuration defines ("loop": 20 descent steps on the mixed
+path's gradient, each energy re-evaluated in FP64), the 64-atom Li/F cluster
+("lif_cluster": 576 functions, 304 DOCC, energy only, block mode) and the
+spin-coupled C/H chain ("ch_chain": 104 functions, 256 determinant pairs,
+energy + gradient).
 
 The headline value is the mixed path (VSVB_MIXED_DF64: FP32 for shell
 quartets whose Schwarz bound is below 1e-6, double-float -- pairs of FP32
@@ -56,9 +59,14 @@ METRIC = "VSVB energy+grad evals/s, mixed vs plain FP64 on 1 GB300 at |ΔE|<=1e-
 # workloads whose configuration defines an energy evaluation only; any
 # workload run in block mode is timed as energy evaluations as well
 ENERGY_ONLY = {"lif_cluster", "lif_cluster_3"}
+# workloads of seconds per step: their FP64 and FP32 + native-FP64 arms run
+# fewer steps than the headline arm
+LARGE = {"lif_cluster", "lif_cluster_3", "alkane_chain"}
 # bounded CPU-oracle samples per phase (Schwarz entries, one-electron terms,
-# two-electron tasks) for workloads whose full CPU evaluation takes hours
-CPU_SAMPLE = {"lif_cluster": (16, 16, 12), "lif_cluster_3": (16, 16, 12)}
+# two-electron tasks) for workloads whose full CPU evaluation takes hours;
+# on the alkane chain one one-electron term or task of the oracle runs its
+# factorisations of all 65,536 determinant pairs (about a minute)
+CPU_SAMPLE = {"lif_cluster": (16, 16, 12), "lif_cluster_3": (16, 16, 12), "alkane_chain": (2, 2, 3)}
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
@@ -122,12 +130,14 @@ def _args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="lif_cluster")
+    ap.add_argument("--workload", default="alkane_chain")
     ap.add_argument("--mixed-threshold", type=float, default=1e-6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
                     help="time only the headline mixed arm (used for per-kernel launch lists)")
     ap.add_argument("--no-optimizer", action="store_true", help="skip the optimiser-path figures")
+    ap.add_argument("--loop-steps", type=int, default=20,
+                    help="descent steps of the alkane chain's optimisation loop; 0 skips it")
     ap.add_argument("--block-mode", default="auto", choices=["auto", "on", "off"],
                     help="vsvb_options.block_mode of the headline workload (auto: on for large s/p systems)")
     ap.add_argument("--batch", type=int, default=256,
@@ -266,7 +276,7 @@ def run_reference(a, rank, world):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    steps = max(1, min(a.steps, 2 if a.workload in CPU_SAMPLE else 3))
+    steps = max(1, min(a.steps, (1 if a.workload == "alkane_chain" else 2) if a.workload in CPU_SAMPLE else 3))
     with tempfile.TemporaryDirectory() as d:
         path = _workload(a.workload, d)
         times = []
@@ -321,7 +331,7 @@ def block_roofline(stats, block_ms, fp64_peak, fp32_peak, step_ms):
             "fp64_fma_tflops": fp64_peak / 1e12, "fp32_fma_tflops": fp32_peak / 1e12}
 
 
-def measure(a, workload, world, dev, stream, flush, steps, warmup, side_steps, side_warmup):
+def measure(a, workload, world, dev, stream, flush, steps, warmup, side_steps, side_warmup, cpu=True):
     """One workload: the mixed (double-float) arm over exactly `steps` timed
     steps with its roofline timing, then the FP64 and VSVB_MIXED arms
     (side_steps each) and the host-API arm (steps), one handle at a time."""
@@ -399,6 +409,12 @@ def measure(a, workload, world, dev, stream, flush, steps, warmup, side_steps, s
         w_pin = torch.from_numpy(smx.coeff0.copy()).pin_memory()
         g_pin = torch.zeros(n, dtype=torch.float64).pin_memory()
         stats = smx.block_stats()
+        core = smx.core_stats()
+        if core["on"]:
+            cfg["determinant_pair_sum"] = (f"core mode (vsvb_options.core_mode): {core['determinant_pairs']} "
+                                           f"determinant pairs summed over the shared doubly occupied core in "
+                                           f"closed form, FP64; pair-summed density GEMM "
+                                           f"{core['gemm_fma']:.3g} FMAs per energy")
         sweep, sweep_wall = {}, []
 
         def collect():
@@ -444,7 +460,7 @@ def measure(a, workload, world, dev, stream, flush, steps, warmup, side_steps, s
         out["mixed_native_over_fp64"] = out["mixed_native_fp64"]["value"] / out["fp64"]["value"]
         out["abs_dE_mixed_vs_fp64"] = abs(r_mx["energy"] - e64)
         out["err_est_mixed"] = r_mx["err_est"]
-        if world == 1 and not a.no_cpu_baseline:
+        if world == 1 and cpu and not a.no_cpu_baseline:
             cores = os.cpu_count() or 1
             dt, sample = _cpu_seconds(workload, path, cores)
             out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "evals/s", "cores": cores, "kind": "port",
@@ -460,12 +476,12 @@ def run_ours(a, rank, world):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 126 MB L2
-    energy_only = a.workload in ENERGY_ONLY or a.block_mode == "on"
-    # the FP64 and FP32 + native FP64 arms of an energy-only (large) workload
-    # are timed on fewer steps than the headline arm: they are reported beside
-    # it, not as the headline
-    side_steps = min(a.steps, 2) if energy_only else a.steps
-    side_warmup = 1 if energy_only else a.warmup
+    large = a.workload in LARGE or a.block_mode == "on"
+    # the FP64 and FP32 + native FP64 arms of a large workload are timed on
+    # fewer steps than the headline arm: they are reported beside it, not as
+    # the headline
+    side_steps = min(a.steps, 3) if large else a.steps
+    side_warmup = 1 if large else a.warmup
     m = measure(a, a.workload, world, dev, stream, flush, a.steps, a.warmup, side_steps, side_warmup)
     if rank != 0:
         return
@@ -487,6 +503,18 @@ def run_ours(a, rank, world):
     for k in ("e2e", "fp64", "mixed_native_fp64", "mixed_over_fp64", "mixed_native_over_fp64",
               "abs_dE_mixed_vs_fp64", "err_est_mixed", "cpu_baseline"):
         out[k] = m.get(k)
+    if a.workload == "alkane_chain" and a.loop_steps > 0:
+        out["loop"] = run_loop(a, dev, stream)
+    if a.workload != "lif_cluster":
+        c = measure(a, "lif_cluster", world, dev, stream, flush, min(a.steps, 3), 1, 2, 1, cpu=False)
+        out["lif_cluster"] = {"config": c["config"], "value": c["value"], "unit": "energy evals/s",
+                              "ms_per_step": statistics.mean(c["ms_mx"]), "e2e": c["e2e"], "fp64": c["fp64"],
+                              "mixed_native_fp64": c["mixed_native_fp64"], "mixed_over_fp64": c["mixed_over_fp64"],
+                              "mixed_native_over_fp64": c["mixed_native_over_fp64"],
+                              "abs_dE_mixed_vs_fp64": c["abs_dE_mixed_vs_fp64"], "err_est_mixed": c["err_est_mixed"],
+                              "roofline": c["roofline"], "gpu_launches": c["launches"], "clocks": c["clocks"],
+                              "cpu_baseline_note": "the CPU oracle's sampled cluster evaluation is timed by "
+                                                   "bench.py --workload lif_cluster"}
     if a.workload != "ch_chain":
         c = measure(a, "ch_chain", world, dev, stream, flush, a.steps, a.warmup, a.steps, a.warmup)
         out["ch_chain"] = {"config": c["config"], "value": c["value"], "unit": "energy+grad evals/s",
@@ -521,6 +549,39 @@ def run_ours(a, rank, world):
     if not a.no_optimizer:
         out["optimizer"] = run_optimizer(a, dev)
     print(json.dumps(out))
+
+
+def run_loop(a, dev, stream):
+    """The alkane chain's optimisation loop: a.loop_steps steepest-descent
+    steps on all weights with the mixed path's adjoint gradient and an Armijo
+    line search on mixed energies (valence_gb300.loop.descend), each
+    accepted point's energy re-evaluated in plain FP64 (|dE| <= 1e-6 Eh is
+    the acceptance bar of the configuration)."""
+    import valence_gb300 as vg
+    from valence_gb300 import loop
+    with tempfile.TemporaryDirectory() as d:
+        path = _workload("alkane_chain", d)
+        smx = vg.System(path, precision=vg.MIXED_DF64, mixed_threshold=a.mixed_threshold, device=dev)
+        s64 = vg.System(path, precision=vg.FP64, device=dev)
+        smx.set_stream(stream.cuda_stream)
+        s64.set_stream(stream.cuda_stream)
+        smx.energy_grad()
+        s64.energy()
+        t = time.perf_counter()
+        _, recs = loop.descend(smx, steps=a.loop_steps, check=s64)
+        wall = time.perf_counter() - t
+        smx.close()
+        s64.close()
+    dmax = max(r["abs_dE_vs_check"] for r in recs)
+    return {"steps": len(recs), "wall_s": wall, "s_per_step": wall / len(recs),
+            "mixed_s_per_step": sum(r["seconds"] for r in recs) / len(recs),
+            "fp64_check_s_per_step": sum(r["check_seconds"] for r in recs) / len(recs),
+            "evaluations": sum(r["evaluations"] for r in recs),
+            "energy_first": recs[0]["energy"], "energy_last": recs[-1]["energy"],
+            "max_abs_dE_mixed_vs_fp64": dmax, "within_1e-6": dmax <= 1e-6,
+            "energies": [r["energy"] for r in recs], "abs_dE": [r["abs_dE_vs_check"] for r in recs],
+            "method": "steepest descent on all weights, Armijo backtracking on mixed energies "
+                      "(valence_gb300.loop.descend); FP64 energy at every accepted point"}
 
 
 def run_optimizer(a, dev):

@@ -107,13 +107,21 @@ static void setangn(vo_state *st, int nang) {
 
 static size_t tri(size_t i) { return i * (i + 1) / 2; }
 
+/* without a cache (its pointer table did not fit in memory) the block is
+ * computed into a per-thread buffer, valid until the thread's next call */
+static __thread double tl_eri_blk[10000];
+
 static const double *eri_block_canon(vo_state *st, int a, int b, int c, int d) {
   size_t ab = tri((size_t)a) + (size_t)b, cd = tri((size_t)c) + (size_t)d;
   size_t key = tri(ab) + cd;
-  double *p = __atomic_load_n(&st->eri_cache[key], __ATOMIC_ACQUIRE);
-  if (p) return p;
   int n = shell_size(st->gsh[a].l) * shell_size(st->gsh[b].l) * shell_size(st->gsh[c].l) *
           shell_size(st->gsh[d].l);
+  if (!st->eri_cache) {
+    vo_shell_eri(&st->gsh[a], &st->gsh[b], &st->gsh[c], &st->gsh[d], tl_eri_blk);
+    return tl_eri_blk;
+  }
+  double *p = __atomic_load_n(&st->eri_cache[key], __ATOMIC_ACQUIRE);
+  if (p) return p;
   double *blk = (double *)malloc(sizeof(double) * (size_t)n);
   vo_shell_eri(&st->gsh[a], &st->gsh[b], &st->gsh[c], &st->gsh[d], blk);
   double *expected = NULL;
@@ -902,7 +910,7 @@ static vo_state *state_new(vo_input *in) {
   }
   size_t np = tri((size_t)ng);
   st->ncanon = tri(np);
-  st->eri_cache = (double **)calloc(st->ncanon + 1, sizeof(double *));
+  st->eri_cache = (double **)calloc(st->ncanon + 1, sizeof(double *)); /* NULL: blocks computed uncached */
   /* max OBS size (:118-130) */
   st->max_obs = 0;
   for (int i = 1; i <= in->norbs; ++i) {

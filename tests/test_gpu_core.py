@@ -139,3 +139,17 @@ def test_core_full_chain_eight_pairs(vg, tmp_path):
         em = s64.energy(w)["energy"]
         # central-difference noise: 1e-16 |E| / h
         assert abs((ep - em) / 2e-5 - g64[i]) < 1e-6 * gmax + 1e-16 * abs(r64["energy"]) / 1e-5
+
+
+def test_descent_loop_on_the_chain(vg, tmp_path):
+    """Two steps of the optimisation loop (valence_gb300.loop.descend) on the
+    65,536-pair chain: mixed-path gradient steps lower the energy, and the
+    FP64 energy at each accepted point is within 1e-6 Eh of the mixed one."""
+    from valence_gb300 import configs, loop
+    p = configs.alkane_chain(str(tmp_path / "ac8.inp"))
+    smx = vg.System(p, precision=vg.MIXED_DF64)
+    s64 = vg.System(p)
+    e0 = smx.energy()["energy"]
+    _, recs = loop.descend(smx, steps=2, check=s64)
+    assert recs[0]["energy"] < e0 and recs[1]["energy"] < recs[0]["energy"]
+    assert all(r["abs_dE_vs_check"] < 1e-6 for r in recs)
