@@ -121,7 +121,7 @@ typedef struct vsvb_options {
                            * pair and spin (P coupled pairs) and one pass over the orbital-pair
                            * ERIs, in place of the per-pair task loop (valence.F90:1153-1433).
                            * Needs 1-10 spin-coupled pairs and no unpaired orbitals.
-                           * 0 (default): on from 4096 determinant pairs, 1: on (else
+                           * 0 (default): on from 4096 determinant pairs with grad_mode 0, 1: on (else
                            * VSVB_ERR_UNSUPPORTED at create), -1: off.  Gradients with
                            * grad_mode 0 only (VSVB_ERR_UNSUPPORTED otherwise) */
 } vsvb_options;

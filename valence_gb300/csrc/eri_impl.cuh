@@ -970,6 +970,34 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args0, const in
       if (CTA) __syncthreads();
       else __syncwarp();
     };
+    /* adjoint of one ket chunk (with Y[jl][ab] = (E X_Q^T)[ab][jl] staged):
+     * dX_P[ik][ab] += sum_jl W(ik,jl) Y[jl][ab], W(ik,jl) = Tbar[ik][jl]
+     * (+ Tbar[jl][ik] when the pairs differ).  A thread takes BA components
+     * of one bra orbital pair, so each W element is gathered once per BA
+     * components; every output keeps its jl order. */
+    constexpr int BA = S::NEA < 8 ? S::NEA : 8, NBA = (S::NEA + BA - 1) / BA;
+    auto adj_bra = [&](int j0, int nj) {
+      double *XPb = args.xbar + P.xh0;
+      for (int o = tid; o < P.nop * NBA; o += nthr) {
+        const int ik = o / NBA, ab0 = (o - ik * NBA) * BA;
+        const int a = __ldg(opP + ik);
+        TT acc[BA];
+#pragma unroll
+        for (int u = 0; u < BA; ++u) acc[u] = TT(0);
+        for (int jl = 0; jl < nj; ++jl) {
+          const int b = __ldg(opQ + j0 + jl);
+          TT wv = ldt(TbarT + (size_t)a * args.np + b);
+          if (!same) wv += ldt(TbarT + (size_t)b * args.np + a);
+          const TT *y = Y + jl * S::NEA + ab0;
+#pragma unroll
+          for (int u = 0; u < BA; ++u)
+            if (ab0 + u < S::NEA) mad(acc[u], wv, y[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < BA; ++u)
+          if (ab0 + u < S::NEA) atomicAdd(XPb + (size_t)ik * S::NEA + ab0 + u, (double)acc[u]);
+      }
+    };
     if (MODE == 0 || MODE == 3) {
       for (int j0 = 0; j0 < Q.nop; j0 += S::JCH) {
         const int nj = min(S::JCH, Q.nop - j0);
@@ -995,6 +1023,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args0, const in
           const int a = __ldg(opP + ik), b = __ldg(opQ + j0 + jl);
           atomicAdd(args.T + (size_t)a * args.np + b, same ? 0.5 * (double)s : (double)s);
         }
+        if (MODE == 3) adj_bra(j0, nj); /* the same Y serves the bra adjoint */
         sync();
       }
     }
@@ -1003,9 +1032,8 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args0, const in
        * (Tbar[ik][jl] (+ Tbar[jl][ik] when the pairs differ)):
        * dX_P[ik][ab] += sum_jl W(ik,jl) (E X_Q^T)[ab][jl] and
        * dX_Q[jl][cd] += sum_ik W(ik,jl) (X_P E)[ik][cd] */
-      double *XPb = args.xbar + P.xh0;
       double *XQb = args.xbar + Q.xh0;
-      for (int j0 = 0; j0 < Q.nop; j0 += S::JCH) {
+      for (int j0 = 0; MODE == 2 && j0 < Q.nop; j0 += S::JCH) {
         const int nj = min(S::JCH, Q.nop - j0);
         for (int o = tid; o < nj * S::NEA; o += nthr) {
           const int jl = o / S::NEA, abi = o - jl * S::NEA;
@@ -1017,18 +1045,7 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args0, const in
           Y[o] = s;
         }
         sync();
-        for (int o = tid; o < P.nop * S::NEA; o += nthr) {
-          const int ik = o / S::NEA, abi = o - ik * S::NEA;
-          const int a = __ldg(opP + ik);
-          TT s = TT(0);
-          for (int jl = 0; jl < nj; ++jl) {
-            const int b = __ldg(opQ + j0 + jl);
-            TT wv = ldt(TbarT + (size_t)a * args.np + b);
-            if (!same) wv += ldt(TbarT + (size_t)b * args.np + a);
-            mad(s, wv, Y[jl * S::NEA + abi]);
-          }
-          atomicAdd(XPb + (size_t)ik * S::NEA + abi, (double)s);
-        }
+        adj_bra(j0, nj);
         sync();
       }
       constexpr int ICH = S::JCH;
@@ -1043,17 +1060,27 @@ __global__ void __launch_bounds__(WARPS * 32) eri_kernel(EriArgs args0, const in
           Y[o] = s;
         }
         sync();
-        for (int o = tid; o < Q.nop * S::NEC; o += nthr) {
-          const int jl = o / S::NEC, cdi = o - jl * S::NEC;
+        /* dX_Q[jl][cd] += sum_ik W(ik,jl) Y[ik][cd], BC components of one
+         * ket orbital pair per thread */
+        constexpr int BC = S::NEC < 8 ? S::NEC : 8, NBC = (S::NEC + BC - 1) / BC;
+        for (int o = tid; o < Q.nop * NBC; o += nthr) {
+          const int jl = o / NBC, cd0 = (o - jl * NBC) * BC;
           const int b = __ldg(opQ + jl);
-          TT s = TT(0);
+          TT acc[BC];
+#pragma unroll
+          for (int u = 0; u < BC; ++u) acc[u] = TT(0);
           for (int ik = 0; ik < ni; ++ik) {
             const int a = __ldg(opP + i0 + ik);
             TT wv = ldt(TbarT + (size_t)a * args.np + b);
             if (!same) wv += ldt(TbarT + (size_t)b * args.np + a);
-            mad(s, wv, Y[ik * S::NEC + cdi]);
+            const TT *y = Y + ik * S::NEC + cd0;
+#pragma unroll
+            for (int u = 0; u < BC; ++u)
+              if (cd0 + u < S::NEC) mad(acc[u], wv, y[u]);
           }
-          atomicAdd(XQb + (size_t)jl * S::NEC + cdi, (double)s);
+#pragma unroll
+          for (int u = 0; u < BC; ++u)
+            if (cd0 + u < S::NEC) atomicAdd(XQb + (size_t)jl * S::NEC + cd0 + u, (double)acc[u]);
         }
         sync();
       }

@@ -1503,7 +1503,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
       h->err = "core mode needs spin-coupled pairs (at most 10) and no unpaired orbitals";
       return VSVB_ERR_UNSUPPORTED;
     }
-    h->core_on = fits && (h->opt.core_mode > 0 || (h->opt.core_mode == 0 && nq_all >= 4096));
+    h->core_on = fits && (h->opt.core_mode > 0 || (h->opt.core_mode == 0 && nq_all >= 4096 && h->opt.grad_mode == 0));
   }
   if (h->core_on) {
     int rc = setup_core(h, pslot);

@@ -687,6 +687,7 @@ int vsvb_opt_create(const vsvb_system_desc *d, const vsvb_options *opt, vsvb_opt
   vsvb_default_options(&o->opt);
   if (opt) o->opt = *opt;
   o->opt.autotune = 0;
+  o->opt.core_mode = -1; /* the H/S builds read the per-pair walk's quantities */
   copy_desc(d, o->desc);
   o->nnd = 2 * d->npair + d->nunpd;
   o->nsp = o->nnd + d->ndocc;
