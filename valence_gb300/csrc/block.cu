@@ -45,23 +45,7 @@ namespace {
  * Knuth. */
 __device__ __forceinline__ void to_t(double x, double &y) { y = x; }
 __device__ __forceinline__ void to_t(double x, float &y) { y = (float)x; }
-/* double -> double-float without FP64 arithmetic (whose rate is 1/58 of
- * FP32 on this part): hi takes the sign, exponent and top 23 mantissa bits
- * (a truncation, exact in FP32), lo the remaining 29 mantissa bits scaled by
- * their weight (rounded to 24 bits: ~48 significant bits in all).  Values
- * below the FP32 normal range (2^-126) become zero. */
-__device__ __forceinline__ void to_t(double x, df64 &y) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int e = (int)((b >> 52) & 0x7ff);
-  if (e <= 1023 - 127) {
-    y = df64(0.f, 0.f);
-    return;
-  }
-  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-  const float hi = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
-  const float lo = ldexpf(__uint2float_rn((unsigned)(b & 0x1fffffffu)), e - 1075);
-  y = df64(hi, sign ? -lo : lo);
-}
+__device__ __forceinline__ void to_t(double x, df64 &y) { y = df64_split(x); }
 __device__ __forceinline__ double dbl(double v) { return v; }
 __device__ __forceinline__ double dbl(float v) { return (double)v; }
 __device__ __forceinline__ double dbl(df64 v) { return (double)v.hi + (double)v.lo; }

@@ -63,6 +63,23 @@ struct df64 {
   VSVB_HD explicit operator double() const { return (double)hi + (double)lo; }
 };
 
+#ifdef __CUDACC__
+/* double -> double-float without FP64 arithmetic (whose rate is 1/58 of
+ * FP32 on this part): hi takes the sign, exponent and top 23 mantissa bits
+ * (a truncation, exact in FP32), lo the remaining 29 mantissa bits scaled by
+ * their weight (rounded to 24 bits: ~48 significant bits in all).  Values
+ * below the FP32 normal range (2^-126) become zero. */
+__device__ __forceinline__ df64 df64_split(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e <= 1023 - 127) return df64(0.f, 0.f);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const float hi = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+  const float lo = ldexpf(__uint2float_rn((unsigned)(b & 0x1fffffffu)), e - 1075);
+  return df64(hi, sign ? -lo : lo);
+}
+#endif
+
 /* primitive-pair and pair-geometry data in the arithmetic type R of a kernel */
 template <typename R>
 struct PrimT {
