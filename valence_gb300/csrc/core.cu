@@ -48,6 +48,7 @@
 #include <cmath>
 
 #include "core.cuh"
+#include "vsvb_internal.h"
 
 namespace {
 
@@ -570,10 +571,23 @@ __device__ __forceinline__ double core_exch(const CoreArgs &a, double A0, int i,
 
 constexpr int GT = 64, GK = 16;
 
+/* the GEMMs' arithmetic AT: FP64, or double-float (48-bit, on the FP32
+ * pipe, whose rate is 58x the FP64 rate here) for the mixed path */
+template <typename AT>
+__device__ __forceinline__ AT to_at(double v);
+template <>
+__device__ __forceinline__ double to_at<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ df64 to_at<df64>(double v) { return df64_split(v); }
+__device__ __forceinline__ void fmad(double &acc, double x, double y) { acc = fma(x, y, acc); }
+__device__ __forceinline__ void fmad(df64 &acc, df64 x, df64 y) { acc += x * y; }
+__device__ __forceinline__ double as_d(double v) { return v; }
+__device__ __forceinline__ double as_d(df64 v) { return (double)v.hi + (double)v.lo; }
+
 /* Gamma tile (I, J), I <= J, of X Wv^T plus the core's exchange terms:
  * contracted with the masked T tile (off-diagonal tiles count twice), or
  * with STORE written to Gam with its mirror tile */
-template <bool STORE>
+template <bool STORE, typename AT>
 __global__ void __launch_bounds__(256) core_gemm_kernel(CoreArgs a, double *Gam) {
   const int I = blockIdx.y, J = blockIdx.x;
   double *part = a.part + (size_t)I * a.ntile + J;
@@ -581,26 +595,26 @@ __global__ void __launch_bounds__(256) core_gemm_kernel(CoreArgs a, double *Gam)
     if (!STORE && threadIdx.x == 0) *part = 0.0;
     return;
   }
-  __shared__ double As[GK][GT + 1], Bs[GK][GT + 1];
+  __shared__ AT As[GK][GT + 1], Bs[GK][GT + 1];
   __shared__ double red[8];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int p0 = I * GT, q0 = J * GT, np = a.np, kx = a.kx;
-  double acc[4][4];
+  AT acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    for (int j = 0; j < 4; ++j) acc[i][j] = to_at<AT>(0.0);
   for (int k0 = 0; k0 < kx; k0 += GK) {
     for (int e = tid; e < GT * GK; e += 256) {
       const int m = e / GK, kk = e - m * GK, k = k0 + kk;
       const int p = p0 + m, q = q0 + m;
-      As[kk][m] = (p < np && k < kx) ? a.X[(size_t)p * kx + k] : 0.0;
-      Bs[kk][m] = (q < np && k < kx) ? a.Wv[(size_t)q * kx + k] : 0.0;
+      As[kk][m] = to_at<AT>((p < np && k < kx) ? a.X[(size_t)p * kx + k] : 0.0);
+      Bs[kk][m] = to_at<AT>((q < np && k < kx) ? a.Wv[(size_t)q * kx + k] : 0.0);
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < GK; ++kk) {
-      double av[4], bv[4];
+      AT av[4], bv[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) av[i] = As[kk][ty + 16 * i];
 #pragma unroll
@@ -608,7 +622,7 @@ __global__ void __launch_bounds__(256) core_gemm_kernel(CoreArgs a, double *Gam)
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+        for (int j = 0; j < 4; ++j) fmad(acc[i][j], av[i], bv[j]);
     }
     __syncthreads();
   }
@@ -626,14 +640,14 @@ __global__ void __launch_bounds__(256) core_gemm_kernel(CoreArgs a, double *Gam)
       if (q >= np) continue;
       const int2 jl = a.pik[q];
       if (STORE) {
-        const double gv = acc[i][j] + core_exch(a, A0, ik.x, ik.y, jl.x, jl.y);
+        const double gv = as_d(acc[i][j]) + core_exch(a, A0, ik.x, ik.y, jl.x, jl.y);
         Gam[(size_t)p * np + q] = gv;
         Gam[(size_t)q * np + p] = gv;
         continue;
       }
       const double t = a.T[(size_t)p * np + q];
       if (!(sp * a.sq[q] > itol && fabs(t) > itol)) continue;
-      e += t * (acc[i][j] + core_exch(a, A0, ik.x, ik.y, jl.x, jl.y));
+      e += t * (as_d(acc[i][j]) + core_exch(a, A0, ik.x, ik.y, jl.x, jl.y));
     }
   }
   if (STORE) return;
@@ -710,31 +724,32 @@ __device__ __forceinline__ double masked_t(const CoreArgs &a, int p, int q) {
 }
 
 /* Yg = (T_masked / W) Wv: tiles of 64 orbital pairs x 64 columns */
+template <typename AT>
 __global__ void __launch_bounds__(256) core_ygemm_kernel(CoreArgs a, CoreGrad g) {
-  __shared__ double As[GK][GT + 1], Bs[GK][GT + 1];
+  __shared__ AT As[GK][GT + 1], Bs[GK][GT + 1];
   const int vt = blockIdx.x, I = blockIdx.y;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int p0 = I * GT, v0 = vt * GT, np = a.np, kx = a.kx;
-  double acc[4][4];
+  AT acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    for (int j = 0; j < 4; ++j) acc[i][j] = to_at<AT>(0.0);
   for (int q0 = 0; q0 < np; q0 += GK) {
     for (int e = tid; e < GT * GK; e += 256) {
       const int m = e / GK, kk = e - m * GK;
       const int p = p0 + m, q = q0 + kk;
-      As[kk][m] = (p < np && q < np) ? masked_t(a, p, q) : 0.0;
+      As[kk][m] = to_at<AT>((p < np && q < np) ? masked_t(a, p, q) : 0.0);
     }
     for (int e = tid; e < GK * GT; e += 256) {
       const int kk = e / GT, n = e - kk * GT;
       const int q = q0 + kk, v = v0 + n;
-      Bs[kk][n] = (q < np && v < kx) ? a.Wv[(size_t)q * kx + v] : 0.0;
+      Bs[kk][n] = to_at<AT>((q < np && v < kx) ? a.Wv[(size_t)q * kx + v] : 0.0);
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < GK; ++kk) {
-      double av[4], bv[4];
+      AT av[4], bv[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) av[i] = As[kk][ty + 16 * i];
 #pragma unroll
@@ -742,7 +757,7 @@ __global__ void __launch_bounds__(256) core_ygemm_kernel(CoreArgs a, CoreGrad g)
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+        for (int j = 0; j < 4; ++j) fmad(acc[i][j], av[i], bv[j]);
     }
     __syncthreads();
   }
@@ -754,7 +769,7 @@ __global__ void __launch_bounds__(256) core_ygemm_kernel(CoreArgs a, CoreGrad g)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int v = v0 + tx + 16 * j;
-      if (v < kx) g.Yg[(size_t)p * kx + v] = acc[i][j] * iw;
+      if (v < kx) g.Yg[(size_t)p * kx + v] = as_d(acc[i][j]) * iw;
     }
   }
 }
@@ -1102,7 +1117,10 @@ int core_pre(const CoreArgs &a, cudaStream_t st) {
 }
 
 int core_gamma(const CoreArgs &a, double *Gam, cudaStream_t st) {
-  core_gemm_kernel<true><<<dim3(a.ntile, a.ntile), 256, 0, st>>>(a, Gam);
+  if (a.df)
+    core_gemm_kernel<true, df64><<<dim3(a.ntile, a.ntile), 256, 0, st>>>(a, Gam);
+  else
+    core_gemm_kernel<true, double><<<dim3(a.ntile, a.ntile), 256, 0, st>>>(a, Gam);
   return cudaGetLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -1110,7 +1128,7 @@ int core_post(const CoreArgs &a, const double *Gam, cudaStream_t st) {
   if (Gam)
     core_e2_kernel<<<a.ntile * a.ntile, 256, 0, st>>>(a, Gam);
   else
-    core_gemm_kernel<false><<<dim3(a.ntile, a.ntile), 256, 0, st>>>(a, nullptr);
+    core_gemm_kernel<false, double><<<dim3(a.ntile, a.ntile), 256, 0, st>>>(a, nullptr);
   core_result_kernel<<<1, 1024, 0, st>>>(a);
   return cudaGetLastError() == cudaSuccess ? 2 : -1;
 }
@@ -1119,7 +1137,10 @@ int core_post(const CoreArgs &a, const double *Gam, cudaStream_t st) {
 int core_adjoint(const CoreArgs &a, const CoreGrad &g, cudaStream_t st) {
   const int n = a.nsp, nC = a.nC, kx = a.kx;
   const int nn = n * n;
-  core_ygemm_kernel<<<dim3((kx + GT - 1) / GT, a.ntile), 256, 0, st>>>(a, g);
+  if (a.df)
+    core_ygemm_kernel<df64><<<dim3((kx + GT - 1) / GT, a.ntile), 256, 0, st>>>(a, g);
+  else
+    core_ygemm_kernel<double><<<dim3((kx + GT - 1) / GT, a.ntile), 256, 0, st>>>(a, g);
   core_axp_kernel<<<dim3(kx, g.nchunk), 256, 0, st>>>(a, g);
   core_axr_kernel<<<nblk((long long)kx * kx, 256), 256, 0, st>>>(a, g);
   core_rowmat_kernel<<<nblk((long long)a.np * kx, 256), 256, 0, st>>>(g.Yg, a.A2x, g.Wvb, a.np, kx, 2.0);

@@ -41,6 +41,7 @@ struct CoreArgs {
   double *part;           /* [ntile * ntile] per GEMM tile */
   int ntile;
   double enuc;
+  int df;                 /* 1: the orbital-pair GEMMs in double-float (mixed path) */
   double *out;            /* [5] energy, e_num, e1, e2, wfnorm */
   int *nsing;             /* flagged determinant pairs */
 };

@@ -125,30 +125,7 @@ constexpr int RYS_DF_SPLIT = 5; /* Chebyshev terms >= this index are summed in F
 
 /* ---- double-float arithmetic -------------------------------------------- */
 
-__device__ __forceinline__ df64 df_quick(float s, float e) {
-  const float r = s + e;
-  return df64(r, e - (r - s));
-}
-__device__ __forceinline__ df64 operator+(df64 a, df64 b) {
-  const float s = a.hi + b.hi;
-  const float v = s - a.hi;
-  float e = (a.hi - (s - v)) + (b.hi - v);
-  e += a.lo + b.lo;
-  return df_quick(s, e);
-}
-__device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
-__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
-__device__ __forceinline__ df64 operator*(df64 a, df64 b) {
-  const float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  return df_quick(p, e);
-}
-__device__ __forceinline__ df64 &operator+=(df64 &a, df64 b) {
-  a = a + b;
-  return a;
-}
+/* df_quick, +, -, * and += on df64: vsvb_internal.h */
 
 /* reciprocal, square root and inverse square root in double-float: an
  * FP32 first guess refined by one Newton step in df64 (~2^-46 relative) */

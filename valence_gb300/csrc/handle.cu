@@ -495,6 +495,7 @@ CoreArgs core_args(vsvb_gpu *h) {
   c.part = h->core_part.p;
   c.ntile = h->core_nt;
   c.enuc = h->enuc;
+  c.df = h->opt.precision == VSVB_MIXED_DF64;
   c.out = h->result.p;
   c.nsing = h->nsing.p;
   return c;

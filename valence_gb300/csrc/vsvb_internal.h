@@ -64,6 +64,33 @@ struct df64 {
 };
 
 #ifdef __CUDACC__
+/* double-float arithmetic: Knuth's TwoSum and an FMA-based TwoProduct
+ * (Dekker), renormalised by a quick two-sum */
+__device__ __forceinline__ df64 df_quick(float s, float e) {
+  const float r = s + e;
+  return df64(r, e - (r - s));
+}
+__device__ __forceinline__ df64 operator+(df64 a, df64 b) {
+  const float s = a.hi + b.hi;
+  const float v = s - a.hi;
+  float e = (a.hi - (s - v)) + (b.hi - v);
+  e += a.lo + b.lo;
+  return df_quick(s, e);
+}
+__device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
+__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
+__device__ __forceinline__ df64 operator*(df64 a, df64 b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_quick(p, e);
+}
+__device__ __forceinline__ df64 &operator+=(df64 &a, df64 b) {
+  a = a + b;
+  return a;
+}
+
 /* double -> double-float without FP64 arithmetic (whose rate is 1/58 of
  * FP32 on this part): hi takes the sign, exponent and top 23 mantissa bits
  * (a truncation, exact in FP32), lo the remaining 29 mantissa bits scaled by
