@@ -1,0 +1,259 @@
+"""CPU check of core mode's closed form (core.cu) against the oracle: the
+determinant-pair sum over the shared doubly occupied core, written out in
+numpy from the oracle's orbital overlaps, core Hamiltonian and orbital-pair
+ERIs, reproduces the oracle's guess energy (the reference's task loop,
+valence.F90:1010-1434) on golden cases with spin-coupled pairs, singular
+blocks included; and its adjoint (dE/dS, dE/dh, dE/dT) matches central
+differences.  This pins the algebra the CUDA kernels implement; the GPU
+kernels themselves are tested in test_gpu_core.py."""
+import itertools
+import os
+
+import numpy as np
+import pytest
+
+from tests.oracle_py import GOLDEN, OptOracle
+
+
+def _pert(r, c, s):
+    """the fixed rank-2 matrix of the exact path (core.cu pert_entry)"""
+    w1, w2 = np.sin(1.0 + 0.7548776662466927 * r), np.sin(2.0 + 0.5698402909980532 * r)
+    z1, z2 = np.cos(0.5 + 0.6180339887498949 * c), np.cos(1.5 + 0.4142135623730950 * c)
+    return s * (w1 * z1 + w2 * z2)
+
+
+class Core:
+    """One golden case: S, h, masked T from the oracle and the spin-coupled
+    determinant expansion (pair_sc, coeff_sc)."""
+
+    def __init__(self, path):
+        o = OptOracle(path)
+        r = o.guess_energy()
+        inp = o.inp
+        self.P, self.nsc = inp.npair, max(inp.nspinc, 1)
+        self.nC = 2 * self.P
+        self.nsp = self.nC + inp.ndocc
+        n = self.nsp
+        self.ps = np.ctypeslib.as_array(inp.pair_sc, shape=(2 * self.P * self.nsc,)).copy()
+        self.csc = (np.ctypeslib.as_array(inp.coeff_sc, shape=(self.nsc,)).copy() if inp.nspinc > 0
+                    else np.ones(1))
+        self.S = np.array([[o.ovint(i + 1, j + 1) for j in range(n)] for i in range(n)])
+        self.H = np.array([[o.int1e(i + 1, j + 1) for j in range(n)] for i in range(n)])
+        self.pairs = [(i, k) for i in range(n) for k in range(i + 1)]
+        npr = len(self.pairs)
+        T = np.zeros((npr, npr))
+        for p, (i, k) in enumerate(self.pairs):
+            for q, (j, l) in enumerate(self.pairs):
+                T[p, q] = T[q, p] if q < p else o.int2e(i + 1, k + 1, j + 1, l + 1)
+        sq = np.sqrt(np.maximum(np.diag(T), 0.0))
+        self.T = np.where((np.outer(sq, sq) > inp.itol) & (np.abs(T) > inp.itol), T, 0.0)
+        self.nelec = 2 * self.P + 2 * inp.ndocc
+        self.enuc, self.ref = r.enucrep, r.energy
+        self.dets = [(sc, b) for sc in range(self.nsc) for b in range(1 << self.P)]
+
+    @staticmethod
+    def opair(i, k):
+        return i * (i + 1) // 2 + k if i >= k else k * (k + 1) // 2 + i
+
+    def orb(self, sc, bits, s, r):
+        return self.ps[r + self.P * ((s ^ ((bits >> r) & 1)) + 2 * sc)] - 1
+
+    def blocks(self, M, s0):
+        """per determinant pair and spin: the exact (d, L) and the
+        factorisations they come from, [(coefficient, d_k, M_k^-1)]"""
+        import scipy.linalg
+        P, out = self.P, []
+        for (isc, bb) in self.dets:
+            for (jsc, kb) in self.dets:
+                sp = []
+                for s in (0, 1):
+                    ro = [self.orb(isc, bb, s, x) for x in range(P)]
+                    co = [self.orb(jsc, kb, s, x) for x in range(P)]
+                    Ms = M[np.ix_(ro, co)]
+                    amax = np.abs(Ms).max()
+                    lu = scipy.linalg.lu_factor(Ms, check_finite=False)
+                    if np.min(np.abs(np.diag(lu[0]))) > 1e-7 * amax:
+                        mats = [(1.0, Ms)]
+                    else:
+                        pm = np.array([[_pert(r, c, 0.1 * amax / np.sqrt(P)) for c in range(P)] for r in range(P)])
+                        mats = [(cf, Ms + k * pm) for cf, k in ((3.0, 1), (-3.0, 2), (1.0, 3))]
+                    V = [(cf, s0 * np.linalg.det(A), np.linalg.inv(A)) for cf, A in mats]
+                    sp.append({"ro": ro, "co": co, "V": V, "d": sum(cf * d for cf, d, _ in V),
+                               "L": sum(cf * d * Z.T for cf, d, Z in V)})
+                out.append((self.csc[isc] * self.csc[jsc], sp))
+        return out
+
+    @staticmethod
+    def second(o):
+        return sum(cf * 0.5 * d * (np.einsum('ba,dc->abcd', Z, Z) - np.einsum('da,bc->abcd', Z, Z))
+                   for cf, d, Z in o["V"])
+
+    def energy(self, S, H, T, full=False):
+        nC, n = self.nC, self.nsp
+        D, C = list(range(nC, n)), list(range(nC))
+        G = np.linalg.inv(S[np.ix_(D, D)])
+        s0 = np.linalg.det(S[np.ix_(D, D)])
+        Y = G @ S[np.ix_(D, C)]
+        M = S[np.ix_(C, C)] - S[np.ix_(C, D)] @ Y
+        U = np.zeros((n, nC))
+        U[:nC] = np.eye(nC)
+        U[nC:] = -Y
+        P0 = np.zeros((n, n))
+        P0[nC:, nC:] = G
+        A0, A1, A2 = 0.0, np.zeros((nC, nC)), np.zeros((nC,) * 4)
+        for w, (a, b) in self.blocks(M, s0):
+            A0 += w * a["d"] * b["d"]
+            Lc = []
+            for s, o in ((a, b), (b, a)):
+                L = np.zeros((nC, nC))
+                L[np.ix_(s["ro"], s["co"])] = s["L"]
+                Q = np.zeros((nC,) * 4)
+                Q[np.ix_(s["ro"], s["co"], s["ro"], s["co"])] = self.second(s)
+                A1 += w * o["d"] * L
+                A2 += w * o["d"] * Q
+                Lc.append(L)
+            A2 += 0.5 * w * (np.einsum('ab,cd->abcd', Lc[0], Lc[1]) + np.einsum('ab,cd->abcd', Lc[1], Lc[0]))
+        R1 = U @ A1 @ U.T
+        gam = 2 * A0 * P0 + R1
+        cp = [(x, y) for x in range(nC) for y in range(x + 1)]
+        ncp = len(cp)
+        Wv = np.zeros((len(self.pairs), ncp + 2))
+        for p, (i, k) in enumerate(self.pairs):
+            for u, (x, y) in enumerate(cp):
+                Wv[p, u] = U[i, x] * U[k, y] + (U[k, x] * U[i, y] if i != k else 0.0)
+            Wv[p, ncp] = P0[i, k] + (P0[k, i] if i != k else 0.0)
+            Wv[p, ncp + 1] = R1[i, k] + (R1[k, i] if i != k else 0.0)
+        A2x = np.zeros((ncp + 2, ncp + 2))
+        for u, (x, y) in enumerate(cp):
+            for v, (z, t) in enumerate(cp):
+                A2x[u, v] = sum(A2[i1, k1, j1, l1] for (i1, k1) in {(x, y), (y, x)} for (j1, l1) in {(z, t), (t, z)})
+        A2x[ncp, ncp] = 2 * A0
+        A2x[ncp, ncp + 1] = A2x[ncp + 1, ncp] = 1.0
+        Gp = Wv @ A2x @ Wv.T
+        for p, (i, k) in enumerate(self.pairs):
+            for q, (j, l) in enumerate(self.pairs):
+                for (i1, k1) in {(i, k), (k, i)}:
+                    for (j1, l1) in {(j, l), (l, j)}:
+                        Gp[p, q] += (-A0 * P0[i1, l1] * P0[j1, k1]
+                                     - 0.5 * (P0[i1, l1] * R1[j1, k1] + R1[i1, l1] * P0[j1, k1]))
+        e1, wf, e2 = np.sum(H * gam), np.sum(S * gam) / self.nelec, np.sum(T * Gp)
+        E = (e1 + e2) / wf + self.enuc
+        return (E, locals()) if full else E
+
+    def grad(self):
+        """dE/dS, dE/dh, dE/dT: the adjoint of core.cu (core_adjoint)"""
+        E, v = self.energy(self.S, self.H, self.T, full=True)
+        n, nC, P = self.nsp, self.nC, self.P
+        W, en = v["wf"], v["e1"] + v["e2"]
+        A0, A1, U, P0, R1, Wv, A2x, ncp = v["A0"], v["A1"], v["U"], v["P0"], v["R1"], v["Wv"], v["A2x"], v["ncp"]
+        Tb = self.T / W
+        Hb = self.H / W - en / W ** 2 * self.S / self.nelec
+        Sbar = -en / W ** 2 * v["gam"] / self.nelec
+        Yg = Tb @ Wv
+        Ax, Wvb = Wv.T @ Yg, 2 * Yg @ A2x
+        KP, KR = np.zeros((n, n)), np.zeros((n, n))
+        for j, k in itertools.product(range(n), repeat=2):
+            t = np.array([[Tb[self.opair(i, k), self.opair(j, l)] for l in range(n)] for i in range(n)])
+            KP[j, k], KR[j, k] = np.sum(t * P0), np.sum(t * R1)
+        R1b = Hb - KP
+        P0b = 2 * A0 * Hb - 2 * A0 * KP - KR
+        A0b = 2 * np.sum(Hb * P0) + 2 * Ax[ncp, ncp] - np.sum(KP * P0)
+        for p, (i, k) in enumerate(self.pairs):
+            for (i1, k1) in {(i, k), (k, i)}:
+                P0b[i1, k1] += Wvb[p, ncp]
+                R1b[i1, k1] += Wvb[p, ncp + 1]
+        A1b = U.T @ R1b @ U
+        Ub = R1b @ U @ A1.T + R1b.T @ U @ A1
+        for m in range(n):
+            for c in range(nC):
+                Ub[m, c] += sum(Wvb[self.opair(m, nn), self.opair(c, z)] * U[nn, z] * (2 if z == c else 1)
+                                for nn in range(n) for z in range(nC))
+        A2b = np.zeros((nC,) * 4)
+        for a, b, c, d in itertools.product(range(nC), repeat=4):
+            A2b[a, b, c, d] = Ax[self.opair(a, b), self.opair(c, d)]
+        Mb, lam = np.zeros((nC, nC)), 0.0
+        for w, sp in self.blocks(v["M"], v["s0"]):
+            a, b = sp
+            f = [np.sum(A1b[np.ix_(o["ro"], o["co"])] * o["L"])
+                 + np.sum(A2b[np.ix_(o["ro"], o["co"], o["ro"], o["co"])] * self.second(o)) for o in sp]
+            Xi = A2b[np.ix_(a["ro"], a["co"], b["ro"], b["co"])]
+            B = [np.einsum('abcd,cd->ab', Xi, b["L"]), np.einsum('abcd,ab->cd', Xi, a["L"])]
+            lam += w * (A0b * a["d"] * b["d"] + b["d"] * f[0] + a["d"] * f[1] + np.sum(B[0] * a["L"]))
+            for s in (0, 1):
+                o, ot = sp[s], sp[1 - s]
+                Psi = A2b[np.ix_(o["ro"], o["co"], o["ro"], o["co"])]
+                php = ot["d"] * A1b[np.ix_(o["ro"], o["co"])] + B[s]
+                aco = A0b * ot["d"] + f[1 - s]
+                mb = np.zeros((P, P))
+                for cf, dk, Z in o["V"]:
+                    om = 2 * (np.einsum('ca,bdac->bd', Z, Psi) - np.einsum('ca,bcad->bd', Z, Psi))
+                    h = 0.25 * dk * np.sum(Z.T * om)
+                    mb += cf * w * (aco * dk * Z.T + dk * (np.trace(php @ Z) * Z.T - (Z @ php @ Z).T)
+                                    + ot["d"] * (h * Z.T - 0.5 * dk * (Z @ om @ Z).T))
+                Mb[np.ix_(o["ro"], o["co"])] += mb
+        Sbar += U @ Mb @ U.T - P0 @ P0b @ P0 - P0 @ Ub @ U.T + 2 * lam * P0
+        return E, Sbar, v["gam"] / W, v["Gp"] / W
+
+
+CASES = ["lih", "be-sc", "h2o-vdz-sc1", "be-sv", "he1s2s"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_core_closed_form_matches_oracle(name):
+    c = Core(os.path.join(GOLDEN, "cases", "testing", name))
+    assert abs(c.energy(c.S, c.H, c.T) - c.ref) < 1e-10
+
+
+def test_core_closed_form_singular_blocks():
+    """n2.sc4val-b.p2: 4 spin couplings, 5 pairs, 19,200 flagged spin
+    blocks through the three-point extrapolation"""
+    if not os.environ.get("VSVB_SLOW"):
+        pytest.skip("about 30 s of numpy; VSVB_SLOW=1 runs it")
+    c = Core(os.path.join(GOLDEN, "cases", "testing", "n2.sc4val-b.p2"))
+    assert abs(c.energy(c.S, c.H, c.T) - c.ref) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["lih", "be-sc"])
+def test_core_adjoint_matches_differences(name):
+    c = Core(os.path.join(GOLDEN, "cases", "testing", name))
+    _, Sb, Hb, Tb = c.grad()
+    h = 1e-6
+    rng = np.random.default_rng(0)
+    for _ in range(4):
+        i, j = rng.integers(0, c.nsp, 2)
+        d = np.zeros_like(c.S)
+        d[i, j] += h
+        d[j, i] += h
+        fd = (c.energy(c.S + d, c.H, c.T) - c.energy(c.S - d, c.H, c.T)) / (2 * h)
+        an = Sb[i, j] + Sb[j, i] if i != j else 2 * Sb[i, i]
+        assert abs(fd - an) < 1e-6 * max(1.0, abs(fd))
+        fd = (c.energy(c.S, c.H + d, c.T) - c.energy(c.S, c.H - d, c.T)) / (2 * h)
+        an = Hb[i, j] + Hb[j, i] if i != j else 2 * Hb[i, i]
+        assert abs(fd - an) < 1e-6 * max(1.0, abs(fd))
+    for _ in range(3):
+        p, q = rng.integers(0, len(c.pairs), 2)
+        d = np.zeros_like(c.T)
+        d[p, q] += h
+        fd = (c.energy(c.S, c.H, c.T + d) - c.energy(c.S, c.H, c.T - d)) / (2 * h)
+        assert abs(fd - Tb[p, q]) < 1e-6 * max(1.0, abs(fd))
+
+
+def test_core_three_pairs_synthetic(tmp_path):
+    """A 4-carbon chain with 3 Rumer pairs (64 determinant pairs, s/p/d):
+    the second-cofactor terms of the adjoint are exercised (with 2 pairs
+    they vanish), energy against the oracle, dE/dS against differences."""
+    from valence_gb300 import configs
+    p = configs.alkane_chain(str(tmp_path / "ac3.inp"), ncarbon=4, nh=10, npair=3, ndocc=1)
+    c = Core(p)
+    assert abs(c.energy(c.S, c.H, c.T) - c.ref) < 1e-9 * max(1.0, abs(c.ref))
+    _, Sb, _, _ = c.grad()
+    h = 1e-6
+    rng = np.random.default_rng(1)
+    for _ in range(3):
+        i, j = rng.integers(0, c.nsp, 2)
+        d = np.zeros_like(c.S)
+        d[i, j] += h
+        d[j, i] += h
+        fd = (c.energy(c.S + d, c.H, c.T) - c.energy(c.S - d, c.H, c.T)) / (2 * h)
+        an = Sb[i, j] + Sb[j, i] if i != j else 2 * Sb[i, i]
+        assert abs(fd - an) < 1e-7 * max(1.0, abs(fd)) + 1e-16 * abs(c.ref) / h
