@@ -30,6 +30,7 @@
 #include <string>
 #include <thread>
 #include <tuple>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/vsvb_gpu.h"
@@ -1436,10 +1437,33 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
                 it.nprimq += n;
               }
               if (kept.empty()) continue;
-              std::stable_sort(kept.begin(), kept.end(), [](const std::pair<double, int4> &x,
-                                                            const std::pair<double, int4> &y) { return x.first > y.first; });
-              std::vector<int4> lst(kept.size());
-              for (size_t k = 0; k < kept.size(); ++k) lst[k] = kept[k].second;
+              /* the quartets of one atom quartet update and read the same
+               * blocks of T and dE/dT (every shell pair of an atom pair has
+               * the same orbital pairs), so they run next to each other,
+               * where those blocks stay in L2: items grouped by atom
+               * quartet, groups by their total work, largest first, items
+               * within a group by work */
+              const long long na = d->natom;
+              auto aq = [&](const int4 &q) -> long long {
+                const ShellPair &P = pairs[q.x], &Q = pairs[q.y];
+                return ((sh[P.shA].atom * na + sh[P.shB].atom) * na + sh[Q.shA].atom) * na + sh[Q.shB].atom;
+              };
+              std::unordered_map<long long, double> gwork;
+              gwork.reserve(kept.size());
+              for (const auto &k : kept) gwork[aq(k.second)] += k.first;
+              std::vector<std::tuple<double, long long, double, int4>> ord;
+              ord.reserve(kept.size());
+              for (const auto &k : kept) {
+                const long long g = aq(k.second);
+                ord.emplace_back(gwork[g], g, k.first, k.second);
+              }
+              std::stable_sort(ord.begin(), ord.end(), [](const auto &x, const auto &y) {
+                if (std::get<0>(x) != std::get<0>(y)) return std::get<0>(x) > std::get<0>(y);
+                if (std::get<1>(x) != std::get<1>(y)) return std::get<1>(x) < std::get<1>(y);
+                return std::get<2>(x) > std::get<2>(y);
+              });
+              std::vector<int4> lst(ord.size());
+              for (size_t k = 0; k < ord.size(); ++k) lst[k] = std::get<3>(ord[k]);
               it.wl = (int)iwl.size();
               iwl.push_back(std::move(lst));
               h->sweep.push_back(it);
