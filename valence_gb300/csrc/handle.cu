@@ -179,7 +179,9 @@ struct vsvb_gpu {
   int nsplit = 1, nsplit_max = 1; /* task splits per determinant pair (assembly grids) */
   std::vector<double> coeff0;
   /* schedules: [prec][cp][cq] */
-  std::vector<int2> work_h[2][6][6];
+  /* [0] FP64-class quartets (their FP32 tail split off on the mixed paths),
+   * [1] FP32-class, [2] FP64-class kept whole on the mixed paths */
+  std::vector<int2> work_h[3][6][6];
   long long nq_fp64 = 0, nq_fp32 = 0;
   double nprimq_fp32 = 0.0, nprimq_all = 0.0; /* primitive quartets evaluated in FP32 / in total */
   double err_bound = 0.0; /* sum over FP32 quartets of the Schwarz bound */
@@ -1323,6 +1325,26 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     }
     return n;
   };
+  /* the primitive split of an FP64-class quartet on the mixed paths (its
+   * small primitive quartets in a second, FP32 launch) pays when the
+   * quartet's double-float integrals outweigh its transform.  In the
+   * double-float launch the transform runs on the FP64 pipe and the
+   * integrals on the FP32 pipe side by side; while the FP64 transform is the
+   * longer of the two, the small primitives cost nothing there, and the FP32
+   * launch would only repeat the transform.  Rates as in the roofline:
+   * double-float integrals at 3/16 of the FP32 FMA rate against the
+   * transform at the FP64 rate, a factor 5.5 on this part.  Measured with
+   * the split everywhere / nowhere / this rule at factors 5.5, 1.5: the C/H
+   * chain 14.8 / 18.1 / 16.1, 15.1 ms; the 128-atom chain (transforms of
+   * ~36 x 36 orbital pairs) 491 / 465 / 459, 470 ms; the rule takes 3 */
+  auto split_pays = [&](int a, int c) -> bool {
+    if (!split) return false;
+    double sb = 0.0;
+    const double nall = window(a, c, eps, INFINITY, sb);
+    const double pf = eri_flops(0, pairs[a].cls, pairs[c].cls, 1.0, 0, 0);
+    const double tr = eri_flops(3, pairs[a].cls, pairs[c].cls, 0.0, pairs[a].nop, pairs[c].nop);
+    return nall * pf > 3.0 * tr;
+  };
   /* the same per row of P's primitive pairs (rows[i] for i < na) */
   auto window_rows = [&](int P, int Q, float lo, float hi, std::vector<int> &rows) {
     const float *a = q0f.data() + pairs[P].prim0, *b = q0f.data() + pairs[Q].prim0;
@@ -1376,7 +1398,9 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
           h->err_bound += amp[P] * amp[Q];
         } else {
           h->nq_fp64++;
-          if (split) {
+          if (!split_pays(a, c)) {
+            if (split) prec = 2;
+          } else {
             /* the FP32 tail: its bound mass in units of the pair bounds, with
              * the transfer norms of both pairs */
             const double nt = window(a, c, eps, tau, sb);
@@ -1393,7 +1417,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
        * quartets do not leave a tail of lone CTAs at the end of the launch */
       constexpr int SPLIT_PRIMQ = 512;
       std::vector<int> rows;
-      for (int p = 0; p < 2; ++p)
+      for (int p = 0; p < 3; ++p)
         for (int a = 0; a < 6; ++a)
           for (int c = 0; c < 6; ++c) {
             const auto &w = h->work_h[p][a][c];
@@ -1404,6 +1428,8 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
             std::vector<vsvb_gpu::SweepItem> items;
             if (p == 1) {
               items.push_back({p, ERI_F32, a, c, eps, INFINITY, 0, 0, 0, 100 * ERI_F32 + 10 * a + c});
+            } else if (p == 2) {
+              items.push_back({p, eri_kind(h, 0), a, c, eps, INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
             } else if (split) {
               items.push_back({p, eri_kind(h, 0), a, c, std::max(eps, tau), INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
               items.push_back({p, ERI_F32, a, c, eps, tau, 0, 0, 0, 300 + 10 * a + c});
