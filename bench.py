@@ -77,7 +77,10 @@ CPU_SAMPLE = {"lif_cluster": (16, 16, 12), "lif_cluster_3": (16, 16, 12), "alkan
 # chunk.  Per-quartet path: keys (workload, class code).
 PROFILED_TRAFFIC = {("lif_cluster", "transform_df64"): 2322444656,
                     # eri_kernel<2,2,2,1,df64,3> on the chain (profiles/eri_ch_chain.md)
-                    ("ch_chain", 254): 1279232}
+                    ("ch_chain", 254): 1279232,
+                    # eri_kernel<2,1,2,0,df64,3> on the 128-atom chain: the mean of its
+                    # two launches per sweep (profiles/eri_alkane_chain.md)
+                    ("alkane_chain", 243): 365088718}
 
 
 def eri_roofline(sweep, sweep_wall, fp64_peak, fp32_peak, step_ms, workload):

@@ -429,11 +429,15 @@ __global__ void __launch_bounds__(256) core_a1_kernel(CoreArgs a) {
   for (int s = 0; s < 2; ++s) {
     const int *Bl = a.lst1 + a.off1[2 * x + s], *Kl = a.lst1 + a.off1[2 * y + s];
     const int nb = a.off1[2 * x + s + 1] - a.off1[2 * x + s], nk = a.off1[2 * y + s + 1] - a.off1[2 * y + s];
-    for (long long t = lane; t < (long long)nb * nk; t += 32) {
-      const int bd = Bl[t / nk], kd = Kl[t % nk];
-      const long long q = pair_of(a, bd, kd);
-      const int ra = a.detpos[(size_t)bd * nC + x] & 31, cb = a.detpos[(size_t)kd * nC + y] & 31;
-      acc += weight_of(a, bd, kd) * a.dd[2 * q + 1 - s] * a.L[((size_t)q * 2 + s) * P * P + ra * P + cb];
+    for (int ib = 0; ib < nb; ++ib) {
+      const int bd = Bl[ib];
+      const int ra = a.detpos[(size_t)bd * nC + x] & 31;
+      for (int ik = lane; ik < nk; ik += 32) {
+        const int kd = Kl[ik];
+        const long long q = pair_of(a, bd, kd);
+        const int cb = a.detpos[(size_t)kd * nC + y] & 31;
+        acc += weight_of(a, bd, kd) * a.dd[2 * q + 1 - s] * a.L[((size_t)q * 2 + s) * P * P + ra * P + cb];
+      }
     }
   }
   acc = warp_sum(acc);
@@ -456,20 +460,23 @@ __global__ void __launch_bounds__(256) core_a2_kernel(CoreArgs a) {
     const int ib = 4 * (a4 * nC + c4) + g, ik = 4 * (b4 * nC + d4) + g;
     const int *Bl = a.lst2 + a.off2[ib], *Kl = a.lst2 + a.off2[ik];
     const int nb = a.off2[ib + 1] - a.off2[ib], nk = a.off2[ik + 1] - a.off2[ik];
-    for (long long t = lane; t < (long long)nb * nk; t += 32) {
-      const int bd = Bl[t / nk], kd = Kl[t % nk];
-      const long long q = pair_of(a, bd, kd);
-      const double w = weight_of(a, bd, kd);
+    for (int jb = 0; jb < nb; ++jb) {
+      const int bd = Bl[jb];
       const int ra = a.detpos[(size_t)bd * nC + a4] & 31, rc = a.detpos[(size_t)bd * nC + c4] & 31;
-      const int cb = a.detpos[(size_t)kd * nC + b4] & 31, cd = a.detpos[(size_t)kd * nC + d4] & 31;
-      if (same) {
-        const int s = g == 0 ? 0 : 1;
-        acc += w * a.dd[2 * q + 1 - s] * second_cof(a, q, s, ra, rc, cb, cd);
-      } else {
-        /* g = 1: a, b alpha and c, d beta; g = 2: the reverse */
-        const int s1 = g == 1 ? 0 : 1;
-        const double *L1 = a.L + ((size_t)q * 2 + s1) * P2, *L2 = a.L + ((size_t)q * 2 + 1 - s1) * P2;
-        acc += 0.5 * w * L1[ra * P + cb] * L2[rc * P + cd];
+      for (int jk = lane; jk < nk; jk += 32) {
+        const int kd = Kl[jk];
+        const long long q = pair_of(a, bd, kd);
+        const double w = weight_of(a, bd, kd);
+        const int cb = a.detpos[(size_t)kd * nC + b4] & 31, cd = a.detpos[(size_t)kd * nC + d4] & 31;
+        if (same) {
+          const int s = g == 0 ? 0 : 1;
+          acc += w * a.dd[2 * q + 1 - s] * second_cof(a, q, s, ra, rc, cb, cd);
+        } else {
+          /* g = 1: a, b alpha and c, d beta; g = 2: the reverse */
+          const int s1 = g == 1 ? 0 : 1;
+          const double *L1 = a.L + ((size_t)q * 2 + s1) * P2, *L2 = a.L + ((size_t)q * 2 + 1 - s1) * P2;
+          acc += 0.5 * w * L1[ra * P + cb] * L2[rc * P + cd];
+        }
       }
     }
   }
@@ -1038,11 +1045,15 @@ __global__ void __launch_bounds__(256) core_mbar_kernel(CoreArgs a, CoreGrad g) 
   for (int s = 0; s < 2; ++s) {
     const int *Bl = a.lst1 + a.off1[2 * x + s], *Kl = a.lst1 + a.off1[2 * y + s];
     const int nb = a.off1[2 * x + s + 1] - a.off1[2 * x + s], nk = a.off1[2 * y + s + 1] - a.off1[2 * y + s];
-    for (long long t = lane; t < (long long)nb * nk; t += 32) {
-      const int bd = Bl[t / nk], kd = Kl[t % nk];
-      const long long q = pair_of(a, bd, kd);
-      const int ra = a.detpos[(size_t)bd * nC + x] & 31, cb = a.detpos[(size_t)kd * nC + y] & 31;
-      acc += g.Mbp[((size_t)q * 2 + s) * P * P + ra * P + cb];
+    for (int ib = 0; ib < nb; ++ib) {
+      const int bd = Bl[ib];
+      const int ra = a.detpos[(size_t)bd * nC + x] & 31;
+      for (int ik = lane; ik < nk; ik += 32) {
+        const int kd = Kl[ik];
+        const long long q = pair_of(a, bd, kd);
+        const int cb = a.detpos[(size_t)kd * nC + y] & 31;
+        acc += g.Mbp[((size_t)q * 2 + s) * P * P + ra * P + cb];
+      }
     }
   }
   acc = warp_sum(acc);
