@@ -396,7 +396,12 @@ __global__ void __launch_bounds__(256) core_pairs_kernel(CoreArgs a) {
     if (lane == 0) a.dd[2 * q + s] = dsum;
     __syncwarp();
   }
-  if (lane == 0) a.pslot[q] = (slot >= 0 && slot < a.cap) ? slot * 4 + flags : -1;
+  if (lane == 0) {
+    a.pslot[q] = (slot >= 0 && slot < a.cap) ? slot * 4 + flags : -1;
+    const double w = a.csc[isc] * a.csc[jsc], d0 = a.dd[2 * q], d1 = a.dd[2 * q + 1];
+    a.qf[2 * q] = d0 != 0.0 ? 0.5 * w * d1 / d0 : 0.0;
+    a.qf[2 * q + 1] = d1 != 0.0 ? 0.5 * w * d0 / d1 : 0.0;
+  }
 }
 
 /* A0 = sum_q w d_a d_b, fixed order; the flagged pair count */
@@ -470,7 +475,13 @@ __global__ void __launch_bounds__(256) core_a2_kernel(CoreArgs a) {
         const int cb = a.detpos[(size_t)kd * nC + b4] & 31, cd = a.detpos[(size_t)kd * nC + d4] & 31;
         if (same) {
           const int s = g == 0 ? 0 : 1;
-          acc += w * a.dd[2 * q + 1 - s] * second_cof(a, q, s, ra, rc, cb, cd);
+          const int ps = a.pslot[q];
+          if (ps >= 0 && ((ps >> s) & 1)) {
+            acc += w * a.dd[2 * q + 1 - s] * second_cof(a, q, s, ra, rc, cb, cd);
+          } else {
+            const double *Ls = a.L + ((size_t)q * 2 + s) * P2;
+            acc += a.qf[2 * q + s] * (Ls[ra * P + cb] * Ls[rc * P + cd] - Ls[ra * P + cd] * Ls[rc * P + cb]);
+          }
         } else {
           /* g = 1: a, b alpha and c, d beta; g = 2: the reverse */
           const int s1 = g == 1 ? 0 : 1;
@@ -905,10 +916,29 @@ __global__ void __launch_bounds__(256) core_pair_adj_kernel(CoreArgs a, CoreGrad
       const int r = t / P, c = t - r * P;
       acc += g.A1b[ob[r] * nC + ok[c]] * L2[s][t];
     }
-    for (int t = lane; t < P2 * P2; t += 32) {
-      const int r1 = t / (P * P2), c1 = (t / P2) % P, r2 = (t / P) % P, c2 = t % P;
-      if (r1 == r2 || c1 == c2) continue;
-      acc += a2bar(a, g, ob[r1], ok[c1], ob[r2], ok[c2]) * second_cof(a, q, s, r1, r2, c1, c2);
+    /* <A2-bar, Q_s>: per factorisation sum Psi (L L - L L), then / (2 d) */
+    const int ps0 = a.pslot[q];
+    const bool fl = ps0 >= 0 && ((ps0 >> s) & 1);
+    for (int k = 0; k < (fl ? 3 : 1); ++k) {
+      double dk;
+      const double *Lk;
+      if (fl) {
+        const double *e = a.pool + ((size_t)(ps0 >> 2) * 6 + (size_t)(2 * k + s)) * (1 + P2);
+        dk = e[0];
+        Lk = e + 1;
+      } else {
+        dk = d2[s];
+        Lk = L2[s];
+      }
+      if (dk == 0.0) continue;
+      double hs = 0.0;
+      for (int t = lane; t < P2 * P2; t += 32) {
+        const int r1 = t / (P * P2), c1 = (t / P2) % P, r2 = (t / P) % P, c2 = t % P;
+        if (r1 == r2 || c1 == c2) continue;
+        hs += a2bar(a, g, ob[r1], ok[c1], ob[r2], ok[c2]) *
+              (Lk[r1 * P + c1] * Lk[r2 * P + c2] - Lk[r1 * P + c2] * Lk[r2 * P + c1]);
+      }
+      acc += (fl ? (k == 0 ? 3.0 : (k == 1 ? -3.0 : 1.0)) : 1.0) * 0.5 * hs / dk;
     }
     f[s] = warp_sum(acc);
   }
@@ -961,9 +991,10 @@ __global__ void __launch_bounds__(256) core_pair_adj_kernel(CoreArgs a, CoreGrad
         if (lane == 0 && (flagged || d2[s] == 0.0)) atomicOr(a.status, 2);
         continue;
       }
+      const double idk = 1.0 / dk;
       for (int t = lane; t < P2; t += 32) {
         const int r = t / P, c = t - r * P;
-        Zs[c * P + r] = Lk[t] / dk;
+        Zs[c * P + r] = Lk[t] * idk;
       }
       __syncwarp();
       /* Omega[r1][c1] = 2 sum Z[c2][r2] (Psi[r1 c1 r2 c2] - Psi[r1 c2 r2 c1]) */

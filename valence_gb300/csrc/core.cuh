@@ -29,6 +29,8 @@ struct CoreArgs {
   double *s0;             /* det S_DD */
   double *dd;             /* [nq][2]: determinant of each spin block */
   double *L;              /* [nq][2][P*P]: first cofactors of the block, (bra position, ket position) */
+  double *qf;             /* [nq][2]: w d_other / (2 d_s), the factor of the second cofactors of an
+                           * unflagged block in the pair sums */
   int *pslot;             /* [nq]: 4 slot + flagged spins, or -1 */
   double *pool;           /* [cap][3][2][1 + P*P]: det and cofactors of block + k Pert, k = 1..3 */
   int *pcount;

@@ -262,7 +262,7 @@ struct vsvb_gpu {
   DBuf<unsigned char> core_detorb, core_detpos;
   DBuf<int> core_lst1, core_off1, core_lst2, core_off2, core_pslot, core_pcount;
   DBuf<int2> core_pik;
-  DBuf<double> core_fw, core_G, core_Y, core_M, core_P0, core_U, core_s0, core_dd, core_L, core_pool;
+  DBuf<double> core_fw, core_G, core_Y, core_M, core_P0, core_U, core_s0, core_dd, core_L, core_qf, core_pool;
   DBuf<double> core_A0, core_A1, core_A2, core_A2x, core_R1, core_Wv, core_X, core_part;
   int core_cap = 0;
   /* core-mode adjoint (core.cu CoreGrad) */
@@ -480,6 +480,7 @@ CoreArgs core_args(vsvb_gpu *h) {
   c.s0 = h->core_s0.p;
   c.dd = h->core_dd.p;
   c.L = h->core_L.p;
+  c.qf = h->core_qf.p;
   c.pslot = h->core_pslot.p;
   c.pool = h->core_pool.p;
   c.pcount = h->core_pcount.p;
@@ -1665,6 +1666,7 @@ int setup_core(vsvb_gpu *h, const std::vector<int> &pslot) {
   CK(h->core_s0.alloc(1), "alloc core");
   CK(h->core_dd.alloc((size_t)nq * 2), "alloc core");
   CK(h->core_L.alloc((size_t)nq * 2 * P2), "alloc core");
+  CK(h->core_qf.alloc((size_t)nq * 2), "alloc core");
   CK(h->core_pslot.alloc((size_t)nq), "alloc core");
   CK(h->core_pcount.alloc(1), "alloc core");
   /* flagged-pair pool: three perturbed factorisations per spin, up to 512 MiB */
