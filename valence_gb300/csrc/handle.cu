@@ -1034,7 +1034,7 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
     a.S = h->S_ao.p;
     a.H = h->H_ao.p;
     int npairs = h->nsh * (h->nsh + 1) / 2;
-    ao_1e_kernel<<<(npairs + 63) / 64, 64, 0, h->st>>>(a);
+    ao_1e_kernel<<<(unsigned)(((long long)npairs * 32 + 127) / 128), 128, 0, h->st>>>(a);
     CK(cudaGetLastError(), "ao_1e_kernel");
   }
   CK(h->obs_n.upload(obs_n), "upload obs");

@@ -78,8 +78,12 @@ __device__ void os1d(double a, double b, double xa, double xb, int imax, int jma
 }  // namespace
 
 /* one thread per unique shell pair (A >= B); writes both triangles */
+/* one warp per shell pair: overlap and kinetic in every lane, the nuclear
+ * attraction split over the nuclei by lane and summed over the warp in a
+ * fixed order */
 __global__ void ao_1e_kernel(Ao1eArgs a) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   int ns = a.nshell;
   if (t >= ns * (ns + 1) / 2) return;
   int A = (int)((sqrt(8.0 * t + 1.0) - 1.0) / 2.0);
@@ -130,7 +134,10 @@ __global__ void ao_1e_kernel(Ao1eArgs a) {
         PA[d] = P[d] - sa.xyz[d];
       }
       const double base = 2.0 * 3.14159265358979323846 / p * exp(-al * be / p * ab2) * cc;
-      for (int c = 0; c < a.natom; ++c) {
+      /* a primitive pair with a prefactor below 1e-40 adds below 1e-32 to
+       * any element (Boys values <= 1, distance factors up to ~1e8) */
+      if (fabs(base) < 1e-40) continue;
+      for (int c = lane; c < a.natom; c += 32) {
         const double zc = a.charge[c];
         if (fabs(zc) <= 1e-12) continue;
         double PC[3];
@@ -186,6 +193,9 @@ __global__ void ao_1e_kernel(Ao1eArgs a) {
         }
       }
     }
+  for (int k = 0; k < na * nb; ++k)
+    for (int o = 16; o > 0; o >>= 1) V[k] += __shfl_xor_sync(0xffffffffu, V[k], o);
+  if (lane != 0) return;
   const int nao = a.nao;
   for (int i = 0; i < na; ++i)
     for (int j = 0; j < nb; ++j) {
