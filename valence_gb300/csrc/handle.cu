@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1382,120 +1384,177 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
   } else {
     h->err_bound = 0.0;
     h->bound_all = 0.0;
-    for (size_t P = 0; P < pairs.size(); ++P)
-      for (size_t Q = 0; Q <= P; ++Q) {
-        double b = pairs[P].qmax * pairs[Q].qmax;
-        if (b < h->opt.ao_screen) continue;
-        int a = (int)P, c = (int)Q;
-        if (pairs[a].cls < pairs[c].cls) std::swap(a, c);
-        int prec = (mixed && b < h->opt.mixed_threshold) ? 1 : 0;
-        h->bound_all += b;
-        double sb = 0.0;
-        const double nall = window(a, c, eps, INFINITY, sb);
-        h->nprimq_all += nall;
-        if (prec) {
-          h->nq_fp32++;
-          h->nprimq_fp32 += nall;
-          h->err_bound += amp[P] * amp[Q];
-        } else {
-          h->nq_fp64++;
-          if (!split_pays(a, c)) {
-            if (split) prec = 2;
-          } else {
-            /* the FP32 tail: its bound mass in units of the pair bounds, with
-             * the transfer norms of both pairs */
-            const double nt = window(a, c, eps, tau, sb);
-            h->nprimq_fp32 += nt;
-            h->err_bound += sb * (amp[P] / std::max(q0[P], 1e-300)) * (amp[Q] / std::max(q0[Q], 1e-300));
-          }
-        }
-        h->work_h[prec][pairs[a].cls][pairs[c].cls].push_back(make_int2(a, c));
-      }
+    /* host threads over contiguous ranges of P (equal numbers of (P, Q)
+     * candidates), merged in P order: the same lists as one thread */
+    const size_t npr = pairs.size();
+    const int nthr = npr > 2000 ? std::max(1, std::min(16, (int)std::thread::hardware_concurrency())) : 1;
+    auto run_threads = [&](int n, const std::function<void(int)> &f) {
+      std::vector<std::thread> th;
+      for (int k = 1; k < n; ++k) th.emplace_back(f, k);
+      f(0);
+      for (auto &t : th) t.join();
+    };
     {
-      std::vector<std::vector<int4>> iwl;
+      struct Part {
+        double bound_all = 0.0, nprimq_all = 0.0, nprimq_fp32 = 0.0, err_bound = 0.0;
+        long long nq32 = 0, nq64 = 0;
+        std::vector<int2> w[3][6][6];
+      };
+      std::vector<size_t> cut(nthr + 1);
+      for (int k = 0; k <= nthr; ++k) cut[k] = (size_t)std::llround((double)npr * std::sqrt((double)k / nthr));
+      cut[nthr] = npr;
+      std::vector<Part> parts(nthr);
+      run_threads(nthr, [&](int k) {
+        Part &pt = parts[k];
+        for (size_t P = cut[k]; P < cut[k + 1]; ++P)
+          for (size_t Q = 0; Q <= P; ++Q) {
+            double b = pairs[P].qmax * pairs[Q].qmax;
+            if (b < h->opt.ao_screen) continue;
+            int a = (int)P, c = (int)Q;
+            if (pairs[a].cls < pairs[c].cls) std::swap(a, c);
+            int prec = (mixed && b < h->opt.mixed_threshold) ? 1 : 0;
+            pt.bound_all += b;
+            double sb = 0.0;
+            const double nall = window(a, c, eps, INFINITY, sb);
+            pt.nprimq_all += nall;
+            if (prec) {
+              pt.nq32++;
+              pt.nprimq_fp32 += nall;
+              pt.err_bound += amp[P] * amp[Q];
+            } else {
+              pt.nq64++;
+              if (!split_pays(a, c)) {
+                if (split) prec = 2;
+              } else {
+                /* the FP32 tail: its bound mass in units of the pair bounds,
+                 * with the transfer norms of both pairs */
+                const double nt = window(a, c, eps, tau, sb);
+                pt.nprimq_fp32 += nt;
+                pt.err_bound += sb * (amp[P] / std::max(q0[P], 1e-300)) * (amp[Q] / std::max(q0[Q], 1e-300));
+              }
+            }
+            pt.w[prec][pairs[a].cls][pairs[c].cls].push_back(make_int2(a, c));
+          }
+      });
+      for (const Part &pt : parts) {
+        h->bound_all += pt.bound_all;
+        h->nprimq_all += pt.nprimq_all;
+        h->nprimq_fp32 += pt.nprimq_fp32;
+        h->err_bound += pt.err_bound;
+        h->nq_fp32 += pt.nq32;
+        h->nq_fp64 += pt.nq64;
+        for (int p = 0; p < 3; ++p)
+          for (int a = 0; a < 6; ++a)
+            for (int c = 0; c < 6; ++c) {
+              auto &dst = h->work_h[p][a][c];
+              dst.insert(dst.end(), pt.w[p][a][c].begin(), pt.w[p][a][c].end());
+            }
+      }
+    }
+    {
       /* a quartet with more than this many primitive quartets in a launch's
        * window is split into row ranges of P's primitives, so that the largest
        * quartets do not leave a tail of lone CTAs at the end of the launch */
       constexpr int SPLIT_PRIMQ = 512;
-      std::vector<int> rows;
+      /* one task per (list, bra class, ket class), on host threads; results
+       * appended in task order */
+      struct Task {
+        int p, a, c;
+        std::vector<vsvb_gpu::SweepItem> items;
+        std::vector<std::vector<int4>> lists;
+      };
+      std::vector<Task> tasks;
       for (int p = 0; p < 3; ++p)
         for (int a = 0; a < 6; ++a)
-          for (int c = 0; c < 6; ++c) {
-            const auto &w = h->work_h[p][a][c];
-            if (w.empty()) continue;
-            /* launches over this list: FP32-class lists in FP32; FP64-class
-             * lists in the handle's FP64-class arithmetic, and with the split
-             * their primitive quartets below tau in FP32 */
-            std::vector<vsvb_gpu::SweepItem> items;
-            if (p == 1) {
-              items.push_back({p, ERI_F32, a, c, eps, INFINITY, 0, 0, 0, 100 * ERI_F32 + 10 * a + c});
-            } else if (p == 2) {
-              items.push_back({p, eri_kind(h, 0), a, c, eps, INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
-            } else if (split) {
-              items.push_back({p, eri_kind(h, 0), a, c, std::max(eps, tau), INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
-              items.push_back({p, ERI_F32, a, c, eps, tau, 0, 0, 0, 300 + 10 * a + c});
-            } else {
-              items.push_back({p, eri_kind(h, 0), a, c, eps, INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
-            }
-            for (auto &it : items) {
-              std::vector<std::pair<double, int4>> kept;
-              for (const int2 &q : w) {
-                window_rows(q.x, q.y, it.lo, it.hi, rows);
-                double n = 0.0;
-                for (int r : rows) n += r;
-                if (n <= 0.0) continue;
-                const int parts = (int)std::ceil(n / SPLIT_PRIMQ);
-                const double target = n / parts;
-                int r0 = 0;
-                double acc = 0.0;
-                for (int r = 0; r < (int)rows.size(); ++r) {
-                  acc += rows[r];
-                  const bool last = r + 1 == (int)rows.size();
-                  if (acc > 0.0 && (acc >= target || last)) {
-                    kept.push_back({acc, make_int4(q.x, q.y, r0, last ? 1 << 30 : r + 1)});
-                    it.flops_fwd += eri_flops(0, a, c, acc, pairs[q.x].nop, pairs[q.y].nop);
-                    it.flops_grad += eri_flops(3, a, c, acc, pairs[q.x].nop, pairs[q.y].nop);
-                    r0 = r + 1;
-                    acc = 0.0;
-                  } else if (acc == 0.0) {
-                    r0 = r + 1;
-                  }
-                }
-                it.nprimq += n;
-              }
-              if (kept.empty()) continue;
-              /* the quartets of one atom quartet update and read the same
-               * blocks of T and dE/dT (every shell pair of an atom pair has
-               * the same orbital pairs), so they run next to each other,
-               * where those blocks stay in L2: items grouped by atom
-               * quartet, groups by their total work, largest first, items
-               * within a group by work */
-              const long long na = d->natom;
-              auto aq = [&](const int4 &q) -> long long {
-                const ShellPair &P = pairs[q.x], &Q = pairs[q.y];
-                return ((sh[P.shA].atom * na + sh[P.shB].atom) * na + sh[Q.shA].atom) * na + sh[Q.shB].atom;
-              };
-              std::unordered_map<long long, double> gwork;
-              gwork.reserve(kept.size());
-              for (const auto &k : kept) gwork[aq(k.second)] += k.first;
-              std::vector<std::tuple<double, long long, double, int4>> ord;
-              ord.reserve(kept.size());
-              for (const auto &k : kept) {
-                const long long g = aq(k.second);
-                ord.emplace_back(gwork[g], g, k.first, k.second);
-              }
-              std::stable_sort(ord.begin(), ord.end(), [](const auto &x, const auto &y) {
-                if (std::get<0>(x) != std::get<0>(y)) return std::get<0>(x) > std::get<0>(y);
-                if (std::get<1>(x) != std::get<1>(y)) return std::get<1>(x) < std::get<1>(y);
-                return std::get<2>(x) > std::get<2>(y);
-              });
-              std::vector<int4> lst(ord.size());
-              for (size_t k = 0; k < ord.size(); ++k) lst[k] = std::get<3>(ord[k]);
-              it.wl = (int)iwl.size();
-              iwl.push_back(std::move(lst));
-              h->sweep.push_back(it);
-            }
+          for (int c = 0; c < 6; ++c)
+            if (!h->work_h[p][a][c].empty()) tasks.push_back({p, a, c, {}, {}});
+      std::atomic<int> next(0);
+      run_threads(std::min<int>(nthr, (int)tasks.size()), [&](int) {
+        std::vector<int> rows;
+        for (int ti = next++; ti < (int)tasks.size(); ti = next++) {
+          Task &tk = tasks[ti];
+          const int p = tk.p, a = tk.a, c = tk.c;
+          const auto &w = h->work_h[p][a][c];
+          /* launches over this list: FP32-class lists in FP32; FP64-class
+           * lists in the handle's FP64-class arithmetic, and with the split
+           * their primitive quartets below tau in FP32 */
+          std::vector<vsvb_gpu::SweepItem> items;
+          if (p == 1) {
+            items.push_back({p, ERI_F32, a, c, eps, INFINITY, 0, 0, 0, 100 * ERI_F32 + 10 * a + c});
+          } else if (p == 2) {
+            items.push_back({p, eri_kind(h, 0), a, c, eps, INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
+          } else if (split) {
+            items.push_back({p, eri_kind(h, 0), a, c, std::max(eps, tau), INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
+            items.push_back({p, ERI_F32, a, c, eps, tau, 0, 0, 0, 300 + 10 * a + c});
+          } else {
+            items.push_back({p, eri_kind(h, 0), a, c, eps, INFINITY, 0, 0, 0, 100 * eri_kind(h, 0) + 10 * a + c});
           }
+          for (auto &it : items) {
+            std::vector<std::pair<double, int4>> kept;
+            for (const int2 &q : w) {
+              window_rows(q.x, q.y, it.lo, it.hi, rows);
+              double n = 0.0;
+              for (int r : rows) n += r;
+              if (n <= 0.0) continue;
+              const int parts = (int)std::ceil(n / SPLIT_PRIMQ);
+              const double target = n / parts;
+              int r0 = 0;
+              double acc = 0.0;
+              for (int r = 0; r < (int)rows.size(); ++r) {
+                acc += rows[r];
+                const bool last = r + 1 == (int)rows.size();
+                if (acc > 0.0 && (acc >= target || last)) {
+                  kept.push_back({acc, make_int4(q.x, q.y, r0, last ? 1 << 30 : r + 1)});
+                  it.flops_fwd += eri_flops(0, a, c, acc, pairs[q.x].nop, pairs[q.y].nop);
+                  it.flops_grad += eri_flops(3, a, c, acc, pairs[q.x].nop, pairs[q.y].nop);
+                  r0 = r + 1;
+                  acc = 0.0;
+                } else if (acc == 0.0) {
+                  r0 = r + 1;
+                }
+              }
+              it.nprimq += n;
+            }
+            if (kept.empty()) continue;
+            /* the quartets of one atom quartet update and read the same
+             * blocks of T and dE/dT (every shell pair of an atom pair has
+             * the same orbital pairs), so they run next to each other,
+             * where those blocks stay in L2: items grouped by atom
+             * quartet, groups by their total work, largest first, items
+             * within a group by work */
+            const long long na = d->natom;
+            auto aq = [&](const int4 &q) -> long long {
+              const ShellPair &P = pairs[q.x], &Q = pairs[q.y];
+              return ((sh[P.shA].atom * na + sh[P.shB].atom) * na + sh[Q.shA].atom) * na + sh[Q.shB].atom;
+            };
+            std::unordered_map<long long, double> gwork;
+            gwork.reserve(kept.size());
+            for (const auto &k : kept) gwork[aq(k.second)] += k.first;
+            std::vector<std::tuple<double, long long, double, int4>> ord;
+            ord.reserve(kept.size());
+            for (const auto &k : kept) {
+              const long long g = aq(k.second);
+              ord.emplace_back(gwork[g], g, k.first, k.second);
+            }
+            std::stable_sort(ord.begin(), ord.end(), [](const auto &x, const auto &y) {
+              if (std::get<0>(x) != std::get<0>(y)) return std::get<0>(x) > std::get<0>(y);
+              if (std::get<1>(x) != std::get<1>(y)) return std::get<1>(x) < std::get<1>(y);
+              return std::get<2>(x) > std::get<2>(y);
+            });
+            std::vector<int4> lst(ord.size());
+            for (size_t k = 0; k < ord.size(); ++k) lst[k] = std::get<3>(ord[k]);
+            tk.lists.push_back(std::move(lst));
+            tk.items.push_back(it);
+          }
+        }
+      });
+      std::vector<std::vector<int4>> iwl;
+      for (auto &tk : tasks)
+        for (size_t k = 0; k < tk.items.size(); ++k) {
+          tk.items[k].wl = (int)iwl.size();
+          iwl.push_back(std::move(tk.lists[k]));
+          h->sweep.push_back(tk.items[k]);
+        }
       std::sort(h->sweep.begin(), h->sweep.end(), [](const vsvb_gpu::SweepItem &x, const vsvb_gpu::SweepItem &y) {
         return x.flops_fwd > y.flops_fwd;
       });
