@@ -32,8 +32,10 @@
  * over ordered orbital indices: the same sums as the task loop's (its DOCC
  * parity skips and the i = j skips of coupled orbitals are exact zeros of
  * these densities).  The orbital-pair form of the U-part of Gamma is one
- * GEMM, Wv A2x Wv^T, whose epilogue adds the exchange terms of the core
- * and contracts with T on the fly, so Gamma is never stored.
+ * GEMM, Wv A2x Wv^T, whose epilogue adds the exchange terms of the core.
+ * For an energy it contracts with T on the fly and Gamma is never stored;
+ * for a gradient Gamma is stored before the ERI sweep as its dE_num/dT and
+ * contracted with T after it.
  *
  * A spin block whose pivots fall below 1e-7 of its largest entry (exact
  * rank deficiency from molecular symmetry) takes the exact path of the

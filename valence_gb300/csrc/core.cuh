@@ -79,6 +79,7 @@ int core_post(const CoreArgs &a, const double *Gam, cudaStream_t st);
 /* after core_post: dE/dS_orb and dE/dh_orb (and dE/dT = Gam / W for the
  * sweep's adjoint); returns the kernels launched, or -1 */
 int core_adjoint(const CoreArgs &a, const CoreGrad &g, cudaStream_t st);
-/* FMA count of the pre- and post-sweep kernels (for the roofline) */
+/* FMA count of the pair-summed density GEMM of one energy (the upper
+ * triangle of Wv A2x Wv^T) */
 double core_gemm_fma(const CoreArgs &a);
 #endif
