@@ -1339,14 +1339,16 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
    * transform at the FP64 rate, a factor 5.5 on this part.  Measured with
    * the split everywhere / nowhere / this rule at factors 5.5, 1.5: the C/H
    * chain 14.8 / 18.1 / 16.1, 15.1 ms; the 128-atom chain (transforms of
-   * ~36 x 36 orbital pairs) 491 / 465 / 459, 470 ms; the rule takes 3 */
+   * ~36 x 36 orbital pairs) 491 / 465 / 459, 470 ms.  The rule takes 3, and
+   * splits every quartet whose transform block has at most 256 orbital-pair
+   * products (C/H chain 15.5 ms, 128-atom chain 451 ms) */
   auto split_pays = [&](int a, int c) -> bool {
     if (!split) return false;
     double sb = 0.0;
     const double nall = window(a, c, eps, INFINITY, sb);
     const double pf = eri_flops(0, pairs[a].cls, pairs[c].cls, 1.0, 0, 0);
     const double tr = eri_flops(3, pairs[a].cls, pairs[c].cls, 0.0, pairs[a].nop, pairs[c].nop);
-    return nall * pf > 3.0 * tr;
+    return nall * pf > 3.0 * tr || (long long)pairs[a].nop * pairs[c].nop <= 256;
   };
   /* the same per row of P's primitive pairs (rows[i] for i < na) */
   auto window_rows = [&](int P, int Q, float lo, float hi, std::vector<int> &rows) {
