@@ -153,3 +153,35 @@ def test_descent_loop_on_the_chain(vg, tmp_path):
     _, recs = loop.descend(smx, steps=2, check=s64)
     assert recs[0]["energy"] < e0 and recs[1]["energy"] < recs[0]["energy"]
     assert all(r["abs_dE_vs_check"] < 1e-6 for r in recs)
+
+
+def test_chain_integrals_match_oracle(vg, tmp_path):
+    """The optimisation loop's 128-atom chain at full basis size (1,576
+    s/p/d functions, 117 DOCC; one coupled pair so that the oracle's
+    normalisation pass is cheap): sampled orbital overlaps, core-Hamiltonian
+    elements and orbital-quartet ERIs against the oracle's ovint / int1e /
+    int2e (valence.F90:2891-3176, 3184-3438)."""
+    from tests.gpu_helpers import built_oracle
+    from valence_gb300 import configs
+    o_mod = built_oracle()
+    p = configs.alkane_chain(str(tmp_path / "ac1.inp"), npair=1)
+    o = o_mod.Oracle(p)
+    o.guess_energy_timed(0, 10 ** 9, 10 ** 9, 10 ** 12)  # normalised weights; one item per phase
+    s = vg.System(p)
+    s.energy()
+    S, H = s.orbital_1e()
+    n = S.shape[0]
+    rng = np.random.default_rng(11)
+    for i, j in rng.integers(0, n, (40, 2)):
+        assert abs(S[i, j] - o.ovint(int(i) + 1, int(j) + 1)) < 1e-12 * max(1.0, abs(S[i, j]))
+        assert abs(H[i, j] - o.int1e(int(i) + 1, int(j) + 1)) < 1e-11 * max(1.0, abs(H[i, j]))
+    op = lambda a, b: a * (a + 1) // 2 + b if a >= b else b * (b + 1) // 2 + a
+    # quartets of neighbouring orbitals (orbital k sits on carbons k mod 41 + 1, + 2)
+    quads = [(0, 1, 2, 43), (3, 44, 3, 44), (5, 46, 6, 47), (10, 51, 11, 11), (20, 61, 21, 62),
+             (0, 41, 1, 42), (100, 59, 101, 60), (7, 7, 48, 48)]
+    quads = [q for q in quads if max(q) < n]
+    got = s.orbital_eri_at([op(i, k) for i, k, j, l in quads], [op(j, l) for i, k, j, l in quads])
+    for (i, k, j, l), g in zip(quads, got):
+        ref = o.int2e(i + 1, k + 1, j + 1, l + 1)
+        assert abs(g - ref) <= 1e-11 * max(1.0, abs(ref)), (i, k, j, l, g, ref)
+    s.close()
