@@ -1341,7 +1341,8 @@ int build(vsvb_gpu *h, const vsvb_system_desc *d) {
    * chain 14.8 / 18.1 / 16.1, 15.1 ms; the 128-atom chain (transforms of
    * ~36 x 36 orbital pairs) 491 / 465 / 459, 470 ms.  The rule takes 3, and
    * splits every quartet whose transform block has at most 256 orbital-pair
-   * products (C/H chain 15.5 ms, 128-atom chain 451 ms) */
+   * products (C/H chain 15.5 ms, 128-atom chain 451 ms; at most 1024: 14.8
+   * and 475 ms) */
   auto split_pays = [&](int a, int c) -> bool {
     if (!split) return false;
     double sb = 0.0;
