@@ -506,10 +506,12 @@ def run_ours(a, rank, world):
     for k in ("e2e", "fp64", "mixed_native_fp64", "mixed_over_fp64", "mixed_native_over_fp64",
               "abs_dE_mixed_vs_fp64", "err_est_mixed", "cpu_baseline"):
         out[k] = m.get(k)
+    # the figures below run on rank 0 alone (the other ranks have left):
+    # one replica, no cross-rank barrier
     if a.workload == "alkane_chain" and a.loop_steps > 0:
         out["loop"] = run_loop(a, dev, stream)
     if a.workload != "lif_cluster":
-        c = measure(a, "lif_cluster", world, dev, stream, flush, min(a.steps, 3), 1, 2, 1, cpu=False)
+        c = measure(a, "lif_cluster", 1, dev, stream, flush, min(a.steps, 3), 1, 2, 1, cpu=False)
         out["lif_cluster"] = {"config": c["config"], "value": c["value"], "unit": "energy evals/s",
                               "ms_per_step": statistics.mean(c["ms_mx"]), "e2e": c["e2e"], "fp64": c["fp64"],
                               "mixed_native_fp64": c["mixed_native_fp64"], "mixed_over_fp64": c["mixed_over_fp64"],
@@ -519,7 +521,7 @@ def run_ours(a, rank, world):
                               "cpu_baseline_note": "the CPU oracle's sampled cluster evaluation is timed by "
                                                    "bench.py --workload lif_cluster"}
     if a.workload != "ch_chain":
-        c = measure(a, "ch_chain", world, dev, stream, flush, a.steps, a.warmup, a.steps, a.warmup)
+        c = measure(a, "ch_chain", 1, dev, stream, flush, a.steps, a.warmup, a.steps, a.warmup)
         out["ch_chain"] = {"config": c["config"], "value": c["value"], "unit": "energy+grad evals/s",
                            "ms_per_step": statistics.mean(c["ms_mx"]), "e2e": c["e2e"], "fp64": c["fp64"],
                            "mixed_native_fp64": c["mixed_native_fp64"], "mixed_over_fp64": c["mixed_over_fp64"],
@@ -548,7 +550,7 @@ def run_ours(a, rank, world):
 
     out["water"] = run_water(a, timed_simple, dev)
     if a.batch > 0:
-        out["batch"] = run_batch(a, timed_simple, world)
+        out["batch"] = run_batch(a, timed_simple, 1)
     if not a.no_optimizer:
         out["optimizer"] = run_optimizer(a, dev)
     print(json.dumps(out))
