@@ -70,12 +70,14 @@ class Core:
                     ro = [self.orb(isc, bb, s, x) for x in range(P)]
                     co = [self.orb(jsc, kb, s, x) for x in range(P)]
                     Ms = M[np.ix_(ro, co)]
-                    amax = np.abs(Ms).max()
+                    # the Schur complement of normalised orbitals has entries of at most 1:
+                    # pivot floor and perturbation on that scale (a block of a far orbital is ~0)
+                    scl = max(np.abs(Ms).max(), 1.0)
                     lu = scipy.linalg.lu_factor(Ms, check_finite=False)
-                    if np.min(np.abs(np.diag(lu[0]))) > 1e-7 * amax:
+                    if np.min(np.abs(np.diag(lu[0]))) > 1e-7 * scl:
                         mats = [(1.0, Ms)]
                     else:
-                        pm = np.array([[_pert(r, c, 0.1 * amax / np.sqrt(P)) for c in range(P)] for r in range(P)])
+                        pm = np.array([[_pert(r, c, 0.1 * scl / np.sqrt(P)) for c in range(P)] for r in range(P)])
                         mats = [(cf, Ms + k * pm) for cf, k in ((3.0, 1), (-3.0, 2), (1.0, 3))]
                     V = [(cf, s0 * np.linalg.det(A), np.linalg.inv(A)) for cf, A in mats]
                     sp.append({"ro": ro, "co": co, "V": V, "d": sum(cf * d for cf, d, _ in V),
@@ -249,6 +251,28 @@ def test_core_three_pairs_synthetic(tmp_path):
     _, Sb, _, _ = c.grad()
     h = 1e-6
     rng = np.random.default_rng(1)
+    for _ in range(3):
+        i, j = rng.integers(0, c.nsp, 2)
+        d = np.zeros_like(c.S)
+        d[i, j] += h
+        d[j, i] += h
+        fd = (c.energy(c.S + d, c.H, c.T) - c.energy(c.S - d, c.H, c.T)) / (2 * h)
+        an = Sb[i, j] + Sb[j, i] if i != j else 2 * Sb[i, i]
+        assert abs(fd - an) < 1e-7 * max(1.0, abs(fd)) + 1e-16 * abs(c.ref) / h
+
+
+def test_core_closed_form_far_orbital(tmp_path):
+    """A coupled orbital 25 A from everything: every determinant pair that
+    moves it across the spin blocks has an (exactly) zero 1 x 1 Schur block,
+    whose first cofactor is det S_DD, not zero; energy against the oracle and
+    dE/dS against differences."""
+    from valence_gb300 import configs
+    p = configs.singular_pair_large(str(tmp_path / "far.inp"), natom=4, ndocc=2)
+    c = Core(p)
+    assert abs(c.energy(c.S, c.H, c.T) - c.ref) < 1e-9 * max(1.0, abs(c.ref))
+    _, Sb, _, _ = c.grad()
+    h = 1e-6
+    rng = np.random.default_rng(4)
     for _ in range(3):
         i, j = rng.integers(0, c.nsp, 2)
         d = np.zeros_like(c.S)

@@ -71,3 +71,20 @@ def test_gradient_matches_central_differences(vg, case):
         fd = (s.energy(cp)["energy"] - s.energy(cm)["energy"]) / (2 * h)
         assert abs(g[j] - fd) < 1e-6, (j, g[j], fd)
     s.close()
+
+
+def test_core_mode_matches_oracle(vg, case):
+    """The same configuration in core mode (forced; one coupled pair): the
+    far orbital's 1 x 1 Schur blocks are about zero and take the exact path,
+    whose first cofactor is det S_DD; energy against the oracle, gradient
+    against the walk's (which shifts singular blocks by 1e-8 of their
+    scale)."""
+    p, fx = case
+    s = vg.System(p, core_mode=1)
+    assert s.core_stats()["on"]
+    r, g = s.energy_grad()
+    assert r["n_singular_pairs"] > 0
+    assert abs(r["energy"] - fx["energy"]) < 1e-8, (r["energy"], fx["energy"])
+    r0, g0 = vg.System(p, core_mode=-1).energy_grad()
+    assert np.max(np.abs(g - g0)) < 1e-5 * max(1.0, np.max(np.abs(g0)))
+    s.close()

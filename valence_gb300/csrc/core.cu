@@ -37,8 +37,10 @@
  * for a gradient Gamma is stored before the ERI sweep as its dE_num/dT and
  * contracted with T after it.
  *
- * A spin block whose pivots fall below 1e-7 of its largest entry (exact
- * rank deficiency from molecular symmetry) takes the exact path of the
+ * A spin block whose pivots fall below 1e-7 of max(its largest entry, 1)
+ * (exact rank deficiency from molecular symmetry, or an orbital far from
+ * the rest: the Schur complement of normalised orbitals has entries of at
+ * most 1) takes the exact path of the
  * per-pair kernels: with Pert a fixed rank-2 matrix, every determinant,
  * first and second cofactor of the block is a polynomial of degree <= 2 in
  * k over block + k Pert, so its value at k = 0 is 3 f(1) - 3 f(2) + f(3);
@@ -330,9 +332,12 @@ __global__ void __launch_bounds__(256) core_pairs_kernel(CoreArgs a) {
       return mx;
     };
     double *Lq = a.L + ((size_t)q * 2 + s) * P2;
-    const double amax = fill(0.0);
+    /* the Schur complement of normalised orbitals has entries of at most 1:
+     * pivot floor and perturbation on that scale, so that the near-zero
+     * block of an orbital far from the rest is flagged and perturbed */
+    const double scl = fmax(fill(0.0), 1.0);
     bool good;
-    const double det = warp_gj(W, P, lane, 1e-7 * amax, good);
+    const double det = warp_gj(W, P, lane, 1e-7 * scl, good);
     if (good) {
       const double d = s0 * det;
       for (int t = lane; t < P2; t += 32) {
@@ -351,7 +356,7 @@ __global__ void __launch_bounds__(256) core_pairs_kernel(CoreArgs a) {
     flags |= 1 << s;
     const bool room = slot < a.cap;
     if (!room && lane == 0) atomicOr(a.status, 4);
-    const double scale = 0.1 * amax / sqrt((double)P);
+    const double scale = 0.1 * scl / sqrt((double)P);
     const double cf[3] = {3.0, -3.0, 1.0};
     double lacc[8];
 #pragma unroll
@@ -361,7 +366,7 @@ __global__ void __launch_bounds__(256) core_pairs_kernel(CoreArgs a) {
     for (int k = 1; k <= 3 && !zero; ++k) {
       fill(k * scale);
       bool g2;
-      const double det2 = warp_gj(W, P, lane, 1e-7 * amax, g2);
+      const double det2 = warp_gj(W, P, lane, 1e-7 * scl, g2);
       if (!g2) {
         zero = true;
         break;
