@@ -415,12 +415,10 @@ __global__ void __launch_bounds__(256) core_pairs_kernel(CoreArgs a) {
 __global__ void __launch_bounds__(1024) core_a0_kernel(CoreArgs a) {
   __shared__ double red[32];
   const int P = a.P;
-  const int m = (1 << P) - 1;
   double s = 0.0;
   for (long long q = threadIdx.x; q < a.nq; q += blockDim.x) {
     const long long sp = q >> (2 * P);
     const int isc = (int)(sp / a.nsc), jsc = (int)(sp % a.nsc);
-    (void)m;
     s += a.csc[isc] * a.csc[jsc] * a.dd[2 * q] * a.dd[2 * q + 1];
   }
   s = block_sum(s, red);
