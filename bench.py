@@ -416,8 +416,9 @@ def measure(a, workload, world, dev, stream, flush, steps, warmup, side_steps, s
         if core["on"]:
             cfg["determinant_pair_sum"] = (f"core mode (vsvb_options.core_mode): {core['determinant_pairs']} "
                                            f"determinant pairs summed over the shared doubly occupied core in "
-                                           f"closed form, FP64; pair-summed density GEMM "
-                                           f"{core['gemm_fma']:.3g} FMAs per energy")
+                                           f"closed form; pair sums in FP64, the orbital-pair GEMMs in "
+                                           f"double-float on the mixed path (FP64 on the FP64 path); "
+                                           f"pair-summed density GEMM {core['gemm_fma']:.3g} FMAs per energy")
         sweep, sweep_wall = {}, []
 
         def collect():
